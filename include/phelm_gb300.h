@@ -1,0 +1,167 @@
+/*
+ * phelm_gb300.h -- C ABI of the GB300 sphere-FEM library (libphelm_gb300.so).
+ *
+ * This is the drop-in boundary for the reference's sphere hot path
+ * (resetius/mke "Phelm"): the icosahedral sphere mesh, the P1
+ * SphereLaplace / SphereJacobian / SphereNorm operators with their GMRES
+ * solves, and the BarVortex / Baroclin Crank-Nicolson steps.  The C++ facade
+ * in phelm_gb300.hpp keeps the reference's class API on top of it.
+ *
+ * Conventions
+ *   - Every function returns PHG_OK (0) or a PHG_ERR_* code; phg_last_error()
+ *     gives a message for the calling thread's last failure.
+ *   - Sizes follow the mesh: V points, rs inner points, os boundary points.
+ *     Vectors over the mesh are "full" (V entries, point order) or "inner"
+ *     (rs entries, inner order); boundary values have os entries.  A NULL
+ *     boundary pointer means a zero boundary, as in the reference
+ *     (src/proj.cpp:57-67).
+ *   - Vector arguments may be host or device (cudaMalloc'd) pointers.  Device
+ *     pointers are used in place and the call only enqueues work on `stream`
+ *     (NULL = the handle's own stream); host pointers are staged through the
+ *     handle's device buffers and the call returns after the result is back.
+ *   - Scalars (norms) are written to host memory and the call synchronises.
+ *   - A handle may be used from one thread / stream at a time; different
+ *     handles may run concurrently on different streams.
+ *   - Outputs may alias inputs where the reference allows it
+ *     (BarVortex::calc with u1 == u, examples/test_barvortex.cpp:529).
+ */
+#ifndef PHELM_GB300_H
+#define PHELM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PHG_OK 0
+#define PHG_ERR_ARG 1           /* bad argument / size / handle */
+#define PHG_ERR_CUDA 2          /* CUDA runtime error (no device, OOM, launch failure) */
+#define PHG_ERR_NOT_CONVERGED 3 /* a linear solve missed its tolerance */
+#define PHG_ERR_TIMEOUT 4       /* a device-side wait ran out (kernel returned early) */
+#define PHG_ERR_IO 5            /* mesh file unreadable or malformed */
+
+#define PHG_FP64 0   /* every operator, vector and coefficient in double */
+#define PHG_MIXED 1  /* FP32 Krylov vectors and operator inside FP64 iterative refinement */
+
+typedef struct phg_mesh_s *phg_mesh;
+typedef struct phg_ops_s *phg_ops;
+typedef struct phg_barvortex_s *phg_barvortex;
+typedef struct phg_baroclin_s *phg_baroclin;
+
+const char *phg_last_error(void);
+const char *phg_version(void);
+
+/* ------------------------------------------------------------------ mesh --
+ * Host-only (no GPU needed). */
+
+/* Icosahedral sphere mesh, `level` subdivisions (1..9), south pole as the
+ * single boundary point, Cuthill-McKee point order.  Replaces running
+ * "mke_mesh_sphere --type full --coord local --iter level"
+ * (utils/icosahedron.cpp:481-624, utils/mesh_builder.cpp:52-585) and then
+ * Mesh::load (src/mesh.cpp:323-519); the result is identical. */
+int phg_mesh_generate(int level, phg_mesh *out);
+/* Mesh::load(FILE*) (src/mesh.h:411, src/mesh.cpp:323-519) from a file in
+ * the reference's text format (charts stdsphere1..4). */
+int phg_mesh_load_file(const char *path, phg_mesh *out);
+void phg_mesh_destroy(phg_mesh m);
+/* Mesh::size / inner_size / outer_size / tr.size() (src/mesh.h:381-383). */
+int phg_mesh_info(phg_mesh m, int *V, int *T, int *rs, int *os);
+/* Copies of Mesh::ps (xyz: V x 3; uv: V x 4 x 2 chart coordinates), Mesh::tr
+ * (tri: T x 3, tz: T zones), boundary flags (V); any pointer may be NULL. */
+int phg_mesh_arrays(phg_mesh m, double *xyz, double *uv, int *tri, int *tz, int *bnd);
+/* Mesh::inner / outer / p2io (src/mesh.h:375-379); any pointer may be NULL. */
+int phg_mesh_maps(phg_mesh m, int *inner, int *outer, int *p2io);
+/* Host-assembled operator in CSR, as phelm::Solver::add accumulates it.
+ * name: "idt" "lapl" "bnd2" "bnd3" (SphereLaplace, src/impl/slaplace_impl.h:133-145),
+ * "jidt" "d1" "d2" "d1c" "d2c" "d1b" "d2b" "d1cb" "d2cb" (SphereJacobian,
+ * src/sjacobian.cpp:413-454), "norm" (SphereNorm, src/norm.h:70-73).
+ * Call with ptr/col/val NULL to get n (rows) and nnz first. */
+int phg_mesh_csr(phg_mesh m, const char *name, int *n, int *nnz, int *ptr, int *col, double *val);
+
+/* ------------------------------------------------------------- operators --
+ * Uploads the mesh maps and every SphereLaplace / SphereJacobian /
+ * SphereNorm operator to the current CUDA device.  Replaces the three
+ * constructors SphereLaplace(m) (src/impl/slaplace_impl.h:133-145),
+ * SphereJacobian(m) (src/sjacobian.cpp:413-454), SphereNorm(m)
+ * (src/norm.h:67-74).  precision: PHG_FP64 or PHG_MIXED. */
+int phg_ops_create(phg_mesh m, int precision, phg_ops *out);
+void phg_ops_destroy(phg_ops o);
+/* GMRES(restart) tolerance (relative residual ||b - A x|| / ||b||) and
+ * iteration cap for the solves of this handle.  Defaults: restart 30,
+ * tol 1e-12, max_iter 20000; mass-matrix solves inside operator applies use
+ * min(tol, 1e-14). */
+int phg_ops_set_solver(phg_ops o, int restart, double tol, int max_iter);
+/* Statistics of the last solve on this handle (host memory). */
+int phg_ops_last_solve(phg_ops o, int *iters, int *cycles, double *relres);
+
+/* SphereLaplace::calc1 (src/impl/slaplace_impl.h:176-192): ans[V] = Laplacian
+ * of F[V] with boundary values bnd[os] written on the boundary. */
+int phg_laplace_calc1(phg_ops o, double *ans, const double *F, const double *bnd, void *stream);
+/* SphereLaplace::calc2 (src/impl/slaplace_impl.h:147-174): ans[rs] on inner points. */
+int phg_laplace_calc2(phg_ops o, double *ans, const double *F, void *stream);
+/* SphereLaplace::solve (src/impl/slaplace_impl.h:84-131): ans[V] with
+ * Laplacian(ans) = F[V] and ans = bnd[os] on the boundary. */
+int phg_laplace_solve(phg_ops o, double *ans, const double *F, const double *bnd, void *stream);
+/* SphereJacobian::calc1 / calc2 / calc2t (src/sjacobian.cpp:348-408, 456-461). */
+int phg_jacobian_calc1(phg_ops o, double *ans, const double *u, const double *v, const double *bnd, void *stream);
+int phg_jacobian_calc2(phg_ops o, double *ans, const double *u, const double *v, void *stream);
+int phg_jacobian_calc2t(phg_ops o, double *ans, const double *u, const double *v, void *stream);
+/* SphereNorm::norm / dist / scalar (src/norm.h:81-94); result to *out (host). */
+int phg_norm(phg_ops o, const double *u, double *out, void *stream);
+int phg_dist(phg_ops o, const double *u, const double *v, double *out, void *stream);
+int phg_scalar(phg_ops o, const double *u, const double *v, double *out, void *stream);
+
+/* ------------------------------------------------------------- barvortex --
+ * BarVortexConf (examples/barvortex.h:62-96); theta is explicit (the
+ * reference leaves it uninitialised).  picard_iters: Picard iterations per
+ * step; the reference loops up to 1000 and stops when the update is below
+ * 1e-14 of the state norm (examples/barvortex_impl.h:260, 300-306) -- the
+ * same stop test is applied here within picard_iters. */
+typedef struct {
+	double tau, sigma, mu, k1, k2, theta;
+	int picard_iters;
+} phg_bv_conf;
+
+/* BarVortex(m, conf) (examples/barvortex_impl.h:109-154); coriolis[V] is
+ * l + h at every point (the reference evaluates conf.coriolis with proj). */
+int phg_barvortex_create(phg_ops o, const phg_bv_conf *conf, const double *coriolis, phg_barvortex *out);
+void phg_barvortex_destroy(phg_barvortex b);
+/* BarVortex::calc(u1, u, bnd_u, bnd_w, t) (examples/barvortex_impl.h:171-310):
+ * one step of the stream function u[V] -> u1[V]; forcing[V] is f at time t
+ * (NULL = no forcing).  u1 may equal u. */
+int phg_barvortex_calc(phg_barvortex b, double *u1, const double *u, const double *bnd_u,
+                       const double *bnd_w, const double *forcing, void *stream);
+/* nmembers independent states advanced together (member-major: member k at
+ * u + k * V; bnd_u / bnd_w: os values per member; forcing shared, V values).
+ * Each member's result equals a phg_barvortex_calc of that member alone
+ * within the solve tolerance.  No reference counterpart (ensemble mode). */
+int phg_barvortex_calc_batch(phg_barvortex b, int nmembers, double *u1, const double *u,
+                             const double *bnd_u, const double *bnd_w, const double *forcing, void *stream);
+/* Totals of the last calc on this handle: GMRES iterations of each solve
+ * kind (L, A, mass J, mass L) summed over the step, and the worst relative
+ * residual of any solve. */
+int phg_barvortex_last_stats(phg_barvortex b, int *iters_lapl, int *iters_a, int *iters_mj,
+                             int *iters_ml, double *worst_relres);
+
+/* -------------------------------------------------------------- baroclin --
+ * Baroclin(m, f, g, coriolis, tau, sigma, mu, sigma1, mu1, alpha)
+ * (examples/baroclin.cpp:69-106); theta = 0.5 as in the reference.
+ * picard_iters / picard_tol: at most picard_iters iterations, stop when
+ * max(dist(u1), dist(u2)) < picard_tol (reference: 20 and 1e-8,
+ * examples/baroclin.cpp:547, 600). */
+typedef struct {
+	double tau, sigma, mu, sigma1, mu1, alpha;
+	int picard_iters;
+	double picard_tol;
+} phg_bc_conf;
+
+int phg_baroclin_create(phg_ops o, const phg_bc_conf *conf, const double *coriolis, phg_baroclin *out);
+void phg_baroclin_destroy(phg_baroclin b);
+/* Baroclin::calc(u11, u21, u1, u2, bnd, t) (examples/baroclin.cpp:445-606);
+ * f, g: forcing fields at time t (V each, NULL = none). */
+int phg_baroclin_calc(phg_baroclin b, double *u11, double *u21, const double *u1, const double *u2,
+                      const double *bnd, const double *f, const double *g, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

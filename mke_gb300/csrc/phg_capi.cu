@@ -1,0 +1,762 @@
+// phg_capi.cu -- the C ABI (include/phelm_gb300.h): handles, HBM residency of
+// the operators, host/device argument staging and the time-step drivers.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/phelm_gb300.h"
+#include "phg_host.hpp"
+#include "phg_kernels.cuh"
+
+using namespace phg;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) return fail(PHG_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+// owning device allocation
+struct DBuf {
+    void *p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    ~DBuf() { if (p) cudaFree(p); }
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= n) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr; n = 0;
+        cudaError_t e = cudaMalloc(&p, bytes ? bytes : 1);
+        if (e == cudaSuccess) n = bytes;
+        return e;
+    }
+    template <typename T> T *as() const { return (T *)p; }
+};
+
+template <typename T>
+cudaError_t upload(DBuf &b, const std::vector<T> &v) {
+    cudaError_t e = b.ensure(sizeof(T) * v.size());
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpy(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice);
+}
+
+bool is_device_ptr(const void *p) {
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------- mesh ---
+struct phg_mesh_s {
+    Mesh m;
+    std::once_flag assembled;
+    SphereOps ops;
+    void assemble() { std::call_once(assembled, [this] { assemble_sphere(m, ops); }); }
+};
+
+extern "C" const char *phg_last_error(void) { return g_err.c_str(); }
+extern "C" const char *phg_version(void) { return "phelm-gb300 0.1 (sm_103a)"; }
+
+extern "C" int phg_mesh_generate(int level, phg_mesh *out) {
+    if (!out) return fail(PHG_ERR_ARG, "out is NULL");
+    auto h = std::make_unique<phg_mesh_s>();
+    std::string err;
+    if (!generate_sphere(level, h->m, err)) return fail(PHG_ERR_ARG, "%s", err.c_str());
+    *out = h.release();
+    return PHG_OK;
+}
+
+extern "C" int phg_mesh_load_file(const char *path, phg_mesh *out) {
+    if (!path || !out) return fail(PHG_ERR_ARG, "NULL argument");
+    FILE *f = fopen(path, "rb");
+    if (!f) return fail(PHG_ERR_IO, "cannot open %s", path);
+    auto h = std::make_unique<phg_mesh_s>();
+    std::string err;
+    bool ok = load_mesh_text(f, h->m, err);
+    fclose(f);
+    if (!ok) return fail(PHG_ERR_IO, "%s: %s", path, err.c_str());
+    *out = h.release();
+    return PHG_OK;
+}
+
+extern "C" void phg_mesh_destroy(phg_mesh m) { delete m; }
+
+extern "C" int phg_mesh_info(phg_mesh h, int *V, int *T, int *rs, int *os) {
+    if (!h) return fail(PHG_ERR_ARG, "NULL mesh");
+    if (V) *V = h->m.V;
+    if (T) *T = h->m.T;
+    if (rs) *rs = h->m.rs;
+    if (os) *os = h->m.os;
+    return PHG_OK;
+}
+
+extern "C" int phg_mesh_arrays(phg_mesh h, double *xyz, double *uv, int *tri, int *tz, int *bnd) {
+    if (!h) return fail(PHG_ERR_ARG, "NULL mesh");
+    const Mesh &m = h->m;
+    if (xyz) memcpy(xyz, m.xyz.data(), 8 * m.xyz.size());
+    if (uv) memcpy(uv, m.uv.data(), 8 * m.uv.size());
+    if (tri) memcpy(tri, m.tri.data(), 4 * m.tri.size());
+    if (tz) memcpy(tz, m.tz.data(), 4 * m.tz.size());
+    if (bnd) memcpy(bnd, m.bnd.data(), 4 * m.bnd.size());
+    return PHG_OK;
+}
+
+extern "C" int phg_mesh_maps(phg_mesh h, int *inner, int *outer, int *p2io) {
+    if (!h) return fail(PHG_ERR_ARG, "NULL mesh");
+    const Mesh &m = h->m;
+    if (inner) memcpy(inner, m.inner.data(), 4 * m.inner.size());
+    if (outer) memcpy(outer, m.outer.data(), 4 * m.outer.size());
+    if (p2io) memcpy(p2io, m.p2io.data(), 4 * m.p2io.size());
+    return PHG_OK;
+}
+
+static const Csr *find_csr(phg_mesh_s *h, const char *name) {
+    SphereOps &o = h->ops;
+    struct { const char *n; const Csr *c; } t[] = {
+        {"idt", &o.idt}, {"lapl", &o.lapl}, {"bnd2", &o.bnd2}, {"bnd3", &o.bnd3}, {"jidt", &o.jidt},
+        {"d1", &o.d1}, {"d2", &o.d2}, {"d1c", &o.d1c}, {"d2c", &o.d2c}, {"d1b", &o.d1b}, {"d2b", &o.d2b},
+        {"d1cb", &o.d1cb}, {"d2cb", &o.d2cb}, {"norm", &o.norm}};
+    for (auto &e : t)
+        if (!strcmp(e.n, name)) return e.c;
+    return nullptr;
+}
+
+extern "C" int phg_mesh_csr(phg_mesh h, const char *name, int *n, int *nnz, int *ptr, int *col, double *val) {
+    if (!h || !name) return fail(PHG_ERR_ARG, "NULL argument");
+    h->assemble();
+    const Csr *c = find_csr(h, name);
+    if (!c) return fail(PHG_ERR_ARG, "unknown operator '%s'", name);
+    if (n) *n = c->n;
+    if (nnz) *nnz = c->nnz();
+    if (ptr) memcpy(ptr, c->ptr.data(), 4 * c->ptr.size());
+    if (col) memcpy(col, c->col.data(), 4 * c->col.size());
+    if (val) memcpy(val, c->val.data(), 8 * c->val.size());
+    return PHG_OK;
+}
+
+// ------------------------------------------------------- device operators ---
+namespace {
+
+// slot-major ELL of an rs x rs CSR on a given pattern
+void to_ell(const Csr &c, int W, std::vector<int> *col, std::vector<double> &val) {
+    const int n = c.n;
+    if (col) col->assign((size_t)W * n, 0);
+    val.assign((size_t)W * n, 0.0);
+    for (int i = 0; i < n; ++i) {
+        int k = 0;
+        for (int q = c.ptr[i]; q < c.ptr[i + 1]; ++q, ++k) {
+            if (col) (*col)[(size_t)k * n + i] = c.col[q];
+            val[(size_t)k * n + i] = c.val[q];
+        }
+        for (; k < W; ++k)
+            if (col) (*col)[(size_t)k * n + i] = i;
+    }
+}
+
+struct SolveOpBufs {
+    DBuf val, as64, as32, dinv;
+    DevSolveOp op;
+};
+
+struct ColsBufs {
+    DBuf ptr, col, val;
+    DevCols c;
+};
+
+}  // namespace
+
+struct phg_ops_s {
+    phg_mesh_s *mesh = nullptr;
+    int prec = PHG_FP64;
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    int V = 0, rs = 0, os = 0, W = 0;
+    DBuf inner, outer, p2io, isb;
+    DBuf pcol;                       // shared rs x rs pattern (W x rs)
+    SolveOpBufs ML, L, MJ;           // mass (Laplace), Laplacian, mass (Jacobian)
+    DBuf vd1, vd2, vd1c, vd2c;
+    ColsBufs bnd2, bnd3, d1b, d2b, d1cb, d2cb;
+    JacOps J;
+    DBuf ncol, nval;                 // V x V norm matrix (its own pattern)
+    DevEll norm;
+    int restart = 30, max_iter = 20000;
+    double tol = 1e-12;
+    // scratch
+    DBuf work, stats, s_a, s_b, s_c, s_d, s_e, s_part, s_out;
+    GmresStats last{};
+    bool stats_pending = false;
+    // staging for host pointers
+    DBuf st[6];
+
+    DevEll ell(const DBuf &vals) const { DevEll e; e.n = rs; e.W = W; e.col = pcol.as<int>(); e.val = vals.as<double>(); return e; }
+    const int *imap() const { return inner.as<int>(); }
+    const int *bmap() const { return outer.as<int>(); }
+    cudaStream_t str(void *s) const { return s ? (cudaStream_t)s : stream; }
+};
+
+namespace {
+
+int build_solve_op(phg_ops_s *o, const Csr &c, SolveOpBufs &b) {
+    std::vector<double> v;
+    to_ell(c, o->W, nullptr, v);
+    std::vector<double> dinv(o->rs, 0.0), as64(v.size());
+    std::vector<float> as32(v.size());
+    for (int i = 0; i < c.n; ++i)
+        for (int q = c.ptr[i]; q < c.ptr[i + 1]; ++q)
+            if (c.col[q] == i) dinv[i] = 1.0 / c.val[q];
+    for (int i = 0; i < o->rs; ++i)
+        if (!(dinv[i] != 0.0) || !std::isfinite(dinv[i])) return fail(PHG_ERR_ARG, "zero diagonal in row %d", i);
+    const int n = o->rs;
+    std::vector<int> col;
+    to_ell(c, o->W, &col, v);
+    for (size_t e = 0; e < v.size(); ++e) {
+        as64[e] = v[e] * dinv[col[e]];
+        as32[e] = (float)as64[e];
+    }
+    (void)n;
+    CK(upload(b.val, v)); CK(upload(b.as64, as64)); CK(upload(b.as32, as32)); CK(upload(b.dinv, dinv));
+    b.op.A = o->ell(b.val);
+    b.op.as64 = b.as64.as<double>(); b.op.as32 = b.as32.as<float>(); b.op.dinv = b.dinv.as<double>();
+    return PHG_OK;
+}
+
+int build_cols(const Csr &c, ColsBufs &b) {
+    b.c = DevCols();
+    b.c.n = c.n;
+    if (c.nnz() == 0) return PHG_OK;
+    CK(upload(b.ptr, c.ptr)); CK(upload(b.col, c.col)); CK(upload(b.val, c.val));
+    b.c.ptr = b.ptr.as<int>(); b.c.col = b.col.as<int>(); b.c.val = b.val.as<double>();
+    return PHG_OK;
+}
+
+int build_vals(phg_ops_s *o, const Csr &c, DBuf &b) {
+    std::vector<double> v;
+    to_ell(c, o->W, nullptr, v);
+    CK(upload(b, v));
+    return PHG_OK;
+}
+
+bool same_pattern(const Csr &a, const Csr &b) { return a.n == b.n && a.ptr == b.ptr && a.col == b.col; }
+
+}  // namespace
+
+extern "C" int phg_ops_create(phg_mesh h, int precision, phg_ops *out) {
+    if (!h || !out) return fail(PHG_ERR_ARG, "NULL argument");
+    if (precision != PHG_FP64 && precision != PHG_MIXED) return fail(PHG_ERR_ARG, "bad precision %d", precision);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(PHG_ERR_CUDA, "no CUDA device");
+    }
+    h->assemble();
+    const Mesh &m = h->m;
+    const SphereOps &so = h->ops;
+    if (m.rs < 1) return fail(PHG_ERR_ARG, "mesh has no inner points");
+    const Csr *shared[] = {&so.lapl, &so.jidt, &so.d1, &so.d2, &so.d1c, &so.d2c};
+    for (const Csr *c : shared)
+        if (!same_pattern(so.idt, *c)) return fail(PHG_ERR_ARG, "operators do not share one pattern");
+    auto o = std::make_unique<phg_ops_s>();
+    o->mesh = h;
+    o->prec = precision;
+    CK(cudaGetDevice(&o->dev));
+    CK(cudaStreamCreateWithFlags(&o->stream, cudaStreamNonBlocking));
+    o->V = m.V; o->rs = m.rs; o->os = m.os;
+    int W = 0;
+    for (int i = 0; i < m.rs; ++i) W = std::max(W, so.idt.ptr[i + 1] - so.idt.ptr[i]);
+    o->W = W;
+    std::vector<int> col;
+    std::vector<double> tmp;
+    to_ell(so.idt, W, &col, tmp);
+    CK(upload(o->pcol, col));
+    CK(upload(o->inner, m.inner)); CK(upload(o->outer, m.outer.empty() ? std::vector<int>{0} : m.outer));
+    CK(upload(o->p2io, m.p2io)); CK(upload(o->isb, m.bnd));
+    int r;
+    if ((r = build_solve_op(o.get(), so.idt, o->ML))) return r;
+    if ((r = build_solve_op(o.get(), so.lapl, o->L))) return r;
+    if ((r = build_solve_op(o.get(), so.jidt, o->MJ))) return r;
+    if ((r = build_vals(o.get(), so.d1, o->vd1)) || (r = build_vals(o.get(), so.d2, o->vd2)) ||
+        (r = build_vals(o.get(), so.d1c, o->vd1c)) || (r = build_vals(o.get(), so.d2c, o->vd2c)))
+        return r;
+    if ((r = build_cols(so.bnd2, o->bnd2)) || (r = build_cols(so.bnd3, o->bnd3)) ||
+        (r = build_cols(so.d1b, o->d1b)) || (r = build_cols(so.d2b, o->d2b)) ||
+        (r = build_cols(so.d1cb, o->d1cb)) || (r = build_cols(so.d2cb, o->d2cb)))
+        return r;
+    o->J.d1 = o->ell(o->vd1); o->J.d2 = o->ell(o->vd2); o->J.d1c = o->ell(o->vd1c); o->J.d2c = o->ell(o->vd2c);
+    o->J.d1b = o->d1b.c; o->J.d2b = o->d2b.c; o->J.d1cb = o->d1cb.c; o->J.d2cb = o->d2cb.c;
+    // norm matrix: V x V on its own pattern
+    int Wn = 0;
+    for (int i = 0; i < m.V; ++i) Wn = std::max(Wn, so.norm.ptr[i + 1] - so.norm.ptr[i]);
+    std::vector<int> ncol;
+    std::vector<double> nval;
+    {
+        Csr c = so.norm;
+        ncol.assign((size_t)Wn * m.V, 0);
+        nval.assign((size_t)Wn * m.V, 0.0);
+        for (int i = 0; i < m.V; ++i) {
+            int k = 0;
+            for (int q = c.ptr[i]; q < c.ptr[i + 1]; ++q, ++k) {
+                ncol[(size_t)k * m.V + i] = c.col[q];
+                nval[(size_t)k * m.V + i] = c.val[q];
+            }
+            for (; k < Wn; ++k) ncol[(size_t)k * m.V + i] = i;
+        }
+    }
+    CK(upload(o->ncol, ncol)); CK(upload(o->nval, nval));
+    o->norm.n = m.V; o->norm.W = Wn; o->norm.col = o->ncol.as<int>(); o->norm.val = o->nval.as<double>();
+    CK(o->stats.ensure(sizeof(GmresStats) * 64));
+    CK(cudaMemset(o->stats.p, 0, sizeof(GmresStats) * 64));
+    *out = o.release();
+    return PHG_OK;
+}
+
+extern "C" void phg_ops_destroy(phg_ops o) {
+    if (!o) return;
+    if (o->stream) { cudaStreamSynchronize(o->stream); cudaStreamDestroy(o->stream); }
+    delete o;
+}
+
+extern "C" int phg_ops_set_solver(phg_ops o, int restart, double tol, int max_iter) {
+    if (!o) return fail(PHG_ERR_ARG, "NULL handle");
+    if (restart < 1 || restart > 48) return fail(PHG_ERR_ARG, "restart must be in 1..48");
+    if (!(tol > 0) || max_iter < 1) return fail(PHG_ERR_ARG, "bad tolerance / iteration cap");
+    o->restart = restart; o->tol = tol; o->max_iter = max_iter;
+    return PHG_OK;
+}
+
+namespace {
+
+Precision prec_of(const phg_ops_s *o) { return o->prec == PHG_MIXED ? PREC_MIXED : PREC_FP64; }
+
+// enqueue one solve; stats go to slot `slot` of the handle's device stats array
+int solve(phg_ops_s *o, const DevSolveOp &op, const double *B, double *X, int nv, int ld, double tol,
+          int slot, cudaStream_t s) {
+    size_t need = gmres_work_bytes(op.A.n, nv, o->restart, prec_of(o));
+    if (need > o->work.n) {
+        CK(cudaStreamSynchronize(s));
+        CK(o->work.ensure(need));
+    }
+    CK(gmres_solve(op, B, X, nv, ld, o->restart, o->max_iter, tol, prec_of(o), o->work.p,
+                   o->stats.as<GmresStats>() + slot, s));
+    o->stats_pending = true;
+    return PHG_OK;
+}
+
+// read back and judge the stats of slots [0, nslots)
+int check_stats(phg_ops_s *o, int nslots, cudaStream_t s, GmresStats *agg = nullptr, GmresStats *each = nullptr) {
+    std::vector<GmresStats> st(nslots);
+    CK(cudaMemcpyAsync(st.data(), o->stats.p, sizeof(GmresStats) * nslots, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    GmresStats a{0, 0, 0.0, 0};
+    for (auto &x : st) {
+        a.iters += x.iters; a.cycles += x.cycles;
+        a.relres = std::max(a.relres, x.relres);
+        a.status = std::max(a.status, x.status);
+    }
+    if (each) memcpy(each, st.data(), sizeof(GmresStats) * nslots);
+    o->last = a;
+    o->stats_pending = false;
+    if (agg) *agg = a;
+    if (a.status == 2) return fail(PHG_ERR_TIMEOUT, "device barrier wait timed out");
+    if (a.status == 1 && !(a.relres <= std::max(1e3 * o->tol, 1e-8)))
+        return fail(PHG_ERR_NOT_CONVERGED, "GMRES stopped at relative residual %.3e", a.relres);
+    return PHG_OK;
+}
+
+// host/device argument staging
+struct Stage {
+    phg_ops_s *o;
+    cudaStream_t s;
+    bool host = false;
+    int next = 0;
+    struct Out { double *host; double *dev; size_t n; };
+    std::vector<Out> outs;
+    Stage(phg_ops_s *o_, cudaStream_t s_) : o(o_), s(s_) {}
+    cudaError_t in(const double *p, size_t n, const double **dp) {
+        if (!p || is_device_ptr(p)) { *dp = p; return cudaSuccess; }
+        host = true;
+        DBuf &b = o->st[next++];
+        cudaError_t e = b.ensure(8 * n);
+        if (e != cudaSuccess) return e;
+        *dp = b.as<double>();
+        return cudaMemcpyAsync(b.p, p, 8 * n, cudaMemcpyHostToDevice, s);
+    }
+    cudaError_t out(double *p, size_t n, double **dp) {
+        if (is_device_ptr(p)) { *dp = p; return cudaSuccess; }
+        host = true;
+        DBuf &b = o->st[next++];
+        cudaError_t e = b.ensure(8 * n);
+        if (e != cudaSuccess) return e;
+        *dp = b.as<double>();
+        outs.push_back({p, b.as<double>(), n});
+        return cudaSuccess;
+    }
+    cudaError_t finish() {
+        for (auto &x : outs) {
+            cudaError_t e = cudaMemcpyAsync(x.host, x.dev, 8 * x.n, cudaMemcpyDeviceToHost, s);
+            if (e != cudaSuccess) return e;
+        }
+        return host ? cudaStreamSynchronize(s) : cudaSuccess;
+    }
+};
+
+double mass_tol(const phg_ops_s *o) { return std::min(o->tol, 1e-14); }
+
+// ans (rs) = M_L^{-1} (L F_in + B3 F_bnd) for nv members of full vectors F
+int laplace_calc2_dev(phg_ops_s *o, double *ans, int lda, const double *F, int ldf, int nv, int slot, cudaStream_t s) {
+    CK(o->s_a.ensure(8 * (size_t)o->rs * nv));
+    double *rhs = o->s_a.as<double>();
+    CK(apply_op(o->L.op.A, o->bnd3.c, F, ldf, o->imap(), F, ldf, o->bmap(), rhs, o->rs, nv, s));
+    for (int v = 0; v < nv; ++v) CK(cudaMemsetAsync(ans + (size_t)v * lda, 0, 8 * (size_t)o->rs, s));
+    return solve(o, o->ML.op, rhs, ans, nv, lda, mass_tol(o), slot, s);
+}
+
+// the 8 derivative solves of a Jacobian for nv members; sol: nv x 8 x rs
+int jacobian_derivs_dev(phg_ops_s *o, const double *u, const double *v, int ld, double *sol, int nv, int slot,
+                        cudaStream_t s) {
+    CK(o->s_b.ensure(8 * (size_t)o->rs * 8 * nv));
+    double *rhs = o->s_b.as<double>();
+    CK(jac_rhs(o->J, u, v, ld, o->imap(), o->bmap(), rhs, o->rs, nv, s));
+    CK(cudaMemsetAsync(sol, 0, 8 * (size_t)o->rs * 8 * nv, s));
+    return solve(o, o->MJ.op, rhs, sol, 8 * nv, o->rs, mass_tol(o), slot, s);
+}
+
+int norm_dev(phg_ops_s *o, const double *u, const double *v, int nv, double *out_dev, bool dist, bool take_sqrt,
+             cudaStream_t s) {
+    const int V = o->V;
+    CK(o->s_d.ensure(8 * (size_t)V * nv * 2));
+    double *diff = o->s_d.as<double>(), *y = diff + (size_t)V * nv;
+    const double *x = u;
+    if (dist) { CK(vsub(diff, u, v, (long long)V * nv, s)); x = diff; }
+    CK(apply_op(o->norm, DevCols(), x, V, nullptr, nullptr, 0, nullptr, y, V, nv, s));
+    CK(o->s_part.ensure(8 * (size_t)nv * dot_chunks(V)));
+    const double *a = dist ? x : u;
+    const double *bb = dist ? y : y;
+    if (!dist && v) {  // scalar(u, v) = u . (NORM v)
+        CK(apply_op(o->norm, DevCols(), v, V, nullptr, nullptr, 0, nullptr, y, V, nv, s));
+        a = u;
+    }
+    CK(dot(a, bb, V, V, nv, o->s_part.as<double>(), out_dev, take_sqrt, s));
+    return PHG_OK;
+}
+
+}  // namespace
+
+extern "C" int phg_ops_last_solve(phg_ops o, int *iters, int *cycles, double *relres) {
+    if (!o) return fail(PHG_ERR_ARG, "NULL handle");
+    if (iters) *iters = o->last.iters;
+    if (cycles) *cycles = o->last.cycles;
+    if (relres) *relres = o->last.relres;
+    return PHG_OK;
+}
+
+extern "C" int phg_laplace_calc2(phg_ops o, double *ans, const double *F, void *stream) {
+    if (!o || !ans || !F) return fail(PHG_ERR_ARG, "NULL argument");
+    cudaStream_t s = o->str(stream);
+    Stage st(o, s);
+    const double *dF; double *dA;
+    CK(st.in(F, o->V, &dF)); CK(st.out(ans, o->rs, &dA));
+    int r = laplace_calc2_dev(o, dA, o->rs, dF, o->V, 1, 0, s);
+    if (r) return r;
+    CK(st.finish());
+    return st.host ? check_stats(o, 1, s) : PHG_OK;
+}
+
+extern "C" int phg_laplace_calc1(phg_ops o, double *ans, const double *F, const double *bnd, void *stream) {
+    if (!o || !ans || !F) return fail(PHG_ERR_ARG, "NULL argument");
+    cudaStream_t s = o->str(stream);
+    Stage st(o, s);
+    const double *dF, *dB; double *dA;
+    CK(st.in(F, o->V, &dF)); CK(st.in(bnd, o->os, &dB)); CK(st.out(ans, o->V, &dA));
+    CK(o->s_c.ensure(8 * (size_t)o->rs));
+    int r = laplace_calc2_dev(o, o->s_c.as<double>(), o->rs, dF, o->V, 1, 0, s);
+    if (r) return r;
+    CK(p2u(dA, o->V, o->s_c.as<double>(), o->rs, dB, o->os, o->p2io.as<int>(), o->isb.as<int>(), o->V, 1, s));
+    CK(st.finish());
+    return st.host ? check_stats(o, 1, s) : PHG_OK;
+}
+
+extern "C" int phg_laplace_solve(phg_ops o, double *ans, const double *F, const double *bnd, void *stream) {
+    if (!o || !ans || !F) return fail(PHG_ERR_ARG, "NULL argument");
+    cudaStream_t s = o->str(stream);
+    Stage st(o, s);
+    const double *dF, *dB; double *dA;
+    CK(st.in(F, o->V, &dF)); CK(st.in(bnd, o->os, &dB)); CK(st.out(ans, o->V, &dA));
+    CK(o->s_a.ensure(8 * (size_t)o->rs)); CK(o->s_c.ensure(8 * (size_t)o->rs));
+    double *b = o->s_a.as<double>(), *x = o->s_c.as<double>();
+    // b = M_L F_in + B2 bnd
+    CK(apply_op(o->ML.op.A, o->bnd2.c, dF, o->V, o->imap(), dB, o->os, nullptr, b, o->rs, 1, s));
+    CK(cudaMemsetAsync(x, 0, 8 * (size_t)o->rs, s));
+    int r = solve(o, o->L.op, b, x, 1, o->rs, o->tol, 0, s);
+    if (r) return r;
+    CK(p2u(dA, o->V, x, o->rs, dB, o->os, o->p2io.as<int>(), o->isb.as<int>(), o->V, 1, s));
+    CK(st.finish());
+    return st.host ? check_stats(o, 1, s) : PHG_OK;
+}
+
+static int jacobian_common(phg_ops o, double *ans, const double *u, const double *v, const double *bnd,
+                           bool full, bool transpose, void *stream) {
+    if (!o || !ans || !u || !v) return fail(PHG_ERR_ARG, "NULL argument");
+    cudaStream_t s = o->str(stream);
+    Stage st(o, s);
+    const double *du, *dv, *dB; double *dA;
+    CK(st.in(u, o->V, &du)); CK(st.in(v, o->V, &dv)); CK(st.in(bnd, o->os, &dB));
+    CK(st.out(ans, full ? o->V : o->rs, &dA));
+    CK(o->s_e.ensure(8 * (size_t)o->rs * 8));
+    CK(o->s_c.ensure(8 * (size_t)o->rs));
+    int r = jacobian_derivs_dev(o, du, dv, o->V, o->s_e.as<double>(), 1, 0, s);
+    if (r) return r;
+    double *jac = full ? o->s_c.as<double>() : dA;
+    CK(jac_combine(o->s_e.as<double>(), o->rs, o->rs, jac, o->rs, nullptr, 0, nullptr, 1, s));
+    if (transpose) CK(axpbz(jac, jac, -1.0, jac, 0.0, o->rs, s));
+    if (full) CK(p2u(dA, o->V, jac, o->rs, dB, o->os, o->p2io.as<int>(), o->isb.as<int>(), o->V, 1, s));
+    CK(st.finish());
+    return st.host ? check_stats(o, 1, s) : PHG_OK;
+}
+
+extern "C" int phg_jacobian_calc1(phg_ops o, double *ans, const double *u, const double *v, const double *bnd, void *s) {
+    return jacobian_common(o, ans, u, v, bnd, true, false, s);
+}
+extern "C" int phg_jacobian_calc2(phg_ops o, double *ans, const double *u, const double *v, void *s) {
+    return jacobian_common(o, ans, u, v, nullptr, false, false, s);
+}
+extern "C" int phg_jacobian_calc2t(phg_ops o, double *ans, const double *u, const double *v, void *s) {
+    return jacobian_common(o, ans, u, v, nullptr, false, true, s);
+}
+
+static int norm_common(phg_ops o, const double *u, const double *v, double *out, bool dist, bool sq, void *stream) {
+    if (!o || !u || !out) return fail(PHG_ERR_ARG, "NULL argument");
+    cudaStream_t s = o->str(stream);
+    Stage st(o, s);
+    const double *du, *dv;
+    CK(st.in(u, o->V, &du)); CK(st.in(v, o->V, &dv));
+    CK(o->s_out.ensure(64));
+    int r = norm_dev(o, du, dv, 1, o->s_out.as<double>(), dist, sq, s);
+    if (r) return r;
+    CK(cudaMemcpyAsync(out, o->s_out.p, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return PHG_OK;
+}
+
+extern "C" int phg_norm(phg_ops o, const double *u, double *out, void *s) { return norm_common(o, u, nullptr, out, false, true, s); }
+extern "C" int phg_dist(phg_ops o, const double *u, const double *v, double *out, void *s) {
+    if (!v) return fail(PHG_ERR_ARG, "NULL argument");
+    return norm_common(o, u, v, out, true, true, s);
+}
+extern "C" int phg_scalar(phg_ops o, const double *u, const double *v, double *out, void *s) {
+    if (!v) return fail(PHG_ERR_ARG, "NULL argument");
+    return norm_common(o, u, v, out, false, false, s);
+}
+
+// ------------------------------------------------------------ barvortex ---
+struct phg_barvortex_s {
+    phg_ops_s *o = nullptr;
+    phg_bv_conf c{};
+    SolveOpBufs A;
+    ColsBufs Ab;
+    DBuf lh;
+    int cap = 0;   // members the buffers hold
+    DBuf w, dw, FC, u_n, w_n, u_n1, tmp1, tmp2, uin, F, rp, x, jsol, nr0, nr, done, ubnd, wbnd, frc;
+    GmresStats each[64];
+    int nslots = 0;
+};
+
+extern "C" int phg_barvortex_create(phg_ops o, const phg_bv_conf *c, const double *coriolis, phg_barvortex *out) {
+    if (!o || !c || !out) return fail(PHG_ERR_ARG, "NULL argument");
+    if (!(c->tau > 0) || c->picard_iters < 1) return fail(PHG_ERR_ARG, "bad configuration");
+    auto b = std::make_unique<phg_barvortex_s>();
+    b->o = o;
+    b->c = *c;
+    Csr A, Ab;
+    const double c1 = 1.0 / c->tau + c->sigma * c->theta;
+    const double c2 = -c->theta * c->mu;
+    assemble_barvortex(o->mesh->m, c1, c2, A, Ab);
+    if (!same_pattern(A, o->mesh->ops.idt)) return fail(PHG_ERR_ARG, "barvortex matrix pattern mismatch");
+    int r;
+    if ((r = build_solve_op(o, A, b->A))) return r;
+    if ((r = build_cols(Ab, b->Ab))) return r;
+    std::vector<double> lh(o->V, 0.0);
+    if (coriolis) {
+        if (is_device_ptr(coriolis)) CK(cudaMemcpy(lh.data(), coriolis, 8 * lh.size(), cudaMemcpyDeviceToHost));
+        else memcpy(lh.data(), coriolis, 8 * lh.size());
+    }
+    CK(upload(b->lh, lh));
+    *out = b.release();
+    return PHG_OK;
+}
+
+extern "C" void phg_barvortex_destroy(phg_barvortex b) {
+    if (!b) return;
+    cudaStreamSynchronize(b->o->stream);
+    delete b;
+}
+
+namespace {
+
+int bv_reserve(phg_barvortex_s *b, int nv) {
+    if (nv <= b->cap) return PHG_OK;
+    const size_t V = b->o->V, rs = b->o->rs, os = std::max(1, b->o->os);
+    DBuf *full[] = {&b->w, &b->dw, &b->FC, &b->u_n, &b->w_n, &b->u_n1, &b->tmp1, &b->tmp2, &b->uin};
+    for (DBuf *d : full) CK(d->ensure(8 * V * nv));
+    DBuf *inner[] = {&b->F, &b->rp, &b->x};
+    for (DBuf *d : inner) CK(d->ensure(8 * rs * nv));
+    CK(b->jsol.ensure(8 * rs * 8 * nv));
+    CK(b->nr0.ensure(8 * nv)); CK(b->nr.ensure(8 * nv)); CK(b->done.ensure(4 * nv));
+    CK(b->ubnd.ensure(8 * os * nv)); CK(b->wbnd.ensure(8 * os * nv)); CK(b->frc.ensure(8 * V));
+    b->cap = nv;
+    return PHG_OK;
+}
+
+// One Crank-Nicolson / Picard step for nv members, all arguments on the
+// device (examples/barvortex_impl.h:171-310).
+int bv_step_dev(phg_barvortex_s *b, int nv, double *u1, const double *u, const double *bnd_u,
+                const double *bnd_w, const double *forcing, cudaStream_t s) {
+    phg_ops_s *o = b->o;
+    const int V = o->V, rs = o->rs, os = o->os;
+    const long long NV = (long long)V * nv;
+    const phg_bv_conf &c = b->c;
+    int r, slot = 0;
+    double *w = b->w.as<double>(), *dw = b->dw.as<double>(), *FC = b->FC.as<double>();
+    double *u_n = b->u_n.as<double>(), *w_n = b->w_n.as<double>(), *u_n1 = b->u_n1.as<double>();
+    double *tmp1 = b->tmp1.as<double>(), *tmp2 = b->tmp2.as<double>(), *uu = b->uin.as<double>();
+    double *F = b->F.as<double>(), *rp = b->rp.as<double>(), *x = b->x.as<double>();
+    double *jsol = b->jsol.as<double>();
+    const int *p2io = o->p2io.as<int>(), *isb = o->isb.as<int>();
+    // keep the input: u1 may alias u
+    CK(cudaMemcpyAsync(uu, u, 8 * NV, cudaMemcpyDeviceToDevice, s));
+    // nr0 = norm(u)
+    if ((r = norm_dev(o, uu, nullptr, nv, b->nr0.as<double>(), false, true, s))) return r;
+    // w = L(u) with bnd_w, dw = L(w) with zero boundary
+    if ((r = laplace_calc2_dev(o, x, rs, uu, V, nv, slot++, s))) return r;
+    CK(p2u(w, V, x, rs, bnd_w, os, p2io, isb, V, nv, s));
+    if ((r = laplace_calc2_dev(o, x, rs, w, V, nv, slot++, s))) return r;
+    CK(p2u(dw, V, x, rs, nullptr, os, p2io, isb, V, nv, s));
+    // FC = w/tau + mu(1-theta) dw - sigma(1-theta) w (+ f)
+    if (forcing && nv > 1) return fail(PHG_ERR_ARG, "batched forcing not supported");
+    CK(bv_fc(FC, w, dw, forcing, 1.0 / c.tau, c.mu * (1.0 - c.theta), -c.sigma * (1.0 - c.theta), NV, s));
+    CK(cudaMemsetAsync(u_n, 0, 8 * NV, s));
+    CK(cudaMemsetAsync(w_n, 0, 8 * NV, s));
+    CK(cudaMemsetAsync(b->done.p, 0, 4 * (size_t)nv, s));
+    for (int it = 0; it < c.picard_iters; ++it) {
+        CK(bv_mix(tmp1, tmp2, w_n, w, u_n, uu, b->lh.as<double>(), V, c.k1 * c.theta, c.k1 * (1.0 - c.theta), c.k2,
+                  c.theta, 1.0 - c.theta, NV, s));
+        // F = FC[inner] - J(tmp2, tmp1)
+        if ((r = jacobian_derivs_dev(o, tmp2, tmp1, V, jsol, nv, slot++, s))) return r;
+        CK(jac_combine(jsol, rs, rs, F, rs, FC, V, o->imap(), nv, s));
+        // rp = M_L F + bnd_ bnd_w ; w_n = p2u(A^-1 rp, bnd_w)
+        CK(apply_op(o->ML.op.A, b->Ab.c, F, rs, nullptr, bnd_w, os, nullptr, rp, rs, nv, s));
+        // warm start: previous w_n (first iteration: w), inner part
+        CK(gather(x, rs, it == 0 ? w : w_n, V, o->imap(), rs, nv, s));
+        if ((r = solve(o, b->A.op, rp, x, nv, rs, o->tol, slot++, s))) return r;
+        CK(p2u(w_n, V, x, rs, bnd_w, os, p2io, isb, V, nv, s));
+        // u_n1 = Laplace^-1(w_n) with bnd_u: b = M_L w_n_in + B2 bnd_u
+        CK(apply_op(o->ML.op.A, o->bnd2.c, w_n, V, o->imap(), bnd_u, os, nullptr, rp, rs, nv, s));
+        CK(gather(x, rs, it == 0 ? uu : u_n, V, o->imap(), rs, nv, s));
+        if ((r = solve(o, o->L.op, rp, x, nv, rs, o->tol, slot++, s))) return r;
+        CK(p2u(u_n1, V, x, rs, bnd_u, os, p2io, isb, V, nv, s));
+        // nr = dist(u_n1, u_n); u_n <- u_n1; stop test
+        if ((r = norm_dev(o, u_n1, u_n, nv, b->nr.as<double>(), true, true, s))) return r;
+        CK(bv_commit(u_n, u_n1, b->nr.as<double>(), b->nr0.as<double>(), b->done.as<int>(), V, nv, s));
+    }
+    CK(cudaMemcpyAsync(u1, u_n, 8 * NV, cudaMemcpyDeviceToDevice, s));
+    b->nslots = slot;
+    return PHG_OK;
+}
+
+}  // namespace
+
+static int bv_calc(phg_barvortex b, int nv, double *u1, const double *u, const double *bnd_u,
+                   const double *bnd_w, const double *forcing, void *stream) {
+    if (!b || !u1 || !u || nv < 1) return fail(PHG_ERR_ARG, "NULL argument");
+    phg_ops_s *o = b->o;
+    cudaStream_t s = o->str(stream);
+    int r = bv_reserve(b, nv);
+    if (r) return r;
+    Stage st(o, s);
+    const double *du, *dbu, *dbw, *df; double *du1;
+    CK(st.in(u, (size_t)o->V * nv, &du));
+    CK(st.in(bnd_u, (size_t)o->os * nv, &dbu));
+    CK(st.in(bnd_w, (size_t)o->os * nv, &dbw));
+    CK(st.in(forcing, (size_t)o->V, &df));
+    CK(st.out(u1, (size_t)o->V * nv, &du1));
+    if (o->os == 0) { dbu = nullptr; dbw = nullptr; }
+    if ((r = bv_step_dev(b, nv, du1, du, dbu, dbw, df, s))) return r;
+    CK(st.finish());
+    if (!st.host) return PHG_OK;
+    return check_stats(o, b->nslots, s, nullptr, b->each);
+}
+
+extern "C" int phg_barvortex_calc(phg_barvortex b, double *u1, const double *u, const double *bnd_u,
+                                  const double *bnd_w, const double *forcing, void *stream) {
+    return bv_calc(b, 1, u1, u, bnd_u, bnd_w, forcing, stream);
+}
+
+extern "C" int phg_barvortex_calc_batch(phg_barvortex b, int nmembers, double *u1, const double *u,
+                                        const double *bnd_u, const double *bnd_w, const double *forcing,
+                                        void *stream) {
+    return bv_calc(b, nmembers, u1, u, bnd_u, bnd_w, forcing, stream);
+}
+
+extern "C" int phg_barvortex_last_stats(phg_barvortex b, int *il, int *ia, int *imj, int *iml, double *worst) {
+    if (!b) return fail(PHG_ERR_ARG, "NULL handle");
+    phg_ops_s *o = b->o;
+    int r = check_stats(o, b->nslots, o->stream, nullptr, b->each);
+    // slot layout: 0,1 mass L (calc1 x2); then per Picard iteration: J, A, L
+    int l = 0, a = 0, mj = 0, ml = 0;
+    double wr = 0.0;
+    for (int k = 0; k < b->nslots; ++k) {
+        const GmresStats &g = b->each[k];
+        wr = std::max(wr, g.relres);
+        if (k < 2) ml += g.iters;
+        else if ((k - 2) % 3 == 0) mj += g.iters;
+        else if ((k - 2) % 3 == 1) a += g.iters;
+        else l += g.iters;
+    }
+    if (il) *il = l;
+    if (ia) *ia = a;
+    if (imj) *imj = mj;
+    if (iml) *iml = ml;
+    if (worst) *worst = wr;
+    return r;
+}
+
+// ------------------------------------------------------------- baroclin ---
+struct phg_baroclin_s {
+    phg_ops_s *o = nullptr;
+};
+
+extern "C" int phg_baroclin_create(phg_ops o, const phg_bc_conf *c, const double *coriolis, phg_baroclin *out) {
+    (void)o; (void)c; (void)coriolis; (void)out;
+    return fail(PHG_ERR_ARG, "baroclin step is not built yet");
+}
+
+extern "C" void phg_baroclin_destroy(phg_baroclin b) { delete b; }
+
+extern "C" int phg_baroclin_calc(phg_baroclin b, double *u11, double *u21, const double *u1, const double *u2,
+                                 const double *bnd, const double *f, const double *g, void *stream) {
+    (void)b; (void)u11; (void)u21; (void)u1; (void)u2; (void)bnd; (void)f; (void)g; (void)stream;
+    return fail(PHG_ERR_ARG, "baroclin step is not built yet");
+}

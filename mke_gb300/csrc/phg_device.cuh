@@ -1,0 +1,70 @@
+// phg_device.cuh -- device-side layout of the sphere operators and the kernel
+// entry points shared by the .cu files.
+//
+// HBM layout.  All rs x rs operators of one mesh share a single sparsity
+// pattern (every one is assembled over the same point/triangle adjacency), so
+// the pattern is stored once as a slot-major ELL table: col[k * n + i] is the
+// k-th smallest column of row i (k < W, W = 7 on icosahedral meshes), padded
+// with (col = i, val = 0).  Each operator adds only its value table
+// val[k * n + i].  A warp reading slot k of 32 consecutive rows therefore
+// issues fully coalesced 128-byte (int) / 256-byte (double) loads, and the
+// Cuthill-McKee point order keeps the gathered x[col] within a few cache lines.
+// Vectors of several members (ensemble members, right-hand sides) are stored
+// member-major: x[v * ld + i].
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace phg {
+
+struct DevEll {
+    int n = 0, W = 0;
+    const int *col = nullptr;      // W x n
+    const double *val = nullptr;   // W x n, the assembled values
+};
+
+// Right-preconditioned operator for the Krylov solver: A * D^{-1} with
+// D = diag(A) (Jacobi), in FP64 and FP32, plus 1/diag.
+struct DevSolveOp {
+    DevEll A;                      // exact values for the FP64 residual b - A x
+    const double *as64 = nullptr;  // A D^{-1} (column scaled), FP64
+    const float *as32 = nullptr;   // A D^{-1}, FP32 (mixed precision)
+    const double *dinv = nullptr;  // 1 / diag(A)
+};
+
+// rs x os boundary columns in CSR over rows (few nonzero rows).
+struct DevCols {
+    int n = 0;
+    const int *ptr = nullptr, *col = nullptr;
+    const double *val = nullptr;
+};
+
+enum Precision { PREC_FP64 = 0, PREC_MIXED = 1 };
+
+struct GmresStats {
+    int iters;       // Arnoldi steps taken (max over right-hand sides)
+    int cycles;      // restarts / refinement sweeps
+    double relres;   // max final ||b - A x|| / ||b|| (FP64)
+    int status;      // 0 ok, 1 not converged, 2 barrier timeout, 3 launch error
+};
+
+// Solve A X = B for nv right-hand sides (member-major, leading dim ld) by
+// restarted GMRES(m) right-preconditioned with Jacobi, one cooperative
+// persistent launch; X holds the initial guess on entry.  FP64: every vector
+// and coefficient in double.  MIXED: Arnoldi vectors and the operator in
+// FP32 (FP32 accumulation), Hessenberg / Givens / least squares and the
+// residual b - A x of every restart in FP64 (iterative refinement).
+// `work` must hold gmres_work_bytes(...) bytes; `stats_dev` receives a
+// GmresStats on the device.
+size_t gmres_work_bytes(int n, int nv, int m, Precision p);
+cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv, int ld,
+                        int m, int max_iter, double tol, Precision p,
+                        void *work, GmresStats *stats_dev, cudaStream_t s);
+
+// y[v] = A x_in[v] + C x_bnd[v] with every row summed in ascending column
+// order from 0.0 and no fused multiply-add (same rounding as a CPU CSR
+// product); the two partial sums are added last.  x_bnd may be null.
+cudaError_t apply_exact(const DevEll &A, const DevCols &C, const double *x_in, int ldx,
+                        const double *x_bnd, int ldb, double *y, int ldy, int nv, cudaStream_t s);
+
+}  // namespace phg

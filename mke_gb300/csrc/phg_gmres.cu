@@ -1,0 +1,389 @@
+// phg_gmres.cu -- persistent restarted GMRES on GB300.
+//
+// One cooperative launch solves nv systems A x = b that share A (ensemble
+// members, the 8 derivative right-hand sides of a Jacobian, ...).  The grid is
+// split into groups of G blocks; a group owns one right-hand side at a time
+// and its blocks own contiguous row ranges, so every dot product, AXPY and
+// normalisation touches only rows the block owns -- only the operator apply
+// gathers neighbours.  Groups synchronise among themselves only (G = 1 is a
+// plain __syncthreads), so independent right-hand sides converge independently
+// and nothing ever waits for the whole GPU.
+//
+// Per Arnoldi step: (1) w = (A D^-1) v_j fused with the classical Gram-Schmidt
+// dots <v_l, w>, (2) w -= sum h_l v_l fused with ||w||^2, (3) v_{j+1} = w/|w|
+// and the Givens update (computed redundantly, identically, by every block of
+// the group so all of them take the same branch).  Three group barriers per
+// step.  Every restart recomputes r = b - A x in FP64 with the exact operator,
+// which is also the outer loop of mixed-precision iterative refinement.
+//
+// Every wait is bounded: a barrier that spins longer than ~1 s (clock64)
+// raises a device error flag; all blocks see the flag at their next barrier
+// and return, and the host reports status 2.
+#include <cooperative_groups.h>
+#include <cstdio>
+
+#include "phg_device.cuh"
+
+namespace phg {
+
+namespace {
+
+constexpr int MAXM = 48;         // largest restart length
+constexpr int BLOCK = 256;
+constexpr int NWARP = BLOCK / 32;
+constexpr double INNER_RTOL = 1e-5;  // FP32 cycle: reduce the residual 1e5x, then refine
+constexpr long long SPIN_LIMIT = 2000000000LL;  // clock64 cycles (~1 s)
+
+struct Params {
+    DevSolveOp op;
+    const double *B;
+    double *X;
+    int n, nv, ld, m, max_iter;
+    double tol;
+    void *V;          // nv x (m+1) x n (VT)
+    void *Wv;         // nv x n (VT)
+    double *R;        // nv x n (FP64 residual)
+    double *part;     // groups x G x (MAXM + 2)
+    unsigned *bar;    // groups x 2
+    int *err;
+    GmresStats *stats;
+    int groups, G;
+};
+
+__device__ __forceinline__ unsigned ld_volatile(const unsigned *p) { return *(const volatile unsigned *)p; }
+__device__ __forceinline__ int ld_volatile(const int *p) { return *(const volatile int *)p; }
+
+// Barrier over the G blocks of one group; false if the grid is aborting.
+__device__ bool group_sync(unsigned *bar, int G, int *err) {
+    __shared__ int ok;
+    __syncthreads();
+    if (G == 1) return ld_volatile(err) == 0;
+    if (threadIdx.x == 0) {
+        ok = 1;
+        unsigned *cnt = bar, *gen = bar + 1;
+        unsigned my = ld_volatile(gen);
+        __threadfence();
+        unsigned arrived = atomicAdd(cnt, 1u);
+        if (arrived == (unsigned)G - 1) {
+            atomicExch(cnt, 0u);
+            __threadfence();
+            atomicAdd(gen, 1u);
+        } else {
+            long long t0 = clock64();
+            while (ld_volatile(gen) == my) {
+                if (ld_volatile(err)) { ok = 0; break; }
+                if (clock64() - t0 > SPIN_LIMIT) { atomicExch(err, 1); ok = 0; break; }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        if (ld_volatile(err)) ok = 0;
+    }
+    __syncthreads();
+    return ok;
+}
+
+template <typename T> __device__ __forceinline__ T ldcg(const T *p) { return __ldcg(p); }
+
+// block-reduce K values held per thread in acc[0..K-1] (double), result in red[l][0]
+template <int KMAX>
+__device__ void block_reduce(double (&acc)[KMAX], int K, double (*red)[NWARP]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int l = 0; l < KMAX; ++l) {
+        if (l < K) {
+            double v = acc[l];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) red[l][warp] = v;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        double s = 0.0;
+        for (int w = 0; w < NWARP; ++w) s += red[threadIdx.x][w];
+        red[threadIdx.x][0] = s;
+    }
+    __syncthreads();
+}
+
+template <typename VT>
+__device__ __forceinline__ const VT *scaled_vals(const DevSolveOp &op);
+template <> __device__ __forceinline__ const double *scaled_vals<double>(const DevSolveOp &op) { return op.as64; }
+template <> __device__ __forceinline__ const float *scaled_vals<float>(const DevSolveOp &op) { return op.as32; }
+
+template <typename VT>
+__global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
+    extern __shared__ double smem[];
+    const int m = p.m, n = p.n;
+    double *H = smem;                       // (m+1) x m
+    double *cs = H + (MAXM + 1) * MAXM;     // m
+    double *sn = cs + MAXM;                 // m
+    double *g = sn + MAXM;                  // m+1
+    double *y = g + MAXM + 1;               // m
+    double *hcol = y + MAXM;                // m+2 (current column / scalars)
+    __shared__ double red[MAXM + 2][NWARP];
+    __shared__ int flag[4];
+
+    const int grp = blockIdx.x / p.G, bi = blockIdx.x % p.G;
+    if (grp >= p.groups) return;
+    unsigned *bar = p.bar + 2 * grp;
+    // two partial-sum buffers used alternately: a block can only refill a
+    // buffer after the next barrier, i.e. after every block has read it
+    double *part2 = p.part + (size_t)grp * 2 * p.G * (MAXM + 2);
+    int parity = 0;
+    const int rpb = (n + p.G - 1) / p.G;
+    const int r0 = bi * rpb, r1 = min(n, r0 + rpb);
+    const int W = p.op.A.W;
+    const int *col = p.op.A.col;
+    const double *aval = p.op.A.val;
+    const VT *sval = scaled_vals<VT>(p.op);
+    const double *dinv = p.op.dinv;
+
+    // group-wide sum of K per-block values in red[.][0]: publish, barrier, reduce
+    auto group_sum = [&](int K, double *out) -> bool {
+        double *part = part2 + (size_t)parity * p.G * (MAXM + 2);
+        parity ^= 1;
+        if (threadIdx.x < K) part[bi * (MAXM + 2) + threadIdx.x] = red[threadIdx.x][0];
+        if (!group_sync(bar, p.G, p.err)) return false;
+        if (threadIdx.x < K) {
+            double s = 0.0;
+            for (int b = 0; b < p.G; ++b) s += ldcg(&part[b * (MAXM + 2) + threadIdx.x]);
+            out[threadIdx.x] = s;
+        }
+        __syncthreads();
+        return true;
+    };
+
+    int my_iters = 0, my_cycles = 0, my_status = 0;
+    double my_rel = 0.0;
+
+    for (int v = grp; v < p.nv; v += p.groups) {
+        const double *b = p.B + (size_t)v * p.ld;
+        double *x = p.X + (size_t)v * p.ld;
+        VT *V = (VT *)p.V + (size_t)v * (m + 1) * n;
+        VT *w = (VT *)p.Wv + (size_t)v * n;
+        double *R = p.R + (size_t)v * n;
+
+        // ||b||
+        double acc[MAXM + 2];
+        acc[0] = 0.0;
+        for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) { double t = b[i]; acc[0] += t * t; }
+        block_reduce<MAXM + 2>(acc, 1, red);
+        if (!group_sum(1, hcol)) return;
+        const double bnorm = sqrt(hcol[0]);
+        int iters = 0, cycles = 0, status = 1;
+        double beta_prev = 0.0, rel = 0.0;
+        if (bnorm == 0.0) {
+            for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) x[i] = 0.0;
+            status = 0; rel = 0.0;
+            if (!group_sync(bar, p.G, p.err)) return;
+        }
+        while (bnorm != 0.0) {
+            // r = b - A x (FP64, exact operator); needs all of x
+            if (!group_sync(bar, p.G, p.err)) return;
+            acc[0] = 0.0;
+            for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
+                double s = 0.0;
+                for (int k = 0; k < W; ++k) s += aval[(size_t)k * n + i] * ldcg(&x[col[(size_t)k * n + i]]);
+                double r = b[i] - s;
+                R[i] = r;
+                acc[0] += r * r;
+            }
+            block_reduce<MAXM + 2>(acc, 1, red);
+            if (!group_sum(1, hcol)) return;
+            const double beta = sqrt(hcol[0]);
+            rel = beta / bnorm;
+            if (rel <= p.tol) { status = 0; break; }
+            if (iters >= p.max_iter) { status = 1; break; }
+            if (cycles > 0 && !(beta < 0.9999 * beta_prev)) { status = 1; break; }
+            beta_prev = beta;
+            ++cycles;
+            const double target = fmax(p.tol * bnorm, (sizeof(VT) == 4 ? INNER_RTOL : 0.0) * beta);
+            for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) V[i] = (VT)(R[i] / beta);
+            if (threadIdx.x == 0) {
+                g[0] = beta;
+                for (int l = 1; l <= m; ++l) g[l] = 0.0;
+            }
+            int jlast = 0;
+            for (int j = 0; j < m; ++j) {
+                if (!group_sync(bar, p.G, p.err)) return;   // v_j complete
+                const VT *vj = V + (size_t)j * n;
+                // (1) w = (A D^-1) v_j and dots with v_0..v_j
+#pragma unroll
+                for (int l = 0; l < MAXM + 2; ++l) acc[l] = 0.0;
+                for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
+                    VT s = 0;
+                    for (int k = 0; k < W; ++k) s += sval[(size_t)k * n + i] * ldcg(&vj[col[(size_t)k * n + i]]);
+                    w[i] = s;
+#pragma unroll
+                    for (int l = 0; l < MAXM; ++l)
+                        if (l <= j) acc[l] += (double)(V[(size_t)l * n + i] * s);
+                }
+                block_reduce<MAXM + 2>(acc, j + 1, red);
+                if (!group_sum(j + 1, hcol)) return;
+                // (2) w -= sum h_l v_l, ||w||^2
+                double a2 = 0.0;
+                for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
+                    VT s = w[i];
+                    for (int l = 0; l <= j; ++l) s -= (VT)hcol[l] * V[(size_t)l * n + i];
+                    w[i] = s;
+                    a2 += (double)s * (double)s;
+                }
+                acc[0] = a2;
+                block_reduce<MAXM + 2>(acc, 1, red);
+                if (!group_sum(1, hcol + j + 1)) return;
+                const double hn = sqrt(hcol[j + 1]);
+                // (3) v_{j+1}, Givens
+                if (hn > 0.0) {
+                    const VT inv = (VT)(1.0 / hn);
+                    VT *vn = V + (size_t)(j + 1) * n;
+                    for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) vn[i] = w[i] * inv;
+                }
+                if (threadIdx.x == 0) {
+                    hcol[j + 1] = hn;
+                    for (int l = 0; l < j; ++l) {
+                        double a = hcol[l], c = hcol[l + 1];
+                        hcol[l] = cs[l] * a + sn[l] * c;
+                        hcol[l + 1] = -sn[l] * a + cs[l] * c;
+                    }
+                    double a = hcol[j], c = hcol[j + 1];
+                    double r = hypot(a, c);
+                    cs[j] = r > 0.0 ? a / r : 1.0;
+                    sn[j] = r > 0.0 ? c / r : 0.0;
+                    for (int l = 0; l < j; ++l) H[l * MAXM + j] = hcol[l];
+                    H[j * MAXM + j] = r;
+                    g[j + 1] = -sn[j] * g[j];
+                    g[j] = cs[j] * g[j];
+                    flag[0] = (fabs(g[j + 1]) <= target) || hn == 0.0;
+                }
+                __syncthreads();
+                ++iters;
+                jlast = j + 1;
+                if (flag[0] || iters >= p.max_iter) break;
+            }
+            // y = H^-1 g; x += D^-1 V y
+            if (threadIdx.x == 0) {
+                for (int l = jlast - 1; l >= 0; --l) {
+                    double s = g[l];
+                    for (int k = l + 1; k < jlast; ++k) s -= H[l * MAXM + k] * y[k];
+                    y[l] = s / H[l * MAXM + l];
+                }
+            }
+            __syncthreads();
+            for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
+                double s = 0.0;
+                for (int l = 0; l < jlast; ++l) s += y[l] * (double)V[(size_t)l * n + i];
+                x[i] += dinv[i] * s;
+            }
+        }
+        my_iters = max(my_iters, iters);
+        my_cycles = max(my_cycles, cycles);
+        my_rel = fmax(my_rel, rel);
+        my_status = max(my_status, status);
+    }
+    if (threadIdx.x == 0 && bi == 0) {
+        atomicMax(&p.stats->iters, my_iters);
+        atomicMax(&p.stats->cycles, my_cycles);
+        atomicMax(&p.stats->status, my_status);
+        // relres >= 0: max via the integer order of non-negative doubles
+        atomicMax((unsigned long long *)&p.stats->relres, (unsigned long long)__double_as_longlong(my_rel));
+    }
+}
+
+__global__ void fold_err(const int *err, GmresStats *st) {
+    if (*err) st->status = 2;
+}
+
+size_t smem_bytes() { return sizeof(double) * ((MAXM + 1) * MAXM + 2 * MAXM + (MAXM + 1) + MAXM + (MAXM + 2)); }
+
+struct Layout { size_t v, w, r, part, bar, err, total; };
+
+Layout layout(int n, int nv, int m, Precision prec, int groups_cap) {
+    Layout L;
+    size_t es = prec == PREC_MIXED ? 4 : 8;
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    L.v = 0;
+    L.w = L.v + al(es * (size_t)nv * (m + 1) * n);
+    L.r = L.w + al(es * (size_t)nv * n);
+    L.part = L.r + al(8 * (size_t)nv * n);
+    L.bar = L.part + al(8 * (size_t)groups_cap * 2 * (MAXM + 2));
+    L.err = L.bar + al(8 * (size_t)groups_cap);
+    L.total = L.err + 256;
+    return L;
+}
+
+int g_capacity = 0;   // co-resident blocks of the solver kernel on this device
+int g_sms = 0;
+
+int capacity() {
+    if (!g_capacity) {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaFuncSetAttribute(gmres_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes());
+        cudaFuncSetAttribute(gmres_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes());
+        int a = 0, b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, gmres_kernel<double>, BLOCK, smem_bytes());
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, gmres_kernel<float>, BLOCK, smem_bytes());
+        per = a < b ? a : b;
+        if (per < 1) per = 1;
+        g_sms = sms;
+        g_capacity = sms * per;
+    }
+    return g_capacity;
+}
+
+int rows_per_block_target() {
+    static int v = -1;
+    if (v < 0) {
+        const char *e = getenv("PHG_ROWS_PER_BLOCK");
+        v = e ? atoi(e) : 512;
+        if (v < 32) v = 32;
+    }
+    return v;
+}
+
+}  // namespace
+
+size_t gmres_work_bytes(int n, int nv, int m, Precision p) {
+    return layout(n, nv, m, p, 4096).total;
+}
+
+cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv, int ld,
+                        int m, int max_iter, double tol, Precision prec,
+                        void *work, GmresStats *stats_dev, cudaStream_t s) {
+    if (m < 1 || m > MAXM || nv < 1) return cudaErrorInvalidValue;
+    const int n = op.A.n;
+    const int cap = capacity();
+    int Gt = (n + rows_per_block_target() - 1) / rows_per_block_target();
+    if (Gt < 1) Gt = 1;
+    if (Gt > cap) Gt = cap;
+    int groups = cap / Gt;
+    if (groups > nv) groups = nv;
+    if (groups > 4096) groups = 4096;
+    if (groups < 1) groups = 1;
+    int G = cap / groups;
+    if (G > Gt) G = Gt;
+    Layout L = layout(n, nv, m, prec, 4096);
+    char *w = (char *)work;
+    Params p;
+    p.op = op; p.B = B; p.X = X; p.n = n; p.nv = nv; p.ld = ld; p.m = m; p.max_iter = max_iter; p.tol = tol;
+    p.V = w + L.v; p.Wv = w + L.w; p.R = (double *)(w + L.r); p.part = (double *)(w + L.part);
+    p.bar = (unsigned *)(w + L.bar); p.err = (int *)(w + L.err); p.stats = stats_dev;
+    p.groups = groups; p.G = G;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(w + L.bar, 0, L.total - L.bar, s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(stats_dev, 0, sizeof(GmresStats), s)) != cudaSuccess) return e;
+    void *args[] = {&p};
+    dim3 grid(groups * G), block(BLOCK);
+    if (prec == PREC_MIXED)
+        e = cudaLaunchCooperativeKernel((void *)gmres_kernel<float>, grid, block, args, smem_bytes(), s);
+    else
+        e = cudaLaunchCooperativeKernel((void *)gmres_kernel<double>, grid, block, args, smem_bytes(), s);
+    if (e != cudaSuccess) return e;
+    // a barrier timeout lands in stats->status (2)
+    fold_err<<<1, 1, 0, s>>>(p.err, stats_dev);
+    return cudaGetLastError();
+}
+
+}  // namespace phg

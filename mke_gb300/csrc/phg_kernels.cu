@@ -1,0 +1,292 @@
+// phg_kernels.cu -- operator applies and fused elementwise kernels.
+//
+// This file is compiled with -fmad=false: every product and sum below is
+// rounded separately, in the order written, so an FP64 apply on the GPU
+// returns the same bits as the reference's CPU CSR product
+// (ascending columns, starting from 0.0) and the elementwise formulas of the
+// time steps round exactly like the reference's vec_sum1 / vec_sum2 calls.
+//
+// All kernels take nv members stored member-major (x[v * ld + i]).
+#include "phg_kernels.cuh"
+
+namespace phg {
+
+namespace {
+constexpr int TB = 256;
+
+inline unsigned grid_for(long long work) {
+    long long b = (work + TB - 1) / TB;
+    if (b < 1) b = 1;
+    if (b > 152LL * 64) b = 152LL * 64;
+    return (unsigned)b;
+}
+
+__device__ __forceinline__ double row_sum(const DevEll &A, const double *x, const int *imap, int i) {
+    double s = 0.0;
+    const int n = A.n;
+    for (int k = 0; k < A.W; ++k) {
+        int c = __ldg(&A.col[(size_t)k * n + i]);
+        double xv = imap ? x[imap[c]] : x[c];
+        s += __ldg(&A.val[(size_t)k * n + i]) * xv;
+    }
+    return s;
+}
+
+__device__ __forceinline__ double cols_sum(const DevCols &C, const double *xb, const int *bmap, int i) {
+    double s = 0.0;
+    if (!C.ptr || !xb) return s;
+    for (int k = C.ptr[i]; k < C.ptr[i + 1]; ++k) {
+        int c = C.col[k];
+        s += C.val[k] * (bmap ? xb[bmap[c]] : xb[c]);
+    }
+    return s;
+}
+
+__global__ void k_apply(DevEll A, DevCols C, const double *xin, int ldx, const int *imap,
+                        const double *xb, int ldb, const int *bmap, double *y, int ldy, int nv) {
+    const long long total = (long long)nv * A.n;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+        int v = (int)(t / A.n), i = (int)(t % A.n);
+        double s = row_sum(A, xin + (size_t)v * ldx, imap, i);
+        if (C.ptr && xb) s = s + cols_sum(C, xb + (size_t)v * ldb, bmap, i);
+        y[(size_t)v * ldy + i] = s;
+    }
+}
+
+// the 8 derivative right-hand sides of SphereJacobian::calc2
+// (src/sjacobian.cpp:136-362), out[(v * 8 + k) * ldo + i]:
+//   k: 0 D2c u, 1 D1 v, 2 D1c u, 3 D2 v, 4 D2 u, 5 D1c v, 6 D1 u, 7 D2c v
+__global__ void k_jac_rhs(JacOps J, const double *u, const double *w, int ld, const int *imap,
+                          const int *bmap, double *out, int ldo, int nv) {
+    const int n = J.d1.n;
+    const long long total = (long long)nv * n;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+        int v = (int)(t / n), i = (int)(t % n);
+        const double *fu = u + (size_t)v * ld, *fv = w + (size_t)v * ld;
+        double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int k = 0; k < J.d1.W; ++k) {
+            size_t e = (size_t)k * n + i;
+            int c = __ldg(&J.d1.col[e]);
+            int cc = imap ? imap[c] : c;
+            double xu = fu[cc], xv = fv[cc];
+            double a1 = __ldg(&J.d1.val[e]), a2 = __ldg(&J.d2.val[e]);
+            double c1 = __ldg(&J.d1c.val[e]), c2 = __ldg(&J.d2c.val[e]);
+            s[0] += c2 * xu; s[1] += a1 * xv; s[2] += c1 * xu; s[3] += a2 * xv;
+            s[4] += a2 * xu; s[5] += c1 * xv; s[6] += a1 * xu; s[7] += c2 * xv;
+        }
+        const double *bu = fu, *bv = fv;
+        double b[8];
+        b[0] = cols_sum(J.d2cb, bu, bmap, i); b[1] = cols_sum(J.d1b, bv, bmap, i);
+        b[2] = cols_sum(J.d1cb, bu, bmap, i); b[3] = cols_sum(J.d2b, bv, bmap, i);
+        b[4] = cols_sum(J.d2b, bu, bmap, i); b[5] = cols_sum(J.d1cb, bv, bmap, i);
+        b[6] = cols_sum(J.d1b, bu, bmap, i); b[7] = cols_sum(J.d2cb, bv, bmap, i);
+        for (int k = 0; k < 8; ++k) out[((size_t)v * 8 + k) * ldo + i] = b[k] + s[k];
+    }
+}
+
+// jac = 1/4 sum of the four splittings; optional F = FC[inner] - jac
+__global__ void k_jac_combine(const double *d, int ldd, int n, double *jac, int ldj,
+                              const double *FC, int ldf, const int *inner, int nv) {
+    const long long total = (long long)nv * n;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+        int v = (int)(t / n), i = (int)(t % n);
+        const double *q = d + (size_t)v * 8 * ldd;
+        double c2u = q[0 * ldd + i], a1v = q[1 * ldd + i], c1u = q[2 * ldd + i], a2v = q[3 * ldd + i];
+        double a2u = q[4 * ldd + i], c1v = q[5 * ldd + i], a1u = q[6 * ldd + i], c2v = q[7 * ldd + i];
+        double j1 = c2u * a1v - c1u * a2v;
+        double j2 = a2u * c1v - a1u * c2v;
+        double j3 = c2u * a1v - a1u * c2v;
+        double j4 = a2u * c1v - c1u * a2v;
+        double s = j1;
+        s = s + j2;
+        s = s + j3;
+        s = s + j4;
+        double r = 0.25 * s;
+        if (FC) r = FC[(size_t)v * ldf + (inner ? inner[i] : i)] - r;
+        jac[(size_t)v * ldj + i] = r;
+    }
+}
+
+// u[p] = boundary ? (bnd ? bnd[p2io[p]] : 0) : p[p2io[p]]   (src/proj.cpp:49-75)
+__global__ void k_p2u(double *u, int ldu, const double *p, int ldp, const double *bnd, int ldb,
+                      const int *p2io, const int *isb, int V, int nv) {
+    const long long total = (long long)nv * V;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+        int v = (int)(t / V), i = (int)(t % V);
+        double r;
+        if (isb[i]) r = bnd ? bnd[(size_t)v * ldb + p2io[i]] : 0.0;
+        else r = p[(size_t)v * ldp + p2io[i]];
+        u[(size_t)v * ldu + i] = r;
+    }
+}
+
+// y = a * x + b * z (both products rounded, then the sum) -- vec_sum1
+__global__ void k_axpbz(double *y, const double *x, double a, const double *z, double b, long long n) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        y[t] = a * x[t] + b * z[t];
+}
+
+// FC = (1/tau) w + mu(1-theta) dw ; FC = 1.0 FC + (-sigma(1-theta)) w ; FC += rp
+// (examples/barvortex_impl.h:238-256)
+__global__ void k_bv_fc(double *FC, const double *w, const double *dw, const double *rp,
+                        double c_w, double c_dw, double c_w2, long long n) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        double f = c_w * w[t] + c_dw * dw[t];
+        f = 1.0 * f + c_w2 * w[t];
+        if (rp) f += rp[t];
+        FC[t] = f;
+    }
+}
+
+// tmp1 = k1 theta w_n + k1 (1-theta) w ; tmp1 = tmp1 + k2 lh ; tmp2 = theta u_n + (1-theta) u
+// (examples/barvortex_impl.h:267-272); lh is one field shared by all members
+__global__ void k_bv_mix(double *tmp1, double *tmp2, const double *w_n, const double *w,
+                         const double *u_n, const double *u, const double *lh, int V,
+                         double a1, double a2, double k2, double t1, double t2, long long n) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        double s = a1 * w_n[t] + a2 * w[t];
+        s = s + k2 * lh[t % V];
+        tmp1[t] = s;
+        tmp2[t] = t1 * u_n[t] + t2 * u[t];
+    }
+}
+
+// elementwise a - b
+__global__ void k_sub(double *y, const double *a, const double *b, long long n) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        y[t] = a[t] - b[t];
+}
+
+// per-member partial sums of a[i] * b[i] over chunks of `chunk` rows
+__global__ void k_dot_partial(const double *a, const double *b, int ld, int n, int chunk, int nchunk,
+                              double *part, int nv) {
+    __shared__ double red[TB];
+    int v = blockIdx.x / nchunk, c = blockIdx.x % nchunk;
+    if (v >= nv) return;
+    const double *x = a + (size_t)v * ld, *y = b + (size_t)v * ld;
+    int i0 = c * chunk, i1 = min(n, i0 + chunk);
+    double s = 0.0;
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) s += x[i] * y[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// out[v] = sum of the member's partials (sqrt if take_sqrt)
+__global__ void k_dot_final(const double *part, int nchunk, double *out, int nv, int take_sqrt) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    double s = 0.0;
+    for (int c = 0; c < nchunk; ++c) s += part[(size_t)v * nchunk + c];
+    out[v] = take_sqrt ? sqrt(s) : s;
+}
+
+// Picard bookkeeping: u_n <- u_n1 for members still iterating, then stop a
+// member once dist/norm0 < 1e-14 or the distance is NaN
+// (examples/barvortex_impl.h:300-306)
+__global__ void k_bv_commit(double *u_n, const double *u_n1, const double *nr, const double *nr0,
+                            int *done, int V, int nv) {
+    const long long total = (long long)nv * V;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+        int v = (int)(t / V);
+        if (!done[v]) u_n[t] = u_n1[t];
+    }
+}
+
+__global__ void k_bv_done(const double *nr, const double *nr0, int *done, int nv) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv || done[v]) return;
+    double r = nr[v];
+    if (r / nr0[v] < 1e-14 || isnan(r)) done[v] = 1;
+}
+
+__global__ void k_gather(double *y, int ldy, const double *x, int ldx, const int *map, int n, int nv) {
+    const long long total = (long long)nv * n;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+        int v = (int)(t / n), i = (int)(t % n);
+        y[(size_t)v * ldy + i] = x[(size_t)v * ldx + (map ? map[i] : i)];
+    }
+}
+
+}  // namespace
+
+cudaError_t apply_exact(const DevEll &A, const DevCols &C, const double *x_in, int ldx,
+                        const double *x_bnd, int ldb, double *y, int ldy, int nv, cudaStream_t s) {
+    k_apply<<<grid_for((long long)nv * A.n), TB, 0, s>>>(A, C, x_in, ldx, nullptr, x_bnd, ldb, nullptr, y, ldy, nv);
+    return cudaGetLastError();
+}
+
+cudaError_t apply_op(const DevEll &A, const DevCols &C, const double *xin, int ldx, const int *imap,
+                     const double *xb, int ldb, const int *bmap, double *y, int ldy, int nv, cudaStream_t s) {
+    k_apply<<<grid_for((long long)nv * A.n), TB, 0, s>>>(A, C, xin, ldx, imap, xb, ldb, bmap, y, ldy, nv);
+    return cudaGetLastError();
+}
+
+cudaError_t jac_rhs(const JacOps &J, const double *u, const double *v, int ld, const int *imap,
+                    const int *bmap, double *out, int ldo, int nv, cudaStream_t s) {
+    k_jac_rhs<<<grid_for((long long)nv * J.d1.n), TB, 0, s>>>(J, u, v, ld, imap, bmap, out, ldo, nv);
+    return cudaGetLastError();
+}
+
+cudaError_t jac_combine(const double *d, int ldd, int n, double *jac, int ldj, const double *FC, int ldf,
+                        const int *inner, int nv, cudaStream_t s) {
+    k_jac_combine<<<grid_for((long long)nv * n), TB, 0, s>>>(d, ldd, n, jac, ldj, FC, ldf, inner, nv);
+    return cudaGetLastError();
+}
+
+cudaError_t p2u(double *u, int ldu, const double *p, int ldp, const double *bnd, int ldb,
+                const int *p2io, const int *isb, int V, int nv, cudaStream_t s) {
+    k_p2u<<<grid_for((long long)nv * V), TB, 0, s>>>(u, ldu, p, ldp, bnd, ldb, p2io, isb, V, nv);
+    return cudaGetLastError();
+}
+
+cudaError_t axpbz(double *y, const double *x, double a, const double *z, double b, long long n, cudaStream_t s) {
+    k_axpbz<<<grid_for(n), TB, 0, s>>>(y, x, a, z, b, n);
+    return cudaGetLastError();
+}
+
+cudaError_t bv_fc(double *FC, const double *w, const double *dw, const double *rp, double c_w, double c_dw,
+                  double c_w2, long long n, cudaStream_t s) {
+    k_bv_fc<<<grid_for(n), TB, 0, s>>>(FC, w, dw, rp, c_w, c_dw, c_w2, n);
+    return cudaGetLastError();
+}
+
+cudaError_t bv_mix(double *tmp1, double *tmp2, const double *w_n, const double *w, const double *u_n,
+                   const double *u, const double *lh, int V, double a1, double a2, double k2, double t1,
+                   double t2, long long n, cudaStream_t s) {
+    k_bv_mix<<<grid_for(n), TB, 0, s>>>(tmp1, tmp2, w_n, w, u_n, u, lh, V, a1, a2, k2, t1, t2, n);
+    return cudaGetLastError();
+}
+
+cudaError_t vsub(double *y, const double *a, const double *b, long long n, cudaStream_t s) {
+    k_sub<<<grid_for(n), TB, 0, s>>>(y, a, b, n);
+    return cudaGetLastError();
+}
+
+int dot_chunks(int n) { return (n + 8191) / 8192; }
+
+cudaError_t dot(const double *a, const double *b, int ld, int n, int nv, double *part, double *out,
+                bool take_sqrt, cudaStream_t s) {
+    int nch = dot_chunks(n);
+    k_dot_partial<<<nv * nch, TB, 0, s>>>(a, b, ld, n, 8192, nch, part, nv);
+    k_dot_final<<<(nv + 127) / 128, 128, 0, s>>>(part, nch, out, nv, take_sqrt ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t bv_commit(double *u_n, const double *u_n1, const double *nr, const double *nr0, int *done,
+                      int V, int nv, cudaStream_t s) {
+    k_bv_commit<<<grid_for((long long)nv * V), TB, 0, s>>>(u_n, u_n1, nr, nr0, done, V, nv);
+    k_bv_done<<<(nv + 127) / 128, 128, 0, s>>>(nr, nr0, done, nv);
+    return cudaGetLastError();
+}
+
+cudaError_t gather(double *y, int ldy, const double *x, int ldx, const int *map, int n, int nv, cudaStream_t s) {
+    k_gather<<<grid_for((long long)nv * n), TB, 0, s>>>(y, ldy, x, ldx, map, n, nv);
+    return cudaGetLastError();
+}
+
+}  // namespace phg

@@ -1,0 +1,39 @@
+// phg_kernels.cuh -- launchers of the operator-apply and elementwise kernels.
+#pragma once
+#include "phg_device.cuh"
+
+namespace phg {
+
+// the four derivative operators of SphereJacobian on the shared pattern
+// (d1.col == d2.col == ...) and their boundary columns
+struct JacOps {
+    DevEll d1, d2, d1c, d2c;
+    DevCols d1b, d2b, d1cb, d2cb;
+};
+
+// y = A xin[imap] + C xb[bmap] (null map = identity; null xb or empty C =
+// no boundary term); member v reads xin + v*ldx, xb + v*ldb
+cudaError_t apply_op(const DevEll &A, const DevCols &C, const double *xin, int ldx, const int *imap,
+                     const double *xb, int ldb, const int *bmap, double *y, int ldy, int nv, cudaStream_t s);
+cudaError_t jac_rhs(const JacOps &J, const double *u, const double *v, int ld, const int *imap,
+                    const int *bmap, double *out, int ldo, int nv, cudaStream_t s);
+cudaError_t jac_combine(const double *d, int ldd, int n, double *jac, int ldj, const double *FC, int ldf,
+                        const int *inner, int nv, cudaStream_t s);
+cudaError_t p2u(double *u, int ldu, const double *p, int ldp, const double *bnd, int ldb,
+                const int *p2io, const int *isb, int V, int nv, cudaStream_t s);
+cudaError_t axpbz(double *y, const double *x, double a, const double *z, double b, long long n, cudaStream_t s);
+cudaError_t bv_fc(double *FC, const double *w, const double *dw, const double *rp, double c_w, double c_dw,
+                  double c_w2, long long n, cudaStream_t s);
+cudaError_t bv_mix(double *tmp1, double *tmp2, const double *w_n, const double *w, const double *u_n,
+                   const double *u, const double *lh, int V, double a1, double a2, double k2, double t1,
+                   double t2, long long n, cudaStream_t s);
+cudaError_t vsub(double *y, const double *a, const double *b, long long n, cudaStream_t s);
+int dot_chunks(int n);
+// out[v] = sum_i a[v][i] b[v][i] (sqrt if take_sqrt); part holds nv * dot_chunks(n) doubles
+cudaError_t dot(const double *a, const double *b, int ld, int n, int nv, double *part, double *out,
+                bool take_sqrt, cudaStream_t s);
+cudaError_t bv_commit(double *u_n, const double *u_n1, const double *nr, const double *nr0, int *done,
+                      int V, int nv, cudaStream_t s);
+cudaError_t gather(double *y, int ldy, const double *x, int ldx, const int *map, int n, int nv, cudaStream_t s);
+
+}  // namespace phg

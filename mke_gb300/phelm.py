@@ -1,0 +1,346 @@
+"""Python binding of libphelm_gb300 (include/phelm_gb300.h), shaped like the
+reference's C++ API: ``Mesh``, ``SphereLaplace``, ``SphereJacobian``,
+``SphereNorm``, ``BarVortex``, ``Baroclin``.
+
+Vector arguments are numpy float64 arrays (host memory: the call stages them
+to the GPU and returns when the result is back) or CUDA tensors / any object
+with ``data_ptr()`` (device memory: the call only enqueues work).  There is no
+CPU fallback: without the library or without a GPU the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+PHG_FP64, PHG_MIXED = 0, 1
+_ERRORS = {1: "bad argument", 2: "CUDA error", 3: "solve did not converge", 4: "device wait timed out",
+           5: "mesh I/O error"}
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_vp = C.c_void_p
+
+
+class PhgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{_ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class BvConf(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("tau", "sigma", "mu", "k1", "k2", "theta")] + [("picard_iters", C.c_int)]
+
+
+class BcConf(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("tau", "sigma", "mu", "sigma1", "mu1", "alpha")] + [
+        ("picard_iters", C.c_int), ("picard_tol", C.c_double)]
+
+
+# every symbol the header declares, with its ctypes signature
+SIGNATURES = {
+    "phg_last_error": (C.c_char_p, []),
+    "phg_version": (C.c_char_p, []),
+    "phg_mesh_generate": (C.c_int, [C.c_int, C.POINTER(_vp)]),
+    "phg_mesh_load_file": (C.c_int, [C.c_char_p, C.POINTER(_vp)]),
+    "phg_mesh_destroy": (None, [_vp]),
+    "phg_mesh_info": (C.c_int, [_vp, _ip, _ip, _ip, _ip]),
+    "phg_mesh_arrays": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "phg_mesh_maps": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "phg_mesh_csr": (C.c_int, [_vp, C.c_char_p, _ip, _ip, _vp, _vp, _vp]),
+    "phg_ops_create": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
+    "phg_ops_destroy": (None, [_vp]),
+    "phg_ops_set_solver": (C.c_int, [_vp, C.c_int, C.c_double, C.c_int]),
+    "phg_ops_last_solve": (C.c_int, [_vp, _ip, _ip, _dp]),
+    "phg_laplace_calc1": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "phg_laplace_calc2": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "phg_laplace_solve": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "phg_jacobian_calc1": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "phg_jacobian_calc2": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "phg_jacobian_calc2t": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "phg_norm": (C.c_int, [_vp, _vp, _dp, _vp]),
+    "phg_dist": (C.c_int, [_vp, _vp, _vp, _dp, _vp]),
+    "phg_scalar": (C.c_int, [_vp, _vp, _vp, _dp, _vp]),
+    "phg_barvortex_create": (C.c_int, [_vp, C.POINTER(BvConf), _vp, C.POINTER(_vp)]),
+    "phg_barvortex_destroy": (None, [_vp]),
+    "phg_barvortex_calc": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "phg_barvortex_calc_batch": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "phg_barvortex_last_stats": (C.c_int, [_vp, _ip, _ip, _ip, _ip, _dp]),
+    "phg_baroclin_create": (C.c_int, [_vp, C.POINTER(BcConf), _vp, C.POINTER(_vp)]),
+    "phg_baroclin_destroy": (None, [_vp]),
+    "phg_baroclin_calc": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+}
+
+_lib = None
+
+
+def lib(build_if_missing: bool = True):
+    """Load (building first if needed) the in-tree library."""
+    global _lib
+    if _lib is None:
+        path = _build.LIB
+        if build_if_missing:
+            path = _build.build()
+        if not os.path.exists(path):
+            raise PhgError(2, f"{path} missing (run mke_gb300.build.build())")
+        L = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(code):
+    if code != 0:
+        raise PhgError(code, lib().phg_last_error().decode())
+
+
+def _ptr(x):
+    """Host numpy (float64/int32, C-contiguous) or device tensor -> void*."""
+    if x is None:
+        return None
+    if hasattr(x, "data_ptr"):
+        return C.c_void_p(x.data_ptr())
+    if not isinstance(x, np.ndarray) or not x.flags["C_CONTIGUOUS"]:
+        raise TypeError("expected a C-contiguous numpy array or a CUDA tensor")
+    return C.c_void_p(x.ctypes.data)
+
+
+def _f8(x):
+    if x is None or hasattr(x, "data_ptr"):
+        return x
+    return np.ascontiguousarray(x, dtype=np.float64)
+
+
+def _stream(s):
+    if s is None:
+        return None
+    return C.c_void_p(s if isinstance(s, int) else s.cuda_stream)
+
+
+class Mesh:
+    """phelm::Mesh: ``Mesh.sphere(level)`` or ``Mesh.load(path)``."""
+
+    def __init__(self, handle):
+        self._h = handle
+        V, T, rs, os_ = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        _check(lib().phg_mesh_info(self._h, C.byref(V), C.byref(T), C.byref(rs), C.byref(os_)))
+        self.size, self.ntri, self.inner_size, self.outer_size = V.value, T.value, rs.value, os_.value
+
+    @classmethod
+    def sphere(cls, level: int) -> "Mesh":
+        h = C.c_void_p()
+        _check(lib().phg_mesh_generate(level, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def load(cls, path: str) -> "Mesh":
+        h = C.c_void_p()
+        _check(lib().phg_mesh_load_file(path.encode(), C.byref(h)))
+        return cls(h)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.phg_mesh_destroy(self._h)
+            self._h = None
+
+    def arrays(self):
+        V, T = self.size, self.ntri
+        xyz, uv = np.zeros(V * 3), np.zeros(V * 8)
+        tri, tz, bnd = np.zeros(T * 3, np.int32), np.zeros(T, np.int32), np.zeros(V, np.int32)
+        _check(lib().phg_mesh_arrays(self._h, _ptr(xyz), _ptr(uv), _ptr(tri), _ptr(tz), _ptr(bnd)))
+        return {"xyz": xyz, "uv": uv, "tri": tri, "tz": tz, "bnd": bnd}
+
+    def maps(self):
+        inner, outer = np.zeros(self.inner_size, np.int32), np.zeros(max(self.outer_size, 1), np.int32)
+        p2io = np.zeros(self.size, np.int32)
+        _check(lib().phg_mesh_maps(self._h, _ptr(inner), _ptr(outer), _ptr(p2io)))
+        return {"inner": inner, "outer": outer[: self.outer_size], "p2io": p2io}
+
+    def latlon(self):
+        """Zone-0 chart coordinates (latitude, longitude) of every point."""
+        uv = self.arrays()["uv"].reshape(-1, 4, 2)
+        return uv[:, 0, 0].copy(), uv[:, 0, 1].copy()
+
+    def csr(self, name: str):
+        n, nnz = C.c_int(), C.c_int()
+        _check(lib().phg_mesh_csr(self._h, name.encode(), C.byref(n), C.byref(nnz), None, None, None))
+        ptr, col, val = np.zeros(n.value + 1, np.int32), np.zeros(nnz.value, np.int32), np.zeros(nnz.value)
+        _check(lib().phg_mesh_csr(self._h, name.encode(), None, None, _ptr(ptr), _ptr(col), _ptr(val)))
+        return ptr, col, val
+
+
+class Operators:
+    """Device-resident SphereLaplace + SphereJacobian + SphereNorm of one mesh."""
+
+    def __init__(self, mesh: Mesh, precision: int = PHG_FP64, restart: int = 30, tol: float = 1e-12,
+                 max_iter: int = 20000):
+        self.mesh = mesh
+        self.precision = precision
+        h = C.c_void_p()
+        _check(lib().phg_ops_create(mesh._h, precision, C.byref(h)))
+        self._h = h
+        self.set_solver(restart, tol, max_iter)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.phg_ops_destroy(self._h)
+            self._h = None
+
+    def set_solver(self, restart=30, tol=1e-12, max_iter=20000):
+        _check(lib().phg_ops_set_solver(self._h, restart, tol, max_iter))
+
+    def last_solve(self):
+        it, cy, rr = C.c_int(), C.c_int(), C.c_double()
+        _check(lib().phg_ops_last_solve(self._h, C.byref(it), C.byref(cy), C.byref(rr)))
+        return {"iters": it.value, "cycles": cy.value, "relres": rr.value}
+
+
+def _out(like_dev, n):
+    return np.zeros(n)
+
+
+class SphereLaplace:
+    """SphereLaplace<double> (src/slaplace.h:60-108): calc1, calc2, solve."""
+
+    def __init__(self, ops: Operators):
+        self.ops = ops
+        self.m = ops.mesh
+
+    def calc1(self, F, bnd=None, out=None, stream=None):
+        out = np.zeros(self.m.size) if out is None else out
+        F, bnd = _f8(F), _f8(bnd)
+        _check(lib().phg_laplace_calc1(self.ops._h, _ptr(out), _ptr(F), _ptr(bnd), _stream(stream)))
+        return out
+
+    def calc2(self, F, out=None, stream=None):
+        out = np.zeros(self.m.inner_size) if out is None else out
+        F = _f8(F)
+        _check(lib().phg_laplace_calc2(self.ops._h, _ptr(out), _ptr(F), _stream(stream)))
+        return out
+
+    def solve(self, F, bnd=None, out=None, stream=None):
+        out = np.zeros(self.m.size) if out is None else out
+        F, bnd = _f8(F), _f8(bnd)
+        _check(lib().phg_laplace_solve(self.ops._h, _ptr(out), _ptr(F), _ptr(bnd), _stream(stream)))
+        return out
+
+
+class SphereJacobian:
+    """SphereJacobian (src/sjacobian.h:65-149): calc1, calc2, calc2t."""
+
+    def __init__(self, ops: Operators):
+        self.ops = ops
+        self.m = ops.mesh
+
+    def calc1(self, u, v, bnd=None, out=None, stream=None):
+        out = np.zeros(self.m.size) if out is None else out
+        u, v, bnd = _f8(u), _f8(v), _f8(bnd)
+        _check(lib().phg_jacobian_calc1(self.ops._h, _ptr(out), _ptr(u), _ptr(v), _ptr(bnd), _stream(stream)))
+        return out
+
+    def calc2(self, u, v, out=None, stream=None):
+        out = np.zeros(self.m.inner_size) if out is None else out
+        u, v = _f8(u), _f8(v)
+        _check(lib().phg_jacobian_calc2(self.ops._h, _ptr(out), _ptr(u), _ptr(v), _stream(stream)))
+        return out
+
+    def calc2t(self, u, v, out=None, stream=None):
+        out = np.zeros(self.m.inner_size) if out is None else out
+        u, v = _f8(u), _f8(v)
+        _check(lib().phg_jacobian_calc2t(self.ops._h, _ptr(out), _ptr(u), _ptr(v), _stream(stream)))
+        return out
+
+
+class SphereNorm:
+    """SphereNorm<double> (src/norm.h:58-120): norm, dist, scalar."""
+
+    def __init__(self, ops: Operators):
+        self.ops = ops
+
+    def norm(self, u, stream=None):
+        r = C.c_double()
+        _check(lib().phg_norm(self.ops._h, _ptr(_f8(u)), C.byref(r), _stream(stream)))
+        return r.value
+
+    def dist(self, u, v, stream=None):
+        r = C.c_double()
+        _check(lib().phg_dist(self.ops._h, _ptr(_f8(u)), _ptr(_f8(v)), C.byref(r), _stream(stream)))
+        return r.value
+
+    def scalar(self, u, v, stream=None):
+        r = C.c_double()
+        _check(lib().phg_scalar(self.ops._h, _ptr(_f8(u)), _ptr(_f8(v)), C.byref(r), _stream(stream)))
+        return r.value
+
+
+class BarVortex:
+    """SBarVortex (examples/barvortex.h:109-241): calc (one step), plus calc_batch."""
+
+    def __init__(self, ops: Operators, tau=1e-3, sigma=1.6e-2, mu=8e-5, k1=1.0, k2=1.0, theta=0.5,
+                 picard_iters=3, coriolis=None):
+        self.ops = ops
+        self.m = ops.mesh
+        c = BvConf(tau, sigma, mu, k1, k2, theta, picard_iters)
+        cor = _f8(coriolis)
+        h = C.c_void_p()
+        _check(lib().phg_barvortex_create(ops._h, C.byref(c), _ptr(cor), C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.phg_barvortex_destroy(self._h)
+            self._h = None
+
+    def calc(self, u, bnd_u=None, bnd_w=None, forcing=None, out=None, stream=None):
+        out = np.zeros(self.m.size) if out is None else out
+        u, bnd_u, bnd_w, forcing = _f8(u), _f8(bnd_u), _f8(bnd_w), _f8(forcing)
+        _check(lib().phg_barvortex_calc(self._h, _ptr(out), _ptr(u), _ptr(bnd_u), _ptr(bnd_w), _ptr(forcing),
+                                        _stream(stream)))
+        return out
+
+    def calc_batch(self, u, bnd_u=None, bnd_w=None, forcing=None, out=None, stream=None):
+        """u: members x V (member-major)."""
+        nm = u.shape[0]
+        out = np.zeros((nm, self.m.size)) if out is None else out
+        u, bnd_u, bnd_w, forcing = _f8(u), _f8(bnd_u), _f8(bnd_w), _f8(forcing)
+        _check(lib().phg_barvortex_calc_batch(self._h, nm, _ptr(out), _ptr(u), _ptr(bnd_u), _ptr(bnd_w),
+                                              _ptr(forcing), _stream(stream)))
+        return out
+
+    def last_stats(self):
+        a = [C.c_int() for _ in range(4)]
+        w = C.c_double()
+        _check(lib().phg_barvortex_last_stats(self._h, *[C.byref(x) for x in a], C.byref(w)))
+        return {"iters_lapl": a[0].value, "iters_a": a[1].value, "iters_mj": a[2].value, "iters_ml": a[3].value,
+                "worst_relres": w.value}
+
+
+class Baroclin:
+    """Baroclin (examples/baroclin.h:78-287): calc (one step)."""
+
+    def __init__(self, ops: Operators, tau=1e-3, sigma=0.05, mu=6.77e-5, sigma1=0.05, mu1=6.77e-5,
+                 alpha=0.1 ** 0.5, picard_iters=3, picard_tol=1e-8, coriolis=None):
+        self.ops = ops
+        self.m = ops.mesh
+        c = BcConf(tau, sigma, mu, sigma1, mu1, alpha, picard_iters, picard_tol)
+        h = C.c_void_p()
+        _check(lib().phg_baroclin_create(ops._h, C.byref(c), _ptr(_f8(coriolis)), C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.phg_baroclin_destroy(self._h)
+            self._h = None
+
+    def calc(self, u1, u2, bnd=None, f=None, g=None, out1=None, out2=None, stream=None):
+        out1 = np.zeros(self.m.size) if out1 is None else out1
+        out2 = np.zeros(self.m.size) if out2 is None else out2
+        _check(lib().phg_baroclin_calc(self._h, _ptr(out1), _ptr(out2), _ptr(_f8(u1)), _ptr(_f8(u2)),
+                                       _ptr(_f8(bnd)), _ptr(_f8(f)), _ptr(_f8(g)), _stream(stream)))
+        return out1, out2

@@ -1,0 +1,119 @@
+"""GPU path vs the CPU oracle on the same seeded inputs (through the C ABI).
+
+Tolerances (relative L2 unless stated):
+  * operator applies whose only solve is a mass matrix (Laplace calc1/calc2,
+    Jacobian calc1/calc2): 1e-13 -- the matrices are bit-identical to the
+    reference's and FP64 row sums round like the CPU, so only the mass
+    solve's tolerance separates the two;
+  * norms / dist / scalar: 1e-13;
+  * Laplace solve and barvortex steps: 1e-9, set by the solve tolerance
+    (GMRES to 1e-12 relative residual here, the oracle to 1e-13).
+"""
+import numpy as np
+import pytest
+
+import pyoracle as po
+from mke_gb300 import fields, phelm
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300))
+
+
+_cache = {}
+
+
+def setup(level, precision=phelm.PHG_FP64):
+    key = (level, precision)
+    if key not in _cache:
+        m = phelm.Mesh.sphere(level)
+        ops = phelm.Operators(m, precision, tol=1e-12)
+        o = po.Oracle(level)
+        lat, lon = m.latlon()
+        rng = np.random.default_rng(100 + level)
+        u = fields.sh_field(fields.random_coeffs(rng, 1, 8), lat, lon)
+        v = fields.sh_field(fields.random_coeffs(rng, 1, 8), lat, lon)
+        bnd = u[m.arrays()["bnd"] == 1].copy()
+        _cache[key] = (m, ops, o, u, v, bnd, lat, lon)
+    return _cache[key]
+
+
+@pytest.mark.parametrize("level", [2, 3, 4, 5])
+def test_laplace_apply(level):
+    m, ops, o, u, v, bnd, *_ = setup(level)
+    L = phelm.SphereLaplace(ops)
+    assert rel(L.calc2(u), o.laplace_calc2(u)) <= 1e-13
+    assert rel(L.calc1(u, bnd), o.laplace_calc1(u, bnd)) <= 1e-13
+
+
+@pytest.mark.parametrize("level", [2, 3, 4, 5])
+def test_laplace_solve(level):
+    m, ops, o, u, v, bnd, *_ = setup(level)
+    L = phelm.SphereLaplace(ops)
+    got = L.solve(u, bnd)
+    st = ops.last_solve()
+    assert st["relres"] <= 1e-12
+    assert rel(got, o.laplace_solve(u, bnd)) <= 1e-9
+    # round trip through the apply
+    assert rel(L.calc1(got, bnd), o.laplace_calc1(o.laplace_solve(u, bnd), bnd)) <= 1e-8
+
+
+@pytest.mark.parametrize("level", [2, 3, 4, 5])
+def test_jacobian(level):
+    m, ops, o, u, v, bnd, *_ = setup(level)
+    J = phelm.SphereJacobian(ops)
+    assert rel(J.calc2(u, v), o.jacobian_calc2(u, v)) <= 1e-13
+    assert rel(J.calc1(u, v, bnd), o.jacobian_calc1(u, v, bnd)) <= 1e-13
+    assert rel(J.calc2t(u, v), -o.jacobian_calc2(u, v)) <= 1e-13
+
+
+@pytest.mark.parametrize("level", [2, 4])
+def test_norms(level):
+    m, ops, o, u, v, bnd, *_ = setup(level)
+    N = phelm.SphereNorm(ops)
+    assert abs(N.norm(u) - o.norm(u)) <= 1e-13 * o.norm(u)
+    assert abs(N.dist(u, v) - o.dist(u, v)) <= 1e-13 * o.dist(u, v)
+    assert abs(N.scalar(u, v) - o.scalar(u, v)) <= 1e-13 * abs(o.norm(u) * o.norm(v))
+
+
+@pytest.mark.parametrize("level,steps", [(2, 2), (3, 2), (4, 1)])
+def test_barvortex_steps(level, steps):
+    m, ops, o, u, v, bnd, lat, lon = setup(level)
+    psi, _ = fields.barvortex_initial(lat, lon, seed=7, lmax_noise=8)
+    cor = np.sin(lat)
+    bv = phelm.BarVortex(ops, picard_iters=3, coriolis=cor)
+    obv = o.barvortex(max_iter=3, coriolis=cor)
+    z = np.zeros(m.outer_size)
+    a, b = psi.copy(), psi.copy()
+    for _ in range(steps):
+        a = bv.calc(a, z, z)
+        b = o.bv_step(obv, b, z, z)
+    assert rel(a, b) <= 1e-9
+    st = bv.last_stats()
+    assert st["worst_relres"] <= 1e-11
+
+
+def test_barvortex_batch_equals_single():
+    m, ops, o, u, v, bnd, lat, lon = setup(3)
+    cor = np.sin(lat)
+    bv = phelm.BarVortex(ops, picard_iters=3, coriolis=cor)
+    members = np.stack([fields.barvortex_initial(lat, lon, seed=s, lmax_noise=8)[0] for s in range(5)])
+    z = np.zeros((5, m.outer_size))
+    batch = bv.calc_batch(members, z, z)
+    for k in range(5):
+        single = bv.calc(members[k], z[k], z[k])
+        assert rel(batch[k], single) <= 1e-10
+
+
+def test_mixed_precision_matches_fp64():
+    m, ops, o, u, v, bnd, lat, lon = setup(4)
+    mixed = phelm.Operators(m, phelm.PHG_MIXED, tol=1e-12)
+    L64, L32 = phelm.SphereLaplace(ops), phelm.SphereLaplace(mixed)
+    assert rel(L32.calc2(u), L64.calc2(u)) <= 1e-12
+    s64, s32 = L64.solve(u, bnd), L32.solve(u, bnd)
+    assert mixed.last_solve()["relres"] <= 1e-12
+    assert rel(s32, s64) <= 1e-9
+    J64, J32 = phelm.SphereJacobian(ops), phelm.SphereJacobian(mixed)
+    assert rel(J32.calc2(u, v), J64.calc2(u, v)) <= 1e-12

@@ -1,0 +1,120 @@
+"""The product library on the CPU: it loads, exports every declared entry
+point, and its host-side mesh generator / loader / assembly reproduce the
+reference exactly (golden fixtures from the reference's own sources)."""
+import hashlib
+import os
+import re
+
+import numpy as np
+import pytest
+
+from mke_gb300 import phelm
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+OPS = ["idt", "lapl", "bnd2", "bnd3", "jidt", "d1", "d2", "d1c", "d2c", "d1b", "d2b", "d1cb", "d2cb", "norm"]
+
+
+def header_symbols():
+    txt = open(os.path.join(REPO, "include", "phelm_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(phg_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_exports_every_declared_symbol():
+    L = phelm.lib()
+    names = header_symbols()
+    assert len(names) >= 25
+    for n in names:
+        assert hasattr(L, n), n
+    assert set(names) == set(phelm.SIGNATURES), set(names) ^ set(phelm.SIGNATURES)
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float64).view(np.int64)
+
+
+@pytest.mark.parametrize("level", [1, 2, 3])
+def test_mesh_and_operators_bitexact(level, golden):
+    g = golden(f"ref_L{level}.npz")
+    m = phelm.Mesh.sphere(level)
+    a = m.arrays()
+    for k in ("tri", "tz", "bnd"):
+        assert np.array_equal(a[k], g["mesh_" + k]), k
+    for k in ("xyz", "uv"):
+        assert np.array_equal(bits(a[k]), bits(g["mesh_" + k])), k
+    mp = m.maps()
+    for k in ("inner", "outer", "p2io"):
+        assert np.array_equal(mp[k], g["mesh_" + k]), k
+    for op in OPS:
+        p, c, v = m.csr(op)
+        assert np.array_equal(p, g[op + "_ptr"]) and np.array_equal(c, g[op + "_col"]), op
+        assert np.array_equal(v, g[op + "_val"]), op
+
+
+@pytest.mark.parametrize("level", [4, 5])
+def test_larger_levels_by_digest(level, golden):
+    g = golden(f"ref_L{level}.npz")
+    m = phelm.Mesh.sphere(level)
+    a = m.arrays()
+    for k in ("tri", "tz"):
+        assert np.array_equal(a[k], g["mesh_" + k]), k
+    for op in OPS:
+        h = hashlib.sha256()
+        for x in m.csr(op):
+            h.update(np.ascontiguousarray(x).tobytes())
+        assert h.hexdigest() == str(g["digest_" + op]), op
+
+
+def write_reference_text(path, m):
+    """The reference generator's text format (utils/icosahedron.cpp:268-457)."""
+    a = m.arrays()
+    xyz, uv = a["xyz"].reshape(-1, 3), a["uv"].reshape(-1, 4, 2)
+    with open(path, "w") as f:
+        f.write("#points:%d\n#triangles:%d\n" % (m.size, m.ntri))
+        for k in range(4):
+            f.write("#predef: zone %d stdsphere%d\n" % (k + 1, k + 1))
+        for p in range(m.size):
+            f.write("%.16f %.16f %.16f" % tuple(xyz[p]))
+            for k in range(4):
+                f.write(" ; %.16f %.16f " % tuple(uv[p, k]))
+            f.write("\n")
+        f.write("# triangles %d \n" % m.ntri)
+        tri = a["tri"].reshape(-1, 3)
+        for t in range(m.ntri):
+            f.write("%d %d %d " % tuple(tri[t] + 1))
+            if a["tz"][t] != 0:
+                f.write(" ; %d " % (a["tz"][t] + 1))
+            f.write("\n")
+        f.write("# boundary \n")
+        for p in np.nonzero(a["bnd"])[0]:
+            f.write("%d \n" % (p + 1))
+
+
+def test_load_text_roundtrip(tmp_path):
+    m = phelm.Mesh.sphere(3)
+    path = str(tmp_path / "ss3.txt")
+    write_reference_text(path, m)
+    m2 = phelm.Mesh.load(path)
+    a, b = m.arrays(), m2.arrays()
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    assert np.array_equal(m.csr("lapl")[2], m2.csr("lapl")[2])
+
+
+def test_errors():
+    with pytest.raises(phelm.PhgError) as e:
+        phelm.Mesh.sphere(0)
+    assert e.value.code == 1
+    with pytest.raises(phelm.PhgError) as e:
+        phelm.Mesh.load("/nonexistent/mesh.txt")
+    assert e.value.code == 5
+
+
+def test_no_gpu_fails_loudly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    m = phelm.Mesh.sphere(2)
+    with pytest.raises(phelm.PhgError) as e:
+        phelm.Operators(m)
+    assert e.value.code == 2
