@@ -1,0 +1,335 @@
+#!/usr/bin/env python
+"""Benchmark: barotropic-vorticity (barvortex) steps/s on an icosahedral
+level-6 sphere mesh (40,962 points), mixed precision vs FP64, on GB300.
+
+Workload (one "step" = one BarVortex::calc): tau = 1e-3, theta = 0.5,
+3 Picard iterations, sigma = 1.6e-2, mu = 8e-5, k1 = k2 = 1, l + h = sin(lat)
+(2 Omega = 1), zero boundary; the initial stream function is the inverse
+Laplacian of a wavenumber-4 Rossby-Haurwitz vorticity (amplitude 0.1) plus
+seeded spherical-harmonic noise (l <= 20, amplitude 1e-3).  Every linear
+solve runs to a relative residual of 1e-10.
+
+Arms: the default arm times the GB300 library through its C ABI; ``--impl
+reference`` times the reference algorithm on the host cores (the C oracle,
+the reference's own sources cannot run on this machine) on the same workload.
+Multi-GPU runs are independent replicas (one trajectory per GPU, no
+collective): the path does not shard at this size.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+LEVEL = 6
+CONF = dict(tau=1e-3, sigma=1.6e-2, mu=8e-5, k1=1.0, k2=1.0, theta=0.5, picard_iters=3)
+SEED = 2024
+TOL = 1e-10
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def initial_state(mesh):
+    from mke_gb300 import fields
+    lat, lon = mesh.latlon()
+    psi, _ = fields.barvortex_initial(lat, lon, seed=SEED)
+    return psi, np.sin(lat)
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+    from mke_gb300 import phelm
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    mesh = phelm.Mesh.sphere(args.level)
+    psi0, cor = initial_state(mesh)
+    V, os_ = mesh.size, mesh.outer_size
+    stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > L2 (129 MB)
+
+    def make(prec):
+        ops = phelm.Operators(mesh, prec, restart=30, tol=args.tol, max_iter=20000)
+        return ops, phelm.BarVortex(ops, coriolis=cor, **CONF)
+
+    results = {}
+    zb = torch.zeros(max(os_, 1), dtype=torch.float64, device=dev)
+    for name, prec in (("mixed", phelm.PHG_MIXED), ("fp64", phelm.PHG_FP64)):
+        ops, bv = make(prec)
+        u = torch.tensor(psi0, dtype=torch.float64, device=dev)
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                bv.calc(u, zb, zb, out=u, stream=stream)
+        stream.synchronize()
+        u = torch.tensor(psi0, dtype=torch.float64, device=dev)
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        clocks = ClockSampler(local) if name == "mixed" else None
+        if clocks:
+            clocks.start()
+        ops.profile(True)
+        k0 = phelm.kernel_launches()
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.zero_()
+                starts[k].record(stream)
+                bv.calc(u, zb, zb, out=u, stream=stream)
+                ends[k].record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        wall = time.perf_counter() - t0
+        launches = phelm.kernel_launches() - k0 - 0
+        prof = ops.profile_read()
+        ops.profile(False)
+        dev_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+        st = bv.last_stats()
+        results[name] = {"ms_per_step": dev_ms / args.steps, "wall_s": wall, "prof": prof, "launches": launches,
+                         "state": u.cpu().numpy(), "stats": st,
+                         "clocks": clocks.stop() if clocks else None}
+        # end-to-end through the C ABI with host buffers (H2D/D2H every step)
+        if name == "mixed":
+            uh = psi0.copy()
+            zh = np.zeros(max(os_, 1))
+            out = np.empty_like(uh)
+            bv.calc(uh, zh, zh, out=out)  # warm
+            t1 = time.perf_counter()
+            for _ in range(args.steps):
+                bv.calc(uh, zh, zh, out=out)
+                uh, out = out, uh
+            e2e = time.perf_counter() - t1
+            results[name]["e2e_s"] = e2e
+        del bv, ops
+
+    # max over ranks
+    ms = results["mixed"]["ms_per_step"]
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms, results["fp64"]["ms_per_step"], results["mixed"]["e2e_s"]], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms, ms64, e2e = t.tolist()
+    else:
+        ms64, e2e = results["fp64"]["ms_per_step"], results["mixed"]["e2e_s"]
+    if rank != 0:
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return None
+
+    mixed, fp64 = results["mixed"], results["fp64"]
+    prof = mixed["prof"]
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = prof["bytes"] / (prof["ms"] * 1e-3) / 1e9 if prof["ms"] > 0 else 0.0
+    traffic = None
+    tf = os.path.join(HERE, "profiles", "gmres_traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get("bytes_per_launch")
+        except (OSError, ValueError):
+            traffic = None
+    rel = float(np.linalg.norm(mixed["state"] - fp64["state"]) / np.linalg.norm(fp64["state"]))
+    cpu = None
+    if ws == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args.level, steps=1)
+    line = {
+        "metric": "level-6 barvortex steps/s (mixed precision, 1e-10 rel residual per solve)",
+        "value": ws * 1000.0 / ms,
+        "unit": "steps/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+f64",
+        "data": "synthetic (seeded Rossby-Haurwitz wave 4 + spherical-harmonic noise)",
+        "config": {"workload": "barvortex step, icosahedral level 6 (40962 points, 81920 triangles), "
+                               "tau=1e-3, theta=0.5, 3 Picard iterations, GMRES(30) to 1e-10",
+                   "level": args.level, "members_per_gpu": 1, "parallelism": f"replicas x{ws}",
+                   "l2": "flushed between steps (256 MB write, not timed)"},
+        "fp64": {"value": ws * 1000.0 / ms64, "unit": "steps/s", "ms_per_step": ms64,
+                 "mixed_over_fp64": ms64 / ms},
+        "state_rel_diff_mixed_vs_fp64": rel,
+        "solver": {"mixed": mixed["stats"], "fp64": fp64["stats"]},
+        "roofline": {"kernel": "gmres_kernel (persistent solver)", "bound": "hbm", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "launches_timed": prof["launches"],
+                     "bytes_per_launch": prof["bytes"] / max(prof["launches"], 1),
+                     "ms_per_launch": prof["ms"] / max(prof["launches"], 1),
+                     "share_of_step": prof["ms"] / (ms * args.steps),
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s"},
+        "e2e": {"value": args.steps / mixed["e2e_s"], "unit": "steps/s",
+                "h2d_bytes_per_step": 8 * (V + 2 * max(os_, 1)), "d2h_bytes_per_step": 8 * V},
+        "gpu_launches": mixed["launches"],
+        "clocks": mixed["clocks"],
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return line
+
+
+def cpu_baseline(level, steps=1):
+    """The oracle (C restatement of the reference algorithm) on the host."""
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import pyoracle as po
+    from mke_gb300 import fields
+    o = po.Oracle(level)
+    uv = o.mesh_arrays()["uv"].reshape(-1, 4, 2)
+    lat, lon = uv[:, 0, 0], uv[:, 0, 1]
+    psi, _ = fields.barvortex_initial(lat, lon, seed=SEED)
+    bv = o.barvortex(max_iter=3, coriolis=np.sin(lat), **{k: CONF[k] for k in ("tau", "sigma", "mu", "k1", "k2", "theta")})
+    z = np.zeros(o.os)
+    t0 = time.perf_counter()
+    s = psi
+    for _ in range(steps):
+        s = o.bv_step(bv, s, z, z)
+    dt = time.perf_counter() - t0
+    return {"value": steps / dt, "unit": "steps/s", "cores": 1, "kind": "port",
+            "sample": f"{steps} step(s) of the level-{level} workload after setup (solves by GMRES+ILU(0) to 1e-13)"}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    steps = max(1, min(args.steps, 3))
+    warm = min(args.warmup, 1)
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import pyoracle as po
+    from mke_gb300 import fields
+    po.build()
+    o = po.Oracle(args.level)
+    uv = o.mesh_arrays()["uv"].reshape(-1, 4, 2)
+    lat, lon = uv[:, 0, 0], uv[:, 0, 1]
+    psi, _ = fields.barvortex_initial(lat, lon, seed=SEED)
+    bv = o.barvortex(max_iter=3, coriolis=np.sin(lat), **{k: CONF[k] for k in ("tau", "sigma", "mu", "k1", "k2", "theta")})
+    z = np.zeros(o.os)
+    s = psi
+    for _ in range(warm):
+        s = o.bv_step(bv, s, z, z)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        s = o.bv_step(bv, s, z, z)
+    dt = time.perf_counter() - t0
+    v = steps / dt
+    sample = f"{steps} timed step(s) after {warm} warm-up, level {args.level}, single thread"
+    print(json.dumps({
+        "impl": "reference",
+        "metric": "level-6 barvortex steps/s (mixed precision, 1e-10 rel residual per solve)",
+        "value": v, "unit": "steps/s", "n_gpus": ws, "steps": steps, "warmup": warm,
+        "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded Rossby-Haurwitz wave 4 + spherical-harmonic noise)",
+        "config": {"workload": "barvortex step, icosahedral level 6 (40962 points, 81920 triangles), "
+                               "tau=1e-3, theta=0.5, 3 Picard iterations", "level": args.level},
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--level", type=int, default=LEVEL)
+    ap.add_argument("--tol", type=float, default=TOL)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+    if args.warmup < 3:
+        args.warmup = 3
+    run_ours(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

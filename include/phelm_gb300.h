@@ -49,6 +49,9 @@ typedef struct phg_baroclin_s *phg_baroclin;
 
 const char *phg_last_error(void);
 const char *phg_version(void);
+/* Instrumentation, no reference counterpart: number of CUDA kernels this
+ * library has enqueued since it was loaded. */
+long long phg_kernel_launches(void);
 
 /* ------------------------------------------------------------------ mesh --
  * Host-only (no GPU needed). */
@@ -92,6 +95,14 @@ void phg_ops_destroy(phg_ops o);
 int phg_ops_set_solver(phg_ops o, int restart, double tol, int max_iter);
 /* Statistics of the last solve on this handle (host memory). */
 int phg_ops_last_solve(phg_ops o, int *iters, int *cycles, double *relres);
+/* Instrumentation, no reference counterpart: while enabled, every solver
+ * launch of this handle (and of models built on it) is bracketed by CUDA
+ * events on its stream and its algorithmic byte count is kept (up to 4096
+ * launches).  profile_read synchronises and returns the number of solver
+ * launches, their summed device time in ms and their summed algorithmic
+ * bytes since the last enable. */
+int phg_ops_profile(phg_ops o, int enable);
+int phg_ops_profile_read(phg_ops o, int *launches, double *ms, double *bytes);
 
 /* SphereLaplace::calc1 (src/impl/slaplace_impl.h:176-192): ans[V] = Laplacian
  * of F[V] with boundary values bnd[os] written on the boundary. */

@@ -80,6 +80,7 @@ struct phg_mesh_s {
 
 extern "C" const char *phg_last_error(void) { return g_err.c_str(); }
 extern "C" const char *phg_version(void) { return "phelm-gb300 0.1 (sm_103a)"; }
+extern "C" long long phg_kernel_launches(void) { return g_kernel_launches.load(); }
 
 extern "C" int phg_mesh_generate(int level, phg_mesh *out) {
     if (!out) return fail(PHG_ERR_ARG, "out is NULL");
@@ -211,6 +212,12 @@ struct phg_ops_s {
     bool stats_pending = false;
     // staging for host pointers
     DBuf st[6];
+    // solver-launch profiling
+    bool prof = false;
+    std::vector<cudaEvent_t> ev;
+    int nev = 0;
+    DBuf hist;
+    ~phg_ops_s() { for (auto e : ev) cudaEventDestroy(e); }
 
     DevEll ell(const DBuf &vals) const { DevEll e; e.n = rs; e.W = W; e.col = pcol.as<int>(); e.val = vals.as<double>(); return e; }
     const int *imap() const { return inner.as<int>(); }
@@ -359,8 +366,16 @@ int solve(phg_ops_s *o, const DevSolveOp &op, const double *B, double *X, int nv
         CK(cudaStreamSynchronize(s));
         CK(o->work.ensure(need));
     }
+    const bool rec = o->prof && o->nev + 2 <= (int)o->ev.size();
+    if (rec) CK(cudaEventRecord(o->ev[o->nev], s));
     CK(gmres_solve(op, B, X, nv, ld, o->restart, o->max_iter, tol, prec_of(o), o->work.p,
                    o->stats.as<GmresStats>() + slot, s));
+    if (rec) {
+        CK(cudaEventRecord(o->ev[o->nev + 1], s));
+        CK(cudaMemcpyAsync(o->hist.as<GmresStats>() + o->nev / 2, o->stats.as<GmresStats>() + slot,
+                           sizeof(GmresStats), cudaMemcpyDeviceToDevice, s));
+        o->nev += 2;
+    }
     o->stats_pending = true;
     return PHG_OK;
 }
@@ -370,7 +385,7 @@ int check_stats(phg_ops_s *o, int nslots, cudaStream_t s, GmresStats *agg = null
     std::vector<GmresStats> st(nslots);
     CK(cudaMemcpyAsync(st.data(), o->stats.p, sizeof(GmresStats) * nslots, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    GmresStats a{0, 0, 0.0, 0};
+    GmresStats a{0.0, 0.0, 0, 0, 0, 0};
     for (auto &x : st) {
         a.iters += x.iters; a.cycles += x.cycles;
         a.relres = std::max(a.relres, x.relres);
@@ -470,6 +485,40 @@ extern "C" int phg_ops_last_solve(phg_ops o, int *iters, int *cycles, double *re
     if (iters) *iters = o->last.iters;
     if (cycles) *cycles = o->last.cycles;
     if (relres) *relres = o->last.relres;
+    return PHG_OK;
+}
+
+extern "C" int phg_ops_profile(phg_ops o, int enable) {
+    if (!o) return fail(PHG_ERR_ARG, "NULL handle");
+    if (enable && o->ev.empty()) {
+        o->ev.resize(8192);
+        for (auto &e : o->ev) CK(cudaEventCreate(&e));
+        CK(o->hist.ensure(sizeof(GmresStats) * 4096));
+    }
+    CK(cudaStreamSynchronize(o->stream));
+    o->prof = enable != 0;
+    if (enable) o->nev = 0;
+    return PHG_OK;
+}
+
+extern "C" int phg_ops_profile_read(phg_ops o, int *launches, double *ms, double *bytes) {
+    if (!o) return fail(PHG_ERR_ARG, "NULL handle");
+    const int n = o->nev / 2;
+    double t = 0.0, b = 0.0;
+    if (n > 0) {
+        CK(cudaEventSynchronize(o->ev[o->nev - 1]));
+        std::vector<GmresStats> h(n);
+        CK(cudaMemcpy(h.data(), o->hist.p, sizeof(GmresStats) * n, cudaMemcpyDeviceToHost));
+        for (int k = 0; k < n; ++k) {
+            float dt = 0.f;
+            CK(cudaEventElapsedTime(&dt, o->ev[2 * k], o->ev[2 * k + 1]));
+            t += dt;
+            b += h[k].bytes;
+        }
+    }
+    if (launches) *launches = n;
+    if (ms) *ms = t;
+    if (bytes) *bytes = b;
     return PHG_OK;
 }
 

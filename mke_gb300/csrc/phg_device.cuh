@@ -42,10 +42,12 @@ struct DevCols {
 enum Precision { PREC_FP64 = 0, PREC_MIXED = 1 };
 
 struct GmresStats {
-    int iters;       // Arnoldi steps taken (max over right-hand sides)
-    int cycles;      // restarts / refinement sweeps
     double relres;   // max final ||b - A x|| / ||b|| (FP64)
+    double bytes;    // algorithmic HBM bytes of the launch (model in phg_gmres.cu)
+    int iters;       // Arnoldi steps taken (max over right-hand sides)
+    int cycles;      // restarts / refinement sweeps (max over right-hand sides)
     int status;      // 0 ok, 1 not converged, 2 barrier timeout, 3 launch error
+    int steps_total; // Arnoldi steps summed over right-hand sides
 };
 
 // Solve A X = B for nv right-hand sides (member-major, leading dim ld) by

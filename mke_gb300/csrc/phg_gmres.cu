@@ -22,7 +22,7 @@
 #include <cooperative_groups.h>
 #include <cstdio>
 
-#include "phg_device.cuh"
+#include "phg_kernels.cuh"
 
 namespace phg {
 
@@ -154,8 +154,16 @@ __global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
         return true;
     };
 
-    int my_iters = 0, my_cycles = 0, my_status = 0;
+    int my_iters = 0, my_cycles = 0, my_status = 0, my_steps = 0;
     double my_rel = 0.0;
+    // algorithmic bytes per owned row (minimal traffic, no re-reads):
+    //   residual   W (col 4 B + val 8 B) + gathered x 8 + b 8 + r 8
+    //   Arnoldi j  W (col 4 + val es) + gathered v_j es + w es (write)
+    //              + (j+1) es (V reads, dots) + (j+1) es (V reads, update)
+    //              + 2 es (w read/write) + 2 es (w read, v_{j+1} write)
+    //   correction jlast es (V reads) + 16 (x read/write) + 8 (1/diag)
+    const double es = (double)sizeof(VT), nrows = (double)(r1 > r0 ? r1 - r0 : 0);
+    double my_bytes = 0.0;
 
     for (int v = grp; v < p.nv; v += p.groups) {
         const double *b = p.B + (size_t)v * p.ld;
@@ -192,6 +200,7 @@ __global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
             block_reduce<MAXM + 2>(acc, 1, red);
             if (!group_sum(1, hcol)) return;
             const double beta = sqrt(hcol[0]);
+            my_bytes += nrows * (W * 12.0 + 24.0);
             rel = beta / bnorm;
             if (rel <= p.tol) { status = 0; break; }
             if (iters >= p.max_iter) { status = 1; break; }
@@ -258,6 +267,8 @@ __global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
                 }
                 __syncthreads();
                 ++iters;
+                ++my_steps;
+                my_bytes += nrows * (W * (4.0 + es) + es * (2.0 * (j + 1) + 6.0));
                 jlast = j + 1;
                 if (flag[0] || iters >= p.max_iter) break;
             }
@@ -275,13 +286,16 @@ __global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
                 for (int l = 0; l < jlast; ++l) s += y[l] * (double)V[(size_t)l * n + i];
                 x[i] += dinv[i] * s;
             }
+            my_bytes += nrows * (jlast * es + 24.0);
         }
         my_iters = max(my_iters, iters);
         my_cycles = max(my_cycles, cycles);
         my_rel = fmax(my_rel, rel);
         my_status = max(my_status, status);
     }
+    if (threadIdx.x == 0) atomicAdd(&p.stats->bytes, my_bytes);
     if (threadIdx.x == 0 && bi == 0) {
+        atomicAdd(&p.stats->steps_total, my_steps);
         atomicMax(&p.stats->iters, my_iters);
         atomicMax(&p.stats->cycles, my_cycles);
         atomicMax(&p.stats->status, my_status);
@@ -381,6 +395,7 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     else
         e = cudaLaunchCooperativeKernel((void *)gmres_kernel<double>, grid, block, args, smem_bytes(), s);
     if (e != cudaSuccess) return e;
+    g_kernel_launches += 2;
     // a barrier timeout lands in stats->status (2)
     fold_err<<<1, 1, 0, s>>>(p.err, stats_dev);
     return cudaGetLastError();

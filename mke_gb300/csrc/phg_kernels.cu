@@ -7,9 +7,13 @@
 // time steps round exactly like the reference's vec_sum1 / vec_sum2 calls.
 //
 // All kernels take nv members stored member-major (x[v * ld + i]).
+#include <atomic>
+
 #include "phg_kernels.cuh"
 
 namespace phg {
+
+std::atomic<long long> g_kernel_launches{0};
 
 namespace {
 constexpr int TB = 256;
@@ -217,41 +221,48 @@ __global__ void k_gather(double *y, int ldy, const double *x, int ldx, const int
 cudaError_t apply_exact(const DevEll &A, const DevCols &C, const double *x_in, int ldx,
                         const double *x_bnd, int ldb, double *y, int ldy, int nv, cudaStream_t s) {
     k_apply<<<grid_for((long long)nv * A.n), TB, 0, s>>>(A, C, x_in, ldx, nullptr, x_bnd, ldb, nullptr, y, ldy, nv);
+    g_kernel_launches++;
     return cudaGetLastError();
 }
 
 cudaError_t apply_op(const DevEll &A, const DevCols &C, const double *xin, int ldx, const int *imap,
                      const double *xb, int ldb, const int *bmap, double *y, int ldy, int nv, cudaStream_t s) {
     k_apply<<<grid_for((long long)nv * A.n), TB, 0, s>>>(A, C, xin, ldx, imap, xb, ldb, bmap, y, ldy, nv);
+    g_kernel_launches++;
     return cudaGetLastError();
 }
 
 cudaError_t jac_rhs(const JacOps &J, const double *u, const double *v, int ld, const int *imap,
                     const int *bmap, double *out, int ldo, int nv, cudaStream_t s) {
     k_jac_rhs<<<grid_for((long long)nv * J.d1.n), TB, 0, s>>>(J, u, v, ld, imap, bmap, out, ldo, nv);
+    g_kernel_launches++;
     return cudaGetLastError();
 }
 
 cudaError_t jac_combine(const double *d, int ldd, int n, double *jac, int ldj, const double *FC, int ldf,
                         const int *inner, int nv, cudaStream_t s) {
     k_jac_combine<<<grid_for((long long)nv * n), TB, 0, s>>>(d, ldd, n, jac, ldj, FC, ldf, inner, nv);
+    g_kernel_launches++;
     return cudaGetLastError();
 }
 
 cudaError_t p2u(double *u, int ldu, const double *p, int ldp, const double *bnd, int ldb,
                 const int *p2io, const int *isb, int V, int nv, cudaStream_t s) {
     k_p2u<<<grid_for((long long)nv * V), TB, 0, s>>>(u, ldu, p, ldp, bnd, ldb, p2io, isb, V, nv);
+    g_kernel_launches++;
     return cudaGetLastError();
 }
 
 cudaError_t axpbz(double *y, const double *x, double a, const double *z, double b, long long n, cudaStream_t s) {
     k_axpbz<<<grid_for(n), TB, 0, s>>>(y, x, a, z, b, n);
+    g_kernel_launches++;
     return cudaGetLastError();
 }
 
 cudaError_t bv_fc(double *FC, const double *w, const double *dw, const double *rp, double c_w, double c_dw,
                   double c_w2, long long n, cudaStream_t s) {
     k_bv_fc<<<grid_for(n), TB, 0, s>>>(FC, w, dw, rp, c_w, c_dw, c_w2, n);
+    g_kernel_launches++;
     return cudaGetLastError();
 }
 
@@ -259,11 +270,13 @@ cudaError_t bv_mix(double *tmp1, double *tmp2, const double *w_n, const double *
                    const double *u, const double *lh, int V, double a1, double a2, double k2, double t1,
                    double t2, long long n, cudaStream_t s) {
     k_bv_mix<<<grid_for(n), TB, 0, s>>>(tmp1, tmp2, w_n, w, u_n, u, lh, V, a1, a2, k2, t1, t2, n);
+    g_kernel_launches++;
     return cudaGetLastError();
 }
 
 cudaError_t vsub(double *y, const double *a, const double *b, long long n, cudaStream_t s) {
     k_sub<<<grid_for(n), TB, 0, s>>>(y, a, b, n);
+    g_kernel_launches++;
     return cudaGetLastError();
 }
 
@@ -273,19 +286,24 @@ cudaError_t dot(const double *a, const double *b, int ld, int n, int nv, double 
                 bool take_sqrt, cudaStream_t s) {
     int nch = dot_chunks(n);
     k_dot_partial<<<nv * nch, TB, 0, s>>>(a, b, ld, n, 8192, nch, part, nv);
+    g_kernel_launches++;
     k_dot_final<<<(nv + 127) / 128, 128, 0, s>>>(part, nch, out, nv, take_sqrt ? 1 : 0);
+    g_kernel_launches++;
     return cudaGetLastError();
 }
 
 cudaError_t bv_commit(double *u_n, const double *u_n1, const double *nr, const double *nr0, int *done,
                       int V, int nv, cudaStream_t s) {
     k_bv_commit<<<grid_for((long long)nv * V), TB, 0, s>>>(u_n, u_n1, nr, nr0, done, V, nv);
+    g_kernel_launches++;
     k_bv_done<<<(nv + 127) / 128, 128, 0, s>>>(nr, nr0, done, nv);
+    g_kernel_launches++;
     return cudaGetLastError();
 }
 
 cudaError_t gather(double *y, int ldy, const double *x, int ldx, const int *map, int n, int nv, cudaStream_t s) {
     k_gather<<<grid_for((long long)nv * n), TB, 0, s>>>(y, ldy, x, ldx, map, n, nv);
+    g_kernel_launches++;
     return cudaGetLastError();
 }
 

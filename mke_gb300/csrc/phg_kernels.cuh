@@ -2,7 +2,12 @@
 #pragma once
 #include "phg_device.cuh"
 
+#include <atomic>
+
 namespace phg {
+
+// kernels enqueued by this library since load (instrumentation)
+extern std::atomic<long long> g_kernel_launches;
 
 // the four derivative operators of SphereJacobian on the shared pattern
 // (d1.col == d2.col == ...) and their boundary columns

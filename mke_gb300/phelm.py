@@ -44,6 +44,7 @@ class BcConf(C.Structure):
 SIGNATURES = {
     "phg_last_error": (C.c_char_p, []),
     "phg_version": (C.c_char_p, []),
+    "phg_kernel_launches": (C.c_longlong, []),
     "phg_mesh_generate": (C.c_int, [C.c_int, C.POINTER(_vp)]),
     "phg_mesh_load_file": (C.c_int, [C.c_char_p, C.POINTER(_vp)]),
     "phg_mesh_destroy": (None, [_vp]),
@@ -55,6 +56,8 @@ SIGNATURES = {
     "phg_ops_destroy": (None, [_vp]),
     "phg_ops_set_solver": (C.c_int, [_vp, C.c_int, C.c_double, C.c_int]),
     "phg_ops_last_solve": (C.c_int, [_vp, _ip, _ip, _dp]),
+    "phg_ops_profile": (C.c_int, [_vp, C.c_int]),
+    "phg_ops_profile_read": (C.c_int, [_vp, _ip, _dp, _dp]),
     "phg_laplace_calc1": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "phg_laplace_calc2": (C.c_int, [_vp, _vp, _vp, _vp]),
     "phg_laplace_solve": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
@@ -93,6 +96,10 @@ def lib(build_if_missing: bool = True):
             f.argtypes = args
         _lib = L
     return _lib
+
+
+def kernel_launches() -> int:
+    return int(lib().phg_kernel_launches())
 
 
 def _check(code):
@@ -194,6 +201,18 @@ class Operators:
 
     def set_solver(self, restart=30, tol=1e-12, max_iter=20000):
         _check(lib().phg_ops_set_solver(self._h, restart, tol, max_iter))
+
+    def profile(self, enable=True):
+        _check(lib().phg_ops_profile(self._h, 1 if enable else 0))
+
+    def profile_read(self):
+        n, ms, b = C.c_int(), C.c_double(), C.c_double()
+        _check(lib().phg_ops_profile_read(self._h, C.byref(n), C.byref(ms), C.byref(b)))
+        return {"launches": n.value, "ms": ms.value, "bytes": b.value}
+
+    @property
+    def stream(self):
+        return None
 
     def last_solve(self):
         it, cy, rr = C.c_int(), C.c_int(), C.c_double()
