@@ -364,3 +364,111 @@ void assemble_baroclin(const Mesh &m, const BaroclinParams &c, Csr &A, Csr bcol[
 }
 
 }  // namespace phg
+
+namespace phg {
+
+void assemble_laplacian(const Mesh &m, Csr &lapl) {
+    const int rs = m.rs;
+    CsrBuilder b(rs, rs);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int i = 0; i < rs; ++i) {
+        for_row(m, m.inner[i], [&](const Element &e, int t, int ip, int q) {
+            const int p2 = m.tri[3 * (size_t)t + q];
+            if (!m.bnd[p2]) b.add(i, m.p2io[p2], e.slap(q, ip));
+        });
+    }
+    b.finish(lapl);
+}
+
+namespace {
+
+Csr transpose(const Csr &a) {
+    Csr t;
+    t.n = a.m; t.m = a.n;
+    t.ptr.assign(t.n + 1, 0);
+    for (int k = 0; k < a.nnz(); ++k) t.ptr[a.col[k] + 1]++;
+    for (int i = 0; i < t.n; ++i) t.ptr[i + 1] += t.ptr[i];
+    t.col.resize(a.nnz()); t.val.resize(a.nnz());
+    std::vector<int> fill(t.ptr.begin(), t.ptr.end() - 1);
+    for (int i = 0; i < a.n; ++i)
+        for (int k = a.ptr[i]; k < a.ptr[i + 1]; ++k) {
+            int q = fill[a.col[k]]++;
+            t.col[q] = i; t.val[q] = a.val[k];
+        }
+    return t;
+}
+
+// prolongation from the coarse mesh (one refinement less) to the fine mesh
+Csr prolongation(const Mesh &f, const Mesh &c) {
+    std::vector<int> rcm_of(c.V);
+    for (int i = 0; i < c.V; ++i) rcm_of[c.orig[i]] = i;
+    CsrBuilder b(f.rs, c.rs);
+    for (int r = 0; r < f.rs; ++r) {
+        const int p = f.orig[f.inner[r]];
+        auto put = [&](int pre, double w) {
+            const int ci = rcm_of[pre];
+            if (!c.bnd[ci]) b.add(r, c.p2io[ci], w);
+        };
+        if (p < c.V) put(p, 1.0);
+        else { put(f.par_a[p], 0.5); put(f.par_b[p], 0.5); }
+    }
+    Csr P;
+    b.finish(P);
+    return P;
+}
+
+bool dense_inverse(const Csr &a, std::vector<double> &inv) {
+    const int n = a.n;
+    std::vector<double> M((size_t)n * 2 * n, 0.0);
+    for (int i = 0; i < n; ++i) {
+        for (int k = a.ptr[i]; k < a.ptr[i + 1]; ++k) M[(size_t)i * 2 * n + a.col[k]] = a.val[k];
+        M[(size_t)i * 2 * n + n + i] = 1.0;
+    }
+    for (int c = 0; c < n; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < n; ++r)
+            if (std::fabs(M[(size_t)r * 2 * n + c]) > std::fabs(M[(size_t)piv * 2 * n + c])) piv = r;
+        if (M[(size_t)piv * 2 * n + c] == 0.0) return false;
+        if (piv != c)
+            for (int k = 0; k < 2 * n; ++k) std::swap(M[(size_t)c * 2 * n + k], M[(size_t)piv * 2 * n + k]);
+        const double d = M[(size_t)c * 2 * n + c];
+        for (int k = 0; k < 2 * n; ++k) M[(size_t)c * 2 * n + k] /= d;
+        for (int r = 0; r < n; ++r) {
+            if (r == c) continue;
+            const double f = M[(size_t)r * 2 * n + c];
+            if (f == 0.0) continue;
+            for (int k = 0; k < 2 * n; ++k) M[(size_t)r * 2 * n + k] -= f * M[(size_t)c * 2 * n + k];
+        }
+    }
+    inv.assign((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) inv[(size_t)i * n + j] = M[(size_t)i * 2 * n + n + j];
+    return true;
+}
+
+}  // namespace
+
+bool build_mg(const Mesh &fine, int coarsest_level, MgHierarchy &h, std::string &err) {
+    h = MgHierarchy();
+    if (fine.level < 0 || fine.orig.empty()) { err = "multigrid needs a generated icosahedral mesh"; return false; }
+    if (coarsest_level < 1) coarsest_level = 1;
+    const int nlev = fine.level - coarsest_level + 1;
+    if (nlev < 2) { err = "mesh too coarse for multigrid"; return false; }
+    h.mesh.resize(nlev);
+    h.A.resize(nlev);
+    h.P.resize(nlev - 1);
+    h.R.resize(nlev - 1);
+    for (int k = 1; k < nlev; ++k) {
+        if (!generate_sphere(fine.level - k, h.mesh[k], err)) return false;
+        assemble_laplacian(h.mesh[k], h.A[k]);
+    }
+    for (int k = 0; k + 1 < nlev; ++k) {
+        const Mesh &f = k == 0 ? fine : h.mesh[k];
+        h.P[k] = prolongation(f, h.mesh[k + 1]);
+        h.R[k] = transpose(h.P[k]);
+    }
+    if (!dense_inverse(h.A[nlev - 1], h.coarse_inv)) { err = "coarsest Laplacian is singular"; return false; }
+    return true;
+}
+
+}  // namespace phg

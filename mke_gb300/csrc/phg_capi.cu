@@ -179,8 +179,18 @@ void to_ell(const Csr &c, int W, std::vector<int> *col, std::vector<double> &val
 }
 
 struct SolveOpBufs {
-    DBuf val, as64, as32, dinv;
+    DBuf val, as64, as32, a32, dinv;
     DevSolveOp op;
+};
+
+// one uploaded multigrid level (level 0 reuses the solve operator's arrays)
+struct MgLevelBufs {
+    DBuf col, a64, a32, d64, d32, pc, pw64, pw32, rf, rw64, rw32;
+};
+
+struct MgBufs {
+    std::vector<std::unique_ptr<MgLevelBufs>> lev;
+    DBuf cinv64, cinv32;
 };
 
 struct ColsBufs {
@@ -199,6 +209,7 @@ struct phg_ops_s {
     DBuf inner, outer, p2io, isb;
     DBuf pcol;                       // shared rs x rs pattern (W x rs)
     SolveOpBufs ML, L, MJ;           // mass (Laplace), Laplacian, mass (Jacobian)
+    MgBufs mgL;                      // multigrid hierarchy preconditioning L
     DBuf vd1, vd2, vd1c, vd2c;
     ColsBufs bnd2, bnd3, d1b, d2b, d1cb, d2cb;
     JacOps J;
@@ -231,7 +242,7 @@ int build_solve_op(phg_ops_s *o, const Csr &c, SolveOpBufs &b) {
     std::vector<double> v;
     to_ell(c, o->W, nullptr, v);
     std::vector<double> dinv(o->rs, 0.0), as64(v.size());
-    std::vector<float> as32(v.size());
+    std::vector<float> as32(v.size()), a32(v.size());
     for (int i = 0; i < c.n; ++i)
         for (int q = c.ptr[i]; q < c.ptr[i + 1]; ++q)
             if (c.col[q] == i) dinv[i] = 1.0 / c.val[q];
@@ -243,11 +254,14 @@ int build_solve_op(phg_ops_s *o, const Csr &c, SolveOpBufs &b) {
     for (size_t e = 0; e < v.size(); ++e) {
         as64[e] = v[e] * dinv[col[e]];
         as32[e] = (float)as64[e];
+        a32[e] = (float)v[e];
     }
     (void)n;
-    CK(upload(b.val, v)); CK(upload(b.as64, as64)); CK(upload(b.as32, as32)); CK(upload(b.dinv, dinv));
+    CK(upload(b.val, v)); CK(upload(b.as64, as64)); CK(upload(b.as32, as32)); CK(upload(b.a32, a32));
+    CK(upload(b.dinv, dinv));
     b.op.A = o->ell(b.val);
     b.op.as64 = b.as64.as<double>(); b.op.as32 = b.as32.as<float>(); b.op.dinv = b.dinv.as<double>();
+    b.op.a32 = b.a32.as<float>();
     return PHG_OK;
 }
 
@@ -268,6 +282,101 @@ int build_vals(phg_ops_s *o, const Csr &c, DBuf &b) {
 }
 
 bool same_pattern(const Csr &a, const Csr &b) { return a.n == b.n && a.ptr == b.ptr && a.col == b.col; }
+
+template <typename T>
+std::vector<float> to_f32(const std::vector<T> &v) { return std::vector<float>(v.begin(), v.end()); }
+
+int env_int(const char *name, int dflt) { const char *e = getenv(name); return e ? atoi(e) : dflt; }
+double env_dbl(const char *name, double dflt) { const char *e = getenv(name); return e ? atof(e) : dflt; }
+
+// Geometric multigrid for the Laplacian of a generated icosahedral mesh:
+// levels down to the 42-point icosahedron refinement, Jacobi smoothing,
+// coarse levels of at most `red_max` points solved per block in shared memory.
+int build_mg_dev(phg_ops_s *o, const Mesh &m, SolveOpBufs &Lb, MgBufs &mb, int prec) {
+    Lb.op.mg = MgDev();
+    if (env_int("PHG_MG", 1) == 0 || m.level < 3) return PHG_OK;
+    MgHierarchy h;
+    std::string err;
+    if (!build_mg(m, 1, h, err)) return fail(PHG_ERR_ARG, "multigrid: %s", err.c_str());
+    const int nlev = (int)h.A.size();
+    if (nlev > MG_MAXLEV) return PHG_OK;
+    MgDev &mg = Lb.op.mg;
+    mg.nlev = nlev;
+    mg.omega = env_dbl("PHG_MG_OMEGA", 0.7);
+    mg.nu1 = env_int("PHG_MG_NU", 2);
+    mg.nu2 = mg.nu1;
+    const size_t es = prec == PHG_MIXED ? 4 : 8;
+    const int red_max = env_int("PHG_MG_REDUNDANT", 3000);
+    // shared memory: the solver's own ~21 KB plus 4 vectors per redundant level
+    const size_t smem_cap = 200 * 1024;
+    int nred = nlev - 1;
+    size_t used = 0;
+    for (int l = nlev - 1; l >= 1; --l) {
+        const int n = l == 0 ? m.rs : h.mesh[l].rs;
+        if (n > red_max || 21 * 1024 + es * (used + 4 * (size_t)n) > smem_cap) break;
+        used += 4 * (size_t)n;
+        nred = l;
+    }
+    mg.nred = nred;
+    mb.lev.clear();
+    for (int l = 0; l < nlev; ++l) {
+        mb.lev.emplace_back(new MgLevelBufs());
+        MgLevelBufs &B = *mb.lev.back();
+        MgLevelDev &D = mg.lev[l];
+        if (l == 0) {
+            D.n = o->rs; D.W = o->W; D.col = o->pcol.as<int>();
+            D.a64 = Lb.op.A.val; D.a32 = Lb.op.a32; D.d64 = Lb.op.dinv;
+            std::vector<double> dd(o->rs);
+            CK(cudaMemcpy(dd.data(), Lb.op.dinv, 8 * dd.size(), cudaMemcpyDeviceToHost));
+            CK(upload(B.d32, to_f32(dd)));
+            D.d32 = B.d32.as<float>();
+        } else {
+            const Csr &A = h.A[l];
+            int W = 0;
+            for (int i = 0; i < A.n; ++i) W = std::max(W, A.ptr[i + 1] - A.ptr[i]);
+            std::vector<int> col;
+            std::vector<double> val, dinv(A.n, 0.0);
+            to_ell(A, W, &col, val);
+            for (int i = 0; i < A.n; ++i)
+                for (int q = A.ptr[i]; q < A.ptr[i + 1]; ++q)
+                    if (A.col[q] == i) dinv[i] = 1.0 / A.val[q];
+            CK(upload(B.col, col)); CK(upload(B.a64, val)); CK(upload(B.a32, to_f32(val)));
+            CK(upload(B.d64, dinv)); CK(upload(B.d32, to_f32(dinv)));
+            D.n = A.n; D.W = W; D.col = B.col.as<int>();
+            D.a64 = B.a64.as<double>(); D.a32 = B.a32.as<float>();
+            D.d64 = B.d64.as<double>(); D.d32 = B.d32.as<float>();
+        }
+        if (l + 1 < nlev) {
+            const Csr &P = h.P[l], &R = h.R[l];
+            std::vector<int> pc(2 * (size_t)P.n, -1);
+            std::vector<double> pw(2 * (size_t)P.n, 0.0);
+            for (int i = 0; i < P.n; ++i)
+                for (int q = P.ptr[i], k = 0; q < P.ptr[i + 1] && k < 2; ++q, ++k) {
+                    pc[2 * i + k] = P.col[q];
+                    pw[2 * i + k] = P.val[q];
+                }
+            int Wr = 0;
+            for (int c = 0; c < R.n; ++c) Wr = std::max(Wr, R.ptr[c + 1] - R.ptr[c]);
+            std::vector<int> rf((size_t)Wr * R.n, -1);
+            std::vector<double> rw((size_t)Wr * R.n, 0.0);
+            for (int c = 0; c < R.n; ++c)
+                for (int q = R.ptr[c], k = 0; q < R.ptr[c + 1]; ++q, ++k) {
+                    rf[(size_t)k * R.n + c] = R.col[q];
+                    rw[(size_t)k * R.n + c] = R.val[q];
+                }
+            CK(upload(B.pc, pc)); CK(upload(B.pw64, pw)); CK(upload(B.pw32, to_f32(pw)));
+            CK(upload(B.rf, rf)); CK(upload(B.rw64, rw)); CK(upload(B.rw32, to_f32(rw)));
+            D.pc = B.pc.as<int>(); D.pw64 = B.pw64.as<double>(); D.pw32 = B.pw32.as<float>();
+            D.Wr = Wr; D.rf = B.rf.as<int>(); D.rw64 = B.rw64.as<double>(); D.rw32 = B.rw32.as<float>();
+        }
+    }
+    CK(upload(mb.cinv64, h.coarse_inv));
+    CK(upload(mb.cinv32, to_f32(h.coarse_inv)));
+    mg.nc = h.A[nlev - 1].n;
+    mg.cinv64 = mb.cinv64.as<double>();
+    mg.cinv32 = mb.cinv32.as<float>();
+    return PHG_OK;
+}
 
 }  // namespace
 
@@ -304,6 +413,7 @@ extern "C" int phg_ops_create(phg_mesh h, int precision, phg_ops *out) {
     int r;
     if ((r = build_solve_op(o.get(), so.idt, o->ML))) return r;
     if ((r = build_solve_op(o.get(), so.lapl, o->L))) return r;
+    if ((r = build_mg_dev(o.get(), m, o->L, o->mgL, precision))) return r;
     if ((r = build_solve_op(o.get(), so.jidt, o->MJ))) return r;
     if ((r = build_vals(o.get(), so.d1, o->vd1)) || (r = build_vals(o.get(), so.d2, o->vd2)) ||
         (r = build_vals(o.get(), so.d1c, o->vd1c)) || (r = build_vals(o.get(), so.d2c, o->vd2c)))
@@ -361,7 +471,7 @@ Precision prec_of(const phg_ops_s *o) { return o->prec == PHG_MIXED ? PREC_MIXED
 // enqueue one solve; stats go to slot `slot` of the handle's device stats array
 int solve(phg_ops_s *o, const DevSolveOp &op, const double *B, double *X, int nv, int ld, double tol,
           int slot, cudaStream_t s) {
-    size_t need = gmres_work_bytes(op.A.n, nv, o->restart, prec_of(o));
+    size_t need = gmres_work_bytes(op, nv, o->restart, prec_of(o));
     if (need > o->work.n) {
         CK(cudaStreamSynchronize(s));
         CK(o->work.ensure(need));

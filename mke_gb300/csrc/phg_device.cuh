@@ -23,13 +23,42 @@ struct DevEll {
     const double *val = nullptr;   // W x n, the assembled values
 };
 
-// Right-preconditioned operator for the Krylov solver: A * D^{-1} with
-// D = diag(A) (Jacobi), in FP64 and FP32, plus 1/diag.
+// One level of a geometric multigrid hierarchy in HBM.  Level 0 is the
+// operator being solved; level k+1 is the mesh one refinement coarser.
+struct MgLevelDev {
+    int n = 0, W = 0;
+    const int *col = nullptr;                       // W x n, slot-major
+    const double *a64 = nullptr; const float *a32 = nullptr;  // A
+    const double *d64 = nullptr; const float *d32 = nullptr;  // 1 / diag(A)
+    // prolongation from level k+1: row i takes pc[2i], pc[2i+1] (-1 = none)
+    const int *pc = nullptr; const double *pw64 = nullptr; const float *pw32 = nullptr;
+    // restriction to level k+1: coarse row c sums rw[q*nc+c] * r[rf[q*nc+c]]
+    int Wr = 0;
+    const int *rf = nullptr; const double *rw64 = nullptr; const float *rw32 = nullptr;
+};
+
+constexpr int MG_MAXLEV = 10;
+
+struct MgDev {
+    int nlev = 0;    // 0 = Jacobi preconditioning only
+    int nred = 0;    // levels [nred, nlev) run redundantly per block in shared memory
+    MgLevelDev lev[MG_MAXLEV];
+    int nc = 0;      // coarsest size; dense inverse row-major
+    const double *cinv64 = nullptr; const float *cinv32 = nullptr;
+    double omega = 0.7;
+    int nu1 = 2, nu2 = 2;
+};
+
+// Operator of the Krylov solver: the exact A (FP64 residuals), Jacobi-scaled
+// copies A D^{-1} for the plain Jacobi path, and optionally a multigrid
+// V-cycle used as a flexible right preconditioner instead of Jacobi.
 struct DevSolveOp {
     DevEll A;                      // exact values for the FP64 residual b - A x
     const double *as64 = nullptr;  // A D^{-1} (column scaled), FP64
     const float *as32 = nullptr;   // A D^{-1}, FP32 (mixed precision)
     const double *dinv = nullptr;  // 1 / diag(A)
+    const float *a32 = nullptr;    // A in FP32 (multigrid path, mixed precision)
+    MgDev mg;
 };
 
 // rs x os boundary columns in CSR over rows (few nonzero rows).
@@ -58,7 +87,7 @@ struct GmresStats {
 // residual b - A x of every restart in FP64 (iterative refinement).
 // `work` must hold gmres_work_bytes(...) bytes; `stats_dev` receives a
 // GmresStats on the device.
-size_t gmres_work_bytes(int n, int nv, int m, Precision p);
+size_t gmres_work_bytes(const DevSolveOp &op, int nv, int m, Precision p);
 cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv, int ld,
                         int m, int max_iter, double tol, Precision p,
                         void *work, GmresStats *stats_dev, cudaStream_t s);

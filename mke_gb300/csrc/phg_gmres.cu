@@ -1,25 +1,31 @@
-// phg_gmres.cu -- persistent restarted GMRES on GB300.
+// phg_gmres.cu -- persistent restarted (flexible) GMRES on GB300.
 //
 // One cooperative launch solves nv systems A x = b that share A (ensemble
 // members, the 8 derivative right-hand sides of a Jacobian, ...).  The grid is
 // split into groups of G blocks; a group owns one right-hand side at a time
 // and its blocks own contiguous row ranges, so every dot product, AXPY and
-// normalisation touches only rows the block owns -- only the operator apply
-// gathers neighbours.  Groups synchronise among themselves only (G = 1 is a
+// normalisation touches only rows the block owns -- only operator applies
+// gather neighbours.  Groups synchronise among themselves only (G = 1 is a
 // plain __syncthreads), so independent right-hand sides converge independently
-// and nothing ever waits for the whole GPU.
+// and nothing waits for the whole GPU.
 //
-// Per Arnoldi step: (1) w = (A D^-1) v_j fused with the classical Gram-Schmidt
-// dots <v_l, w>, (2) w -= sum h_l v_l fused with ||w||^2, (3) v_{j+1} = w/|w|
-// and the Givens update (computed redundantly, identically, by every block of
-// the group so all of them take the same branch).  Three group barriers per
-// step.  Every restart recomputes r = b - A x in FP64 with the exact operator,
-// which is also the outer loop of mixed-precision iterative refinement.
+// Preconditioning (right, flexible): Jacobi, folded into the stored values
+// (A D^-1), or a geometric multigrid V-cycle over the nested icosahedral
+// meshes.  In the V-cycle the fine levels are smoothed by the group's blocks
+// with group barriers; the coarse levels (<= a few thousand points) are
+// solved by every block redundantly in shared memory with __syncthreads only,
+// so the coarse half of the cycle costs no cross-block synchronisation.
+//
+// Per Arnoldi step: [V-cycle z_j = M^-1 v_j], (1) w = A z_j fused with the
+// classical Gram-Schmidt dots <v_l, w>, (2) w -= sum h_l v_l fused with
+// ||w||^2, (3) v_{j+1} = w / |w| and the Givens update (computed redundantly,
+// identically, by every block of the group).  Every restart recomputes
+// r = b - A x in FP64 with the exact operator, which is also the outer loop
+// of mixed-precision iterative refinement.
 //
 // Every wait is bounded: a barrier that spins longer than ~1 s (clock64)
 // raises a device error flag; all blocks see the flag at their next barrier
 // and return, and the host reports status 2.
-#include <cooperative_groups.h>
 #include <cstdio>
 
 #include "phg_kernels.cuh"
@@ -41,13 +47,17 @@ struct Params {
     int n, nv, ld, m, max_iter;
     double tol;
     void *V;          // nv x (m+1) x n (VT)
+    void *Z;          // nv x m x n (VT), multigrid path only
     void *Wv;         // nv x n (VT)
     double *R;        // nv x n (FP64 residual)
-    double *part;     // groups x G x (MAXM + 2)
+    void *mgbuf;      // groups x per-group V-cycle buffers (parallel levels)
+    size_t mg_group_elems;
+    double *part;     // groups x 2 x (MAXM + 2) x G
     unsigned *bar;    // groups x 2
     int *err;
     GmresStats *stats;
     int groups, G;
+    int red_off[MG_MAXLEV];  // shared-memory offsets (elements) of the redundant levels
 };
 
 __device__ __forceinline__ unsigned ld_volatile(const unsigned *p) { return *(const volatile unsigned *)p; }
@@ -73,7 +83,7 @@ __device__ bool group_sync(unsigned *bar, int G, int *err) {
             while (ld_volatile(gen) == my) {
                 if (ld_volatile(err)) { ok = 0; break; }
                 if (clock64() - t0 > SPIN_LIMIT) { atomicExch(err, 1); ok = 0; break; }
-                __nanosleep(32);
+                __nanosleep(20);
             }
         }
         __threadfence();
@@ -85,15 +95,19 @@ __device__ bool group_sync(unsigned *bar, int G, int *err) {
 
 template <typename T> __device__ __forceinline__ T ldcg(const T *p) { return __ldcg(p); }
 
-// block-reduce K values held per thread in acc[0..K-1] (double), result in red[l][0]
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// block-reduce K values held per thread in acc[0..K-1], result in red[l][0]
 template <int KMAX>
 __device__ void block_reduce(double (&acc)[KMAX], int K, double (*red)[NWARP]) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int l = 0; l < KMAX; ++l) {
         if (l < K) {
-            double v = acc[l];
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            double v = warp_sum(acc[l]);
             if (lane == 0) red[l][warp] = v;
         }
     }
@@ -106,10 +120,197 @@ __device__ void block_reduce(double (&acc)[KMAX], int K, double (*red)[NWARP]) {
     __syncthreads();
 }
 
+template <typename VT> struct Prec;
+template <> struct Prec<double> {
+    __device__ static const double *as(const DevSolveOp &o) { return o.as64; }
+    __device__ static const double *a(const DevSolveOp &o) { return o.A.val; }
+    __device__ static const double *la(const MgLevelDev &l) { return l.a64; }
+    __device__ static const double *ld(const MgLevelDev &l) { return l.d64; }
+    __device__ static const double *lp(const MgLevelDev &l) { return l.pw64; }
+    __device__ static const double *lr(const MgLevelDev &l) { return l.rw64; }
+    __device__ static const double *ci(const MgDev &m) { return m.cinv64; }
+};
+template <> struct Prec<float> {
+    __device__ static const float *as(const DevSolveOp &o) { return o.as32; }
+    __device__ static const float *a(const DevSolveOp &o) { return o.a32; }
+    __device__ static const float *la(const MgLevelDev &l) { return l.a32; }
+    __device__ static const float *ld(const MgLevelDev &l) { return l.d32; }
+    __device__ static const float *lp(const MgLevelDev &l) { return l.pw32; }
+    __device__ static const float *lr(const MgLevelDev &l) { return l.rw32; }
+    __device__ static const float *ci(const MgDev &m) { return m.cinv32; }
+};
+
+// rows [r0, r1) of a level of size n split over G blocks
+__device__ __forceinline__ void own_rows(int n, int G, int bi, int &r0, int &r1) {
+    const int rpb = (n + G - 1) / G;
+    r0 = min(n, bi * rpb);
+    r1 = min(n, r0 + rpb);
+}
+
+// sum_k A[k][i] x[col]; CG: x read through L2 (written by other blocks)
+template <typename VT, bool CG>
+__device__ __forceinline__ VT spmv_row(const int *col, const VT *val, int n, int W, const VT *x, int i) {
+    VT s = 0;
+    for (int k = 0; k < W; ++k) {
+        const size_t e = (size_t)k * n + i;
+        const VT xv = CG ? ldcg(&x[__ldg(&col[e])]) : x[__ldg(&col[e])];
+        s += __ldg(&val[e]) * xv;
+    }
+    return s;
+}
+
 template <typename VT>
-__device__ __forceinline__ const VT *scaled_vals(const DevSolveOp &op);
-template <> __device__ __forceinline__ const double *scaled_vals<double>(const DevSolveOp &op) { return op.as64; }
-template <> __device__ __forceinline__ const float *scaled_vals<float>(const DevSolveOp &op) { return op.as32; }
+__device__ __forceinline__ VT restrict_row(const MgLevelDev &L, const VT *rw, int nc, const VT *r, int c, bool cg) {
+    VT s = 0;
+    for (int q = 0; q < L.Wr; ++q) {
+        const int f = L.rf[(size_t)q * nc + c];
+        if (f >= 0) s += rw[(size_t)q * nc + c] * (cg ? ldcg(&r[f]) : r[f]);
+    }
+    return s;
+}
+
+// Damped-Jacobi V-cycle: x0 = M^-1 b0 for the group's right-hand side.
+// Returns false if the grid is aborting.
+template <typename VT>
+__device__ bool vcycle(const Params &p, const VT *b0, VT *x0, VT *gbuf, VT *sm, unsigned *bar, int bi) {
+    const MgDev &mg = p.op.mg;
+    const int G = p.G;
+    const VT omega = (VT)mg.omega;
+    VT *xcur[MG_MAXLEV];
+    const VT *bl[MG_MAXLEV];
+    size_t offs[MG_MAXLEV];
+    // ---- parallel levels, down
+    size_t off = 0;
+    for (int l = 0; l < mg.nred; ++l) {
+        const MgLevelDev &L = mg.lev[l];
+        const int n = L.n;
+        offs[l] = off;
+        VT *xa = gbuf + off, *xb = xa + n, *r = xb + n;
+        VT *bn = r + n;  // storage for the rhs of level l+1 when that level is parallel too
+        off += 4 * (size_t)n;
+        const VT *b = l == 0 ? b0 : bl[l];
+        bl[l] = b;
+        const VT *A = Prec<VT>::la(L), *D = Prec<VT>::ld(L);
+        int r0, r1;
+        own_rows(n, G, bi, r0, r1);
+        VT *x = xa, *xo = xb;
+        for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) x[i] = omega * D[i] * ldcg(&b[i]);
+        for (int s = 1; s < mg.nu1; ++s) {
+            if (!group_sync(bar, G, p.err)) return false;
+            for (int i = r0 + threadIdx.x; i < r1; i += BLOCK)
+                xo[i] = x[i] + omega * D[i] * (ldcg(&b[i]) - spmv_row<VT, true>(L.col, A, n, L.W, x, i));
+            VT *t = x; x = xo; xo = t;
+        }
+        if (!group_sync(bar, G, p.err)) return false;
+        for (int i = r0 + threadIdx.x; i < r1; i += BLOCK)
+            r[i] = ldcg(&b[i]) - spmv_row<VT, true>(L.col, A, n, L.W, x, i);
+        xcur[l] = x;
+        if (!group_sync(bar, G, p.err)) return false;
+        const MgLevelDev &C = mg.lev[l + 1];
+        const VT *rw = Prec<VT>::lr(L);
+        if (l + 1 < mg.nred) {
+            int c0, c1;
+            own_rows(C.n, G, bi, c0, c1);
+            for (int c = c0 + threadIdx.x; c < c1; c += BLOCK) bn[c] = restrict_row<VT>(L, rw, C.n, r, c, true);
+            bl[l + 1] = bn;
+        } else {
+            VT *sb = sm + p.red_off[l + 1] + 2 * C.n;
+            for (int c = threadIdx.x; c < C.n; c += BLOCK) sb[c] = restrict_row<VT>(L, rw, C.n, r, c, true);
+        }
+    }
+    __syncthreads();
+    // ---- redundant levels in shared memory (x, xt, b, r per level)
+    const int last = mg.nlev - 1;
+    for (int l = mg.nred; l < last; ++l) {
+        const MgLevelDev &L = mg.lev[l], &C = mg.lev[l + 1];
+        const int n = L.n;
+        VT *x = sm + p.red_off[l], *xt = x + n, *b = xt + n, *r = b + n;
+        const VT *A = Prec<VT>::la(L), *D = Prec<VT>::ld(L);
+        for (int i = threadIdx.x; i < n; i += BLOCK) x[i] = omega * D[i] * b[i];
+        __syncthreads();
+        for (int s = 1; s < mg.nu1; ++s) {
+            for (int i = threadIdx.x; i < n; i += BLOCK)
+                xt[i] = x[i] + omega * D[i] * (b[i] - spmv_row<VT, false>(L.col, A, n, L.W, x, i));
+            __syncthreads();
+            for (int i = threadIdx.x; i < n; i += BLOCK) x[i] = xt[i];
+            __syncthreads();
+        }
+        for (int i = threadIdx.x; i < n; i += BLOCK) r[i] = b[i] - spmv_row<VT, false>(L.col, A, n, L.W, x, i);
+        __syncthreads();
+        VT *cb = sm + p.red_off[l + 1] + 2 * C.n;
+        const VT *rw = Prec<VT>::lr(L);
+        for (int c = threadIdx.x; c < C.n; c += BLOCK) cb[c] = restrict_row<VT>(L, rw, C.n, r, c, false);
+        __syncthreads();
+    }
+    {   // coarsest: dense inverse
+        const int n = mg.nc;
+        VT *x = sm + p.red_off[last], *b = x + 2 * n;
+        const VT *Ci = Prec<VT>::ci(mg);
+        for (int i = threadIdx.x; i < n; i += BLOCK) {
+            VT s = 0;
+            for (int j = 0; j < n; ++j) s += Ci[(size_t)i * n + j] * b[j];
+            x[i] = s;
+        }
+        __syncthreads();
+    }
+    for (int l = last - 1; l >= mg.nred; --l) {
+        const MgLevelDev &L = mg.lev[l];
+        const int n = L.n;
+        VT *x = sm + p.red_off[l], *xt = x + n, *b = xt + n;
+        const VT *xc = sm + p.red_off[l + 1];
+        const VT *A = Prec<VT>::la(L), *D = Prec<VT>::ld(L), *pw = Prec<VT>::lp(L);
+        for (int i = threadIdx.x; i < n; i += BLOCK) {
+            VT s = x[i];
+            for (int q = 0; q < 2; ++q) {
+                const int c = L.pc[2 * i + q];
+                if (c >= 0) s += pw[2 * i + q] * xc[c];
+            }
+            x[i] = s;
+        }
+        __syncthreads();
+        for (int s = 0; s < mg.nu2; ++s) {
+            for (int i = threadIdx.x; i < n; i += BLOCK)
+                xt[i] = x[i] + omega * D[i] * (b[i] - spmv_row<VT, false>(L.col, A, n, L.W, x, i));
+            __syncthreads();
+            for (int i = threadIdx.x; i < n; i += BLOCK) x[i] = xt[i];
+            __syncthreads();
+        }
+    }
+    // ---- parallel levels, up
+    for (int l = mg.nred - 1; l >= 0; --l) {
+        const MgLevelDev &L = mg.lev[l];
+        const int n = L.n;
+        VT *xa = gbuf + offs[l], *xb = xa + n;
+        VT *x = xcur[l], *xo = (x == xa) ? xb : xa;
+        const VT *b = bl[l];
+        const VT *A = Prec<VT>::la(L), *D = Prec<VT>::ld(L), *pw = Prec<VT>::lp(L);
+        const bool coarse_in_smem = (l + 1 == mg.nred);
+        const VT *xc = coarse_in_smem ? sm + p.red_off[l + 1] : xcur[l + 1];
+        if (!coarse_in_smem && !group_sync(bar, G, p.err)) return false;
+        int r0, r1;
+        own_rows(n, G, bi, r0, r1);
+        for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
+            VT s = x[i];
+            for (int q = 0; q < 2; ++q) {
+                const int c = L.pc[2 * i + q];
+                if (c >= 0) s += pw[2 * i + q] * (coarse_in_smem ? xc[c] : ldcg(&xc[c]));
+            }
+            x[i] = s;
+        }
+        for (int s = 0; s < mg.nu2; ++s) {
+            if (!group_sync(bar, G, p.err)) return false;
+            VT *dst = (l == 0 && s == mg.nu2 - 1) ? x0 : xo;
+            for (int i = r0 + threadIdx.x; i < r1; i += BLOCK)
+                dst[i] = x[i] + omega * D[i] * (ldcg(&b[i]) - spmv_row<VT, true>(L.col, A, n, L.W, x, i));
+            if (dst == x0) x = x0;
+            else { VT *t = x; x = xo; xo = t; }
+        }
+        if (l == 0 && x != x0)
+            for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) x0[i] = x[i];
+        xcur[l] = x;
+    }
+    return true;
+}
 
 template <typename VT>
 __global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
@@ -121,34 +322,39 @@ __global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
     double *g = sn + MAXM;                  // m+1
     double *y = g + MAXM + 1;               // m
     double *hcol = y + MAXM;                // m+2 (current column / scalars)
+    VT *msm = (VT *)(hcol + MAXM + 2);      // redundant multigrid levels
     __shared__ double red[MAXM + 2][NWARP];
     __shared__ int flag[4];
 
     const int grp = blockIdx.x / p.G, bi = blockIdx.x % p.G;
     if (grp >= p.groups) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned *bar = p.bar + 2 * grp;
     // two partial-sum buffers used alternately: a block can only refill a
-    // buffer after the next barrier, i.e. after every block has read it
+    // buffer after the next barrier, i.e. after every block has read it;
+    // layout [value][block] so one warp reads one value's partials coalesced
     double *part2 = p.part + (size_t)grp * 2 * p.G * (MAXM + 2);
     int parity = 0;
-    const int rpb = (n + p.G - 1) / p.G;
-    const int r0 = bi * rpb, r1 = min(n, r0 + rpb);
+    int r0, r1;
+    own_rows(n, p.G, bi, r0, r1);
     const int W = p.op.A.W;
     const int *col = p.op.A.col;
     const double *aval = p.op.A.val;
-    const VT *sval = scaled_vals<VT>(p.op);
+    const bool use_mg = p.op.mg.nlev > 0;
+    const VT *sval = use_mg ? Prec<VT>::a(p.op) : Prec<VT>::as(p.op);
     const double *dinv = p.op.dinv;
+    VT *gbuf = use_mg ? (VT *)p.mgbuf + (size_t)grp * p.mg_group_elems : nullptr;
 
-    // group-wide sum of K per-block values in red[.][0]: publish, barrier, reduce
     auto group_sum = [&](int K, double *out) -> bool {
         double *part = part2 + (size_t)parity * p.G * (MAXM + 2);
         parity ^= 1;
-        if (threadIdx.x < K) part[bi * (MAXM + 2) + threadIdx.x] = red[threadIdx.x][0];
+        if (threadIdx.x < K) part[(size_t)threadIdx.x * p.G + bi] = red[threadIdx.x][0];
         if (!group_sync(bar, p.G, p.err)) return false;
-        if (threadIdx.x < K) {
+        for (int l = warp; l < K; l += NWARP) {
             double s = 0.0;
-            for (int b = 0; b < p.G; ++b) s += ldcg(&part[b * (MAXM + 2) + threadIdx.x]);
-            out[threadIdx.x] = s;
+            for (int b = lane; b < p.G; b += 32) s += ldcg(&part[(size_t)l * p.G + b]);
+            s = warp_sum(s);
+            if (lane == 0) out[l] = s;
         }
         __syncthreads();
         return true;
@@ -158,21 +364,29 @@ __global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
     double my_rel = 0.0;
     // algorithmic bytes per owned row (minimal traffic, no re-reads):
     //   residual   W (col 4 B + val 8 B) + gathered x 8 + b 8 + r 8
-    //   Arnoldi j  W (col 4 + val es) + gathered v_j es + w es (write)
+    //   Arnoldi j  W (col 4 + val es) + gathered z_j es + w es (write)
     //              + (j+1) es (V reads, dots) + (j+1) es (V reads, update)
     //              + 2 es (w read/write) + 2 es (w read, v_{j+1} write)
-    //   correction jlast es (V reads) + 16 (x read/write) + 8 (1/diag)
-    const double es = (double)sizeof(VT), nrows = (double)(r1 > r0 ? r1 - r0 : 0);
+    //   V-cycle    per level and sweep: W (4 + es) + 4 es, plus transfers
+    //   correction jlast es (V or Z reads) + 16 (x read/write) + 8
+    const double es = (double)sizeof(VT), nrows = (double)(r1 - r0);
+    double mg_row_bytes = 0.0;
+    if (use_mg)
+        for (int l = 0; l < p.op.mg.nlev; ++l) {
+            const MgLevelDev &L = p.op.mg.lev[l];
+            const double frac = (double)L.n / (double)n;
+            mg_row_bytes += frac * ((p.op.mg.nu1 + p.op.mg.nu2 + 1) * (L.W * (4.0 + es) + 4.0 * es) + 4.0 * es);
+        }
     double my_bytes = 0.0;
 
     for (int v = grp; v < p.nv; v += p.groups) {
         const double *b = p.B + (size_t)v * p.ld;
         double *x = p.X + (size_t)v * p.ld;
         VT *V = (VT *)p.V + (size_t)v * (m + 1) * n;
+        VT *Z = use_mg ? (VT *)p.Z + (size_t)v * m * n : nullptr;
         VT *w = (VT *)p.Wv + (size_t)v * n;
         double *R = p.R + (size_t)v * n;
 
-        // ||b||
         double acc[MAXM + 2];
         acc[0] = 0.0;
         for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) { double t = b[i]; acc[0] += t * t; }
@@ -191,8 +405,7 @@ __global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
             if (!group_sync(bar, p.G, p.err)) return;
             acc[0] = 0.0;
             for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
-                double s = 0.0;
-                for (int k = 0; k < W; ++k) s += aval[(size_t)k * n + i] * ldcg(&x[col[(size_t)k * n + i]]);
+                double s = spmv_row<double, true>(col, aval, n, W, x, i);
                 double r = b[i] - s;
                 R[i] = r;
                 acc[0] += r * r;
@@ -217,12 +430,19 @@ __global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
             for (int j = 0; j < m; ++j) {
                 if (!group_sync(bar, p.G, p.err)) return;   // v_j complete
                 const VT *vj = V + (size_t)j * n;
-                // (1) w = (A D^-1) v_j and dots with v_0..v_j
+                const VT *zj = vj;
+                if (use_mg) {
+                    VT *zz = Z + (size_t)j * n;
+                    if (!vcycle<VT>(p, vj, zz, gbuf, msm, bar, bi)) return;
+                    if (!group_sync(bar, p.G, p.err)) return;   // z_j complete
+                    zj = zz;
+                    my_bytes += nrows * mg_row_bytes;
+                }
+                // (1) w = A z_j (Jacobi: (A D^-1) v_j) and dots with v_0..v_j
 #pragma unroll
                 for (int l = 0; l < MAXM + 2; ++l) acc[l] = 0.0;
                 for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
-                    VT s = 0;
-                    for (int k = 0; k < W; ++k) s += sval[(size_t)k * n + i] * ldcg(&vj[col[(size_t)k * n + i]]);
+                    const VT s = spmv_row<VT, true>(col, sval, n, W, zj, i);
                     w[i] = s;
 #pragma unroll
                     for (int l = 0; l < MAXM; ++l)
@@ -272,7 +492,7 @@ __global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
                 jlast = j + 1;
                 if (flag[0] || iters >= p.max_iter) break;
             }
-            // y = H^-1 g; x += D^-1 V y
+            // y = H^-1 g; x += D^-1 V y (Jacobi) or Z y (multigrid)
             if (threadIdx.x == 0) {
                 for (int l = jlast - 1; l >= 0; --l) {
                     double s = g[l];
@@ -283,8 +503,13 @@ __global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
             __syncthreads();
             for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
                 double s = 0.0;
-                for (int l = 0; l < jlast; ++l) s += y[l] * (double)V[(size_t)l * n + i];
-                x[i] += dinv[i] * s;
+                if (use_mg) {
+                    for (int l = 0; l < jlast; ++l) s += y[l] * (double)Z[(size_t)l * n + i];
+                    x[i] += s;
+                } else {
+                    for (int l = 0; l < jlast; ++l) s += y[l] * (double)V[(size_t)l * n + i];
+                    x[i] += dinv[i] * s;
+                }
             }
             my_bytes += nrows * (jlast * es + 24.0);
         }
@@ -308,92 +533,110 @@ __global__ void fold_err(const int *err, GmresStats *st) {
     if (*err) st->status = 2;
 }
 
-size_t smem_bytes() { return sizeof(double) * ((MAXM + 1) * MAXM + 2 * MAXM + (MAXM + 1) + MAXM + (MAXM + 2)); }
+size_t smem_gmres_bytes() { return sizeof(double) * ((MAXM + 1) * MAXM + 2 * MAXM + (MAXM + 1) + MAXM + (MAXM + 2)); }
 
-struct Layout { size_t v, w, r, part, bar, err, total; };
+// shared-memory element offsets of the redundant levels (x, xt, b, r each n)
+size_t smem_mg_elems(const MgDev &mg, int *offs) {
+    size_t e = 0;
+    for (int l = 0; l < MG_MAXLEV; ++l) offs[l] = 0;
+    for (int l = mg.nred; l < mg.nlev; ++l) {
+        offs[l] = (int)e;
+        e += 4 * (size_t)mg.lev[l].n;
+    }
+    return e;
+}
 
-Layout layout(int n, int nv, int m, Precision prec, int groups_cap) {
+size_t mg_group_elems(const MgDev &mg) {
+    size_t e = 0;
+    for (int l = 0; l < mg.nred; ++l) e += 4 * (size_t)mg.lev[l].n;
+    return e;
+}
+
+constexpr int GROUPS_CAP = 4096;
+
+struct Layout { size_t v, z, w, r, mg, part, bar, err, total; };
+
+Layout layout(const DevSolveOp &op, int nv, int m, Precision prec) {
     Layout L;
+    const int n = op.A.n;
     size_t es = prec == PREC_MIXED ? 4 : 8;
     auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const bool mg = op.mg.nlev > 0;
     L.v = 0;
-    L.w = L.v + al(es * (size_t)nv * (m + 1) * n);
+    L.z = L.v + al(es * (size_t)nv * (m + 1) * n);
+    L.w = L.z + (mg ? al(es * (size_t)nv * m * n) : 0);
     L.r = L.w + al(es * (size_t)nv * n);
-    L.part = L.r + al(8 * (size_t)nv * n);
-    L.bar = L.part + al(8 * (size_t)groups_cap * 2 * (MAXM + 2));
-    L.err = L.bar + al(8 * (size_t)groups_cap);
+    L.mg = L.r + al(8 * (size_t)nv * n);
+    const int groups = nv < GROUPS_CAP ? nv : GROUPS_CAP;
+    L.part = L.mg + (mg ? al(es * mg_group_elems(op.mg) * (size_t)groups) : 0);
+    // groups * G <= co-resident blocks (< 4096)
+    L.bar = L.part + al(8 * (size_t)4096 * 2 * (MAXM + 2));
+    L.err = L.bar + al(8 * (size_t)GROUPS_CAP);
     L.total = L.err + 256;
     return L;
 }
 
-int g_capacity = 0;   // co-resident blocks of the solver kernel on this device
 int g_sms = 0;
 
-int capacity() {
-    if (!g_capacity) {
-        int dev = 0, sms = 0, per = 0;
+int sm_count() {
+    if (!g_sms) {
+        int dev = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaFuncSetAttribute(gmres_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes());
-        cudaFuncSetAttribute(gmres_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes());
-        int a = 0, b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, gmres_kernel<double>, BLOCK, smem_bytes());
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, gmres_kernel<float>, BLOCK, smem_bytes());
-        per = a < b ? a : b;
-        if (per < 1) per = 1;
-        g_sms = sms;
-        g_capacity = sms * per;
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
     }
-    return g_capacity;
+    return g_sms;
 }
 
-int rows_per_block_target() {
-    static int v = -1;
-    if (v < 0) {
-        const char *e = getenv("PHG_ROWS_PER_BLOCK");
-        v = e ? atoi(e) : 512;
-        if (v < 32) v = 32;
-    }
-    return v;
+int env_int(const char *name, int dflt) {
+    const char *e = getenv(name);
+    return e ? atoi(e) : dflt;
 }
 
 }  // namespace
 
-size_t gmres_work_bytes(int n, int nv, int m, Precision p) {
-    return layout(n, nv, m, p, 4096).total;
-}
+size_t gmres_work_bytes(const DevSolveOp &op, int nv, int m, Precision p) { return layout(op, nv, m, p).total; }
 
 cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv, int ld,
                         int m, int max_iter, double tol, Precision prec,
                         void *work, GmresStats *stats_dev, cudaStream_t s) {
     if (m < 1 || m > MAXM || nv < 1) return cudaErrorInvalidValue;
     const int n = op.A.n;
-    const int cap = capacity();
-    int Gt = (n + rows_per_block_target() - 1) / rows_per_block_target();
+    Params p;
+    int offs[MG_MAXLEV];
+    const size_t es = prec == PREC_MIXED ? 4 : 8;
+    const size_t smem = smem_gmres_bytes() + es * smem_mg_elems(op.mg, offs) + 16;
+    if (smem > 227 * 1024) return cudaErrorInvalidValue;
+    void *fn = prec == PREC_MIXED ? (void *)gmres_kernel<float> : (void *)gmres_kernel<double>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, BLOCK, smem);
+    if (e != cudaSuccess) return e;
+    if (per < 1) return cudaErrorInvalidConfiguration;
+    const int cap = sm_count() * per;
+    const int rpb = env_int("PHG_ROWS_PER_BLOCK", op.mg.nlev > 0 ? 384 : 512);
+    int Gt = (n + rpb - 1) / (rpb > 32 ? rpb : 32);
     if (Gt < 1) Gt = 1;
     if (Gt > cap) Gt = cap;
     int groups = cap / Gt;
     if (groups > nv) groups = nv;
-    if (groups > 4096) groups = 4096;
+    if (groups > GROUPS_CAP) groups = GROUPS_CAP;
     if (groups < 1) groups = 1;
     int G = cap / groups;
     if (G > Gt) G = Gt;
-    Layout L = layout(n, nv, m, prec, 4096);
+    Layout L = layout(op, nv, m, prec);
     char *w = (char *)work;
-    Params p;
     p.op = op; p.B = B; p.X = X; p.n = n; p.nv = nv; p.ld = ld; p.m = m; p.max_iter = max_iter; p.tol = tol;
-    p.V = w + L.v; p.Wv = w + L.w; p.R = (double *)(w + L.r); p.part = (double *)(w + L.part);
+    p.V = w + L.v; p.Z = w + L.z; p.Wv = w + L.w; p.R = (double *)(w + L.r);
+    p.mgbuf = w + L.mg; p.mg_group_elems = mg_group_elems(op.mg);
+    p.part = (double *)(w + L.part);
     p.bar = (unsigned *)(w + L.bar); p.err = (int *)(w + L.err); p.stats = stats_dev;
     p.groups = groups; p.G = G;
-    cudaError_t e;
+    for (int l = 0; l < MG_MAXLEV; ++l) p.red_off[l] = offs[l];
     if ((e = cudaMemsetAsync(w + L.bar, 0, L.total - L.bar, s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(stats_dev, 0, sizeof(GmresStats), s)) != cudaSuccess) return e;
     void *args[] = {&p};
-    dim3 grid(groups * G), block(BLOCK);
-    if (prec == PREC_MIXED)
-        e = cudaLaunchCooperativeKernel((void *)gmres_kernel<float>, grid, block, args, smem_bytes(), s);
-    else
-        e = cudaLaunchCooperativeKernel((void *)gmres_kernel<double>, grid, block, args, smem_bytes(), s);
+    e = cudaLaunchCooperativeKernel(fn, dim3(groups * G), dim3(BLOCK), args, smem, s);
     if (e != cudaSuccess) return e;
     g_kernel_launches += 2;
     // a barrier timeout lands in stats->status (2)

@@ -23,6 +23,10 @@ struct Mesh {
     std::vector<int> bnd;      // V (1 = boundary)
     std::vector<int> inner, outer, p2io;
     std::vector<int> adj_ptr, adj;  // point -> triangles, ascending triangle id
+    // generated meshes only: refinement history for multigrid
+    std::vector<int> orig;          // point -> index before the Cuthill-McKee reorder
+    std::vector<int> par_a, par_b;  // pre-reorder index -> endpoints (pre-reorder, level-1
+                                    // numbering) of the coarse edge it bisects; -1 for coarse points
 
     double u(int p, int z) const { return uv[8 * (size_t)p + 2 * z]; }
     double v(int p, int z) const { return uv[8 * (size_t)p + 2 * z + 1]; }
@@ -72,6 +76,20 @@ struct SphereOps {
 };
 
 void assemble_sphere(const Mesh &m, SphereOps &ops);
+// only the Laplacian (slaplace form), rs x rs
+void assemble_laplacian(const Mesh &m, Csr &lapl);
+
+// Geometric multigrid hierarchy over the nested icosahedral meshes: level 0
+// is the mesh itself, level k+1 the mesh one refinement coarser.  P[k] maps
+// level k+1 inner values to level k inner points (1 at coincident points,
+// 1/2 at both ends of the bisected edge; boundary columns dropped) and R[k]
+// = P[k]^T; A[k] is the Laplacian re-assembled on level k (A[0] unused).
+struct MgHierarchy {
+    std::vector<Mesh> mesh;        // mesh[0] unused (the caller's mesh)
+    std::vector<Csr> A, P, R;
+    std::vector<double> coarse_inv;  // dense inverse of the coarsest A (row-major)
+};
+bool build_mg(const Mesh &fine, int coarsest_level, MgHierarchy &h, std::string &err);
 // BarVortex forward matrix c1 * mass + c2 * slaplace (examples/barvortex_impl.h:57-78)
 void assemble_barvortex(const Mesh &m, double c1, double c2, Csr &A, Csr &Abnd);
 // Baroclin 4rs x 4rs block matrix (examples/baroclin.cpp:119-180) and the

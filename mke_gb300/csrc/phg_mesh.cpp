@@ -76,7 +76,11 @@ bool generate_sphere(int level, Mesh &m, std::string &err) {
                            5, 0, 2, 10, 5, 7, 1, 6, 8, 1, 8, 10, 6, 1, 3, 11, 7, 5};
     for (auto &p : pts) to_sphere(p);
 
+    std::vector<int> par_a(12, -1), par_b(12, -1);
     for (int it = 0; it < level; ++it) {
+        const int V_old = (int)pts.size();
+        par_a.assign(V_old, -1);
+        par_b.assign(V_old, -1);
         std::unordered_map<long long, int> mid;
         mid.reserve(tr.size());
         std::vector<int> out;
@@ -90,6 +94,8 @@ bool generate_sphere(int level, Mesh &m, std::string &err) {
             to_sphere(p);
             int id = (int)pts.size();
             pts.push_back(p);
+            par_a.push_back(a);
+            par_b.push_back(b);
             mid.emplace(key, id);
             return id;
         };
@@ -167,6 +173,10 @@ bool generate_sphere(int level, Mesh &m, std::string &err) {
         m.tz[t] = zone - 1;
     }
     finish_mesh(m);
+    m.orig.assign(V, 0);
+    for (int i = 0; i < V; ++i) m.orig[perm[i]] = i;
+    m.par_a = par_a;
+    m.par_b = par_b;
     return true;
 }
 
