@@ -306,7 +306,7 @@ int build_mg_dev(phg_ops_s *o, const Mesh &m, SolveOpBufs &Lb, MgBufs &mb, int p
     mg.nu1 = env_int("PHG_MG_NU", 2);
     mg.nu2 = mg.nu1;
     const size_t es = prec == PHG_MIXED ? 4 : 8;
-    const int red_max = env_int("PHG_MG_REDUNDANT", 3000);
+    const int red_max = env_int("PHG_MG_REDUNDANT", 700);
     // shared memory: the solver's own ~21 KB plus 4 vectors per redundant level
     const size_t smem_cap = 200 * 1024;
     int nred = nlev - 1;

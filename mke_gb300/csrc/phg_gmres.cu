@@ -58,16 +58,26 @@ struct Params {
     GmresStats *stats;
     int groups, G;
     int red_off[MG_MAXLEV];  // shared-memory offsets (elements) of the redundant levels
+    long long *timers;       // optional phase cycle counters (block 0), see PHASES
 };
+
+// phase cycle counters kept by block 0 when PHG_PHASE_TIMING is set
+enum { T_RESID, T_VCYCLE, T_SPMV_DOT, T_DOT_SUM, T_UPDATE, T_NORM_SUM, T_GIVENS, T_CORR, T_BARRIER,
+       T_BARRIERS, T_TOTAL, T_NPHASE };
+__device__ long long g_bar_cycles;  // barrier wait of block 0 (debug timing only)
 
 __device__ __forceinline__ unsigned ld_volatile(const unsigned *p) { return *(const volatile unsigned *)p; }
 __device__ __forceinline__ int ld_volatile(const int *p) { return *(const volatile int *)p; }
 
 // Barrier over the G blocks of one group; false if the grid is aborting.
-__device__ bool group_sync(unsigned *bar, int G, int *err) {
+__device__ bool group_sync(unsigned *bar, int G, int *err, long long *tm = nullptr) {
     __shared__ int ok;
+    long long tb = (tm && threadIdx.x == 0) ? clock64() : 0;
     __syncthreads();
-    if (G == 1) return ld_volatile(err) == 0;
+    if (G == 1) {
+        if (tm && threadIdx.x == 0) { tm[T_BARRIER] += clock64() - tb; tm[T_BARRIERS]++; }
+        return ld_volatile(err) == 0;
+    }
     if (threadIdx.x == 0) {
         ok = 1;
         unsigned *cnt = bar, *gen = bar + 1;
@@ -83,11 +93,11 @@ __device__ bool group_sync(unsigned *bar, int G, int *err) {
             while (ld_volatile(gen) == my) {
                 if (ld_volatile(err)) { ok = 0; break; }
                 if (clock64() - t0 > SPIN_LIMIT) { atomicExch(err, 1); ok = 0; break; }
-                __nanosleep(20);
             }
         }
         __threadfence();
         if (ld_volatile(err)) ok = 0;
+        if (tm) { tm[T_BARRIER] += clock64() - tb; tm[T_BARRIERS]++; }
     }
     __syncthreads();
     return ok;
@@ -100,22 +110,22 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// block-reduce K values held per thread in acc[0..K-1], result in red[l][0]
+// block-reduce K values held per thread in acc[0..K-1], result in red[off + l][0]
 template <int KMAX>
-__device__ void block_reduce(double (&acc)[KMAX], int K, double (*red)[NWARP]) {
+__device__ void block_reduce(double (&acc)[KMAX], int K, double (*red)[NWARP], int off = 0) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int l = 0; l < KMAX; ++l) {
         if (l < K) {
             double v = warp_sum(acc[l]);
-            if (lane == 0) red[l][warp] = v;
+            if (lane == 0) red[off + l][warp] = v;
         }
     }
     __syncthreads();
     if (threadIdx.x < K) {
         double s = 0.0;
-        for (int w = 0; w < NWARP; ++w) s += red[threadIdx.x][w];
-        red[threadIdx.x][0] = s;
+        for (int w = 0; w < NWARP; ++w) s += red[off + threadIdx.x][w];
+        red[off + threadIdx.x][0] = s;
     }
     __syncthreads();
 }
@@ -147,10 +157,27 @@ __device__ __forceinline__ void own_rows(int n, int G, int bi, int &r0, int &r1)
     r1 = min(n, r0 + rpb);
 }
 
-// sum_k A[k][i] x[col]; CG: x read through L2 (written by other blocks)
+// sum_k A[k][i] x[col]; CG: x read through L2 (written by other blocks).
+// All column/value loads of the row are issued together, then all gathers
+// (one memory round trip each instead of one per entry); rows of up to 8
+// entries take this path, wider rows fall back to a plain loop.
 template <typename VT, bool CG>
 __device__ __forceinline__ VT spmv_row(const int *col, const VT *val, int n, int W, const VT *x, int i) {
     VT s = 0;
+    if (W <= 8) {
+        int c[8];
+        VT a[8], xv[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < W) { c[k] = __ldg(&col[(size_t)k * n + i]); a[k] = __ldg(&val[(size_t)k * n + i]); }
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < W) xv[k] = CG ? ldcg(&x[c[k]]) : x[c[k]];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < W) s += a[k] * xv[k];
+        return s;
+    }
     for (int k = 0; k < W; ++k) {
         const size_t e = (size_t)k * n + i;
         const VT xv = CG ? ldcg(&x[__ldg(&col[e])]) : x[__ldg(&col[e])];
@@ -162,6 +189,20 @@ __device__ __forceinline__ VT spmv_row(const int *col, const VT *val, int n, int
 template <typename VT>
 __device__ __forceinline__ VT restrict_row(const MgLevelDev &L, const VT *rw, int nc, const VT *r, int c, bool cg) {
     VT s = 0;
+    if (L.Wr <= 8) {
+        int f[8];
+        VT w[8], rv[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (q < L.Wr) { f[q] = __ldg(&L.rf[(size_t)q * nc + c]); w[q] = __ldg(&rw[(size_t)q * nc + c]); }
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (q < L.Wr) rv[q] = f[q] >= 0 ? (cg ? ldcg(&r[f[q]]) : r[f[q]]) : (VT)0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (q < L.Wr && f[q] >= 0) s += w[q] * rv[q];
+        return s;
+    }
     for (int q = 0; q < L.Wr; ++q) {
         const int f = L.rf[(size_t)q * nc + c];
         if (f >= 0) s += rw[(size_t)q * nc + c] * (cg ? ldcg(&r[f]) : r[f]);
@@ -169,10 +210,30 @@ __device__ __forceinline__ VT restrict_row(const MgLevelDev &L, const VT *rw, in
     return s;
 }
 
+// rows [r0, r1) of this thread, four at a time: every value is computed
+// (all loads issued) before any store, so four rows' memory round trips
+// overlap even when the output may alias the inputs.
+template <typename VT, typename F, typename S>
+__device__ __forceinline__ void rows4(int r0, int r1, F &&compute, S &&store) {
+    for (int i0 = r0 + threadIdx.x; i0 < r1; i0 += 4 * BLOCK) {
+        VT v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int i = i0 + q * BLOCK;
+            v[q] = i < r1 ? compute(i) : (VT)0;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int i = i0 + q * BLOCK;
+            if (i < r1) store(i, v[q]);
+        }
+    }
+}
+
 // Damped-Jacobi V-cycle: x0 = M^-1 b0 for the group's right-hand side.
 // Returns false if the grid is aborting.
 template <typename VT>
-__device__ bool vcycle(const Params &p, const VT *b0, VT *x0, VT *gbuf, VT *sm, unsigned *bar, int bi) {
+__device__ __noinline__ bool vcycle(const Params &p, const VT *b0, VT *x0, VT *gbuf, VT *sm, unsigned *bar, int bi) {
     const MgDev &mg = p.op.mg;
     const int G = p.G;
     const VT omega = (VT)mg.omega;
@@ -196,16 +257,16 @@ __device__ bool vcycle(const Params &p, const VT *b0, VT *x0, VT *gbuf, VT *sm, 
         VT *x = xa, *xo = xb;
         for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) x[i] = omega * D[i] * ldcg(&b[i]);
         for (int s = 1; s < mg.nu1; ++s) {
-            if (!group_sync(bar, G, p.err)) return false;
+            if (!group_sync(bar, G, p.err, p.timers && blockIdx.x == 0 ? p.timers : nullptr)) return false;
             for (int i = r0 + threadIdx.x; i < r1; i += BLOCK)
                 xo[i] = x[i] + omega * D[i] * (ldcg(&b[i]) - spmv_row<VT, true>(L.col, A, n, L.W, x, i));
             VT *t = x; x = xo; xo = t;
         }
-        if (!group_sync(bar, G, p.err)) return false;
+        if (!group_sync(bar, G, p.err, p.timers && blockIdx.x == 0 ? p.timers : nullptr)) return false;
         for (int i = r0 + threadIdx.x; i < r1; i += BLOCK)
             r[i] = ldcg(&b[i]) - spmv_row<VT, true>(L.col, A, n, L.W, x, i);
         xcur[l] = x;
-        if (!group_sync(bar, G, p.err)) return false;
+        if (!group_sync(bar, G, p.err, p.timers && blockIdx.x == 0 ? p.timers : nullptr)) return false;
         const MgLevelDev &C = mg.lev[l + 1];
         const VT *rw = Prec<VT>::lr(L);
         if (l + 1 < mg.nred) {
@@ -226,30 +287,39 @@ __device__ bool vcycle(const Params &p, const VT *b0, VT *x0, VT *gbuf, VT *sm, 
         const int n = L.n;
         VT *x = sm + p.red_off[l], *xt = x + n, *b = xt + n, *r = b + n;
         const VT *A = Prec<VT>::la(L), *D = Prec<VT>::ld(L);
-        for (int i = threadIdx.x; i < n; i += BLOCK) x[i] = omega * D[i] * b[i];
+        rows4<VT>(0, n, [&](int i) { return omega * __ldg(&D[i]) * b[i]; }, [&](int i, VT v) { x[i] = v; });
         __syncthreads();
         for (int s = 1; s < mg.nu1; ++s) {
-            for (int i = threadIdx.x; i < n; i += BLOCK)
-                xt[i] = x[i] + omega * D[i] * (b[i] - spmv_row<VT, false>(L.col, A, n, L.W, x, i));
+            rows4<VT>(0, n, [&](int i) { return x[i] + omega * __ldg(&D[i]) * (b[i] - spmv_row<VT, false>(L.col, A, n, L.W, x, i)); },
+                      [&](int i, VT v) { xt[i] = v; });
             __syncthreads();
             for (int i = threadIdx.x; i < n; i += BLOCK) x[i] = xt[i];
             __syncthreads();
         }
-        for (int i = threadIdx.x; i < n; i += BLOCK) r[i] = b[i] - spmv_row<VT, false>(L.col, A, n, L.W, x, i);
+        rows4<VT>(0, n, [&](int i) { return b[i] - spmv_row<VT, false>(L.col, A, n, L.W, x, i); },
+                  [&](int i, VT v) { r[i] = v; });
         __syncthreads();
         VT *cb = sm + p.red_off[l + 1] + 2 * C.n;
         const VT *rw = Prec<VT>::lr(L);
-        for (int c = threadIdx.x; c < C.n; c += BLOCK) cb[c] = restrict_row<VT>(L, rw, C.n, r, c, false);
+        rows4<VT>(0, C.n, [&](int c) { return restrict_row<VT>(L, rw, C.n, r, c, false); }, [&](int c, VT v) { cb[c] = v; });
         __syncthreads();
     }
-    {   // coarsest: dense inverse
+    {   // coarsest: dense inverse, four independent partial sums per row
         const int n = mg.nc;
         VT *x = sm + p.red_off[last], *b = x + 2 * n;
         const VT *Ci = Prec<VT>::ci(mg);
         for (int i = threadIdx.x; i < n; i += BLOCK) {
-            VT s = 0;
-            for (int j = 0; j < n; ++j) s += Ci[(size_t)i * n + j] * b[j];
-            x[i] = s;
+            VT s4[4] = {0, 0, 0, 0};
+            int j = 0;
+            for (; j + 4 <= n; j += 4) {
+                VT c[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) c[q] = __ldg(&Ci[(size_t)i * n + j + q]);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) s4[q] += c[q] * b[j + q];
+            }
+            for (; j < n; ++j) s4[0] += __ldg(&Ci[(size_t)i * n + j]) * b[j];
+            x[i] = (s4[0] + s4[1]) + (s4[2] + s4[3]);
         }
         __syncthreads();
     }
@@ -259,18 +329,18 @@ __device__ bool vcycle(const Params &p, const VT *b0, VT *x0, VT *gbuf, VT *sm, 
         VT *x = sm + p.red_off[l], *xt = x + n, *b = xt + n;
         const VT *xc = sm + p.red_off[l + 1];
         const VT *A = Prec<VT>::la(L), *D = Prec<VT>::ld(L), *pw = Prec<VT>::lp(L);
-        for (int i = threadIdx.x; i < n; i += BLOCK) {
+        rows4<VT>(0, n, [&](int i) {
             VT s = x[i];
             for (int q = 0; q < 2; ++q) {
-                const int c = L.pc[2 * i + q];
-                if (c >= 0) s += pw[2 * i + q] * xc[c];
+                const int c = __ldg(&L.pc[2 * i + q]);
+                if (c >= 0) s += __ldg(&pw[2 * i + q]) * xc[c];
             }
-            x[i] = s;
-        }
+            return s;
+        }, [&](int i, VT v) { x[i] = v; });
         __syncthreads();
         for (int s = 0; s < mg.nu2; ++s) {
-            for (int i = threadIdx.x; i < n; i += BLOCK)
-                xt[i] = x[i] + omega * D[i] * (b[i] - spmv_row<VT, false>(L.col, A, n, L.W, x, i));
+            rows4<VT>(0, n, [&](int i) { return x[i] + omega * __ldg(&D[i]) * (b[i] - spmv_row<VT, false>(L.col, A, n, L.W, x, i)); },
+                      [&](int i, VT v) { xt[i] = v; });
             __syncthreads();
             for (int i = threadIdx.x; i < n; i += BLOCK) x[i] = xt[i];
             __syncthreads();
@@ -286,7 +356,7 @@ __device__ bool vcycle(const Params &p, const VT *b0, VT *x0, VT *gbuf, VT *sm, 
         const VT *A = Prec<VT>::la(L), *D = Prec<VT>::ld(L), *pw = Prec<VT>::lp(L);
         const bool coarse_in_smem = (l + 1 == mg.nred);
         const VT *xc = coarse_in_smem ? sm + p.red_off[l + 1] : xcur[l + 1];
-        if (!coarse_in_smem && !group_sync(bar, G, p.err)) return false;
+        if (!coarse_in_smem && !group_sync(bar, G, p.err, p.timers && blockIdx.x == 0 ? p.timers : nullptr)) return false;
         int r0, r1;
         own_rows(n, G, bi, r0, r1);
         for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
@@ -298,7 +368,7 @@ __device__ bool vcycle(const Params &p, const VT *b0, VT *x0, VT *gbuf, VT *sm, 
             x[i] = s;
         }
         for (int s = 0; s < mg.nu2; ++s) {
-            if (!group_sync(bar, G, p.err)) return false;
+            if (!group_sync(bar, G, p.err, p.timers && blockIdx.x == 0 ? p.timers : nullptr)) return false;
             VT *dst = (l == 0 && s == mg.nu2 - 1) ? x0 : xo;
             for (int i = r0 + threadIdx.x; i < r1; i += BLOCK)
                 dst[i] = x[i] + omega * D[i] * (ldcg(&b[i]) - spmv_row<VT, true>(L.col, A, n, L.W, x, i));
@@ -313,7 +383,7 @@ __device__ bool vcycle(const Params &p, const VT *b0, VT *x0, VT *gbuf, VT *sm, 
 }
 
 template <typename VT>
-__global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
+__global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(Params p) {
     extern __shared__ double smem[];
     const int m = p.m, n = p.n;
     double *H = smem;                       // (m+1) x m
@@ -344,12 +414,17 @@ __global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
     const VT *sval = use_mg ? Prec<VT>::a(p.op) : Prec<VT>::as(p.op);
     const double *dinv = p.op.dinv;
     VT *gbuf = use_mg ? (VT *)p.mgbuf + (size_t)grp * p.mg_group_elems : nullptr;
+    long long *tm = (p.timers && blockIdx.x == 0) ? p.timers : nullptr;
+    long long t_start = clock64(), tph = 0;
+    auto tick = [&](int ph) {
+        if (tm && threadIdx.x == 0) { long long t = clock64(); tm[ph] += t - tph; tph = t; }
+    };
 
     auto group_sum = [&](int K, double *out) -> bool {
         double *part = part2 + (size_t)parity * p.G * (MAXM + 2);
         parity ^= 1;
         if (threadIdx.x < K) part[(size_t)threadIdx.x * p.G + bi] = red[threadIdx.x][0];
-        if (!group_sync(bar, p.G, p.err)) return false;
+        if (!group_sync(bar, p.G, p.err, tm)) return false;
         for (int l = warp; l < K; l += NWARP) {
             double s = 0.0;
             for (int b = lane; b < p.G; b += 32) s += ldcg(&part[(size_t)l * p.G + b]);
@@ -387,10 +462,10 @@ __global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
         VT *w = (VT *)p.Wv + (size_t)v * n;
         double *R = p.R + (size_t)v * n;
 
-        double acc[MAXM + 2];
+        double acc[1];
         acc[0] = 0.0;
         for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) { double t = b[i]; acc[0] += t * t; }
-        block_reduce<MAXM + 2>(acc, 1, red);
+        block_reduce<1>(acc, 1, red);
         if (!group_sum(1, hcol)) return;
         const double bnorm = sqrt(hcol[0]);
         int iters = 0, cycles = 0, status = 1;
@@ -398,11 +473,12 @@ __global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
         if (bnorm == 0.0) {
             for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) x[i] = 0.0;
             status = 0; rel = 0.0;
-            if (!group_sync(bar, p.G, p.err)) return;
+            if (!group_sync(bar, p.G, p.err, tm)) return;
         }
         while (bnorm != 0.0) {
             // r = b - A x (FP64, exact operator); needs all of x
-            if (!group_sync(bar, p.G, p.err)) return;
+            if (!group_sync(bar, p.G, p.err, tm)) return;
+            if (tm && threadIdx.x == 0) tph = clock64();
             acc[0] = 0.0;
             for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
                 double s = spmv_row<double, true>(col, aval, n, W, x, i);
@@ -410,9 +486,10 @@ __global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
                 R[i] = r;
                 acc[0] += r * r;
             }
-            block_reduce<MAXM + 2>(acc, 1, red);
+            block_reduce<1>(acc, 1, red);
             if (!group_sum(1, hcol)) return;
             const double beta = sqrt(hcol[0]);
+            tick(T_RESID);
             my_bytes += nrows * (W * 12.0 + 24.0);
             rel = beta / bnorm;
             if (rel <= p.tol) { status = 0; break; }
@@ -428,39 +505,56 @@ __global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
             }
             int jlast = 0;
             for (int j = 0; j < m; ++j) {
-                if (!group_sync(bar, p.G, p.err)) return;   // v_j complete
+                if (!group_sync(bar, p.G, p.err, tm)) return;   // v_j complete
+                if (tm && threadIdx.x == 0) tph = clock64();
                 const VT *vj = V + (size_t)j * n;
                 const VT *zj = vj;
                 if (use_mg) {
                     VT *zz = Z + (size_t)j * n;
                     if (!vcycle<VT>(p, vj, zz, gbuf, msm, bar, bi)) return;
-                    if (!group_sync(bar, p.G, p.err)) return;   // z_j complete
+                    if (!group_sync(bar, p.G, p.err, tm)) return;   // z_j complete
+                    tick(T_VCYCLE);
                     zj = zz;
                     my_bytes += nrows * mg_row_bytes;
                 }
-                // (1) w = A z_j (Jacobi: (A D^-1) v_j) and dots with v_0..v_j
+                // (1) w = A z_j (Jacobi: (A D^-1) v_j), then the dots with
+                // v_0..v_j eight basis vectors at a time (8 loads in flight)
+                for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) w[i] = spmv_row<VT, true>(col, sval, n, W, zj, i);
+                for (int l0 = 0; l0 <= j; l0 += 8) {
+                    double a8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                    for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
+                        const VT s = w[i];
+                        VT vv[8];
 #pragma unroll
-                for (int l = 0; l < MAXM + 2; ++l) acc[l] = 0.0;
-                for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
-                    const VT s = spmv_row<VT, true>(col, sval, n, W, zj, i);
-                    w[i] = s;
+                        for (int q = 0; q < 8; ++q) vv[q] = (l0 + q <= j) ? V[(size_t)(l0 + q) * n + i] : (VT)0;
 #pragma unroll
-                    for (int l = 0; l < MAXM; ++l)
-                        if (l <= j) acc[l] += (double)(V[(size_t)l * n + i] * s);
+                        for (int q = 0; q < 8; ++q) a8[q] += (double)(vv[q] * s);
+                    }
+                    block_reduce<8>(a8, min(8, j + 1 - l0), red, l0);
                 }
-                block_reduce<MAXM + 2>(acc, j + 1, red);
+                tick(T_SPMV_DOT);
                 if (!group_sum(j + 1, hcol)) return;
+                tick(T_DOT_SUM);
                 // (2) w -= sum h_l v_l, ||w||^2
                 double a2 = 0.0;
                 for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
                     VT s = w[i];
-                    for (int l = 0; l <= j; ++l) s -= (VT)hcol[l] * V[(size_t)l * n + i];
+                    for (int l0 = 0; l0 <= j; l0 += 8) {
+                        VT vv[8];
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) vv[q] = (l0 + q <= j) ? V[(size_t)(l0 + q) * n + i] : (VT)0;
+#pragma unroll
+                        for (int q = 0; q < 8; ++q)
+                            if (l0 + q <= j) s -= (VT)hcol[l0 + q] * vv[q];
+                    }
                     w[i] = s;
                     a2 += (double)s * (double)s;
                 }
                 acc[0] = a2;
-                block_reduce<MAXM + 2>(acc, 1, red);
+                block_reduce<1>(acc, 1, red);
+                tick(T_UPDATE);
                 if (!group_sum(1, hcol + j + 1)) return;
+                tick(T_NORM_SUM);
                 const double hn = sqrt(hcol[j + 1]);
                 // (3) v_{j+1}, Givens
                 if (hn > 0.0) {
@@ -486,6 +580,7 @@ __global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
                     flag[0] = (fabs(g[j + 1]) <= target) || hn == 0.0;
                 }
                 __syncthreads();
+                tick(T_GIVENS);
                 ++iters;
                 ++my_steps;
                 my_bytes += nrows * (W * (4.0 + es) + es * (2.0 * (j + 1) + 6.0));
@@ -502,22 +597,27 @@ __global__ void __launch_bounds__(BLOCK) gmres_kernel(Params p) {
             }
             __syncthreads();
             for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
+                const VT *B = use_mg ? Z : V;
                 double s = 0.0;
-                if (use_mg) {
-                    for (int l = 0; l < jlast; ++l) s += y[l] * (double)Z[(size_t)l * n + i];
-                    x[i] += s;
-                } else {
-                    for (int l = 0; l < jlast; ++l) s += y[l] * (double)V[(size_t)l * n + i];
-                    x[i] += dinv[i] * s;
+                for (int l0 = 0; l0 < jlast; l0 += 8) {
+                    VT vv[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) vv[q] = (l0 + q < jlast) ? B[(size_t)(l0 + q) * n + i] : (VT)0;
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        if (l0 + q < jlast) s += y[l0 + q] * (double)vv[q];
                 }
+                x[i] += use_mg ? s : dinv[i] * s;
             }
             my_bytes += nrows * (jlast * es + 24.0);
+            tick(T_CORR);
         }
         my_iters = max(my_iters, iters);
         my_cycles = max(my_cycles, cycles);
         my_rel = fmax(my_rel, rel);
         my_status = max(my_status, status);
     }
+    if (tm && threadIdx.x == 0) tm[T_TOTAL] += clock64() - t_start;
     if (threadIdx.x == 0) atomicAdd(&p.stats->bytes, my_bytes);
     if (threadIdx.x == 0 && bi == 0) {
         atomicAdd(&p.stats->steps_total, my_steps);
@@ -614,16 +714,15 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     if (e != cudaSuccess) return e;
     if (per < 1) return cudaErrorInvalidConfiguration;
     const int cap = sm_count() * per;
-    const int rpb = env_int("PHG_ROWS_PER_BLOCK", op.mg.nlev > 0 ? 384 : 512);
-    int Gt = (n + rpb - 1) / (rpb > 32 ? rpb : 32);
-    if (Gt < 1) Gt = 1;
-    if (Gt > cap) Gt = cap;
-    int groups = cap / Gt;
-    if (groups > nv) groups = nv;
+    // as many right-hand sides in flight as there are blocks; the blocks are
+    // shared out evenly, but no block gets fewer than `rpb` rows
+    const int rpb = env_int("PHG_ROWS_PER_BLOCK", 256);
+    int groups = nv < cap ? nv : cap;
     if (groups > GROUPS_CAP) groups = GROUPS_CAP;
-    if (groups < 1) groups = 1;
     int G = cap / groups;
-    if (G > Gt) G = Gt;
+    const int Gmax = (n + rpb - 1) / (rpb > 32 ? rpb : 32);
+    if (G > Gmax) G = Gmax;
+    if (G < 1) G = 1;
     Layout L = layout(op, nv, m, prec);
     char *w = (char *)work;
     p.op = op; p.B = B; p.X = X; p.n = n; p.nv = nv; p.ld = ld; p.m = m; p.max_iter = max_iter; p.tol = tol;
@@ -633,6 +732,11 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     p.bar = (unsigned *)(w + L.bar); p.err = (int *)(w + L.err); p.stats = stats_dev;
     p.groups = groups; p.G = G;
     for (int l = 0; l < MG_MAXLEV; ++l) p.red_off[l] = offs[l];
+    static long long *timers = nullptr;
+    const bool timing = getenv("PHG_PHASE_TIMING") != nullptr;
+    if (timing && !timers) cudaMalloc(&timers, sizeof(long long) * T_NPHASE);
+    p.timers = timing ? timers : nullptr;
+    if (timing) cudaMemsetAsync(timers, 0, sizeof(long long) * T_NPHASE, s);
     if ((e = cudaMemsetAsync(w + L.bar, 0, L.total - L.bar, s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(stats_dev, 0, sizeof(GmresStats), s)) != cudaSuccess) return e;
     void *args[] = {&p};
@@ -641,6 +745,19 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     g_kernel_launches += 2;
     // a barrier timeout lands in stats->status (2)
     fold_err<<<1, 1, 0, s>>>(p.err, stats_dev);
+    if (timing) {   // debug: print block 0's phase cycles for this launch
+        long long h[T_NPHASE];
+        GmresStats st;
+        cudaMemcpyAsync(h, timers, sizeof(h), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(&st, stats_dev, sizeof(st), cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        static const char *nm[T_NPHASE] = {"resid", "vcycle", "spmv_dot", "dot_sum", "update", "norm_sum",
+                                           "givens", "corr", "barrier_wait", "barriers", "total"};
+        fprintf(stderr, "[phases] n=%d nv=%d groups=%d G=%d mg=%d iters=%d cycles=%d |", n, nv, groups, G,
+                op.mg.nlev, st.iters, st.cycles);
+        for (int k = 0; k < T_NPHASE; ++k) fprintf(stderr, " %s=%lld", nm[k], k == T_BARRIERS ? h[k] : h[k] / 1000);
+        fprintf(stderr, " (kcycles)\n");
+    }
     return cudaGetLastError();
 }
 

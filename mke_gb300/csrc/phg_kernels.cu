@@ -25,9 +25,24 @@ inline unsigned grid_for(long long work) {
     return (unsigned)b;
 }
 
+// ascending-column row sum; loads are issued together, the sum keeps the order
 __device__ __forceinline__ double row_sum(const DevEll &A, const double *x, const int *imap, int i) {
     double s = 0.0;
     const int n = A.n;
+    if (A.W <= 8) {
+        int c[8];
+        double a[8], xv[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < A.W) { c[k] = __ldg(&A.col[(size_t)k * n + i]); a[k] = __ldg(&A.val[(size_t)k * n + i]); }
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < A.W) xv[k] = imap ? x[imap[c[k]]] : x[c[k]];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < A.W) s += a[k] * xv[k];
+        return s;
+    }
     for (int k = 0; k < A.W; ++k) {
         int c = __ldg(&A.col[(size_t)k * n + i]);
         double xv = imap ? x[imap[c]] : x[c];
