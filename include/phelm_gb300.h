@@ -112,6 +112,19 @@ int phg_laplace_calc2(phg_ops o, double *ans, const double *F, void *stream);
 /* SphereLaplace::solve (src/impl/slaplace_impl.h:84-131): ans[V] with
  * Laplacian(ans) = F[V] and ans = bnd[os] on the boundary. */
 int phg_laplace_solve(phg_ops o, double *ans, const double *F, const double *bnd, void *stream);
+/* No counterpart in the reference.  phg_laplace_calc2 for callers that cannot
+ * let a library allocate device memory (memory owned by their own pool or
+ * allocator, or loops where the device synchronisation of a cudaMalloc would
+ * stall their other streams).  It calls no cudaMalloc/cudaFree: its
+ * right-hand side and GMRES workspace live in one fixed 16 MiB device array
+ * inside the library (held by every GPU that loads the library until the
+ * process exits), enough for up to level-6 meshes (40,961 inner points) at
+ * restart 30 in FP64; larger needs are rejected with PHG_ERR_ARG.
+ * ans[rs] and F[V] must be device pointers; the call only enqueues work on
+ * `stream`.  The first call on each device looks up the array's device
+ * address (make it before any stream capture).  All calls share the array:
+ * calls that overlap on the GPU (e.g. on two streams) race. */
+int phg_laplace_calc2_noalloc(phg_ops o, double *ans, const double *F, void *stream);
 /* SphereJacobian::calc1 / calc2 / calc2t (src/sjacobian.cpp:348-408, 456-461). */
 int phg_jacobian_calc1(phg_ops o, double *ans, const double *u, const double *v, const double *bnd, void *stream);
 int phg_jacobian_calc2(phg_ops o, double *ans, const double *u, const double *v, void *stream);

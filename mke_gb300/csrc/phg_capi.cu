@@ -919,3 +919,69 @@ extern "C" int phg_baroclin_calc(phg_baroclin b, double *u11, double *u21, const
     (void)b; (void)u11; (void)u21; (void)u1; (void)u2; (void)bnd; (void)f; (void)g; (void)stream;
     return fail(PHG_ERR_ARG, "baroclin step is not built yet");
 }
+
+// ------------------------------------------------------- no allocation ---
+// phg_laplace_calc2_noalloc: SphereLaplace::calc2 for callers that cannot
+// let the library allocate device memory -- e.g. applications whose device
+// memory is owned by their own pool or allocator, or loops where the device
+// synchronisation a cudaMalloc brings would stall their other streams.  The
+// right-hand side and the GMRES workspace live in the fixed array below,
+// which every GPU that loads this library holds until the process exits.
+namespace {
+
+constexpr size_t NOALLOC_BYTES = 16u << 20;   // 16 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[64] = {nullptr};
+
+// Device address of the scratch array on `dev`, looked up once per device
+// with that device current (a host-side use of the symbol's name is not a
+// device address).
+int noalloc_scratch(int dev, unsigned char **out) {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (dev < 0 || dev >= 64) return fail(PHG_ERR_ARG, "device ordinal %d out of range", dev);
+    if (!g_noalloc_ptr[dev]) {
+        int cur = 0;
+        CK(cudaGetDevice(&cur));
+        if (cur != dev) CK(cudaSetDevice(dev));
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (cur != dev) cudaSetDevice(cur);
+        if (e != cudaSuccess) return fail(PHG_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = (unsigned char *)g_noalloc_ptr[dev];
+    return PHG_OK;
+}
+
+}  // namespace
+
+extern "C" int phg_laplace_calc2_noalloc(phg_ops o, double *ans, const double *F, void *stream) {
+    if (!o || !ans || !F) return fail(PHG_ERR_ARG, "NULL argument");
+    if (!is_device_ptr(ans) || !is_device_ptr(F))
+        return fail(PHG_ERR_ARG, "phg_laplace_calc2_noalloc takes device pointers only");
+    const size_t al = 256;
+    const size_t rhs_bytes = (8 * (size_t)o->rs + al - 1) / al * al;
+    const size_t st_bytes = (sizeof(GmresStats) + al - 1) / al * al;
+    const size_t work_bytes = gmres_work_bytes(o->ML.op, 1, o->restart, prec_of(o));
+    const size_t need = rhs_bytes + st_bytes + work_bytes;
+    if (need > NOALLOC_BYTES)
+        return fail(PHG_ERR_ARG,
+                    "phg_laplace_calc2_noalloc needs %zu bytes of scratch for %d inner points at restart %d; "
+                    "it holds %zu (16 MiB: up to level 6 at restart 30 in FP64)",
+                    need, o->rs, o->restart, NOALLOC_BYTES);
+    unsigned char *base = nullptr;
+    int r = noalloc_scratch(o->dev, &base);
+    if (r) return r;
+    cudaStream_t s = o->str(stream);
+    double *rhs = (double *)base;
+    GmresStats *st = (GmresStats *)(base + rhs_bytes);
+    void *work = base + rhs_bytes + st_bytes;
+    // rhs = L F_in + B3 F_bnd ; ans = M_L^-1 rhs from a zero start
+    CK(apply_op(o->L.op.A, o->bnd3.c, F, o->V, o->imap(), F, o->V, o->bmap(), rhs, o->rs, 1, s));
+    CK(cudaMemsetAsync(ans, 0, 8 * (size_t)o->rs, s));
+    CK(gmres_solve(o->ML.op, rhs, ans, 1, o->rs, o->restart, o->max_iter, mass_tol(o), prec_of(o), work, st, s,
+                   /*no_alloc=*/true));
+    return PHG_OK;
+}

@@ -88,9 +88,10 @@ struct GmresStats {
 // `work` must hold gmres_work_bytes(...) bytes; `stats_dev` receives a
 // GmresStats on the device.
 size_t gmres_work_bytes(const DevSolveOp &op, int nv, int m, Precision p);
+// no_alloc: never allocate (the optional debug phase timers stay off)
 cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv, int ld,
                         int m, int max_iter, double tol, Precision p,
-                        void *work, GmresStats *stats_dev, cudaStream_t s);
+                        void *work, GmresStats *stats_dev, cudaStream_t s, bool no_alloc = false);
 
 // y[v] = A x_in[v] + C x_bnd[v] with every row summed in ascending column
 // order from 0.0 and no fused multiply-add (same rounding as a CPU CSR

@@ -698,7 +698,7 @@ size_t gmres_work_bytes(const DevSolveOp &op, int nv, int m, Precision p) { retu
 
 cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv, int ld,
                         int m, int max_iter, double tol, Precision prec,
-                        void *work, GmresStats *stats_dev, cudaStream_t s) {
+                        void *work, GmresStats *stats_dev, cudaStream_t s, bool no_alloc) {
     if (m < 1 || m > MAXM || nv < 1) return cudaErrorInvalidValue;
     const int n = op.A.n;
     Params p;
@@ -733,7 +733,7 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     p.groups = groups; p.G = G;
     for (int l = 0; l < MG_MAXLEV; ++l) p.red_off[l] = offs[l];
     static long long *timers = nullptr;
-    const bool timing = getenv("PHG_PHASE_TIMING") != nullptr;
+    const bool timing = !no_alloc && getenv("PHG_PHASE_TIMING") != nullptr;
     if (timing && !timers) cudaMalloc(&timers, sizeof(long long) * T_NPHASE);
     p.timers = timing ? timers : nullptr;
     if (timing) cudaMemsetAsync(timers, 0, sizeof(long long) * T_NPHASE, s);

@@ -61,6 +61,7 @@ SIGNATURES = {
     "phg_laplace_calc1": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "phg_laplace_calc2": (C.c_int, [_vp, _vp, _vp, _vp]),
     "phg_laplace_solve": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "phg_laplace_calc2_noalloc": (C.c_int, [_vp, _vp, _vp, _vp]),
     "phg_jacobian_calc1": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "phg_jacobian_calc2": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "phg_jacobian_calc2t": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
