@@ -326,6 +326,25 @@ def run_case(args):
     zb = torch.zeros(max(mesh.outer_size, 1), dtype=torch.float64, device="cuda")
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     st = torch.cuda.Stream()   # an explicit stream: the library and the events share it
+    if args.case == "batch":
+        from mke_gb300 import fields
+        lat, lon = mesh.latlon()
+        B = args.members
+        states = np.stack([fields.barvortex_initial(lat, lon, seed=SEED + k, lmax_noise=16)[0] for k in range(B)])
+        U = torch.tensor(states, dtype=torch.float64, device="cuda")
+        zbB = torch.zeros((B, max(mesh.outer_size, 1)), dtype=torch.float64, device="cuda")
+        bv = phelm.BarVortex(ops, coriolis=cor, **CONF)
+        bv.calc_batch(U, zbB, zbB, out=U, stream=st)
+        torch.cuda.synchronize()
+        ev[0].record(st)
+        for _ in range(args.steps):
+            bv.calc_batch(U, zbB, zbB, out=U, stream=st)
+        ev[1].record(st)
+        torch.cuda.synchronize()
+        ms = ev[0].elapsed_time(ev[1]) / args.steps
+        print(json.dumps({"case": "batch", "level": args.level, "members": B, "precision": args.precision,
+                          "ms_per_step": ms, "member_steps_per_s": B * 1000.0 / ms, "stats": bv.last_stats()}))
+        return
     if args.case == "solve":
         L = phelm.SphereLaplace(ops)
         L.solve(u, zb, out=out, stream=st)
@@ -357,7 +376,8 @@ def main():
     ap.add_argument("--level", type=int, default=LEVEL)
     ap.add_argument("--tol", type=float, default=TOL)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--case", choices=["solve", "step"], help="profiling workload only (no JSON bench line)")
+    ap.add_argument("--case", choices=["solve", "step", "batch"], help="profiling workload only (no JSON bench line)")
+    ap.add_argument("--members", type=int, default=16, help="ensemble members for --case batch")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     args = ap.parse_args()
     if args.case:

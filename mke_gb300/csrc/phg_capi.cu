@@ -191,6 +191,7 @@ struct MgLevelBufs {
 struct MgBufs {
     std::vector<std::unique_ptr<MgLevelBufs>> lev;
     DBuf cinv64, cinv32;
+    DBuf desc;   // the MgDev descriptor in device memory
 };
 
 struct ColsBufs {
@@ -375,6 +376,14 @@ int build_mg_dev(phg_ops_s *o, const Mesh &m, SolveOpBufs &Lb, MgBufs &mb, int p
     mg.nc = h.A[nlev - 1].n;
     mg.cinv64 = mb.cinv64.as<double>();
     mg.cinv32 = mb.cinv32.as<float>();
+    size_t e = 0;
+    for (int l = nred; l < nlev; ++l) { mg.red_off[l] = (int)e; e += 4 * (size_t)mg.lev[l].n; }
+    mg.red_elems = e;
+    mg.group_elems = 0;
+    for (int l = 0; l < nred; ++l) mg.group_elems += 4 * (size_t)mg.lev[l].n;
+    CK(mb.desc.ensure(sizeof(MgDev)));
+    CK(cudaMemcpy(mb.desc.p, &mg, sizeof(MgDev), cudaMemcpyHostToDevice));
+    Lb.op.mgd = mb.desc.as<MgDev>();
     return PHG_OK;
 }
 
@@ -550,23 +559,26 @@ struct Stage {
 
 double mass_tol(const phg_ops_s *o) { return std::min(o->tol, 1e-14); }
 
-// ans (rs) = M_L^{-1} (L F_in + B3 F_bnd) for nv members of full vectors F
-int laplace_calc2_dev(phg_ops_s *o, double *ans, int lda, const double *F, int ldf, int nv, int slot, cudaStream_t s) {
+// ans (rs) = M_L^{-1} (L F_in + B3 F_bnd) for nv members of full vectors F;
+// the mass solve runs to `tol` (standalone applies: 1e-14, time steps: the
+// handle's tolerance)
+int laplace_calc2_dev(phg_ops_s *o, double *ans, int lda, const double *F, int ldf, int nv, int slot, cudaStream_t s,
+                      double tol) {
     CK(o->s_a.ensure(8 * (size_t)o->rs * nv));
     double *rhs = o->s_a.as<double>();
     CK(apply_op(o->L.op.A, o->bnd3.c, F, ldf, o->imap(), F, ldf, o->bmap(), rhs, o->rs, nv, s));
     for (int v = 0; v < nv; ++v) CK(cudaMemsetAsync(ans + (size_t)v * lda, 0, 8 * (size_t)o->rs, s));
-    return solve(o, o->ML.op, rhs, ans, nv, lda, mass_tol(o), slot, s);
+    return solve(o, o->ML.op, rhs, ans, nv, lda, tol, slot, s);
 }
 
 // the 8 derivative solves of a Jacobian for nv members; sol: nv x 8 x rs
 int jacobian_derivs_dev(phg_ops_s *o, const double *u, const double *v, int ld, double *sol, int nv, int slot,
-                        cudaStream_t s) {
+                        cudaStream_t s, double tol) {
     CK(o->s_b.ensure(8 * (size_t)o->rs * 8 * nv));
     double *rhs = o->s_b.as<double>();
     CK(jac_rhs(o->J, u, v, ld, o->imap(), o->bmap(), rhs, o->rs, nv, s));
     CK(cudaMemsetAsync(sol, 0, 8 * (size_t)o->rs * 8 * nv, s));
-    return solve(o, o->MJ.op, rhs, sol, 8 * nv, o->rs, mass_tol(o), slot, s);
+    return solve(o, o->MJ.op, rhs, sol, 8 * nv, o->rs, tol, slot, s);
 }
 
 int norm_dev(phg_ops_s *o, const double *u, const double *v, int nv, double *out_dev, bool dist, bool take_sqrt,
@@ -638,7 +650,7 @@ extern "C" int phg_laplace_calc2(phg_ops o, double *ans, const double *F, void *
     Stage st(o, s);
     const double *dF; double *dA;
     CK(st.in(F, o->V, &dF)); CK(st.out(ans, o->rs, &dA));
-    int r = laplace_calc2_dev(o, dA, o->rs, dF, o->V, 1, 0, s);
+    int r = laplace_calc2_dev(o, dA, o->rs, dF, o->V, 1, 0, s, mass_tol(o));
     if (r) return r;
     CK(st.finish());
     return st.host ? check_stats(o, 1, s) : PHG_OK;
@@ -651,7 +663,7 @@ extern "C" int phg_laplace_calc1(phg_ops o, double *ans, const double *F, const 
     const double *dF, *dB; double *dA;
     CK(st.in(F, o->V, &dF)); CK(st.in(bnd, o->os, &dB)); CK(st.out(ans, o->V, &dA));
     CK(o->s_c.ensure(8 * (size_t)o->rs));
-    int r = laplace_calc2_dev(o, o->s_c.as<double>(), o->rs, dF, o->V, 1, 0, s);
+    int r = laplace_calc2_dev(o, o->s_c.as<double>(), o->rs, dF, o->V, 1, 0, s, mass_tol(o));
     if (r) return r;
     CK(p2u(dA, o->V, o->s_c.as<double>(), o->rs, dB, o->os, o->p2io.as<int>(), o->isb.as<int>(), o->V, 1, s));
     CK(st.finish());
@@ -686,7 +698,7 @@ static int jacobian_common(phg_ops o, double *ans, const double *u, const double
     CK(st.out(ans, full ? o->V : o->rs, &dA));
     CK(o->s_e.ensure(8 * (size_t)o->rs * 8));
     CK(o->s_c.ensure(8 * (size_t)o->rs));
-    int r = jacobian_derivs_dev(o, du, dv, o->V, o->s_e.as<double>(), 1, 0, s);
+    int r = jacobian_derivs_dev(o, du, dv, o->V, o->s_e.as<double>(), 1, 0, s, mass_tol(o));
     if (r) return r;
     double *jac = full ? o->s_c.as<double>() : dA;
     CK(jac_combine(o->s_e.as<double>(), o->rs, o->rs, jac, o->rs, nullptr, 0, nullptr, 1, s));
@@ -809,9 +821,9 @@ int bv_step_dev(phg_barvortex_s *b, int nv, double *u1, const double *u, const d
     // nr0 = norm(u)
     if ((r = norm_dev(o, uu, nullptr, nv, b->nr0.as<double>(), false, true, s))) return r;
     // w = L(u) with bnd_w, dw = L(w) with zero boundary
-    if ((r = laplace_calc2_dev(o, x, rs, uu, V, nv, slot++, s))) return r;
+    if ((r = laplace_calc2_dev(o, x, rs, uu, V, nv, slot++, s, o->tol))) return r;
     CK(p2u(w, V, x, rs, bnd_w, os, p2io, isb, V, nv, s));
-    if ((r = laplace_calc2_dev(o, x, rs, w, V, nv, slot++, s))) return r;
+    if ((r = laplace_calc2_dev(o, x, rs, w, V, nv, slot++, s, o->tol))) return r;
     CK(p2u(dw, V, x, rs, nullptr, os, p2io, isb, V, nv, s));
     // FC = w/tau + mu(1-theta) dw - sigma(1-theta) w (+ f)
     if (forcing && nv > 1) return fail(PHG_ERR_ARG, "batched forcing not supported");
@@ -823,7 +835,7 @@ int bv_step_dev(phg_barvortex_s *b, int nv, double *u1, const double *u, const d
         CK(bv_mix(tmp1, tmp2, w_n, w, u_n, uu, b->lh.as<double>(), V, c.k1 * c.theta, c.k1 * (1.0 - c.theta), c.k2,
                   c.theta, 1.0 - c.theta, NV, s));
         // F = FC[inner] - J(tmp2, tmp1)
-        if ((r = jacobian_derivs_dev(o, tmp2, tmp1, V, jsol, nv, slot++, s))) return r;
+        if ((r = jacobian_derivs_dev(o, tmp2, tmp1, V, jsol, nv, slot++, s, o->tol))) return r;
         CK(jac_combine(jsol, rs, rs, F, rs, FC, V, o->imap(), nv, s));
         // rp = M_L F + bnd_ bnd_w ; w_n = p2u(A^-1 rp, bnd_w)
         CK(apply_op(o->ML.op.A, b->Ab.c, F, rs, nullptr, bnd_w, os, nullptr, rp, rs, nv, s));

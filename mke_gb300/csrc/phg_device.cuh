@@ -47,6 +47,9 @@ struct MgDev {
     const double *cinv64 = nullptr; const float *cinv32 = nullptr;
     double omega = 0.7;
     int nu1 = 2, nu2 = 2;
+    int red_off[MG_MAXLEV] = {0};  // shared-memory element offsets of levels [nred, nlev)
+    size_t red_elems = 0;          // shared-memory elements of those levels (x, xt, b, r each)
+    size_t group_elems = 0;        // global elements per group for levels [0, nred)
 };
 
 // Operator of the Krylov solver: the exact A (FP64 residuals), Jacobi-scaled
@@ -58,7 +61,8 @@ struct DevSolveOp {
     const float *as32 = nullptr;   // A D^{-1}, FP32 (mixed precision)
     const double *dinv = nullptr;  // 1 / diag(A)
     const float *a32 = nullptr;    // A in FP32 (multigrid path, mixed precision)
-    MgDev mg;
+    MgDev mg;                      // host copy (sizes)
+    const MgDev *mgd = nullptr;    // the same descriptor in device memory (read by the kernel)
 };
 
 // rs x os boundary columns in CSR over rows (few nonzero rows).

@@ -12,16 +12,21 @@
 // Preconditioning (right, flexible): Jacobi, folded into the stored values
 // (A D^-1), or a geometric multigrid V-cycle over the nested icosahedral
 // meshes.  In the V-cycle the fine levels are smoothed by the group's blocks
-// with group barriers; the coarse levels (<= a few thousand points) are
-// solved by every block redundantly in shared memory with __syncthreads only,
-// so the coarse half of the cycle costs no cross-block synchronisation.
+// with group barriers; the coarse levels (a few hundred points) are solved by
+// every block redundantly in shared memory with __syncthreads only, so the
+// coarse half of the cycle costs no cross-block synchronisation.
 //
-// Per Arnoldi step: [V-cycle z_j = M^-1 v_j], (1) w = A z_j fused with the
+// Per Arnoldi step: [V-cycle z_j = M^-1 v_j], (1) w = A z_j, then the
 // classical Gram-Schmidt dots <v_l, w>, (2) w -= sum h_l v_l fused with
 // ||w||^2, (3) v_{j+1} = w / |w| and the Givens update (computed redundantly,
 // identically, by every block of the group).  Every restart recomputes
 // r = b - A x in FP64 with the exact operator, which is also the outer loop
 // of mixed-precision iterative refinement.
+//
+// Register discipline: the kernel copies the fields it needs out of its
+// parameter block into locals and the hot loops take no references to it,
+// so the parameter block never has to be materialised in local memory; the
+// multigrid descriptor is read from device memory through a pointer.
 //
 // Every wait is bounded: a barrier that spins longer than ~1 s (clock64)
 // raises a device error flag; all blocks see the flag at their next barrier
@@ -51,26 +56,24 @@ struct Params {
     void *Wv;         // nv x n (VT)
     double *R;        // nv x n (FP64 residual)
     void *mgbuf;      // groups x per-group V-cycle buffers (parallel levels)
-    size_t mg_group_elems;
     double *part;     // groups x 2 x (MAXM + 2) x G
     unsigned *bar;    // groups x 2
     int *err;
     GmresStats *stats;
     int groups, G;
-    int red_off[MG_MAXLEV];  // shared-memory offsets (elements) of the redundant levels
-    long long *timers;       // optional phase cycle counters (block 0), see PHASES
+    long long *timers;       // optional phase cycle counters (block 0)
+    double mg_row_bytes;     // algorithmic bytes of one V-cycle per fine row
 };
 
 // phase cycle counters kept by block 0 when PHG_PHASE_TIMING is set
 enum { T_RESID, T_VCYCLE, T_SPMV_DOT, T_DOT_SUM, T_UPDATE, T_NORM_SUM, T_GIVENS, T_CORR, T_BARRIER,
        T_BARRIERS, T_TOTAL, T_NPHASE };
-__device__ long long g_bar_cycles;  // barrier wait of block 0 (debug timing only)
 
 __device__ __forceinline__ unsigned ld_volatile(const unsigned *p) { return *(const volatile unsigned *)p; }
 __device__ __forceinline__ int ld_volatile(const int *p) { return *(const volatile int *)p; }
 
 // Barrier over the G blocks of one group; false if the grid is aborting.
-__device__ bool group_sync(unsigned *bar, int G, int *err, long long *tm = nullptr) {
+__device__ bool group_sync(unsigned *bar, int G, int *err, long long *tm) {
     __shared__ int ok;
     long long tb = (tm && threadIdx.x == 0) ? clock64() : 0;
     __syncthreads();
@@ -110,9 +113,9 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// block-reduce K values held per thread in acc[0..K-1], result in red[off + l][0]
+// block-reduce K (<= KMAX) per-thread values, result in red[off + l][0]
 template <int KMAX>
-__device__ void block_reduce(double (&acc)[KMAX], int K, double (*red)[NWARP], int off = 0) {
+__device__ __forceinline__ void block_reduce(const double (&acc)[KMAX], int K, double (*red)[NWARP], int off) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int l = 0; l < KMAX; ++l) {
@@ -130,10 +133,28 @@ __device__ void block_reduce(double (&acc)[KMAX], int K, double (*red)[NWARP], i
     __syncthreads();
 }
 
+// group-wide sums of K values held in red[l][0] by every block: publish into
+// one of two alternating partial buffers ([value][block] layout), barrier,
+// then warp w sums value l = w, w + NWARP, ... over the G blocks
+__device__ __forceinline__ bool group_sum(int K, double *out, double (*red)[NWARP], double *part2, int &parity,
+                                          int G, int bi, unsigned *bar, int *err, long long *tm) {
+    double *part = part2 + (size_t)parity * G * (MAXM + 2);
+    parity ^= 1;
+    if (threadIdx.x < K) part[(size_t)threadIdx.x * G + bi] = red[threadIdx.x][0];
+    if (!group_sync(bar, G, err, tm)) return false;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int l = warp; l < K; l += NWARP) {
+        double s = 0.0;
+        for (int b = lane; b < G; b += 32) s += ldcg(&part[(size_t)l * G + b]);
+        s = warp_sum(s);
+        if (lane == 0) out[l] = s;
+    }
+    __syncthreads();
+    return true;
+}
+
 template <typename VT> struct Prec;
 template <> struct Prec<double> {
-    __device__ static const double *as(const DevSolveOp &o) { return o.as64; }
-    __device__ static const double *a(const DevSolveOp &o) { return o.A.val; }
     __device__ static const double *la(const MgLevelDev &l) { return l.a64; }
     __device__ static const double *ld(const MgLevelDev &l) { return l.d64; }
     __device__ static const double *lp(const MgLevelDev &l) { return l.pw64; }
@@ -141,8 +162,6 @@ template <> struct Prec<double> {
     __device__ static const double *ci(const MgDev &m) { return m.cinv64; }
 };
 template <> struct Prec<float> {
-    __device__ static const float *as(const DevSolveOp &o) { return o.as32; }
-    __device__ static const float *a(const DevSolveOp &o) { return o.a32; }
     __device__ static const float *la(const MgLevelDev &l) { return l.a32; }
     __device__ static const float *ld(const MgLevelDev &l) { return l.d32; }
     __device__ static const float *lp(const MgLevelDev &l) { return l.pw32; }
@@ -159,10 +178,10 @@ __device__ __forceinline__ void own_rows(int n, int G, int bi, int &r0, int &r1)
 
 // sum_k A[k][i] x[col]; CG: x read through L2 (written by other blocks).
 // All column/value loads of the row are issued together, then all gathers
-// (one memory round trip each instead of one per entry); rows of up to 8
-// entries take this path, wider rows fall back to a plain loop.
+// (one memory round trip each instead of one per entry).
 template <typename VT, bool CG>
-__device__ __forceinline__ VT spmv_row(const int *col, const VT *val, int n, int W, const VT *x, int i) {
+__device__ __forceinline__ VT spmv_row(const int *__restrict__ col, const VT *__restrict__ val, int n, int W,
+                                       const VT *x, int i) {
     VT s = 0;
     if (W <= 8) {
         int c[8];
@@ -186,192 +205,185 @@ __device__ __forceinline__ VT spmv_row(const int *col, const VT *val, int n, int
     return s;
 }
 
-template <typename VT>
-__device__ __forceinline__ VT restrict_row(const MgLevelDev &L, const VT *rw, int nc, const VT *r, int c, bool cg) {
+template <typename VT, bool CG>
+__device__ __forceinline__ VT restrict_row(const int *__restrict__ rf, const VT *__restrict__ rw, int Wr, int nc,
+                                           const VT *r, int c) {
     VT s = 0;
-    if (L.Wr <= 8) {
+    if (Wr <= 8) {
         int f[8];
         VT w[8], rv[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q)
-            if (q < L.Wr) { f[q] = __ldg(&L.rf[(size_t)q * nc + c]); w[q] = __ldg(&rw[(size_t)q * nc + c]); }
+            if (q < Wr) { f[q] = __ldg(&rf[(size_t)q * nc + c]); w[q] = __ldg(&rw[(size_t)q * nc + c]); }
 #pragma unroll
         for (int q = 0; q < 8; ++q)
-            if (q < L.Wr) rv[q] = f[q] >= 0 ? (cg ? ldcg(&r[f[q]]) : r[f[q]]) : (VT)0;
+            if (q < Wr) rv[q] = f[q] >= 0 ? (CG ? ldcg(&r[f[q]]) : r[f[q]]) : (VT)0;
 #pragma unroll
         for (int q = 0; q < 8; ++q)
-            if (q < L.Wr && f[q] >= 0) s += w[q] * rv[q];
+            if (q < Wr && f[q] >= 0) s += w[q] * rv[q];
         return s;
     }
-    for (int q = 0; q < L.Wr; ++q) {
-        const int f = L.rf[(size_t)q * nc + c];
-        if (f >= 0) s += rw[(size_t)q * nc + c] * (cg ? ldcg(&r[f]) : r[f]);
+    for (int q = 0; q < Wr; ++q) {
+        const int f = __ldg(&rf[(size_t)q * nc + c]);
+        if (f >= 0) s += __ldg(&rw[(size_t)q * nc + c]) * (CG ? ldcg(&r[f]) : r[f]);
     }
     return s;
 }
 
-// rows [r0, r1) of this thread, four at a time: every value is computed
-// (all loads issued) before any store, so four rows' memory round trips
-// overlap even when the output may alias the inputs.
-template <typename VT, typename F, typename S>
-__device__ __forceinline__ void rows4(int r0, int r1, F &&compute, S &&store) {
-    for (int i0 = r0 + threadIdx.x; i0 < r1; i0 += 4 * BLOCK) {
-        VT v[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int i = i0 + q * BLOCK;
-            v[q] = i < r1 ? compute(i) : (VT)0;
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int i = i0 + q * BLOCK;
-            if (i < r1) store(i, v[q]);
-        }
+template <typename VT, bool CG>
+__device__ __forceinline__ VT prolong_row(const int *__restrict__ pc, const VT *__restrict__ pw, const VT *xc,
+                                          int i) {
+    const int c0 = __ldg(&pc[2 * i]), c1 = __ldg(&pc[2 * i + 1]);
+    const VT w0 = __ldg(&pw[2 * i]), w1 = __ldg(&pw[2 * i + 1]);
+    VT s = 0;
+    if (c0 >= 0) s += w0 * (CG ? ldcg(&xc[c0]) : xc[c0]);
+    if (c1 >= 0) s += w1 * (CG ? ldcg(&xc[c1]) : xc[c1]);
+    return s;
+}
+
+// one damped-Jacobi sweep on rows [r0, r1): xo = x + w D^-1 (b - A x)
+// (first == true: x = 0, so xo = w D^-1 b)
+template <typename VT, bool CG>
+__device__ __forceinline__ void jacobi_rows(const MgLevelDev &L, const VT *b, const VT *x, VT *xo, VT omega,
+                                            int r0, int r1, bool first) {
+    const VT *A = Prec<VT>::la(L), *D = Prec<VT>::ld(L);
+    const int n = L.n, W = L.W;
+    const int *cl = L.col;
+    for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
+        const VT bi_ = CG ? ldcg(&b[i]) : b[i];
+        const VT d = __ldg(&D[i]);
+        xo[i] = first ? omega * d * bi_ : x[i] + omega * d * (bi_ - spmv_row<VT, CG>(cl, A, n, W, x, i));
     }
+}
+
+template <typename VT, bool CG>
+__device__ __forceinline__ void residual_rows(const MgLevelDev &L, const VT *b, const VT *x, VT *r, int r0, int r1) {
+    const VT *A = Prec<VT>::la(L);
+    for (int i = r0 + threadIdx.x; i < r1; i += BLOCK)
+        r[i] = (CG ? ldcg(&b[i]) : b[i]) - spmv_row<VT, CG>(L.col, A, L.n, L.W, x, i);
 }
 
 // Damped-Jacobi V-cycle: x0 = M^-1 b0 for the group's right-hand side.
 // Returns false if the grid is aborting.
 template <typename VT>
-__device__ __noinline__ bool vcycle(const Params &p, const VT *b0, VT *x0, VT *gbuf, VT *sm, unsigned *bar, int bi) {
-    const MgDev &mg = p.op.mg;
-    const int G = p.G;
-    const VT omega = (VT)mg.omega;
+__device__ __noinline__ bool vcycle(const MgDev *__restrict__ mgp, const VT *b0, VT *x0, VT *gbuf, VT *sm,
+                                    unsigned *bar, int G, int bi, int *err, long long *tm) {
+    const int nred = mgp->nred, nlev = mgp->nlev, nu1 = mgp->nu1, nu2 = mgp->nu2;
+    const VT omega = (VT)mgp->omega;
     VT *xcur[MG_MAXLEV];
     const VT *bl[MG_MAXLEV];
     size_t offs[MG_MAXLEV];
     // ---- parallel levels, down
     size_t off = 0;
-    for (int l = 0; l < mg.nred; ++l) {
-        const MgLevelDev &L = mg.lev[l];
+    for (int l = 0; l < nred; ++l) {
+        const MgLevelDev &L = mgp->lev[l];
         const int n = L.n;
         offs[l] = off;
         VT *xa = gbuf + off, *xb = xa + n, *r = xb + n;
-        VT *bn = r + n;  // storage for the rhs of level l+1 when that level is parallel too
+        VT *bn = r + n;  // rhs of level l+1 when that level is parallel too
         off += 4 * (size_t)n;
         const VT *b = l == 0 ? b0 : bl[l];
         bl[l] = b;
-        const VT *A = Prec<VT>::la(L), *D = Prec<VT>::ld(L);
         int r0, r1;
         own_rows(n, G, bi, r0, r1);
         VT *x = xa, *xo = xb;
-        for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) x[i] = omega * D[i] * ldcg(&b[i]);
-        for (int s = 1; s < mg.nu1; ++s) {
-            if (!group_sync(bar, G, p.err, p.timers && blockIdx.x == 0 ? p.timers : nullptr)) return false;
-            for (int i = r0 + threadIdx.x; i < r1; i += BLOCK)
-                xo[i] = x[i] + omega * D[i] * (ldcg(&b[i]) - spmv_row<VT, true>(L.col, A, n, L.W, x, i));
+        jacobi_rows<VT, true>(L, b, nullptr, x, omega, r0, r1, true);
+        for (int s = 1; s < nu1; ++s) {
+            if (!group_sync(bar, G, err, tm)) return false;
+            jacobi_rows<VT, true>(L, b, x, xo, omega, r0, r1, false);
             VT *t = x; x = xo; xo = t;
         }
-        if (!group_sync(bar, G, p.err, p.timers && blockIdx.x == 0 ? p.timers : nullptr)) return false;
-        for (int i = r0 + threadIdx.x; i < r1; i += BLOCK)
-            r[i] = ldcg(&b[i]) - spmv_row<VT, true>(L.col, A, n, L.W, x, i);
+        if (!group_sync(bar, G, err, tm)) return false;
+        residual_rows<VT, true>(L, b, x, r, r0, r1);
         xcur[l] = x;
-        if (!group_sync(bar, G, p.err, p.timers && blockIdx.x == 0 ? p.timers : nullptr)) return false;
-        const MgLevelDev &C = mg.lev[l + 1];
+        if (!group_sync(bar, G, err, tm)) return false;
+        const MgLevelDev &C = mgp->lev[l + 1];
         const VT *rw = Prec<VT>::lr(L);
-        if (l + 1 < mg.nred) {
+        if (l + 1 < nred) {
             int c0, c1;
             own_rows(C.n, G, bi, c0, c1);
-            for (int c = c0 + threadIdx.x; c < c1; c += BLOCK) bn[c] = restrict_row<VT>(L, rw, C.n, r, c, true);
+            for (int c = c0 + threadIdx.x; c < c1; c += BLOCK) bn[c] = restrict_row<VT, true>(L.rf, rw, L.Wr, C.n, r, c);
             bl[l + 1] = bn;
         } else {
-            VT *sb = sm + p.red_off[l + 1] + 2 * C.n;
-            for (int c = threadIdx.x; c < C.n; c += BLOCK) sb[c] = restrict_row<VT>(L, rw, C.n, r, c, true);
+            VT *sb = sm + mgp->red_off[l + 1] + 2 * C.n;
+            for (int c = threadIdx.x; c < C.n; c += BLOCK) sb[c] = restrict_row<VT, true>(L.rf, rw, L.Wr, C.n, r, c);
         }
     }
     __syncthreads();
     // ---- redundant levels in shared memory (x, xt, b, r per level)
-    const int last = mg.nlev - 1;
-    for (int l = mg.nred; l < last; ++l) {
-        const MgLevelDev &L = mg.lev[l], &C = mg.lev[l + 1];
-        const int n = L.n;
-        VT *x = sm + p.red_off[l], *xt = x + n, *b = xt + n, *r = b + n;
-        const VT *A = Prec<VT>::la(L), *D = Prec<VT>::ld(L);
-        rows4<VT>(0, n, [&](int i) { return omega * __ldg(&D[i]) * b[i]; }, [&](int i, VT v) { x[i] = v; });
+    const int last = nlev - 1;
+    for (int l = nred; l < last; ++l) {
+        const MgLevelDev &L = mgp->lev[l];
+        const int n = L.n, nc = mgp->lev[l + 1].n;
+        VT *x = sm + mgp->red_off[l], *xt = x + n, *b = xt + n, *r = b + n;
+        jacobi_rows<VT, false>(L, b, nullptr, x, omega, 0, n, true);
         __syncthreads();
-        for (int s = 1; s < mg.nu1; ++s) {
-            rows4<VT>(0, n, [&](int i) { return x[i] + omega * __ldg(&D[i]) * (b[i] - spmv_row<VT, false>(L.col, A, n, L.W, x, i)); },
-                      [&](int i, VT v) { xt[i] = v; });
+        for (int s = 1; s < nu1; ++s) {
+            jacobi_rows<VT, false>(L, b, x, xt, omega, 0, n, false);
             __syncthreads();
             for (int i = threadIdx.x; i < n; i += BLOCK) x[i] = xt[i];
             __syncthreads();
         }
-        rows4<VT>(0, n, [&](int i) { return b[i] - spmv_row<VT, false>(L.col, A, n, L.W, x, i); },
-                  [&](int i, VT v) { r[i] = v; });
+        residual_rows<VT, false>(L, b, x, r, 0, n);
         __syncthreads();
-        VT *cb = sm + p.red_off[l + 1] + 2 * C.n;
+        VT *cb = sm + mgp->red_off[l + 1] + 2 * nc;
         const VT *rw = Prec<VT>::lr(L);
-        rows4<VT>(0, C.n, [&](int c) { return restrict_row<VT>(L, rw, C.n, r, c, false); }, [&](int c, VT v) { cb[c] = v; });
+        for (int c = threadIdx.x; c < nc; c += BLOCK) cb[c] = restrict_row<VT, false>(L.rf, rw, L.Wr, nc, r, c);
         __syncthreads();
     }
     {   // coarsest: dense inverse, four independent partial sums per row
-        const int n = mg.nc;
-        VT *x = sm + p.red_off[last], *b = x + 2 * n;
-        const VT *Ci = Prec<VT>::ci(mg);
+        const int n = mgp->nc;
+        VT *x = sm + mgp->red_off[last], *b = x + 2 * n;
+        const VT *Ci = Prec<VT>::ci(*mgp);
         for (int i = threadIdx.x; i < n; i += BLOCK) {
-            VT s4[4] = {0, 0, 0, 0};
+            VT s0 = 0, s1 = 0, s2 = 0, s3 = 0;
             int j = 0;
             for (; j + 4 <= n; j += 4) {
-                VT c[4];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) c[q] = __ldg(&Ci[(size_t)i * n + j + q]);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) s4[q] += c[q] * b[j + q];
+                const VT c0 = __ldg(&Ci[(size_t)i * n + j]), c1 = __ldg(&Ci[(size_t)i * n + j + 1]);
+                const VT c2 = __ldg(&Ci[(size_t)i * n + j + 2]), c3 = __ldg(&Ci[(size_t)i * n + j + 3]);
+                s0 += c0 * b[j]; s1 += c1 * b[j + 1]; s2 += c2 * b[j + 2]; s3 += c3 * b[j + 3];
             }
-            for (; j < n; ++j) s4[0] += __ldg(&Ci[(size_t)i * n + j]) * b[j];
-            x[i] = (s4[0] + s4[1]) + (s4[2] + s4[3]);
+            for (; j < n; ++j) s0 += __ldg(&Ci[(size_t)i * n + j]) * b[j];
+            x[i] = (s0 + s1) + (s2 + s3);
         }
         __syncthreads();
     }
-    for (int l = last - 1; l >= mg.nred; --l) {
-        const MgLevelDev &L = mg.lev[l];
+    for (int l = last - 1; l >= nred; --l) {
+        const MgLevelDev &L = mgp->lev[l];
         const int n = L.n;
-        VT *x = sm + p.red_off[l], *xt = x + n, *b = xt + n;
-        const VT *xc = sm + p.red_off[l + 1];
-        const VT *A = Prec<VT>::la(L), *D = Prec<VT>::ld(L), *pw = Prec<VT>::lp(L);
-        rows4<VT>(0, n, [&](int i) {
-            VT s = x[i];
-            for (int q = 0; q < 2; ++q) {
-                const int c = __ldg(&L.pc[2 * i + q]);
-                if (c >= 0) s += __ldg(&pw[2 * i + q]) * xc[c];
-            }
-            return s;
-        }, [&](int i, VT v) { x[i] = v; });
+        VT *x = sm + mgp->red_off[l], *xt = x + n, *b = xt + n;
+        const VT *xc = sm + mgp->red_off[l + 1];
+        const VT *pw = Prec<VT>::lp(L);
+        for (int i = threadIdx.x; i < n; i += BLOCK) x[i] += prolong_row<VT, false>(L.pc, pw, xc, i);
         __syncthreads();
-        for (int s = 0; s < mg.nu2; ++s) {
-            rows4<VT>(0, n, [&](int i) { return x[i] + omega * __ldg(&D[i]) * (b[i] - spmv_row<VT, false>(L.col, A, n, L.W, x, i)); },
-                      [&](int i, VT v) { xt[i] = v; });
+        for (int s = 0; s < nu2; ++s) {
+            jacobi_rows<VT, false>(L, b, x, xt, omega, 0, n, false);
             __syncthreads();
             for (int i = threadIdx.x; i < n; i += BLOCK) x[i] = xt[i];
             __syncthreads();
         }
     }
     // ---- parallel levels, up
-    for (int l = mg.nred - 1; l >= 0; --l) {
-        const MgLevelDev &L = mg.lev[l];
+    for (int l = nred - 1; l >= 0; --l) {
+        const MgLevelDev &L = mgp->lev[l];
         const int n = L.n;
         VT *xa = gbuf + offs[l], *xb = xa + n;
         VT *x = xcur[l], *xo = (x == xa) ? xb : xa;
         const VT *b = bl[l];
-        const VT *A = Prec<VT>::la(L), *D = Prec<VT>::ld(L), *pw = Prec<VT>::lp(L);
-        const bool coarse_in_smem = (l + 1 == mg.nred);
-        const VT *xc = coarse_in_smem ? sm + p.red_off[l + 1] : xcur[l + 1];
-        if (!coarse_in_smem && !group_sync(bar, G, p.err, p.timers && blockIdx.x == 0 ? p.timers : nullptr)) return false;
+        const VT *pw = Prec<VT>::lp(L);
+        const bool coarse_in_smem = (l + 1 == nred);
+        const VT *xc = coarse_in_smem ? sm + mgp->red_off[l + 1] : xcur[l + 1];
+        if (!coarse_in_smem && !group_sync(bar, G, err, tm)) return false;
         int r0, r1;
         own_rows(n, G, bi, r0, r1);
-        for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
-            VT s = x[i];
-            for (int q = 0; q < 2; ++q) {
-                const int c = L.pc[2 * i + q];
-                if (c >= 0) s += pw[2 * i + q] * (coarse_in_smem ? xc[c] : ldcg(&xc[c]));
-            }
-            x[i] = s;
-        }
-        for (int s = 0; s < mg.nu2; ++s) {
-            if (!group_sync(bar, G, p.err, p.timers && blockIdx.x == 0 ? p.timers : nullptr)) return false;
-            VT *dst = (l == 0 && s == mg.nu2 - 1) ? x0 : xo;
-            for (int i = r0 + threadIdx.x; i < r1; i += BLOCK)
-                dst[i] = x[i] + omega * D[i] * (ldcg(&b[i]) - spmv_row<VT, true>(L.col, A, n, L.W, x, i));
+        if (coarse_in_smem)
+            for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) x[i] += prolong_row<VT, false>(L.pc, pw, xc, i);
+        else
+            for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) x[i] += prolong_row<VT, true>(L.pc, pw, xc, i);
+        for (int s = 0; s < nu2; ++s) {
+            if (!group_sync(bar, G, err, tm)) return false;
+            VT *dst = (l == 0 && s == nu2 - 1) ? x0 : xo;
+            jacobi_rows<VT, true>(L, b, x, dst, omega, r0, r1, false);
             if (dst == x0) x = x0;
             else { VT *t = x; x = xo; xo = t; }
         }
@@ -383,9 +395,8 @@ __device__ __noinline__ bool vcycle(const Params &p, const VT *b0, VT *x0, VT *g
 }
 
 template <typename VT>
-__global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(Params p) {
+__global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
     extern __shared__ double smem[];
-    const int m = p.m, n = p.n;
     double *H = smem;                       // (m+1) x m
     double *cs = H + (MAXM + 1) * MAXM;     // m
     double *sn = cs + MAXM;                 // m
@@ -396,44 +407,41 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(Params p) {
     __shared__ double red[MAXM + 2][NWARP];
     __shared__ int flag[4];
 
-    const int grp = blockIdx.x / p.G, bi = blockIdx.x % p.G;
-    if (grp >= p.groups) return;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // everything the loops need, copied out of the parameter block
+    const int m = p.m, n = p.n, G = p.G, nv = p.nv, groups = p.groups, max_iter = p.max_iter;
+    const size_t ld = (size_t)p.ld;
+    const double tol = p.tol;
+    const int grp = blockIdx.x / G, bi = blockIdx.x % G;
+    if (grp >= groups) return;
     unsigned *bar = p.bar + 2 * grp;
-    // two partial-sum buffers used alternately: a block can only refill a
-    // buffer after the next barrier, i.e. after every block has read it;
-    // layout [value][block] so one warp reads one value's partials coalesced
-    double *part2 = p.part + (size_t)grp * 2 * p.G * (MAXM + 2);
+    int *err = p.err;
+    double *part2 = p.part + (size_t)grp * 2 * G * (MAXM + 2);
     int parity = 0;
     int r0, r1;
-    own_rows(n, p.G, bi, r0, r1);
+    own_rows(n, G, bi, r0, r1);
     const int W = p.op.A.W;
-    const int *col = p.op.A.col;
-    const double *aval = p.op.A.val;
-    const bool use_mg = p.op.mg.nlev > 0;
-    const VT *sval = use_mg ? Prec<VT>::a(p.op) : Prec<VT>::as(p.op);
-    const double *dinv = p.op.dinv;
-    VT *gbuf = use_mg ? (VT *)p.mgbuf + (size_t)grp * p.mg_group_elems : nullptr;
+    const int *__restrict__ col = p.op.A.col;
+    const double *__restrict__ aval = p.op.A.val;
+    const MgDev *mgp = p.op.mgd;
+    const bool use_mg = mgp != nullptr;
+    const VT *__restrict__ sval;
+    if (sizeof(VT) == 8) sval = (const VT *)(use_mg ? (const void *)p.op.A.val : (const void *)p.op.as64);
+    else sval = (const VT *)(use_mg ? (const void *)p.op.a32 : (const void *)p.op.as32);
+    const double *__restrict__ dinv = p.op.dinv;
+    VT *gbuf = use_mg ? (VT *)p.mgbuf + (size_t)grp * p.op.mg.group_elems : nullptr;
     long long *tm = (p.timers && blockIdx.x == 0) ? p.timers : nullptr;
+    const double *Bp = p.B;
+    double *Xp = p.X;
+    VT *Vp = (VT *)p.V, *Zp = (VT *)p.Z, *Wp = (VT *)p.Wv;
+    double *Rp = p.R;
+    const double inner_rtol = sizeof(VT) == 4 ? INNER_RTOL : 0.0;
+    const double es = (double)sizeof(VT), nrows = (double)(r1 - r0);
+    const double mg_row_bytes = p.mg_row_bytes;
     long long t_start = clock64(), tph = 0;
-    auto tick = [&](int ph) {
-        if (tm && threadIdx.x == 0) { long long t = clock64(); tm[ph] += t - tph; tph = t; }
-    };
-
-    auto group_sum = [&](int K, double *out) -> bool {
-        double *part = part2 + (size_t)parity * p.G * (MAXM + 2);
-        parity ^= 1;
-        if (threadIdx.x < K) part[(size_t)threadIdx.x * p.G + bi] = red[threadIdx.x][0];
-        if (!group_sync(bar, p.G, p.err, tm)) return false;
-        for (int l = warp; l < K; l += NWARP) {
-            double s = 0.0;
-            for (int b = lane; b < p.G; b += 32) s += ldcg(&part[(size_t)l * p.G + b]);
-            s = warp_sum(s);
-            if (lane == 0) out[l] = s;
-        }
-        __syncthreads();
-        return true;
-    };
+#define PHG_TICK(ph)                                                         \
+    do {                                                                     \
+        if (tm && threadIdx.x == 0) { long long t_ = clock64(); tm[ph] += t_ - tph; tph = t_; } \
+    } while (0)
 
     int my_iters = 0, my_cycles = 0, my_status = 0, my_steps = 0;
     double my_rel = 0.0;
@@ -444,117 +452,143 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(Params p) {
     //              + 2 es (w read/write) + 2 es (w read, v_{j+1} write)
     //   V-cycle    per level and sweep: W (4 + es) + 4 es, plus transfers
     //   correction jlast es (V or Z reads) + 16 (x read/write) + 8
-    const double es = (double)sizeof(VT), nrows = (double)(r1 - r0);
-    double mg_row_bytes = 0.0;
-    if (use_mg)
-        for (int l = 0; l < p.op.mg.nlev; ++l) {
-            const MgLevelDev &L = p.op.mg.lev[l];
-            const double frac = (double)L.n / (double)n;
-            mg_row_bytes += frac * ((p.op.mg.nu1 + p.op.mg.nu2 + 1) * (L.W * (4.0 + es) + 4.0 * es) + 4.0 * es);
-        }
     double my_bytes = 0.0;
 
-    for (int v = grp; v < p.nv; v += p.groups) {
-        const double *b = p.B + (size_t)v * p.ld;
-        double *x = p.X + (size_t)v * p.ld;
-        VT *V = (VT *)p.V + (size_t)v * (m + 1) * n;
-        VT *Z = use_mg ? (VT *)p.Z + (size_t)v * m * n : nullptr;
-        VT *w = (VT *)p.Wv + (size_t)v * n;
-        double *R = p.R + (size_t)v * n;
+    for (int v = grp; v < nv; v += groups) {
+        const double *__restrict__ b = Bp + (size_t)v * ld;
+        double *x = Xp + (size_t)v * ld;
+        VT *V = Vp + (size_t)v * (m + 1) * n;
+        VT *Z = use_mg ? Zp + (size_t)v * m * n : nullptr;
+        VT *w = Wp + (size_t)v * n;
+        double *R = Rp + (size_t)v * n;
 
         double acc[1];
-        acc[0] = 0.0;
-        for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) { double t = b[i]; acc[0] += t * t; }
-        block_reduce<1>(acc, 1, red);
-        if (!group_sum(1, hcol)) return;
+        {
+            double s = 0.0;
+            for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) { const double t = b[i]; s += t * t; }
+            acc[0] = s;
+        }
+        block_reduce<1>(acc, 1, red, 0);
+        if (!group_sum(1, hcol, red, part2, parity, G, bi, bar, err, tm)) return;
         const double bnorm = sqrt(hcol[0]);
         int iters = 0, cycles = 0, status = 1;
         double beta_prev = 0.0, rel = 0.0;
         if (bnorm == 0.0) {
             for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) x[i] = 0.0;
             status = 0; rel = 0.0;
-            if (!group_sync(bar, p.G, p.err, tm)) return;
+            if (!group_sync(bar, G, err, tm)) return;
         }
         while (bnorm != 0.0) {
             // r = b - A x (FP64, exact operator); needs all of x
-            if (!group_sync(bar, p.G, p.err, tm)) return;
+            if (!group_sync(bar, G, err, tm)) return;
             if (tm && threadIdx.x == 0) tph = clock64();
-            acc[0] = 0.0;
-            for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
-                double s = spmv_row<double, true>(col, aval, n, W, x, i);
-                double r = b[i] - s;
-                R[i] = r;
-                acc[0] += r * r;
+            {
+                double s = 0.0;
+                for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
+                    const double q = b[i] - spmv_row<double, true>(col, aval, n, W, x, i);
+                    R[i] = q;
+                    s += q * q;
+                }
+                acc[0] = s;
             }
-            block_reduce<1>(acc, 1, red);
-            if (!group_sum(1, hcol)) return;
+            block_reduce<1>(acc, 1, red, 0);
+            if (!group_sum(1, hcol, red, part2, parity, G, bi, bar, err, tm)) return;
             const double beta = sqrt(hcol[0]);
-            tick(T_RESID);
+            PHG_TICK(T_RESID);
             my_bytes += nrows * (W * 12.0 + 24.0);
             rel = beta / bnorm;
-            if (rel <= p.tol) { status = 0; break; }
-            if (iters >= p.max_iter) { status = 1; break; }
+            if (rel <= tol) { status = 0; break; }
+            if (iters >= max_iter) { status = 1; break; }
             if (cycles > 0 && !(beta < 0.9999 * beta_prev)) { status = 1; break; }
             beta_prev = beta;
             ++cycles;
-            const double target = fmax(p.tol * bnorm, (sizeof(VT) == 4 ? INNER_RTOL : 0.0) * beta);
-            for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) V[i] = (VT)(R[i] / beta);
+            const double target = fmax(tol * bnorm, inner_rtol * beta);
+            {
+                const double ib = 1.0 / beta;
+                for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) V[i] = (VT)(R[i] * ib);
+            }
             if (threadIdx.x == 0) {
                 g[0] = beta;
                 for (int l = 1; l <= m; ++l) g[l] = 0.0;
             }
             int jlast = 0;
             for (int j = 0; j < m; ++j) {
-                if (!group_sync(bar, p.G, p.err, tm)) return;   // v_j complete
+                if (!group_sync(bar, G, err, tm)) return;   // v_j complete
                 if (tm && threadIdx.x == 0) tph = clock64();
                 const VT *vj = V + (size_t)j * n;
                 const VT *zj = vj;
                 if (use_mg) {
                     VT *zz = Z + (size_t)j * n;
-                    if (!vcycle<VT>(p, vj, zz, gbuf, msm, bar, bi)) return;
-                    if (!group_sync(bar, p.G, p.err, tm)) return;   // z_j complete
-                    tick(T_VCYCLE);
+                    if (!vcycle<VT>(mgp, vj, zz, gbuf, msm, bar, G, bi, err, tm)) return;
+                    if (!group_sync(bar, G, err, tm)) return;   // z_j complete
+                    PHG_TICK(T_VCYCLE);
                     zj = zz;
                     my_bytes += nrows * mg_row_bytes;
                 }
-                // (1) w = A z_j (Jacobi: (A D^-1) v_j), then the dots with
-                // v_0..v_j eight basis vectors at a time (8 loads in flight)
+                // (1) w = A z_j (Jacobi: (A D^-1) v_j); each row issues all
+                // its loads at once
                 for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) w[i] = spmv_row<VT, true>(col, sval, n, W, zj, i);
+                // dots with v_0..v_j, eight basis vectors per pass; per-thread
+                // sums in the Krylov precision (FP32 in the mixed path: GB300's
+                // FP64 rate is a small fraction of FP32), FP64 across threads
                 for (int l0 = 0; l0 <= j; l0 += 8) {
-                    double a8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                    VT t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0, t5 = 0, t6 = 0, t7 = 0;
+                    const int kk = min(8, j + 1 - l0);
+                    const VT *Vl = V + (size_t)l0 * n;
                     for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
                         const VT s = w[i];
-                        VT vv[8];
-#pragma unroll
-                        for (int q = 0; q < 8; ++q) vv[q] = (l0 + q <= j) ? V[(size_t)(l0 + q) * n + i] : (VT)0;
-#pragma unroll
-                        for (int q = 0; q < 8; ++q) a8[q] += (double)(vv[q] * s);
+                        const VT q0 = Vl[i];
+                        const VT q1 = kk > 1 ? Vl[(size_t)n + i] : (VT)0;
+                        const VT q2 = kk > 2 ? Vl[(size_t)2 * n + i] : (VT)0;
+                        const VT q3 = kk > 3 ? Vl[(size_t)3 * n + i] : (VT)0;
+                        const VT q4 = kk > 4 ? Vl[(size_t)4 * n + i] : (VT)0;
+                        const VT q5 = kk > 5 ? Vl[(size_t)5 * n + i] : (VT)0;
+                        const VT q6 = kk > 6 ? Vl[(size_t)6 * n + i] : (VT)0;
+                        const VT q7 = kk > 7 ? Vl[(size_t)7 * n + i] : (VT)0;
+                        t0 += q0 * s; t1 += q1 * s; t2 += q2 * s; t3 += q3 * s;
+                        t4 += q4 * s; t5 += q5 * s; t6 += q6 * s; t7 += q7 * s;
                     }
-                    block_reduce<8>(a8, min(8, j + 1 - l0), red, l0);
+                    const double a8[8] = {(double)t0, (double)t1, (double)t2, (double)t3,
+                                          (double)t4, (double)t5, (double)t6, (double)t7};
+                    block_reduce<8>(a8, kk, red, l0);
                 }
-                tick(T_SPMV_DOT);
-                if (!group_sum(j + 1, hcol)) return;
-                tick(T_DOT_SUM);
+                PHG_TICK(T_SPMV_DOT);
+                if (!group_sum(j + 1, hcol, red, part2, parity, G, bi, bar, err, tm)) return;
+                PHG_TICK(T_DOT_SUM);
                 // (2) w -= sum h_l v_l, ||w||^2
-                double a2 = 0.0;
-                for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
-                    VT s = w[i];
-                    for (int l0 = 0; l0 <= j; l0 += 8) {
-                        VT vv[8];
-#pragma unroll
-                        for (int q = 0; q < 8; ++q) vv[q] = (l0 + q <= j) ? V[(size_t)(l0 + q) * n + i] : (VT)0;
-#pragma unroll
-                        for (int q = 0; q < 8; ++q)
-                            if (l0 + q <= j) s -= (VT)hcol[l0 + q] * vv[q];
+                {
+                    VT a2 = 0;
+                    for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
+                        VT s = w[i];
+                        for (int l0 = 0; l0 <= j; l0 += 8) {
+                            const int kk = min(8, j + 1 - l0);
+                            const VT *Vl = V + (size_t)l0 * n;
+                            const VT q0 = Vl[i];
+                            const VT q1 = kk > 1 ? Vl[(size_t)n + i] : (VT)0;
+                            const VT q2 = kk > 2 ? Vl[(size_t)2 * n + i] : (VT)0;
+                            const VT q3 = kk > 3 ? Vl[(size_t)3 * n + i] : (VT)0;
+                            const VT q4 = kk > 4 ? Vl[(size_t)4 * n + i] : (VT)0;
+                            const VT q5 = kk > 5 ? Vl[(size_t)5 * n + i] : (VT)0;
+                            const VT q6 = kk > 6 ? Vl[(size_t)6 * n + i] : (VT)0;
+                            const VT q7 = kk > 7 ? Vl[(size_t)7 * n + i] : (VT)0;
+                            s -= (VT)hcol[l0] * q0;
+                            if (kk > 1) s -= (VT)hcol[l0 + 1] * q1;
+                            if (kk > 2) s -= (VT)hcol[l0 + 2] * q2;
+                            if (kk > 3) s -= (VT)hcol[l0 + 3] * q3;
+                            if (kk > 4) s -= (VT)hcol[l0 + 4] * q4;
+                            if (kk > 5) s -= (VT)hcol[l0 + 5] * q5;
+                            if (kk > 6) s -= (VT)hcol[l0 + 6] * q6;
+                            if (kk > 7) s -= (VT)hcol[l0 + 7] * q7;
+                        }
+                        w[i] = s;
+                        a2 += s * s;
                     }
-                    w[i] = s;
-                    a2 += (double)s * (double)s;
+                    acc[0] = (double)a2;
                 }
-                acc[0] = a2;
-                block_reduce<1>(acc, 1, red);
-                tick(T_UPDATE);
-                if (!group_sum(1, hcol + j + 1)) return;
-                tick(T_NORM_SUM);
+                block_reduce<1>(acc, 1, red, 0);
+                PHG_TICK(T_UPDATE);
+                if (!group_sum(1, hcol + j + 1, red, part2, parity, G, bi, bar, err, tm)) return;
+                PHG_TICK(T_NORM_SUM);
                 const double hn = sqrt(hcol[j + 1]);
                 // (3) v_{j+1}, Givens
                 if (hn > 0.0) {
@@ -580,12 +614,12 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(Params p) {
                     flag[0] = (fabs(g[j + 1]) <= target) || hn == 0.0;
                 }
                 __syncthreads();
-                tick(T_GIVENS);
+                PHG_TICK(T_GIVENS);
                 ++iters;
                 ++my_steps;
                 my_bytes += nrows * (W * (4.0 + es) + es * (2.0 * (j + 1) + 6.0));
                 jlast = j + 1;
-                if (flag[0] || iters >= p.max_iter) break;
+                if (flag[0] || iters >= max_iter) break;
             }
             // y = H^-1 g; x += D^-1 V y (Jacobi) or Z y (multigrid)
             if (threadIdx.x == 0) {
@@ -596,27 +630,23 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(Params p) {
                 }
             }
             __syncthreads();
-            for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
-                const VT *B = use_mg ? Z : V;
-                double s = 0.0;
-                for (int l0 = 0; l0 < jlast; l0 += 8) {
-                    VT vv[8];
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) vv[q] = (l0 + q < jlast) ? B[(size_t)(l0 + q) * n + i] : (VT)0;
-#pragma unroll
-                    for (int q = 0; q < 8; ++q)
-                        if (l0 + q < jlast) s += y[l0 + q] * (double)vv[q];
+            {
+                const VT *Bb = use_mg ? Z : V;
+                for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
+                    double s = 0.0;
+                    for (int l = 0; l < jlast; ++l) s += y[l] * (double)Bb[(size_t)l * n + i];
+                    x[i] += use_mg ? s : dinv[i] * s;
                 }
-                x[i] += use_mg ? s : dinv[i] * s;
             }
             my_bytes += nrows * (jlast * es + 24.0);
-            tick(T_CORR);
+            PHG_TICK(T_CORR);
         }
         my_iters = max(my_iters, iters);
         my_cycles = max(my_cycles, cycles);
         my_rel = fmax(my_rel, rel);
         my_status = max(my_status, status);
     }
+#undef PHG_TICK
     if (tm && threadIdx.x == 0) tm[T_TOTAL] += clock64() - t_start;
     if (threadIdx.x == 0) atomicAdd(&p.stats->bytes, my_bytes);
     if (threadIdx.x == 0 && bi == 0) {
@@ -635,23 +665,6 @@ __global__ void fold_err(const int *err, GmresStats *st) {
 
 size_t smem_gmres_bytes() { return sizeof(double) * ((MAXM + 1) * MAXM + 2 * MAXM + (MAXM + 1) + MAXM + (MAXM + 2)); }
 
-// shared-memory element offsets of the redundant levels (x, xt, b, r each n)
-size_t smem_mg_elems(const MgDev &mg, int *offs) {
-    size_t e = 0;
-    for (int l = 0; l < MG_MAXLEV; ++l) offs[l] = 0;
-    for (int l = mg.nred; l < mg.nlev; ++l) {
-        offs[l] = (int)e;
-        e += 4 * (size_t)mg.lev[l].n;
-    }
-    return e;
-}
-
-size_t mg_group_elems(const MgDev &mg) {
-    size_t e = 0;
-    for (int l = 0; l < mg.nred; ++l) e += 4 * (size_t)mg.lev[l].n;
-    return e;
-}
-
 constexpr int GROUPS_CAP = 4096;
 
 struct Layout { size_t v, z, w, r, mg, part, bar, err, total; };
@@ -661,14 +674,14 @@ Layout layout(const DevSolveOp &op, int nv, int m, Precision prec) {
     const int n = op.A.n;
     size_t es = prec == PREC_MIXED ? 4 : 8;
     auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
-    const bool mg = op.mg.nlev > 0;
+    const bool mg = op.mgd != nullptr;
     L.v = 0;
     L.z = L.v + al(es * (size_t)nv * (m + 1) * n);
     L.w = L.z + (mg ? al(es * (size_t)nv * m * n) : 0);
     L.r = L.w + al(es * (size_t)nv * n);
     L.mg = L.r + al(8 * (size_t)nv * n);
     const int groups = nv < GROUPS_CAP ? nv : GROUPS_CAP;
-    L.part = L.mg + (mg ? al(es * mg_group_elems(op.mg) * (size_t)groups) : 0);
+    L.part = L.mg + (mg ? al(es * op.mg.group_elems * (size_t)groups) : 0);
     // groups * G <= co-resident blocks (< 4096)
     L.bar = L.part + al(8 * (size_t)4096 * 2 * (MAXM + 2));
     L.err = L.bar + al(8 * (size_t)GROUPS_CAP);
@@ -702,9 +715,8 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     if (m < 1 || m > MAXM || nv < 1) return cudaErrorInvalidValue;
     const int n = op.A.n;
     Params p;
-    int offs[MG_MAXLEV];
     const size_t es = prec == PREC_MIXED ? 4 : 8;
-    const size_t smem = smem_gmres_bytes() + es * smem_mg_elems(op.mg, offs) + 16;
+    const size_t smem = smem_gmres_bytes() + (op.mgd ? es * op.mg.red_elems : 0) + 16;
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
     void *fn = prec == PREC_MIXED ? (void *)gmres_kernel<float> : (void *)gmres_kernel<double>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -727,11 +739,17 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     char *w = (char *)work;
     p.op = op; p.B = B; p.X = X; p.n = n; p.nv = nv; p.ld = ld; p.m = m; p.max_iter = max_iter; p.tol = tol;
     p.V = w + L.v; p.Z = w + L.z; p.Wv = w + L.w; p.R = (double *)(w + L.r);
-    p.mgbuf = w + L.mg; p.mg_group_elems = mg_group_elems(op.mg);
+    p.mgbuf = w + L.mg;
     p.part = (double *)(w + L.part);
     p.bar = (unsigned *)(w + L.bar); p.err = (int *)(w + L.err); p.stats = stats_dev;
     p.groups = groups; p.G = G;
-    for (int l = 0; l < MG_MAXLEV; ++l) p.red_off[l] = offs[l];
+    p.mg_row_bytes = 0.0;
+    if (op.mgd)
+        for (int l = 0; l < op.mg.nlev; ++l) {
+            const MgLevelDev &Lv = op.mg.lev[l];
+            const double frac = (double)Lv.n / (double)n;
+            p.mg_row_bytes += frac * ((op.mg.nu1 + op.mg.nu2 + 1) * (Lv.W * (4.0 + es) + 4.0 * es) + 4.0 * es);
+        }
     static long long *timers = nullptr;
     const bool timing = !no_alloc && getenv("PHG_PHASE_TIMING") != nullptr;
     if (timing && !timers) cudaMalloc(&timers, sizeof(long long) * T_NPHASE);
@@ -754,7 +772,7 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
         static const char *nm[T_NPHASE] = {"resid", "vcycle", "spmv_dot", "dot_sum", "update", "norm_sum",
                                            "givens", "corr", "barrier_wait", "barriers", "total"};
         fprintf(stderr, "[phases] n=%d nv=%d groups=%d G=%d mg=%d iters=%d cycles=%d |", n, nv, groups, G,
-                op.mg.nlev, st.iters, st.cycles);
+                op.mgd ? op.mg.nlev : 0, st.iters, st.cycles);
         for (int k = 0; k < T_NPHASE; ++k) fprintf(stderr, " %s=%lld", nm[k], k == T_BARRIERS ? h[k] : h[k] / 1000);
         fprintf(stderr, " (kcycles)\n");
     }
