@@ -179,6 +179,37 @@ def run_ours(args, ws, rank, local):
             results[name]["e2e_s"] = e2e
         del bv, ops
 
+    # batched ensembles (BASELINE config 3: 256 members on level 5, and 32 on level 6)
+    batched = {}
+    if not args.no_batch:
+        from mke_gb300 import fields
+        for lvl, B in ((5, 256), (args.level, 32)):
+            bm = mesh if lvl == args.level else phelm.Mesh.sphere(lvl)
+            blat, blon = bm.latlon()
+            states = np.stack([fields.barvortex_initial(blat, blon, seed=SEED + k, lmax_noise=16)[0] for k in range(B)])
+            row = {"level": lvl, "members": B}
+            for name, prec in (("mixed", phelm.PHG_MIXED), ("fp64", phelm.PHG_FP64)):
+                bops = phelm.Operators(bm, prec, restart=30, tol=args.tol)
+                bbv = phelm.BarVortex(bops, coriolis=np.sin(blat), **CONF)
+                U = torch.tensor(states, dtype=torch.float64, device=dev)
+                zB = torch.zeros((B, max(bm.outer_size, 1)), dtype=torch.float64, device=dev)
+                with torch.cuda.stream(stream):
+                    bbv.calc_batch(U, zB, zB, out=U, stream=stream)
+                    stream.synchronize()
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    nb = 3
+                    flush.zero_()
+                    e0.record(stream)
+                    for _ in range(nb):
+                        bbv.calc_batch(U, zB, zB, out=U, stream=stream)
+                    e1.record(stream)
+                stream.synchronize()
+                bms = e0.elapsed_time(e1) / nb
+                row[name] = {"member_steps_per_s": B * 1000.0 / bms, "ms_per_step": bms}
+                del bbv, bops
+            row["mixed_over_fp64"] = row["mixed"]["member_steps_per_s"] / row["fp64"]["member_steps_per_s"]
+            batched[f"L{lvl}x{B}"] = row
+
     # max over ranks
     ms = results["mixed"]["ms_per_step"]
     if ws > 1:
@@ -234,6 +265,7 @@ def run_ours(args, ws, rank, local):
         "fp64": {"value": ws * 1000.0 / ms64, "unit": "steps/s", "ms_per_step": ms64,
                  "mixed_over_fp64": ms64 / ms},
         "state_rel_diff_mixed_vs_fp64": rel,
+        "batched": batched,
         "solver": {"mixed": mixed["stats"], "fp64": fp64["stats"]},
         "roofline": {"kernel": "gmres_kernel (persistent solver)", "bound": "hbm", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -376,6 +408,7 @@ def main():
     ap.add_argument("--level", type=int, default=LEVEL)
     ap.add_argument("--tol", type=float, default=TOL)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurements")
     ap.add_argument("--case", choices=["solve", "step", "batch"], help="profiling workload only (no JSON bench line)")
     ap.add_argument("--members", type=int, default=16, help="ensemble members for --case batch")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])

@@ -24,6 +24,9 @@
  *     handles may run concurrently on different streams.
  *   - Outputs may alias inputs where the reference allows it
  *     (BarVortex::calc with u1 == u, examples/test_barvortex.cpp:529).
+ *   - Handles may be destroyed in any order: an operator set holds its mesh
+ *     and a time stepper holds its operator set until it is destroyed itself
+ *     (the reference's classes keep references to the mesh in the same way).
  */
 #ifndef PHELM_GB300_H
 #define PHELM_GB300_H

@@ -1,5 +1,7 @@
 // phg_capi.cu -- the C ABI (include/phelm_gb300.h): handles, HBM residency of
 // the operators, host/device argument staging and the time-step drivers.
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -72,6 +74,7 @@ bool is_device_ptr(const void *p) {
 
 // ----------------------------------------------------------------- mesh ---
 struct phg_mesh_s {
+    std::atomic<int> refs{1};   // the caller's, plus one per operator set
     Mesh m;
     std::once_flag assembled;
     SphereOps ops;
@@ -104,7 +107,11 @@ extern "C" int phg_mesh_load_file(const char *path, phg_mesh *out) {
     return PHG_OK;
 }
 
-extern "C" void phg_mesh_destroy(phg_mesh m) { delete m; }
+static void mesh_release(phg_mesh m) {
+    if (m && m->refs.fetch_sub(1) == 1) delete m;
+}
+
+extern "C" void phg_mesh_destroy(phg_mesh m) { mesh_release(m); }
 
 extern "C" int phg_mesh_info(phg_mesh h, int *V, int *T, int *rs, int *os) {
     if (!h) return fail(PHG_ERR_ARG, "NULL mesh");
@@ -202,6 +209,7 @@ struct ColsBufs {
 }  // namespace
 
 struct phg_ops_s {
+    std::atomic<int> refs{1};   // the caller's, plus one per time stepper
     phg_mesh_s *mesh = nullptr;
     int prec = PHG_FP64;
     int dev = 0;
@@ -223,7 +231,7 @@ struct phg_ops_s {
     GmresStats last{};
     bool stats_pending = false;
     // staging for host pointers
-    DBuf st[6];
+    DBuf st[8];
     // solver-launch profiling
     bool prof = false;
     std::vector<cudaEvent_t> ev;
@@ -455,15 +463,20 @@ extern "C" int phg_ops_create(phg_mesh h, int precision, phg_ops *out) {
     o->norm.n = m.V; o->norm.W = Wn; o->norm.col = o->ncol.as<int>(); o->norm.val = o->nval.as<double>();
     CK(o->stats.ensure(sizeof(GmresStats) * 64));
     CK(cudaMemset(o->stats.p, 0, sizeof(GmresStats) * 64));
+    h->refs++;
     *out = o.release();
     return PHG_OK;
 }
 
-extern "C" void phg_ops_destroy(phg_ops o) {
-    if (!o) return;
+static void ops_release(phg_ops o) {
+    if (!o || o->refs.fetch_sub(1) != 1) return;
     if (o->stream) { cudaStreamSynchronize(o->stream); cudaStreamDestroy(o->stream); }
+    phg_mesh_s *m = o->mesh;
     delete o;
+    mesh_release(m);
 }
+
+extern "C" void phg_ops_destroy(phg_ops o) { ops_release(o); }
 
 extern "C" int phg_ops_set_solver(phg_ops o, int restart, double tol, int max_iter) {
     if (!o) return fail(PHG_ERR_ARG, "NULL handle");
@@ -775,14 +788,17 @@ extern "C" int phg_barvortex_create(phg_ops o, const phg_bv_conf *c, const doubl
         else memcpy(lh.data(), coriolis, 8 * lh.size());
     }
     CK(upload(b->lh, lh));
+    o->refs++;
     *out = b.release();
     return PHG_OK;
 }
 
 extern "C" void phg_barvortex_destroy(phg_barvortex b) {
     if (!b) return;
-    cudaStreamSynchronize(b->o->stream);
+    phg_ops_s *o = b->o;
+    cudaStreamSynchronize(o->stream);
     delete b;
+    ops_release(o);
 }
 
 namespace {
@@ -915,21 +931,208 @@ extern "C" int phg_barvortex_last_stats(phg_barvortex b, int *il, int *ia, int *
 }
 
 // ------------------------------------------------------------- baroclin ---
+// The 4rs x 4rs system of Baroclin (examples/baroclin.cpp:107-243) is stored
+// vertex-interleaved: the reference's unknown q*rs + i (blocks w1 | w2 | u1 |
+// u2) is 4i + q, so one ELL row slice covers the four fields of a vertex.
+// The w rows carry the mass matrix times 1/tau, the u rows (M w - L u) only
+// the mass matrix, so a relative residual over all rows would leave the u
+// rows 1/tau times less accurate: the u rows and the u unknowns are scaled
+// by su, the power of two nearest 1/tau (exact scaling; the solution is the
+// same).
 struct phg_baroclin_s {
     phg_ops_s *o = nullptr;
+    phg_bc_conf c{};
+    double theta = 0.5;
+    double su = 1.0;
+    DBuf col, val, a32, dinv, as64, as32, cpl64, cpl32;
+    DevSolveOp op;
+    ColsBufs bc[4];
+    BcCols bcols;
+    DBuf lh;
+    DBuf U, w, dw, FC, un, wn, un1, ju, jv, jsol, jac, FG, MFG, rp, x, xi, nr, done;
+    GmresStats each[64];
+    int nslots = 0;
 };
 
 extern "C" int phg_baroclin_create(phg_ops o, const phg_bc_conf *c, const double *coriolis, phg_baroclin *out) {
-    (void)o; (void)c; (void)coriolis; (void)out;
-    return fail(PHG_ERR_ARG, "baroclin step is not built yet");
+    if (!o || !c || !out) return fail(PHG_ERR_ARG, "NULL argument");
+    if (!(c->tau > 0) || c->picard_iters < 1 || c->picard_iters > 30) return fail(PHG_ERR_ARG, "bad configuration");
+    auto b = std::make_unique<phg_baroclin_s>();
+    b->o = o;
+    b->c = *c;
+    const Mesh &m = o->mesh->m;
+    const int rs = o->rs, n = 4 * rs;
+    BaroclinParams bp;
+    bp.tau = c->tau; bp.sigma = c->sigma; bp.mu = c->mu; bp.sigma1 = c->sigma1; bp.mu1 = c->mu1;
+    bp.alpha = c->alpha; bp.theta = b->theta;
+    Csr A, bcol[4];
+    assemble_baroclin(m, bp, A, bcol);
+    // interleave: block-order row/column q*rs + i -> 4i + q, columns ascending
+    std::vector<std::vector<std::pair<int, double>>> rows(n);
+    for (int r = 0; r < A.n; ++r) {
+        const int nr_ = 4 * (r % rs) + r / rs;
+        for (int k = A.ptr[r]; k < A.ptr[r + 1]; ++k) rows[nr_].push_back({4 * (A.col[k] % rs) + A.col[k] / rs, A.val[k]});
+    }
+    b->su = std::ldexp(1.0, (int)std::lround(std::log2(1.0 / c->tau)));
+    const double su = b->su;
+    int W = 0;
+    for (int i = 0; i < n; ++i) {
+        auto &row = rows[i];
+        std::sort(row.begin(), row.end());
+        W = std::max(W, (int)row.size());
+        for (auto &e : row) {
+            const bool urow = (i & 3) >= 2, ucol = (e.first & 3) >= 2;
+            if (urow && !ucol) e.second *= su;
+            if (!urow && ucol) e.second /= su;
+        }
+    }
+    std::vector<int> col((size_t)W * n);
+    std::vector<double> val((size_t)W * n, 0.0), dinv(n, 0.0);
+    for (int i = 0; i < n; ++i) {
+        int k = 0;
+        for (auto &e : rows[i]) {
+            col[(size_t)k * n + i] = e.first;
+            val[(size_t)k * n + i] = e.second;
+            if (e.first == i) dinv[i] = 1.0 / e.second;
+            ++k;
+        }
+        for (; k < W; ++k) col[(size_t)k * n + i] = i;
+        if (!(dinv[i] != 0.0) || !std::isfinite(dinv[i])) return fail(PHG_ERR_ARG, "zero diagonal in row %d", i);
+    }
+    CK(upload(b->col, col)); CK(upload(b->val, val)); CK(upload(b->a32, to_f32(val))); CK(upload(b->dinv, dinv));
+    DevSolveOp &op = b->op;
+    op.A.n = n; op.A.W = W; op.A.col = b->col.as<int>(); op.A.val = b->val.as<double>();
+    op.a32 = b->a32.as<float>(); op.dinv = b->dinv.as<double>();
+    if (o->L.op.mgd) {
+        // w rows: Jacobi; u rows: -L u = r_u - M w with the Laplacian's multigrid
+        op.mg = o->L.op.mg; op.mgd = o->L.op.mgd;
+        op.block4 = 1;
+        std::vector<double> mv;
+        to_ell(o->mesh->ops.idt, o->W, nullptr, mv);
+        for (auto &x : mv) x *= su;
+        CK(upload(b->cpl64, mv)); CK(upload(b->cpl32, to_f32(mv)));
+        op.cpl = o->ell(b->cpl64); op.cpl32 = b->cpl32.as<float>();
+    } else {
+        // small meshes (no multigrid hierarchy): Jacobi-scaled GMRES
+        std::vector<double> as64(val.size());
+        for (size_t e = 0; e < val.size(); ++e) as64[e] = val[e] * dinv[col[e]];
+        CK(upload(b->as64, as64)); CK(upload(b->as32, to_f32(as64)));
+        op.as64 = b->as64.as<double>(); op.as32 = b->as32.as<float>();
+    }
+    int r;
+    for (int q = 0; q < 4; ++q) {
+        if ((r = build_cols(bcol[q], b->bc[q]))) return r;
+        b->bcols.c[q] = b->bc[q].c;
+    }
+    std::vector<double> lh(o->V, 0.0);
+    if (coriolis) {
+        if (is_device_ptr(coriolis)) CK(cudaMemcpy(lh.data(), coriolis, 8 * lh.size(), cudaMemcpyDeviceToHost));
+        else memcpy(lh.data(), coriolis, 8 * lh.size());
+    }
+    CK(upload(b->lh, lh));
+    const size_t V = o->V;
+    DBuf *two[] = {&b->U, &b->w, &b->dw, &b->FC, &b->un, &b->wn, &b->un1};
+    for (DBuf *d : two) CK(d->ensure(8 * 2 * V));
+    CK(b->ju.ensure(8 * 5 * V)); CK(b->jv.ensure(8 * 5 * V));
+    CK(b->jsol.ensure(8 * 5 * 8 * (size_t)rs)); CK(b->jac.ensure(8 * 5 * (size_t)rs));
+    CK(b->FG.ensure(8 * 2 * (size_t)rs)); CK(b->MFG.ensure(8 * 2 * (size_t)rs)); CK(b->xi.ensure(8 * 2 * (size_t)rs));
+    CK(b->rp.ensure(8 * (size_t)n)); CK(b->x.ensure(8 * (size_t)n));
+    CK(b->nr.ensure(16)); CK(b->done.ensure(4));
+    o->refs++;
+    *out = b.release();
+    return PHG_OK;
 }
 
-extern "C" void phg_baroclin_destroy(phg_baroclin b) { delete b; }
+extern "C" void phg_baroclin_destroy(phg_baroclin b) {
+    if (!b) return;
+    phg_ops_s *o = b->o;
+    cudaStreamSynchronize(o->stream);
+    delete b;
+    ops_release(o);
+}
+
+namespace {
+
+// One Crank-Nicolson / Picard step (examples/baroclin.cpp:445-606), all
+// arguments on the device.
+int bc_step_dev(phg_baroclin_s *b, double *u11, double *u21, const double *u1, const double *u2,
+                const double *bnd, const double *f, const double *g, cudaStream_t s) {
+    phg_ops_s *o = b->o;
+    const int V = o->V, rs = o->rs, os = o->os;
+    const phg_bc_conf &c = b->c;
+    const double th = b->theta;
+    int r, slot = 0;
+    double *U = b->U.as<double>(), *w = b->w.as<double>(), *dw = b->dw.as<double>();
+    double *FC = b->FC.as<double>(), *GC = FC + V;
+    double *un = b->un.as<double>(), *wn = b->wn.as<double>(), *un1 = b->un1.as<double>();
+    double *xi = b->xi.as<double>(), *x = b->x.as<double>(), *rp = b->rp.as<double>();
+    const int *p2io = o->p2io.as<int>(), *isb = o->isb.as<int>();
+    // inputs first: the outputs may alias them
+    CK(cudaMemcpyAsync(U, u1, 8 * (size_t)V, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(U + V, u2, 8 * (size_t)V, cudaMemcpyDeviceToDevice, s));
+    // w = L(u), dw = L(w), both layers at once, with the boundary values bnd
+    if ((r = laplace_calc2_dev(o, xi, rs, U, V, 2, slot++, s, o->tol))) return r;
+    CK(p2u(w, V, xi, rs, bnd, 0, p2io, isb, V, 2, s));
+    if ((r = laplace_calc2_dev(o, xi, rs, w, V, 2, slot++, s, o->tol))) return r;
+    CK(p2u(dw, V, xi, rs, bnd, 0, p2io, isb, V, 2, s));
+    BcCoef k;
+    k.a = -0.5 * (1.0 - th) * c.sigma;
+    k.b = 0.5 * (1.0 - th) * c.sigma;
+    k.mu1t = c.mu * (1.0 - th);
+    k.itau = 1.0 / c.tau;
+    k.g_u2 = -c.alpha * c.alpha / c.tau;
+    k.g_w2 = -c.alpha * c.alpha * c.mu1 * (1 - th);
+    k.g_u2b = c.alpha * c.alpha * c.sigma1 * (1 - th);
+    k.alpha2 = c.alpha * c.alpha;
+    CK(bc_fcgc(FC, GC, w, w + V, dw, dw + V, U + V, f, g, k, V, s));
+    CK(cudaMemcpyAsync(un, U, 16 * (size_t)V, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(wn, w, 16 * (size_t)V, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemsetAsync(b->done.p, 0, 4, s));
+    double *F = b->FG.as<double>(), *G = F + rs, *MF = b->MFG.as<double>(), *MG = MF + rs;
+    for (int it = 0; it < c.picard_iters; ++it) {
+        // the five Jacobians J(U1, W1 + l), J(U2, W2), J(U1, W2), J(U2, W1 + l), J(U1, U2)
+        CK(bc_jin(b->ju.as<double>(), b->jv.as<double>(), U, U + V, w, w + V, un, un + V, wn, wn + V,
+                  b->lh.as<double>(), th, V, s));
+        if ((r = jacobian_derivs_dev(o, b->ju.as<double>(), b->jv.as<double>(), V, b->jsol.as<double>(), 5, slot++, s,
+                                     o->tol)))
+            return r;
+        CK(jac_combine(b->jsol.as<double>(), rs, rs, b->jac.as<double>(), rs, nullptr, 0, nullptr, 5, s));
+        CK(bc_fg(F, G, b->jac.as<double>(), FC, GC, o->imap(), k.alpha2, rs, s));
+        // rp = [M F, M G, 0, 0] - boundary columns * bnd, interleaved
+        CK(apply_op(o->ML.op.A, DevCols(), F, rs, nullptr, nullptr, 0, nullptr, MF, rs, 2, s));
+        CK(bc_rhs(rp, MF, MG, b->bcols, os ? bnd : nullptr, b->su, rs, s));
+        // warm start from the current iterate
+        CK(bc_pack(x, wn, wn + V, un, un + V, o->imap(), b->su, rs, s));
+        if ((r = solve(o, b->op, rp, x, 1, 4 * rs, o->tol, slot++, s))) return r;
+        CK(bc_unpack(wn, wn + V, un1, un1 + V, x, os ? bnd : nullptr, p2io, isb, 1.0 / b->su, V, s));
+        // nr = max(dist(u1_n1, u1_n), dist(u2_n1, u2_n)); commit unless stopped
+        if ((r = norm_dev(o, un1, un, 2, b->nr.as<double>(), true, true, s))) return r;
+        CK(bc_commit(un, un1, b->nr.as<double>(), b->done.as<int>(), c.picard_tol, 2 * V, s));
+    }
+    CK(cudaMemcpyAsync(u11, un, 8 * (size_t)V, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(u21, un + V, 8 * (size_t)V, cudaMemcpyDeviceToDevice, s));
+    b->nslots = slot;
+    return PHG_OK;
+}
+
+}  // namespace
 
 extern "C" int phg_baroclin_calc(phg_baroclin b, double *u11, double *u21, const double *u1, const double *u2,
                                  const double *bnd, const double *f, const double *g, void *stream) {
-    (void)b; (void)u11; (void)u21; (void)u1; (void)u2; (void)bnd; (void)f; (void)g; (void)stream;
-    return fail(PHG_ERR_ARG, "baroclin step is not built yet");
+    if (!b || !u11 || !u21 || !u1 || !u2) return fail(PHG_ERR_ARG, "NULL argument");
+    phg_ops_s *o = b->o;
+    cudaStream_t s = o->str(stream);
+    Stage st(o, s);
+    const double *d1, *d2, *db, *df, *dg; double *o1, *o2;
+    CK(st.in(u1, o->V, &d1)); CK(st.in(u2, o->V, &d2)); CK(st.in(bnd, o->os, &db));
+    CK(st.in(f, o->V, &df)); CK(st.in(g, o->V, &dg));
+    CK(st.out(u11, o->V, &o1)); CK(st.out(u21, o->V, &o2));
+    if (o->os == 0) db = nullptr;
+    int r = bc_step_dev(b, o1, o2, d1, d2, db, df, dg, s);
+    if (r) return r;
+    CK(st.finish());
+    if (!st.host) return PHG_OK;
+    return check_stats(o, b->nslots, s, nullptr, b->each);
 }
 
 // ------------------------------------------------------- no allocation ---

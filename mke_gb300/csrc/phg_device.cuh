@@ -63,6 +63,14 @@ struct DevSolveOp {
     const float *a32 = nullptr;    // A in FP32 (multigrid path, mixed precision)
     MgDev mg;                      // host copy (sizes)
     const MgDev *mgd = nullptr;    // the same descriptor in device memory (read by the kernel)
+    // Block preconditioner of a vertex-interleaved 4-field system (unknown
+    // 4i+q, q = 0,1 "w" rows, q = 2,3 "u" rows whose diagonal blocks are -L):
+    // z_w = D^-1 v_w, z_u = -Vcycle_L(v_u - M z_w); mgd is then the hierarchy
+    // of L and cpl the coupling mass matrix (rs x rs).
+    int block4 = 0;
+    DevEll cpl;
+    const float *cpl32 = nullptr;
+    const float *dinv32 = nullptr;
 };
 
 // rs x os boundary columns in CSR over rows (few nonzero rows).

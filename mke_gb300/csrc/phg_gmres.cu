@@ -63,6 +63,7 @@ struct Params {
     int groups, G;
     long long *timers;       // optional phase cycle counters (block 0)
     double mg_row_bytes;     // algorithmic bytes of one V-cycle per fine row
+    size_t group_elems;      // per-group scratch elements (V-cycle + block preconditioner)
 };
 
 // phase cycle counters kept by block 0 when PHG_PHASE_TIMING is set
@@ -201,6 +202,27 @@ __device__ __forceinline__ VT spmv_row(const int *__restrict__ col, const VT *__
         const size_t e = (size_t)k * n + i;
         const VT xv = CG ? ldcg(&x[__ldg(&col[e])]) : x[__ldg(&col[e])];
         s += __ldg(&val[e]) * xv;
+    }
+    return s;
+}
+
+// wide rows (block systems, W > 8): eight entries' loads in flight at a time
+template <typename VT>
+__device__ __noinline__ VT spmv_row_wide(const int *__restrict__ col, const VT *__restrict__ val, int n, int W,
+                                         const VT *x, int i) {
+    VT s = 0;
+    for (int k0 = 0; k0 < W; k0 += 8) {
+        int c[8];
+        VT a[8], xv[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k0 + k < W) { c[k] = __ldg(&col[(size_t)(k0 + k) * n + i]); a[k] = __ldg(&val[(size_t)(k0 + k) * n + i]); }
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k0 + k < W) xv[k] = ldcg(&x[c[k]]);
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k0 + k < W) s += a[k] * xv[k];
     }
     return s;
 }
@@ -428,7 +450,17 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
     if (sizeof(VT) == 8) sval = (const VT *)(use_mg ? (const void *)p.op.A.val : (const void *)p.op.as64);
     else sval = (const VT *)(use_mg ? (const void *)p.op.a32 : (const void *)p.op.as32);
     const double *__restrict__ dinv = p.op.dinv;
-    VT *gbuf = use_mg ? (VT *)p.mgbuf + (size_t)grp * p.op.mg.group_elems : nullptr;
+    VT *gbuf = use_mg ? (VT *)p.mgbuf + (size_t)grp * p.group_elems : nullptr;
+    const int block4 = p.op.block4;
+    const int rsb = block4 ? n / 4 : 0;          // vertices of a block system
+    // block preconditioner: the second V-cycle gets its own level scratch so
+    // that it can start while other blocks still read the first one's
+    VT *gbuf2 = (gbuf && block4) ? gbuf + p.op.mg.group_elems : nullptr;
+    VT *bt3 = gbuf2 ? gbuf2 + p.op.mg.group_elems : nullptr;
+    VT *bt4 = bt3 ? bt3 + rsb : nullptr, *bu3 = bt4 ? bt4 + rsb : nullptr, *bu4 = bu3 ? bu3 + rsb : nullptr;
+    const int *cpl_col = p.op.cpl.col;
+    const VT *cpl_val = (const VT *)(sizeof(VT) == 8 ? (const void *)p.op.cpl.val : (const void *)p.op.cpl32);
+    const int cpl_W = p.op.cpl.W;
     long long *tm = (p.timers && blockIdx.x == 0) ? p.timers : nullptr;
     const double *Bp = p.B;
     double *Xp = p.X;
@@ -485,7 +517,8 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
             {
                 double s = 0.0;
                 for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
-                    const double q = b[i] - spmv_row<double, true>(col, aval, n, W, x, i);
+                    const double q = b[i] - (W <= 8 ? spmv_row<double, true>(col, aval, n, W, x, i)
+                                                    : spmv_row_wide<double>(col, aval, n, W, x, i));
                     R[i] = q;
                     s += q * q;
                 }
@@ -517,7 +550,37 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
                 if (tm && threadIdx.x == 0) tph = clock64();
                 const VT *vj = V + (size_t)j * n;
                 const VT *zj = vj;
-                if (use_mg) {
+                if (use_mg && block4) {
+                    // z_w = D^-1 v_w ; t = v_u - M z_w ; z_u = -Vcycle(t)
+                    VT *zz = Z + (size_t)j * n;
+                    for (int i = r0 + threadIdx.x; i < r1; i += BLOCK)
+                        if ((i & 3) < 2) zz[i] = (VT)(dinv[i] * (double)vj[i]);
+                    if (!group_sync(bar, G, err, tm)) return;
+                    int k0, k1;
+                    own_rows(rsb, G, bi, k0, k1);
+                    for (int k = k0 + threadIdx.x; k < k1; k += BLOCK) {
+                        VT s3 = 0, s4 = 0;
+                        for (int e = 0; e < cpl_W; ++e) {
+                            const int c = __ldg(&cpl_col[(size_t)e * rsb + k]);
+                            const VT a = __ldg(&cpl_val[(size_t)e * rsb + k]);
+                            s3 += a * ldcg(&zz[4 * c]);
+                            s4 += a * ldcg(&zz[4 * c + 1]);
+                        }
+                        bt3[k] = ldcg(&vj[4 * k + 2]) - s3;
+                        bt4[k] = ldcg(&vj[4 * k + 3]) - s4;
+                    }
+                    if (!vcycle<VT>(mgp, bt3, bu3, gbuf, msm, bar, G, bi, err, tm)) return;
+                    if (!vcycle<VT>(mgp, bt4, bu4, gbuf2, msm, bar, G, bi, err, tm)) return;
+                    if (!group_sync(bar, G, err, tm)) return;
+                    for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
+                        const int q = i & 3;
+                        if (q >= 2) zz[i] = -ldcg(q == 2 ? &bu3[i >> 2] : &bu4[i >> 2]);
+                    }
+                    if (!group_sync(bar, G, err, tm)) return;   // z_j complete
+                    PHG_TICK(T_VCYCLE);
+                    zj = zz;
+                    my_bytes += nrows * mg_row_bytes;
+                } else if (use_mg) {
                     VT *zz = Z + (size_t)j * n;
                     if (!vcycle<VT>(mgp, vj, zz, gbuf, msm, bar, G, bi, err, tm)) return;
                     if (!group_sync(bar, G, err, tm)) return;   // z_j complete
@@ -527,7 +590,8 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
                 }
                 // (1) w = A z_j (Jacobi: (A D^-1) v_j); each row issues all
                 // its loads at once
-                for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) w[i] = spmv_row<VT, true>(col, sval, n, W, zj, i);
+                for (int i = r0 + threadIdx.x; i < r1; i += BLOCK)
+                    w[i] = W <= 8 ? spmv_row<VT, true>(col, sval, n, W, zj, i) : spmv_row_wide<VT>(col, sval, n, W, zj, i);
                 // dots with v_0..v_j, eight basis vectors per pass; per-thread
                 // sums in the Krylov precision (FP32 in the mixed path: GB300's
                 // FP64 rate is a small fraction of FP32), FP64 across threads
@@ -669,6 +733,13 @@ constexpr int GROUPS_CAP = 4096;
 
 struct Layout { size_t v, z, w, r, mg, part, bar, err, total; };
 
+// per-group multigrid scratch: one V-cycle's levels, or two V-cycles' levels
+// and the 4 vertex vectors of the block preconditioner
+size_t block_group_elems(const DevSolveOp &op) {
+    if (!op.block4) return op.mg.group_elems;
+    return 2 * op.mg.group_elems + 4 * (size_t)(op.A.n / 4);
+}
+
 Layout layout(const DevSolveOp &op, int nv, int m, Precision prec) {
     Layout L;
     const int n = op.A.n;
@@ -681,7 +752,8 @@ Layout layout(const DevSolveOp &op, int nv, int m, Precision prec) {
     L.r = L.w + al(es * (size_t)nv * n);
     L.mg = L.r + al(8 * (size_t)nv * n);
     const int groups = nv < GROUPS_CAP ? nv : GROUPS_CAP;
-    L.part = L.mg + (mg ? al(es * op.mg.group_elems * (size_t)groups) : 0);
+    const size_t ge = block_group_elems(op);
+    L.part = L.mg + (mg ? al(es * ge * (size_t)groups) : 0);
     // groups * G <= co-resident blocks (< 4096)
     L.bar = L.part + al(8 * (size_t)4096 * 2 * (MAXM + 2));
     L.err = L.bar + al(8 * (size_t)GROUPS_CAP);
@@ -740,6 +812,7 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     p.op = op; p.B = B; p.X = X; p.n = n; p.nv = nv; p.ld = ld; p.m = m; p.max_iter = max_iter; p.tol = tol;
     p.V = w + L.v; p.Z = w + L.z; p.Wv = w + L.w; p.R = (double *)(w + L.r);
     p.mgbuf = w + L.mg;
+    p.group_elems = block_group_elems(op);
     p.part = (double *)(w + L.part);
     p.bar = (unsigned *)(w + L.bar); p.err = (int *)(w + L.err); p.stats = stats_dev;
     p.groups = groups; p.G = G;
@@ -747,7 +820,7 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     if (op.mgd)
         for (int l = 0; l < op.mg.nlev; ++l) {
             const MgLevelDev &Lv = op.mg.lev[l];
-            const double frac = (double)Lv.n / (double)n;
+            const double frac = (double)Lv.n / (double)n * (op.block4 ? 2.0 : 1.0);
             p.mg_row_bytes += frac * ((op.mg.nu1 + op.mg.nu2 + 1) * (Lv.W * (4.0 + es) + 4.0 * es) + 4.0 * es);
         }
     static long long *timers = nullptr;

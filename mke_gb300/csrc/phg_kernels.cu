@@ -323,3 +323,172 @@ cudaError_t gather(double *y, int ldy, const double *x, int ldx, const int *map,
 }
 
 }  // namespace phg
+
+// ------------------------------------------------------------ baroclin ----
+namespace phg {
+namespace {
+
+// FC / GC of Baroclin::calc (examples/baroclin.cpp:501-536), vectors of V
+__global__ void k_bc_fcgc(double *FC, double *GC, const double *w1, const double *w2, const double *dw1,
+                          const double *dw2, const double *u2, const double *f, const double *g, BcCoef c, int V) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < V; t += gridDim.x * blockDim.x) {
+        double fc = c.a * w1[t] + c.b * w2[t];
+        fc = 1.0 * fc + c.mu1t * dw1[t];
+        fc = 1.0 * fc + c.itau * w1[t];
+        double gc = c.a * w1[t] + c.a * w2[t];
+        gc = 1.0 * gc + c.mu1t * dw2[t];
+        gc = 1.0 * gc + c.itau * w2[t];
+        gc = 1.0 * gc + c.g_u2 * u2[t];
+        gc = 1.0 * gc + c.g_w2 * w2[t];
+        gc = 1.0 * gc + c.g_u2b * u2[t];
+        if (f) fc += f[t];
+        if (g) gc += c.alpha2 * g[t];
+        FC[t] = fc;
+        GC[t] = gc;
+    }
+}
+
+// the five Jacobian argument pairs of one Picard iteration
+// (examples/baroclin.cpp:551-575): out ju[k], jv[k] for k = 0..4
+__global__ void k_bc_jin(double *ju, double *jv, const double *u1, const double *u2, const double *w1,
+                         const double *w2, const double *u1n, const double *u2n, const double *w1n,
+                         const double *w2n, const double *lh, double th, int V) {
+    const double a = 1.0 - th;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < V; t += gridDim.x * blockDim.x) {
+        const double U1 = a * u1[t] + th * u1n[t];
+        const double U2 = a * u2[t] + th * u2n[t];
+        double W1 = a * w1[t] + th * w1n[t];
+        const double W1l = W1 + lh[t];
+        const double W2 = a * w2[t] + th * w2n[t];
+        ju[t] = U1;              jv[t] = W1l;
+        ju[V + t] = U2;          jv[V + t] = W2;
+        ju[2 * (size_t)V + t] = U1; jv[2 * (size_t)V + t] = W2;
+        ju[3 * (size_t)V + t] = U2; jv[3 * (size_t)V + t] = W1l;
+        ju[4 * (size_t)V + t] = U1; jv[4 * (size_t)V + t] = U2;
+    }
+}
+
+// F = -jac0 - jac1 + FC[inner]; G = -jac2 - jac3 + alpha^2 jac4 + GC[inner]
+__global__ void k_bc_fg(double *F, double *G, const double *jac, const double *FC, const double *GC,
+                        const int *inner, double alpha2, int rs) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rs; i += gridDim.x * blockDim.x) {
+        double f = -1.0 * jac[i] + -1.0 * jac[rs + i];
+        double g = -1.0 * jac[2 * (size_t)rs + i] + -1.0 * jac[3 * (size_t)rs + i];
+        g = 1.0 * g + alpha2 * jac[4 * (size_t)rs + i];
+        const int p = inner ? inner[i] : i;
+        F[i] = f + FC[p];
+        G[i] = g + GC[p];
+    }
+}
+
+// interleaved right-hand side: [M F, M G, 0, 0] minus the boundary columns,
+// the u rows scaled by su
+__global__ void k_bc_rhs(double *rp, const double *MF, const double *MG, BcCols bc, const double *bnd, double su,
+                         int rs) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rs; i += gridDim.x * blockDim.x) {
+        double t[4] = {0, 0, 0, 0};
+        if (bnd)
+            for (int q = 0; q < 4; ++q)
+                if (bc.c[q].ptr)
+                    for (int k = bc.c[q].ptr[i]; k < bc.c[q].ptr[i + 1]; ++k) t[q] += -bnd[bc.c[q].col[k]] * bc.c[q].val[k];
+        rp[4 * (size_t)i] = MF[i] + t[0];
+        rp[4 * (size_t)i + 1] = MG[i] + t[1];
+        rp[4 * (size_t)i + 2] = su * t[2];
+        rp[4 * (size_t)i + 3] = su * t[3];
+    }
+}
+
+// interleave the inner parts of four full vectors (initial guess), the u
+// unknowns scaled by su
+__global__ void k_bc_pack(double *x, const double *a, const double *b, const double *c, const double *d,
+                          const int *inner, double su, int rs) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rs; i += gridDim.x * blockDim.x) {
+        const int p = inner[i];
+        x[4 * (size_t)i] = a[p];
+        x[4 * (size_t)i + 1] = b[p];
+        x[4 * (size_t)i + 2] = su * c[p];
+        x[4 * (size_t)i + 3] = su * d[p];
+    }
+}
+
+// de-interleave into four full vectors with the boundary values (p2u)
+__global__ void k_bc_unpack(double *a, double *b, double *c, double *d, const double *x, const double *bnd,
+                            const int *p2io, const int *isb, double isu, int V) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < V; p += gridDim.x * blockDim.x) {
+        const int j = p2io[p];
+        if (isb[p]) {
+            const double v = bnd ? bnd[j] : 0.0;
+            a[p] = v; b[p] = v; c[p] = v; d[p] = v;
+        } else {
+            a[p] = x[4 * (size_t)j]; b[p] = x[4 * (size_t)j + 1];
+            c[p] = isu * x[4 * (size_t)j + 2]; d[p] = isu * x[4 * (size_t)j + 3];
+        }
+    }
+}
+
+// u_n <- u_n1 (both layers) unless stopped; stop once max(nr) < tol
+__global__ void k_bc_commit(double *un, const double *un1, const int *done, int n) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+        if (!*done) un[t] = un1[t];
+}
+
+__global__ void k_bc_done(const double *nr, int *done, double tol) {
+    if (threadIdx.x == 0 && blockIdx.x == 0 && !*done) {
+        const double m = nr[0] > nr[1] ? nr[0] : nr[1];
+        if (m < tol) *done = 1;
+    }
+}
+
+}  // namespace
+
+cudaError_t bc_fcgc(double *FC, double *GC, const double *w1, const double *w2, const double *dw1, const double *dw2,
+                    const double *u2, const double *f, const double *g, const BcCoef &c, int V, cudaStream_t s) {
+    k_bc_fcgc<<<grid_for(V), TB, 0, s>>>(FC, GC, w1, w2, dw1, dw2, u2, f, g, c, V);
+    g_kernel_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t bc_jin(double *ju, double *jv, const double *u1, const double *u2, const double *w1, const double *w2,
+                   const double *u1n, const double *u2n, const double *w1n, const double *w2n, const double *lh,
+                   double th, int V, cudaStream_t s) {
+    k_bc_jin<<<grid_for(V), TB, 0, s>>>(ju, jv, u1, u2, w1, w2, u1n, u2n, w1n, w2n, lh, th, V);
+    g_kernel_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t bc_fg(double *F, double *G, const double *jac, const double *FC, const double *GC, const int *inner,
+                  double alpha2, int rs, cudaStream_t s) {
+    k_bc_fg<<<grid_for(rs), TB, 0, s>>>(F, G, jac, FC, GC, inner, alpha2, rs);
+    g_kernel_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t bc_rhs(double *rp, const double *MF, const double *MG, const BcCols &bc, const double *bnd, double su,
+                   int rs, cudaStream_t s) {
+    k_bc_rhs<<<grid_for(rs), TB, 0, s>>>(rp, MF, MG, bc, bnd, su, rs);
+    g_kernel_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t bc_pack(double *x, const double *a, const double *b, const double *c, const double *d, const int *inner,
+                    double su, int rs, cudaStream_t s) {
+    k_bc_pack<<<grid_for(rs), TB, 0, s>>>(x, a, b, c, d, inner, su, rs);
+    g_kernel_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t bc_unpack(double *a, double *b, double *c, double *d, const double *x, const double *bnd,
+                      const int *p2io, const int *isb, double isu, int V, cudaStream_t s) {
+    k_bc_unpack<<<grid_for(V), TB, 0, s>>>(a, b, c, d, x, bnd, p2io, isb, isu, V);
+    g_kernel_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t bc_commit(double *un, const double *un1, const double *nr, int *done, double tol, int n, cudaStream_t s) {
+    k_bc_commit<<<grid_for(n), TB, 0, s>>>(un, un1, done, n);
+    k_bc_done<<<1, 32, 0, s>>>(nr, done, tol);
+    g_kernel_launches += 2;
+    return cudaGetLastError();
+}
+
+}  // namespace phg

@@ -41,4 +41,31 @@ cudaError_t bv_commit(double *u_n, const double *u_n1, const double *nr, const d
                       int V, int nv, cudaStream_t s);
 cudaError_t gather(double *y, int ldy, const double *x, int ldx, const int *map, int n, int nv, cudaStream_t s);
 
+// Baroclin step helpers (examples/baroclin.cpp:445-606)
+struct BcCoef {
+    double a;       // -0.5 (1-theta) sigma
+    double b;       //  0.5 (1-theta) sigma
+    double mu1t;    // mu (1-theta)
+    double itau;    // 1/tau
+    double g_u2;    // -alpha^2 / tau
+    double g_w2;    // -alpha^2 mu1 (1-theta)
+    double g_u2b;   //  alpha^2 sigma1 (1-theta)
+    double alpha2;  //  alpha^2
+};
+struct BcCols { DevCols c[4]; };
+cudaError_t bc_fcgc(double *FC, double *GC, const double *w1, const double *w2, const double *dw1, const double *dw2,
+                    const double *u2, const double *f, const double *g, const BcCoef &c, int V, cudaStream_t s);
+cudaError_t bc_jin(double *ju, double *jv, const double *u1, const double *u2, const double *w1, const double *w2,
+                   const double *u1n, const double *u2n, const double *w1n, const double *w2n, const double *lh,
+                   double th, int V, cudaStream_t s);
+cudaError_t bc_fg(double *F, double *G, const double *jac, const double *FC, const double *GC, const int *inner,
+                  double alpha2, int rs, cudaStream_t s);
+cudaError_t bc_rhs(double *rp, const double *MF, const double *MG, const BcCols &bc, const double *bnd, double su,
+                   int rs, cudaStream_t s);
+cudaError_t bc_pack(double *x, const double *a, const double *b, const double *c, const double *d, const int *inner,
+                    double su, int rs, cudaStream_t s);
+cudaError_t bc_unpack(double *a, double *b, double *c, double *d, const double *x, const double *bnd,
+                      const int *p2io, const int *isb, double isu, int V, cudaStream_t s);
+cudaError_t bc_commit(double *un, const double *un1, const double *nr, int *done, double tol, int n, cudaStream_t s);
+
 }  // namespace phg

@@ -1,0 +1,160 @@
+"""Baroclin step on the GPU vs the reference's own outputs and the oracle.
+
+One step (examples/baroclin.cpp:445-606) solves 2 + 2 x picard_iters systems:
+two two-layer Laplace applies (mass solves) and, per Picard iteration, one
+batch of 5 Jacobians (40 mass solves) and the 4rs x 4rs Crank-Nicolson block
+system.  Every solve runs to 1e-12 relative residual here, so the step
+outputs agree with the discrete solution to 1e-9 relative L2 (the tolerance
+of the other time-step tests).
+
+The reference's block solve stops at a 1e-13 relative residual of the
+unscaled system, whose w rows are 1/tau times larger than its u rows; from
+level 5 on that leaves ~1e-8 in its u fields (the oracle, identical to it,
+moves by 1.2e-8 at level 5 when driven to 1e-16).  Levels 4-5 are therefore
+checked against the oracle driven to 1e-16, and against its default
+(reference) answer only to the reference's own accuracy.
+"""
+import numpy as np
+import pytest
+
+import pyoracle as po
+from mke_gb300 import fields, phelm
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-9
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300))
+
+
+_ops = {}
+
+
+def ops_for(level, precision=phelm.PHG_FP64):
+    key = (level, precision)
+    if key not in _ops:
+        m = phelm.Mesh.sphere(level)
+        _ops[key] = (m, phelm.Operators(m, precision, tol=1e-12))
+    return _ops[key]
+
+
+@pytest.mark.parametrize("precision", [phelm.PHG_FP64, phelm.PHG_MIXED])
+@pytest.mark.parametrize("level", [1, 2, 3])
+def test_step_vs_reference(golden, level, precision):
+    """Against the reference's own step (3 Picard iterations, coriolis sin(lat))."""
+    g = golden(f"ref_L{level}.npz")
+    m, ops = ops_for(level, precision)
+    lat, _ = m.latlon()
+    bc = phelm.Baroclin(ops, picard_iters=3, coriolis=np.sin(lat))
+    z = np.zeros(m.outer_size)
+    a, b = bc.calc(g["in_u"], g["in_v"], z)
+    assert rel(a, g["out_bc_step1_u1"]) <= TOL
+    assert rel(b, g["out_bc_step1_u2"]) <= TOL
+
+
+_tight = {}
+
+
+def oracle_step(level, u1, u2, tight):
+    o = po.Oracle(level)
+    lat = o.mesh_arrays()["uv"].reshape(-1, 4, 2)[:, 0, 0]
+    bc = o.baroclin(max_iter=3, coriolis=np.sin(lat))
+    if tight:
+        po.set_solver(1e-16, 60, 40000)
+    try:
+        return o.bc_step(bc, u1, u2, np.zeros(o.os))
+    finally:
+        po.set_solver(1e-13, 60, 40000)
+
+
+@pytest.mark.parametrize("precision", [phelm.PHG_FP64, phelm.PHG_MIXED])
+@pytest.mark.parametrize("level", [4, 5])
+def test_step_vs_oracle(golden, level, precision):
+    g = golden(f"ref_L{level}.npz")
+    if level not in _tight:
+        _tight[level] = (oracle_step(level, g["in_u"], g["in_v"], True),
+                         oracle_step(level, g["in_u"], g["in_v"], False))
+    (t1, t2), (r1, r2) = _tight[level]
+    m, ops = ops_for(level, precision)
+    lat, _ = m.latlon()
+    bc = phelm.Baroclin(ops, picard_iters=3, coriolis=np.sin(lat))
+    a, b = bc.calc(g["in_u"], g["in_v"], np.zeros(m.outer_size))
+    assert rel(a, t1) <= TOL and rel(b, t2) <= TOL
+    # the reference's answer is itself this far from the discrete solution
+    ref_err = max(rel(r1, t1), rel(r2, t2))
+    assert rel(a, r1) <= ref_err + TOL and rel(b, r2) <= ref_err + TOL
+
+
+@pytest.mark.parametrize("level", [3, 4])
+def test_boundary_forcing_two_steps(level):
+    """Non-zero pole value, both forcing fields, two steps in a row."""
+    m, ops = ops_for(level)
+    o = po.Oracle(level)
+    lat, lon = m.latlon()
+    rng = np.random.default_rng(700 + level)
+    u1 = fields.sh_field(fields.random_coeffs(rng, 1, 6), lat, lon)
+    u2 = fields.sh_field(fields.random_coeffs(rng, 1, 6, amp=0.5), lat, lon)
+    f = fields.sh_field(fields.random_coeffs(rng, 1, 4, amp=0.1), lat, lon)
+    gg = fields.sh_field(fields.random_coeffs(rng, 1, 4, amp=0.1), lat, lon)
+    bnd = np.array([0.25])
+    cor = np.sin(lat)
+    bc = phelm.Baroclin(ops, picard_iters=3, coriolis=cor)
+    obc = o.baroclin(max_iter=3, coriolis=cor)
+    a, b = bc.calc(u1, u2, bnd, f, gg)
+    a2, b2 = bc.calc(a, b, bnd, f, gg)
+    po.set_solver(1e-16, 60, 40000)   # the discrete solution (see above)
+    try:
+        ra, rb = o.bc_step(obc, u1, u2, bnd, f, gg)
+        ra2, rb2 = o.bc_step(obc, ra, rb, bnd, f, gg)
+    finally:
+        po.set_solver(1e-13, 60, 40000)
+    assert rel(a, ra) <= TOL and rel(b, rb) <= TOL
+    assert rel(a2, ra2) <= TOL and rel(b2, rb2) <= TOL
+    # the boundary value is carried through
+    isb = m.arrays()["bnd"] == 1
+    assert np.all(a2[isb] == 0.25) and np.all(b2[isb] == 0.25)
+
+
+def test_device_pointers_match_host():
+    torch = pytest.importorskip("torch")
+    m, ops = ops_for(4)
+    lat, lon = m.latlon()
+    rng = np.random.default_rng(9)
+    u1 = fields.sh_field(fields.random_coeffs(rng, 1, 6), lat, lon)
+    u2 = fields.sh_field(fields.random_coeffs(rng, 1, 6), lat, lon)
+    bc = phelm.Baroclin(ops, picard_iters=2, coriolis=np.sin(lat))
+    a, b = bc.calc(u1, u2)
+    s = torch.cuda.Stream()
+    d1 = torch.from_numpy(u1).cuda()
+    d2 = torch.from_numpy(u2).cuda()
+    o1 = torch.empty_like(d1)
+    o2 = torch.empty_like(d2)
+    torch.cuda.synchronize()
+    bc.calc(d1, d2, out1=o1, out2=o2, stream=s)
+    s.synchronize()
+    assert np.array_equal(o1.cpu().numpy(), a) and np.array_equal(o2.cpu().numpy(), b)
+    # outputs may alias the inputs
+    bc.calc(d1, d2, out1=d1, out2=d2, stream=s)
+    s.synchronize()
+    assert np.array_equal(d1.cpu().numpy(), a) and np.array_equal(d2.cpu().numpy(), b)
+
+
+def test_handles_destroyed_in_any_order():
+    """The stepper keeps its operator set (and that its mesh) alive."""
+    m = phelm.Mesh.sphere(3)
+    ops = phelm.Operators(m, phelm.PHG_FP64, tol=1e-12)
+    lat, lon = m.latlon()
+    u1 = np.cos(lat) * np.sin(lon)
+    u2 = 0.5 * np.sin(lat)
+    bc = phelm.Baroclin(ops, picard_iters=2, coriolis=np.sin(lat))
+    a, b = bc.calc(u1, u2)
+    lib = phelm.lib()
+    lib.phg_ops_destroy(ops._h)
+    ops._h = None
+    lib.phg_mesh_destroy(m._h)
+    m._h = None
+    a2, b2 = bc.calc(u1, u2)
+    assert np.array_equal(a, a2) and np.array_equal(b, b2)
+    del bc
