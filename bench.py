@@ -33,6 +33,7 @@ sys.path.insert(0, HERE)
 LEVEL = 6
 CONF = dict(tau=1e-3, sigma=1.6e-2, mu=8e-5, k1=1.0, k2=1.0, theta=0.5, picard_iters=3)
 SEED = 2024
+METRIC = "level-6 barvortex steps/s, mixed vs FP64 at 1e-10 rel err; serve p50/p99 ms"
 TOL = 1e-12  # every solve: relative residual <= 1e-12 (within the 1e-10 bound)
 
 
@@ -210,6 +211,15 @@ def run_ours(args, ws, rank, local):
             row["mixed_over_fp64"] = row["mixed"]["member_steps_per_s"] / row["fp64"]["member_steps_per_s"]
             batched[f"L{lvl}x{B}"] = row
 
+    # serving trace (the first --bench-serve-requests requests of the 10,000-request trace)
+    served = None
+    if not args.no_serve and args.bench_serve_requests > 0:
+        served = {"trace": f"first {args.bench_serve_requests} of 10,000 requests, Poisson arrivals at "
+                           f"{args.serve_rate:g}/s, levels 3..7, 60% Laplace solves to 1e-10, 40% 10-step "
+                           "barvortex integrations, HBM budget 150 GB, lanes opened before the trace"}
+        for name in ("mixed", "fp64"):
+            served[name] = run_serve(name, args.bench_serve_requests, args.serve_rate)
+
     # max over ranks
     ms = results["mixed"]["ms_per_step"]
     if ws > 1:
@@ -246,7 +256,7 @@ def run_ours(args, ws, rank, local):
     if ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args.level, steps=1)
     line = {
-        "metric": "level-6 barvortex steps/s (mixed precision, <=1e-10 rel residual per solve)",
+        "metric": METRIC,
         "value": ws * 1000.0 / ms,
         "unit": "steps/s",
         "n_gpus": ws,
@@ -266,6 +276,7 @@ def run_ours(args, ws, rank, local):
                  "mixed_over_fp64": ms64 / ms},
         "state_rel_diff_mixed_vs_fp64": rel,
         "batched": batched,
+        "serve": served,
         "solver": {"mixed": mixed["stats"], "fp64": fp64["stats"]},
         "roofline": {"kernel": "gmres_kernel (persistent solver)", "bound": "hbm", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -333,7 +344,7 @@ def run_reference(args, ws, rank):
     sample = f"{steps} timed step(s) after {warm} warm-up, level {args.level}, single thread"
     print(json.dumps({
         "impl": "reference",
-        "metric": "level-6 barvortex steps/s (mixed precision, <=1e-10 rel residual per solve)",
+        "metric": METRIC,
         "value": v, "unit": "steps/s", "n_gpus": ws, "steps": steps, "warmup": warm,
         "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded Rossby-Haurwitz wave 4 + spherical-harmonic noise)",
@@ -344,9 +355,35 @@ def run_reference(args, ws, rank):
     }))
 
 
+def run_serve(precision: str, n: int, rate: float, levels=(3, 4, 5, 6, 7)):
+    """The serving trace: n requests with Poisson arrivals at `rate`/s, levels
+    uniform over `levels`, 60% Laplace solves to 1e-10 (RHS l <= 10), 40%
+    10-step barotropic integrations (RH4 + noise), HBM budget 150 GB.  Lanes
+    are opened before the trace (cold start reported separately)."""
+    from mke_gb300 import phelm, serve
+    prec = phelm.PHG_MIXED if precision == "mixed" else phelm.PHG_FP64
+    trace = serve.make_trace(n=n, rate=rate, levels=levels, seed=SEED)
+    pools = serve.make_pools(trace, seed=SEED)
+    srv = phelm.Server(precision=prec, hbm_budget_bytes=150e9, max_slots=64, solve_tol=1e-10, step_tol=TOL,
+                       **CONF)
+    t0 = time.perf_counter()
+    for kind, level in sorted(pools):
+        srv.preload(kind, level)
+    cold = time.perf_counter() - t0
+    stats, _ = serve.run_trace(srv, trace, pools)
+    stats["cold_start_s"] = cold
+    stats["bytes_in_use"] = srv.stats()["bytes_in_use"]
+    stats["precision"] = precision
+    srv.close()
+    return stats
+
+
 def run_case(args):
     """Small fixed workloads for profilers: `solve` = Laplace solves,
     `step` = barvortex steps, at --level with --steps repetitions."""
+    if args.case == "serve":
+        print(json.dumps(run_serve(args.precision, args.serve_requests, args.serve_rate)))
+        return
     import torch
     from mke_gb300 import phelm
     mesh = phelm.Mesh.sphere(args.level)
@@ -409,7 +446,12 @@ def main():
     ap.add_argument("--tol", type=float, default=TOL)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurements")
-    ap.add_argument("--case", choices=["solve", "step", "batch"], help="profiling workload only (no JSON bench line)")
+    ap.add_argument("--case", choices=["solve", "step", "batch", "serve"],
+                    help="one workload only (no bench line): profiling cases, or the serving trace")
+    ap.add_argument("--serve-requests", type=int, default=10000, help="requests of --case serve")
+    ap.add_argument("--bench-serve-requests", type=int, default=2000, help="requests of the bench line's serve block")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving trace")
+    ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--members", type=int, default=16, help="ensemble members for --case batch")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     args = ap.parse_args()

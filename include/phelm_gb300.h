@@ -41,6 +41,7 @@ extern "C" {
 #define PHG_ERR_NOT_CONVERGED 3 /* a linear solve missed its tolerance */
 #define PHG_ERR_TIMEOUT 4       /* a device-side wait ran out (kernel returned early) */
 #define PHG_ERR_IO 5            /* mesh file unreadable or malformed */
+#define PHG_ERR_BUDGET 6        /* serving: the request's lane does not fit in the HBM budget */
 
 #define PHG_FP64 0   /* every operator, vector and coefficient in double */
 #define PHG_MIXED 1  /* FP32 Krylov vectors and operator inside FP64 iterative refinement */
@@ -96,8 +97,21 @@ void phg_ops_destroy(phg_ops o);
  * tol 1e-12, max_iter 20000; mass-matrix solves inside operator applies use
  * min(tol, 1e-14). */
 int phg_ops_set_solver(phg_ops o, int restart, double tol, int max_iter);
+/* Persistent solver launches of this handle fill at most max_sms SMs
+ * (0 = the whole GPU, the default).  Launches of different handles that run
+ * at the same time on different streams then share the GPU instead of
+ * queueing behind each other.  No reference counterpart. */
+int phg_ops_set_sms(phg_ops o, int max_sms);
 /* Statistics of the last solve on this handle (host memory). */
 int phg_ops_last_solve(phg_ops o, int *iters, int *cycles, double *relres);
+/* Synchronise `stream` and judge the solves enqueued on this handle since the
+ * last check (calls with device pointers do not wait for their solves):
+ * PHG_ERR_NOT_CONVERGED / PHG_ERR_TIMEOUT as a host-pointer call would
+ * return.  No reference counterpart (the reference's calls are synchronous). */
+int phg_ops_check(phg_ops o, void *stream);
+/* Device bytes held by the library: in total, and allocated by the calling
+ * thread.  Instrumentation for memory budgets, no reference counterpart. */
+int phg_device_bytes(long long *total, long long *this_thread);
 /* Instrumentation, no reference counterpart: while enabled, every solver
  * launch of this handle (and of models built on it) is bracketed by CUDA
  * events on its stream and its algorithmic byte count is kept (up to 4096
@@ -115,6 +129,10 @@ int phg_laplace_calc2(phg_ops o, double *ans, const double *F, void *stream);
 /* SphereLaplace::solve (src/impl/slaplace_impl.h:84-131): ans[V] with
  * Laplacian(ans) = F[V] and ans = bnd[os] on the boundary. */
 int phg_laplace_solve(phg_ops o, double *ans, const double *F, const double *bnd, void *stream);
+/* nv independent SphereLaplace::solve calls in one persistent launch
+ * (member-major: ans, F: nv x V; bnd: nv x os or NULL).  The reference calls
+ * solve once per right-hand side. */
+int phg_laplace_solve_batch(phg_ops o, int nv, double *ans, const double *F, const double *bnd, void *stream);
 /* No counterpart in the reference.  phg_laplace_calc2 for callers that cannot
  * let a library allocate device memory (memory owned by their own pool or
  * allocator, or loops where the device synchronisation of a cudaMalloc would
@@ -187,6 +205,65 @@ void phg_baroclin_destroy(phg_baroclin b);
  * f, g: forcing fields at time t (V each, NULL = none). */
 int phg_baroclin_calc(phg_baroclin b, double *u11, double *u21, const double *u1, const double *u2,
                       const double *bnd, const double *f, const double *g, void *stream);
+
+/* --------------------------------------------------------------- serving --
+ * Request loop with continuous batching; no reference counterpart (the
+ * reference has no serving layer).  Requests are Laplace solves and short
+ * barotropic integrations on icosahedral meshes of mixed levels.  Each
+ * (kind, level) gets a lane: resident operators, a CUDA stream, a host
+ * thread and a number of member slots whose device memory is reserved when
+ * the lane opens and counted against the HBM budget.  Requests join a lane as
+ * slots free up (barotropic members between two time steps, Laplace solves in
+ * the next batched solve) and lanes run concurrently on their streams.  Idle
+ * lanes are closed when a new lane needs their memory.  Barotropic lanes use
+ * l + h = sin(latitude) (2 Omega = 1, no orography) and conf.bv. */
+#define PHG_REQ_LAPLACE_SOLVE 0 /* input: F[V]; output: solution[V]; bnd: os values or NULL */
+#define PHG_REQ_BARVORTEX 1     /* input: stream function u[V]; `steps` BarVortex::calc steps;
+                                   bnd: bnd_u (os values or NULL), bnd_w = 0 */
+
+typedef struct {
+	double hbm_budget_bytes; /* device memory the lanes may reserve */
+	int precision;           /* PHG_FP64 or PHG_MIXED */
+	int max_slots;           /* members per lane (0 = 64); fewer if the budget is short */
+	double solve_tol;        /* relative residual of Laplace solve requests */
+	double step_tol;         /* relative residual of the solves inside time steps */
+	phg_bv_conf bv;          /* barotropic step configuration */
+} phg_serve_conf;
+
+typedef struct {
+	int kind;              /* PHG_REQ_* */
+	int level;             /* icosahedral level 1..9 */
+	int steps;             /* PHG_REQ_BARVORTEX: time steps (>= 1) */
+	const double *input;   /* host, V values; read when the request is admitted */
+	const double *bnd;     /* host, os values or NULL */
+	double *output;        /* host, V values; written before the completion is reported */
+	long long tag;         /* returned in the completion */
+} phg_request;
+
+typedef struct {
+	long long tag;
+	int status;            /* PHG_OK or the request's PHG_ERR_* */
+	int kind, level;
+	double t_submit, t_admit, t_done;  /* seconds on phg_serve_clock */
+	int batch;             /* members in the launch that finished it */
+	char error[128];       /* message when status != PHG_OK */
+} phg_completion;
+
+typedef struct phg_serve_s *phg_serve;
+
+int phg_serve_create(const phg_serve_conf *conf, phg_serve *out);
+/* Open the lane of (kind, level) ahead of traffic and wait until it is ready. */
+int phg_serve_preload(phg_serve s, int kind, int level);
+/* Queue a request; input/output must stay valid until its completion is
+ * polled.  Bad requests and requests whose lane cannot open complete with
+ * their error status (the call itself returns PHG_OK). */
+int phg_serve_submit(phg_serve s, const phg_request *req);
+/* Up to `max` completions; waits up to wait_s seconds when none is ready. */
+int phg_serve_poll(phg_serve s, phg_completion *out, int max, double wait_s, int *n);
+int phg_serve_stats(phg_serve s, double *bytes_in_use, int *lanes_open, long long *completed);
+double phg_serve_clock(phg_serve s);
+/* Finishes every queued request, then frees the lanes. */
+void phg_serve_destroy(phg_serve s);
 
 #ifdef __cplusplus
 }

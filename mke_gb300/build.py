@@ -26,6 +26,7 @@ UNITS = [
     ("phg_kernels.cu", "cuda", ["-fmad=false"]),
     ("phg_gmres.cu", "cuda", []),
     ("phg_capi.cu", "cuda", []),
+    ("phg_serve.cu", "cuda", []),
 ]
 
 

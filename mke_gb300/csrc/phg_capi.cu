@@ -38,19 +38,36 @@ int fail(int code, const char *fmt, ...) {
     } while (0)
 
 // owning device allocation
+// device bytes held by the library: in total, and allocated by this thread
+// (a serving lane creates, uses and frees its handles on its own thread)
+std::atomic<long long> g_dev_bytes{0};
+thread_local long long t_dev_bytes = 0;
+
 struct DBuf {
     void *p = nullptr;
     size_t n = 0;
     DBuf() = default;
     DBuf(const DBuf &) = delete;
     DBuf &operator=(const DBuf &) = delete;
-    ~DBuf() { if (p) cudaFree(p); }
+    ~DBuf() { release(); }
+    void release() {
+        if (!p) return;
+        cudaFree(p);
+        g_dev_bytes -= (long long)n;
+        t_dev_bytes -= (long long)n;
+        p = nullptr; n = 0;
+    }
     cudaError_t ensure(size_t bytes) {
         if (bytes <= n) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr; n = 0;
+        release();
         cudaError_t e = cudaMalloc(&p, bytes ? bytes : 1);
-        if (e == cudaSuccess) n = bytes;
+        if (e == cudaSuccess) {
+            n = bytes;
+            g_dev_bytes += (long long)n;
+            t_dev_bytes += (long long)n;
+        } else {
+            p = nullptr;
+        }
         return e;
     }
     template <typename T> T *as() const { return (T *)p; }
@@ -79,6 +96,16 @@ struct phg_mesh_s {
     std::once_flag assembled;
     SphereOps ops;
     void assemble() { std::call_once(assembled, [this] { assemble_sphere(m, ops); }); }
+    // multigrid hierarchy of the Laplacian, built once per mesh
+    std::once_flag mg_once;
+    MgHierarchy mg;
+    bool mg_ok = false;
+    std::string mg_err;
+    const MgHierarchy *hierarchy(std::string &err) {
+        std::call_once(mg_once, [this] { mg_ok = build_mg(m, 1, mg, mg_err); });
+        if (!mg_ok) err = mg_err;
+        return mg_ok ? &mg : nullptr;
+    }
 };
 
 extern "C" const char *phg_last_error(void) { return g_err.c_str(); }
@@ -226,10 +253,12 @@ struct phg_ops_s {
     DevEll norm;
     int restart = 30, max_iter = 20000;
     double tol = 1e-12;
+    int max_sms = 0;                 // SMs the persistent solver may fill (0 = all)
     // scratch
     DBuf work, stats, s_a, s_b, s_c, s_d, s_e, s_part, s_out;
     GmresStats last{};
     bool stats_pending = false;
+    int pending_slots = 0;           // stats slots written since the last check
     // staging for host pointers
     DBuf st[8];
     // solver-launch profiling
@@ -301,12 +330,14 @@ double env_dbl(const char *name, double dflt) { const char *e = getenv(name); re
 // Geometric multigrid for the Laplacian of a generated icosahedral mesh:
 // levels down to the 42-point icosahedron refinement, Jacobi smoothing,
 // coarse levels of at most `red_max` points solved per block in shared memory.
-int build_mg_dev(phg_ops_s *o, const Mesh &m, SolveOpBufs &Lb, MgBufs &mb, int prec) {
+int build_mg_dev(phg_ops_s *o, phg_mesh_s *mh, SolveOpBufs &Lb, MgBufs &mb, int prec) {
+    const Mesh &m = mh->m;
     Lb.op.mg = MgDev();
     if (env_int("PHG_MG", 1) == 0 || m.level < 3) return PHG_OK;
-    MgHierarchy h;
     std::string err;
-    if (!build_mg(m, 1, h, err)) return fail(PHG_ERR_ARG, "multigrid: %s", err.c_str());
+    const MgHierarchy *hp = mh->hierarchy(err);
+    if (!hp) return fail(PHG_ERR_ARG, "multigrid: %s", err.c_str());
+    const MgHierarchy &h = *hp;
     const int nlev = (int)h.A.size();
     if (nlev > MG_MAXLEV) return PHG_OK;
     MgDev &mg = Lb.op.mg;
@@ -430,7 +461,7 @@ extern "C" int phg_ops_create(phg_mesh h, int precision, phg_ops *out) {
     int r;
     if ((r = build_solve_op(o.get(), so.idt, o->ML))) return r;
     if ((r = build_solve_op(o.get(), so.lapl, o->L))) return r;
-    if ((r = build_mg_dev(o.get(), m, o->L, o->mgL, precision))) return r;
+    if ((r = build_mg_dev(o.get(), h, o->L, o->mgL, precision))) return r;
     if ((r = build_solve_op(o.get(), so.jidt, o->MJ))) return r;
     if ((r = build_vals(o.get(), so.d1, o->vd1)) || (r = build_vals(o.get(), so.d2, o->vd2)) ||
         (r = build_vals(o.get(), so.d1c, o->vd1c)) || (r = build_vals(o.get(), so.d2c, o->vd2c)))
@@ -501,7 +532,7 @@ int solve(phg_ops_s *o, const DevSolveOp &op, const double *B, double *X, int nv
     const bool rec = o->prof && o->nev + 2 <= (int)o->ev.size();
     if (rec) CK(cudaEventRecord(o->ev[o->nev], s));
     CK(gmres_solve(op, B, X, nv, ld, o->restart, o->max_iter, tol, prec_of(o), o->work.p,
-                   o->stats.as<GmresStats>() + slot, s));
+                   o->stats.as<GmresStats>() + slot, s, false, o->max_sms));
     if (rec) {
         CK(cudaEventRecord(o->ev[o->nev + 1], s));
         CK(cudaMemcpyAsync(o->hist.as<GmresStats>() + o->nev / 2, o->stats.as<GmresStats>() + slot,
@@ -509,6 +540,7 @@ int solve(phg_ops_s *o, const DevSolveOp &op, const double *B, double *X, int nv
         o->nev += 2;
     }
     o->stats_pending = true;
+    o->pending_slots = std::max(o->pending_slots, slot + 1);
     return PHG_OK;
 }
 
@@ -526,6 +558,7 @@ int check_stats(phg_ops_s *o, int nslots, cudaStream_t s, GmresStats *agg = null
     if (each) memcpy(each, st.data(), sizeof(GmresStats) * nslots);
     o->last = a;
     o->stats_pending = false;
+    o->pending_slots = 0;
     if (agg) *agg = a;
     if (a.status == 2) return fail(PHG_ERR_TIMEOUT, "device barrier wait timed out");
     if (a.status == 1 && !(a.relres <= std::max(1e3 * o->tol, 1e-8)))
@@ -615,6 +648,12 @@ int norm_dev(phg_ops_s *o, const double *u, const double *v, int nv, double *out
 
 }  // namespace
 
+extern "C" int phg_ops_set_sms(phg_ops o, int max_sms) {
+    if (!o || max_sms < 0) return fail(PHG_ERR_ARG, "bad argument");
+    o->max_sms = max_sms;
+    return PHG_OK;
+}
+
 extern "C" int phg_ops_last_solve(phg_ops o, int *iters, int *cycles, double *relres) {
     if (!o) return fail(PHG_ERR_ARG, "NULL handle");
     if (iters) *iters = o->last.iters;
@@ -701,6 +740,42 @@ extern "C" int phg_laplace_solve(phg_ops o, double *ans, const double *F, const 
     return st.host ? check_stats(o, 1, s) : PHG_OK;
 }
 
+extern "C" int phg_laplace_solve_batch(phg_ops o, int nv, double *ans, const double *F, const double *bnd,
+                                       void *stream) {
+    if (!o || !ans || !F || nv < 1) return fail(PHG_ERR_ARG, "NULL argument");
+    cudaStream_t s = o->str(stream);
+    Stage st(o, s);
+    const int V = o->V, rs = o->rs, os = o->os;
+    const double *dF, *dB; double *dA;
+    CK(st.in(F, (size_t)V * nv, &dF)); CK(st.in(bnd, (size_t)os * nv, &dB)); CK(st.out(ans, (size_t)V * nv, &dA));
+    if (os == 0) dB = nullptr;
+    CK(o->s_a.ensure(8 * (size_t)rs * nv)); CK(o->s_c.ensure(8 * (size_t)rs * nv));
+    double *b = o->s_a.as<double>(), *x = o->s_c.as<double>();
+    CK(apply_op(o->ML.op.A, o->bnd2.c, dF, V, o->imap(), dB, os, nullptr, b, rs, nv, s));
+    CK(cudaMemsetAsync(x, 0, 8 * (size_t)rs * nv, s));
+    int r = solve(o, o->L.op, b, x, nv, rs, o->tol, 0, s);
+    if (r) return r;
+    CK(p2u(dA, V, x, rs, dB, os, o->p2io.as<int>(), o->isb.as<int>(), V, nv, s));
+    CK(st.finish());
+    return st.host ? check_stats(o, 1, s) : PHG_OK;
+}
+
+extern "C" int phg_ops_check(phg_ops o, void *stream) {
+    if (!o) return fail(PHG_ERR_ARG, "NULL handle");
+    cudaStream_t s = o->str(stream);
+    if (o->pending_slots == 0) {
+        CK(cudaStreamSynchronize(s));
+        return PHG_OK;
+    }
+    return check_stats(o, o->pending_slots, s);
+}
+
+extern "C" int phg_device_bytes(long long *total, long long *this_thread) {
+    if (total) *total = g_dev_bytes.load();
+    if (this_thread) *this_thread = t_dev_bytes;
+    return PHG_OK;
+}
+
 static int jacobian_common(phg_ops o, double *ans, const double *u, const double *v, const double *bnd,
                            bool full, bool transpose, void *stream) {
     if (!o || !ans || !u || !v) return fail(PHG_ERR_ARG, "NULL argument");
@@ -766,6 +841,7 @@ struct phg_barvortex_s {
     DBuf w, dw, FC, u_n, w_n, u_n1, tmp1, tmp2, uin, F, rp, x, jsol, nr0, nr, done, ubnd, wbnd, frc;
     GmresStats each[64];
     int nslots = 0;
+    cudaStream_t last_stream = nullptr;   // stream of the last step (its stats live there)
 };
 
 extern "C" int phg_barvortex_create(phg_ops o, const phg_bv_conf *c, const double *coriolis, phg_barvortex *out) {
@@ -891,6 +967,7 @@ static int bv_calc(phg_barvortex b, int nv, double *u1, const double *u, const d
     CK(st.out(u1, (size_t)o->V * nv, &du1));
     if (o->os == 0) { dbu = nullptr; dbw = nullptr; }
     if ((r = bv_step_dev(b, nv, du1, du, dbu, dbw, df, s))) return r;
+    b->last_stream = s;
     CK(st.finish());
     if (!st.host) return PHG_OK;
     return check_stats(o, b->nslots, s, nullptr, b->each);
@@ -910,7 +987,7 @@ extern "C" int phg_barvortex_calc_batch(phg_barvortex b, int nmembers, double *u
 extern "C" int phg_barvortex_last_stats(phg_barvortex b, int *il, int *ia, int *imj, int *iml, double *worst) {
     if (!b) return fail(PHG_ERR_ARG, "NULL handle");
     phg_ops_s *o = b->o;
-    int r = check_stats(o, b->nslots, o->stream, nullptr, b->each);
+    int r = check_stats(o, b->nslots, b->last_stream ? b->last_stream : o->stream, nullptr, b->each);
     // slot layout: 0,1 mass L (calc1 x2); then per Picard iteration: J, A, L
     int l = 0, a = 0, mj = 0, ml = 0;
     double wr = 0.0;

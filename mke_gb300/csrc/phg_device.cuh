@@ -101,9 +101,12 @@ struct GmresStats {
 // GmresStats on the device.
 size_t gmres_work_bytes(const DevSolveOp &op, int nv, int m, Precision p);
 // no_alloc: never allocate (the optional debug phase timers stay off)
+// max_sms: use at most this many SMs' worth of co-resident blocks (0 = all);
+// callers that run several persistent launches at once partition the SMs
 cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv, int ld,
                         int m, int max_iter, double tol, Precision p,
-                        void *work, GmresStats *stats_dev, cudaStream_t s, bool no_alloc = false);
+                        void *work, GmresStats *stats_dev, cudaStream_t s, bool no_alloc = false,
+                        int max_sms = 0);
 
 // y[v] = A x_in[v] + C x_bnd[v] with every row summed in ascending column
 // order from 0.0 and no fused multiply-add (same rounding as a CPU CSR

@@ -32,6 +32,7 @@
 // raises a device error flag; all blocks see the flag at their next barrier
 // and return, and the host reports status 2.
 #include <cstdio>
+#include <mutex>
 
 #include "phg_kernels.cuh"
 
@@ -779,11 +780,31 @@ int env_int(const char *name, int dflt) {
 
 }  // namespace
 
+// The kernels may use all the opt-in shared memory; set once per kernel, so
+// that threads launching with different sizes never race on the attribute.
+static cudaError_t allow_smem(Precision prec) {
+    static std::once_flag once[2];
+    static cudaError_t err[2] = {cudaSuccess, cudaSuccess};
+    const int k = prec == PREC_MIXED ? 1 : 0;
+    std::call_once(once[k], [k] {
+        void *fn = k ? (void *)gmres_kernel<float> : (void *)gmres_kernel<double>;
+        int dev = 0, optin = 0;
+        cudaFuncAttributes fa;
+        if ((err[k] = cudaGetDevice(&dev)) != cudaSuccess) return;
+        if ((err[k] = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess)
+            return;
+        if ((err[k] = cudaFuncGetAttributes(&fa, fn)) != cudaSuccess) return;
+        err[k] = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      optin - (int)fa.sharedSizeBytes);
+    });
+    return err[k];
+}
+
 size_t gmres_work_bytes(const DevSolveOp &op, int nv, int m, Precision p) { return layout(op, nv, m, p).total; }
 
 cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv, int ld,
                         int m, int max_iter, double tol, Precision prec,
-                        void *work, GmresStats *stats_dev, cudaStream_t s, bool no_alloc) {
+                        void *work, GmresStats *stats_dev, cudaStream_t s, bool no_alloc, int max_sms) {
     if (m < 1 || m > MAXM || nv < 1) return cudaErrorInvalidValue;
     const int n = op.A.n;
     Params p;
@@ -791,13 +812,14 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     const size_t smem = smem_gmres_bytes() + (op.mgd ? es * op.mg.red_elems : 0) + 16;
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
     void *fn = prec == PREC_MIXED ? (void *)gmres_kernel<float> : (void *)gmres_kernel<double>;
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_smem(prec);
     if (e != cudaSuccess) return e;
     int per = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, BLOCK, smem);
     if (e != cudaSuccess) return e;
     if (per < 1) return cudaErrorInvalidConfiguration;
-    const int cap = sm_count() * per;
+    const int sms = (max_sms > 0 && max_sms < sm_count()) ? max_sms : sm_count();
+    const int cap = sms * per;
     // as many right-hand sides in flight as there are blocks; the blocks are
     // shared out evenly, but no block gets fewer than `rpb` rows
     const int rpb = env_int("PHG_ROWS_PER_BLOCK", 256);

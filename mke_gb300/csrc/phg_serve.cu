@@ -1,0 +1,560 @@
+// phg_serve.cu -- request loop with continuous batching over the sphere
+// operators (host code; no reference counterpart: the reference has no
+// serving layer, its drivers call the classes directly).
+//
+// Requests are Laplace solves and short barotropic integrations on
+// icosahedral meshes of mixed levels.  Each (kind, level) gets a lane: its own
+// operator handles, CUDA stream and host thread, and `cap` member slots whose
+// device memory is reserved when the lane opens and counted against the HBM
+// budget.  Requests join a lane as slots free up: a barotropic member enters
+// between two time steps and leaves after its last one, while the others keep
+// stepping; Laplace solves go into the lane's next batched solve.  Lanes run
+// concurrently on their streams, so work of different levels overlaps on the
+// device.  A lane that cannot get memory evicts idle lanes; a request whose
+// lane can never fit in the budget completes with PHG_ERR_BUDGET.
+//
+// The solver runs as persistent cooperative launches whose blocks must all be
+// resident at once.  Lanes therefore take SMs from a shared pool for each
+// launch sequence (one time step, one batched solve): a lane alone gets what
+// its work can fill, lanes running together get equal shares, and the SMs of
+// concurrent launches never add up to more than the GPU has.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/phelm_gb300.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Pending {
+    phg_request r;
+    double t_submit = 0.0, t_admit = 0.0;
+    int steps_left = 0;
+};
+
+struct Server;
+
+struct Lane {
+    Server *srv = nullptr;
+    int kind = 0, level = 0;
+    // device resources, owned by the lane thread
+    phg_ops ops = nullptr;
+    phg_barvortex bv = nullptr;
+    cudaStream_t stream = nullptr;
+    int V = 0, os = 0, osb = 1, cap = 0;
+    double *dU = nullptr, *dOut = nullptr, *dB = nullptr, *dBw = nullptr;
+    double *hIn = nullptr, *hOut = nullptr, *hB = nullptr;
+    long long bytes = 0;   // reserved against the budget
+    // shared state, under Server::mu
+    std::deque<Pending *> queue;
+    bool ready = false, failed = false, stop = false, closing = false, closed = false;
+    int fail_status = PHG_OK;
+    std::string fail_msg;
+    int active = 0;
+    double last_busy = 0.0;
+    std::condition_variable cv;
+    std::thread th;
+};
+
+struct Server {
+    phg_serve_conf conf{};
+    int dev = 0;
+    Clock::time_point t0;
+    std::mutex mu;
+    std::condition_variable done_cv, mem_cv, ready_cv;
+    std::map<std::pair<int, int>, Lane *> lanes;   // current lane per (kind, level)
+    std::vector<std::unique_ptr<Lane>> all;        // every lane ever opened (joined at destroy)
+    std::deque<phg_completion> done;
+    long long budget = 0, in_use = 0, ndone = 0;
+    bool shutting = false;
+    int sm_total = 0, sm_free = 0, sm_users = 0;   // SM pool (under mu)
+    std::condition_variable sm_cv;
+    std::mutex mesh_mu;
+    std::map<int, phg_mesh> meshes;
+    double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+};
+
+// under S->mu; the message is the calling thread's last library error
+void push_done(Server *S, Pending *p, int status, int batch, const char *msg = nullptr) {
+    phg_completion c;
+    memset(&c, 0, sizeof(c));
+    if (status != PHG_OK) {
+        const char *m = msg ? msg : phg_last_error();
+        strncpy(c.error, m ? m : "", sizeof(c.error) - 1);
+    }
+    c.tag = p->r.tag;
+    c.status = status;
+    c.kind = p->r.kind;
+    c.level = p->r.level;
+    c.t_submit = p->t_submit;
+    c.t_admit = p->t_admit;
+    c.t_done = S->now();
+    c.batch = batch;
+    S->done.push_back(c);
+    S->ndone++;
+    delete p;
+    S->done_cv.notify_all();
+}
+
+int get_mesh(Server *S, int level, phg_mesh *out) {
+    std::lock_guard<std::mutex> lk(S->mesh_mu);
+    auto it = S->meshes.find(level);
+    if (it != S->meshes.end()) { *out = it->second; return PHG_OK; }
+    phg_mesh m = nullptr;
+    int r = phg_mesh_generate(level, &m);
+    if (r) return r;
+    S->meshes[level] = m;
+    *out = m;
+    return PHG_OK;
+}
+
+long long thread_bytes() {
+    long long t = 0;
+    phg_device_bytes(nullptr, &t);
+    return t;
+}
+
+// SMs the lane's launches can fill: the largest solve of one call has
+// rows x right-hand sides work items, two blocks of 256 rows per SM
+int natural_sms(const Lane *L, int nv) {
+    const long long rows = (long long)(L->V - L->os) * nv * (L->kind == PHG_REQ_BARVORTEX ? 8 : 1);
+    return (int)std::max(1LL, std::min<long long>(L->srv->sm_total, (rows + 511) / 512));
+}
+
+// take SMs from the pool: at most the fair share of the lanes now using it
+int sm_acquire(Server *S, int want) {
+    std::unique_lock<std::mutex> lk(S->mu);
+    S->sm_users++;
+    int grant = 0;
+    for (;;) {
+        const int fair = std::max(1, S->sm_total / S->sm_users);
+        grant = std::min(want, fair);
+        if (S->sm_free >= grant) break;
+        S->sm_cv.wait(lk);
+    }
+    S->sm_free -= grant;
+    return grant;
+}
+
+void sm_release(Server *S, int grant) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->sm_free += grant;
+    S->sm_users--;
+    S->sm_cv.notify_all();
+}
+
+// one call of the lane's kernel work on members [0, nv) of the slot buffers
+int lane_run(Lane *L, int nv) {
+    Server *S = L->srv;
+    const int grant = sm_acquire(S, natural_sms(L, nv));
+    int r = phg_ops_set_sms(L->ops, grant);
+    if (r == PHG_OK) {
+        if (L->kind == PHG_REQ_LAPLACE_SOLVE)
+            r = phg_laplace_solve_batch(L->ops, nv, L->dOut, L->dU, L->os ? L->dB : nullptr, L->stream);
+        else
+            r = phg_barvortex_calc_batch(L->bv, nv, L->dU, L->dU, L->os ? L->dB : nullptr,
+                                         L->os ? L->dBw : nullptr, nullptr, L->stream);
+    }
+    int r2 = phg_ops_check(L->ops, L->stream);   // waits for the launches
+    sm_release(S, grant);
+    return r ? r : r2;
+}
+
+void free_slots(Lane *L) {
+    cudaFree(L->dU); cudaFree(L->dOut); cudaFree(L->dB); cudaFree(L->dBw);
+    cudaFreeHost(L->hIn); cudaFreeHost(L->hOut); cudaFreeHost(L->hB);
+    L->dU = L->dOut = L->dB = L->dBw = nullptr;
+    L->hIn = L->hOut = L->hB = nullptr;
+}
+
+int alloc_slots(Lane *L, int n) {
+    const size_t v = (size_t)L->V * n * 8, b = (size_t)L->osb * n * 8;
+    if (cudaMalloc(&L->dU, v) || cudaMalloc(&L->dB, b) || cudaMalloc(&L->dBw, b) ||
+        (L->kind == PHG_REQ_LAPLACE_SOLVE && cudaMalloc(&L->dOut, v)) ||
+        cudaHostAlloc(&L->hIn, v, cudaHostAllocDefault) || cudaHostAlloc(&L->hOut, v, cudaHostAllocDefault) ||
+        cudaHostAlloc(&L->hB, b, cudaHostAllocDefault)) {
+        cudaGetLastError();
+        free_slots(L);
+        return PHG_ERR_CUDA;
+    }
+    cudaMemset(L->dU, 0, v);
+    cudaMemset(L->dB, 0, b);
+    cudaMemset(L->dBw, 0, b);
+    return PHG_OK;
+}
+
+long long slot_bytes(const Lane *L) {
+    return (long long)L->V * 8 * (L->kind == PHG_REQ_LAPLACE_SOLVE ? 2 : 1) + (long long)L->osb * 8 * 2;
+}
+
+// Build the handles, size the slots from two probe calls, reserve the budget
+// and allocate everything the lane will use.
+int lane_open(Lane *L) {
+    Server *S = L->srv;
+    const phg_serve_conf &c = S->conf;
+    phg_mesh m = nullptr;
+    int r = get_mesh(S, L->level, &m);
+    if (r) return r;
+    int T = 0, rs = 0;
+    if ((r = phg_mesh_info(m, &L->V, &T, &rs, &L->os))) return r;
+    L->osb = std::max(L->os, 1);
+    const long long b0 = thread_bytes();
+    if ((r = phg_ops_create(m, c.precision, &L->ops))) return r;
+    const double tol = L->kind == PHG_REQ_LAPLACE_SOLVE ? c.solve_tol : c.step_tol;
+    if ((r = phg_ops_set_solver(L->ops, 30, tol, 20000))) return r;
+    if (cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking) != cudaSuccess) return PHG_ERR_CUDA;
+    if (L->kind == PHG_REQ_BARVORTEX) {
+        // l + h = sin(latitude) in the zone-0 chart (2 Omega = 1, no orography)
+        std::vector<double> uv((size_t)L->V * 8), lh(L->V);
+        if ((r = phg_mesh_arrays(m, nullptr, uv.data(), nullptr, nullptr, nullptr))) return r;
+        for (int p = 0; p < L->V; ++p) lh[p] = std::sin(uv[(size_t)p * 8]);
+        if ((r = phg_barvortex_create(L->ops, &c.bv, lh.data(), &L->bv))) return r;
+    }
+    // probes: device bytes of the handles at 1 and 2 members
+    if ((r = alloc_slots(L, 2))) return r;
+    if ((r = lane_run(L, 1))) return r;
+    const long long b1 = thread_bytes() - b0;
+    if ((r = lane_run(L, 2))) return r;
+    const long long b2 = thread_bytes() - b0;
+    free_slots(L);
+    const long long per = std::max(0LL, b2 - b1) + slot_bytes(L);
+    const long long base = b1 - (b2 - b1);
+    int cap = c.max_slots > 0 ? c.max_slots : 64;
+    {
+        std::unique_lock<std::mutex> lk(S->mu);
+        for (;;) {
+            const long long freeb = S->budget - S->in_use;
+            const long long fit = per > 0 ? (freeb - base) / per : cap;
+            if (fit >= 1) {
+                cap = (int)std::min<long long>(cap, fit);
+                break;
+            }
+            if (base + per > S->budget) return PHG_ERR_BUDGET;   // never fits
+            // evict idle lanes, then wait for their memory
+            bool any = false;
+            for (auto &kv : S->lanes) {
+                Lane *o = kv.second;
+                if (o != L && o->ready && !o->stop && o->active == 0 && o->queue.empty()) {
+                    o->stop = true;
+                    o->cv.notify_all();
+                    any = true;
+                }
+            }
+            bool busy = false;
+            for (auto &kv : S->lanes) busy |= kv.second != L && !kv.second->closed;
+            if (!any && !busy) return PHG_ERR_BUDGET;
+            if (S->shutting) return PHG_ERR_BUDGET;
+            S->mem_cv.wait_for(lk, std::chrono::milliseconds(50));
+        }
+        L->bytes = base + (long long)cap * per;
+        S->in_use += L->bytes;
+    }
+    L->cap = cap;
+    if ((r = alloc_slots(L, cap))) return r;
+    if ((r = lane_run(L, cap))) return r;   // allocate every workspace now
+    // keep the reservation honest: what the handles really hold
+    const long long actual = thread_bytes() - b0 + (long long)cap * slot_bytes(L);
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->in_use += actual - L->bytes;
+        L->bytes = actual;
+    }
+    return PHG_OK;
+}
+
+void lane_close(Lane *L) {
+    Server *S = L->srv;
+    if (L->stream) cudaStreamSynchronize(L->stream);
+    if (L->bv) phg_barvortex_destroy(L->bv);
+    if (L->ops) phg_ops_destroy(L->ops);
+    L->bv = nullptr;
+    L->ops = nullptr;
+    free_slots(L);
+    if (L->stream) cudaStreamDestroy(L->stream);
+    L->stream = nullptr;
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->in_use -= L->bytes;
+    L->bytes = 0;
+    L->closed = true;
+    // requests that raced with the close go to a fresh lane on next submit;
+    // any left here are failed rather than lost
+    while (!L->queue.empty()) {
+        push_done(S, L->queue.front(), L->failed ? L->fail_status : PHG_ERR_BUDGET, 0,
+                  L->failed ? L->fail_msg.c_str() : "lane closed");
+        L->queue.pop_front();
+    }
+    S->mem_cv.notify_all();
+    S->ready_cv.notify_all();
+}
+
+void laplace_loop(Lane *L) {
+    Server *S = L->srv;
+    const int V = L->V, os = L->os;
+    std::vector<Pending *> batch;
+    for (;;) {
+        batch.clear();
+        {
+            std::unique_lock<std::mutex> lk(S->mu);
+            L->cv.wait(lk, [&] { return L->stop || !L->queue.empty(); });
+            if (L->queue.empty()) { L->closing = true; return; }
+            while (!L->queue.empty() && (int)batch.size() < L->cap) {
+                batch.push_back(L->queue.front());
+                L->queue.pop_front();
+            }
+            L->active = (int)batch.size();
+        }
+        const int n = (int)batch.size();
+        const double ta = S->now();
+        for (int k = 0; k < n; ++k) {
+            Pending *p = batch[k];
+            p->t_admit = ta;
+            memcpy(L->hIn + (size_t)k * V, p->r.input, 8 * (size_t)V);
+            if (os) {
+                if (p->r.bnd) memcpy(L->hB + (size_t)k * os, p->r.bnd, 8 * (size_t)os);
+                else memset(L->hB + (size_t)k * os, 0, 8 * (size_t)os);
+            }
+        }
+        int st = PHG_OK;
+        if (cudaMemcpyAsync(L->dU, L->hIn, 8 * (size_t)V * n, cudaMemcpyHostToDevice, L->stream) ||
+            (os && cudaMemcpyAsync(L->dB, L->hB, 8 * (size_t)os * n, cudaMemcpyHostToDevice, L->stream)))
+            st = PHG_ERR_CUDA;
+        if (!st) st = lane_run(L, n);
+        if (!st && (cudaMemcpyAsync(L->hOut, L->dOut, 8 * (size_t)V * n, cudaMemcpyDeviceToHost, L->stream) ||
+                    cudaStreamSynchronize(L->stream)))
+            st = PHG_ERR_CUDA;
+        for (int k = 0; k < n; ++k)
+            if (!st) memcpy(batch[k]->r.output, L->hOut + (size_t)k * V, 8 * (size_t)V);
+        std::lock_guard<std::mutex> lk(S->mu);
+        for (int k = 0; k < n; ++k) push_done(S, batch[k], st, n);
+        L->active = 0;
+        L->last_busy = S->now();
+    }
+}
+
+void bv_loop(Lane *L) {
+    Server *S = L->srv;
+    const int V = L->V, os = L->os;
+    std::vector<Pending *> act;   // act[k] owns slot k
+    std::vector<int> fin;
+    for (;;) {
+        int n0;
+        {
+            std::unique_lock<std::mutex> lk(S->mu);
+            if (act.empty()) {
+                L->cv.wait(lk, [&] { return L->stop || !L->queue.empty(); });
+                if (L->queue.empty()) { L->closing = true; return; }
+            }
+            n0 = (int)act.size();
+            while (!L->queue.empty() && (int)act.size() < L->cap) {
+                act.push_back(L->queue.front());
+                L->queue.pop_front();
+            }
+            L->active = (int)act.size();
+        }
+        const int n = (int)act.size();
+        const double ta = S->now();
+        int st = PHG_OK;
+        for (int k = n0; k < n && !st; ++k) {
+            Pending *p = act[k];
+            p->t_admit = ta;
+            p->steps_left = p->r.steps;
+            memcpy(L->hIn + (size_t)k * V, p->r.input, 8 * (size_t)V);
+            if (cudaMemcpyAsync(L->dU + (size_t)k * V, L->hIn + (size_t)k * V, 8 * (size_t)V, cudaMemcpyHostToDevice,
+                                L->stream))
+                st = PHG_ERR_CUDA;
+            if (os) {
+                if (p->r.bnd) memcpy(L->hB + (size_t)k * os, p->r.bnd, 8 * (size_t)os);
+                else memset(L->hB + (size_t)k * os, 0, 8 * (size_t)os);
+                if (cudaMemcpyAsync(L->dB + (size_t)k * os, L->hB + (size_t)k * os, 8 * (size_t)os,
+                                    cudaMemcpyHostToDevice, L->stream))
+                    st = PHG_ERR_CUDA;
+            }
+        }
+        if (!st) st = lane_run(L, n);   // one time step of every member
+        if (st) {
+            std::lock_guard<std::mutex> lk(S->mu);
+            for (Pending *p : act) push_done(S, p, st, n);
+            act.clear();
+            L->active = 0;
+            continue;
+        }
+        fin.clear();
+        for (int k = n - 1; k >= 0; --k)
+            if (--act[k]->steps_left == 0) {
+                fin.push_back(k);
+                if (cudaMemcpyAsync(L->hOut + (size_t)k * V, L->dU + (size_t)k * V, 8 * (size_t)V,
+                                    cudaMemcpyDeviceToHost, L->stream))
+                    st = PHG_ERR_CUDA;
+            }
+        if (fin.empty()) continue;
+        if (cudaStreamSynchronize(L->stream)) st = PHG_ERR_CUDA;
+        std::vector<std::pair<Pending *, int>> out;
+        for (int k : fin) {   // descending: slots above k are live members
+            Pending *p = act[k];
+            if (!st) memcpy(p->r.output, L->hOut + (size_t)k * V, 8 * (size_t)V);
+            out.push_back({p, st});
+            const int last = (int)act.size() - 1;
+            if (k != last) {
+                cudaMemcpyAsync(L->dU + (size_t)k * V, L->dU + (size_t)last * V, 8 * (size_t)V,
+                                cudaMemcpyDeviceToDevice, L->stream);
+                if (os)
+                    cudaMemcpyAsync(L->dB + (size_t)k * os, L->dB + (size_t)last * os, 8 * (size_t)os,
+                                    cudaMemcpyDeviceToDevice, L->stream);
+                act[k] = act[last];
+            }
+            act.pop_back();
+        }
+        std::lock_guard<std::mutex> lk(S->mu);
+        for (auto &x : out) push_done(S, x.first, x.second, n);
+        L->active = (int)act.size();
+        L->last_busy = S->now();
+    }
+}
+
+void lane_main(Lane *L) {
+    Server *S = L->srv;
+    cudaSetDevice(S->dev);
+    int st = lane_open(L);
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        if (st) {
+            L->failed = true;
+            L->fail_status = st;
+            L->fail_msg = st == PHG_ERR_BUDGET ? "the lane does not fit in the HBM budget" : phg_last_error();
+            L->closing = true;
+        } else {
+            L->ready = true;
+        }
+        S->ready_cv.notify_all();
+    }
+    if (!st) {
+        if (L->kind == PHG_REQ_LAPLACE_SOLVE) laplace_loop(L);
+        else bv_loop(L);
+    }
+    lane_close(L);
+}
+
+// under S->mu: the lane that takes new requests for (kind, level)
+Lane *lane_for(Server *S, int kind, int level) {
+    auto key = std::make_pair(kind, level);
+    auto it = S->lanes.find(key);
+    if (it != S->lanes.end() && !it->second->closing && !it->second->closed) return it->second;
+    auto L = std::make_unique<Lane>();
+    L->srv = S;
+    L->kind = kind;
+    L->level = level;
+    Lane *raw = L.get();
+    S->lanes[key] = raw;
+    S->all.push_back(std::move(L));
+    raw->th = std::thread(lane_main, raw);
+    return raw;
+}
+
+}  // namespace
+
+struct phg_serve_s : Server {};
+
+extern "C" int phg_serve_create(const phg_serve_conf *conf, phg_serve *out) {
+    if (!conf || !out) return PHG_ERR_ARG;
+    if (!(conf->hbm_budget_bytes > 0) || (conf->precision != PHG_FP64 && conf->precision != PHG_MIXED) ||
+        !(conf->solve_tol > 0) || !(conf->step_tol > 0) || conf->max_slots < 0)
+        return PHG_ERR_ARG;
+    auto s = std::make_unique<phg_serve_s>();
+    s->conf = *conf;
+    s->budget = (long long)conf->hbm_budget_bytes;
+    if (cudaGetDevice(&s->dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&s->sm_total, cudaDevAttrMultiProcessorCount, s->dev) != cudaSuccess)
+        return PHG_ERR_CUDA;
+    s->sm_free = s->sm_total;
+    s->t0 = Clock::now();
+    *out = s.release();
+    return PHG_OK;
+}
+
+extern "C" double phg_serve_clock(phg_serve s) { return s ? s->now() : 0.0; }
+
+extern "C" int phg_serve_preload(phg_serve s, int kind, int level) {
+    if (!s || (kind != PHG_REQ_LAPLACE_SOLVE && kind != PHG_REQ_BARVORTEX) || level < 1 || level > 9)
+        return PHG_ERR_ARG;
+    std::unique_lock<std::mutex> lk(s->mu);
+    Lane *L = lane_for(s, kind, level);
+    s->ready_cv.wait(lk, [&] { return L->ready || L->failed || L->closed; });
+    return L->failed ? L->fail_status : PHG_OK;
+}
+
+extern "C" int phg_serve_submit(phg_serve s, const phg_request *req) {
+    if (!s || !req) return PHG_ERR_ARG;
+    auto p = new Pending();
+    p->r = *req;
+    p->t_submit = s->now();
+    const bool ok = (req->kind == PHG_REQ_LAPLACE_SOLVE || (req->kind == PHG_REQ_BARVORTEX && req->steps >= 1)) &&
+                    req->level >= 1 && req->level <= 9 && req->input && req->output;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (!ok || s->shutting) {
+        push_done(s, p, PHG_ERR_ARG, 0, s->shutting ? "server is shutting down" : "bad request");
+        return PHG_OK;
+    }
+    Lane *L = lane_for(s, req->kind, req->level);
+    if (L->failed) {
+        push_done(s, p, L->fail_status, 0, L->fail_msg.c_str());
+        return PHG_OK;
+    }
+    L->queue.push_back(p);
+    L->cv.notify_all();
+    return PHG_OK;
+}
+
+extern "C" int phg_serve_poll(phg_serve s, phg_completion *out, int max, double wait_s, int *n) {
+    if (!s || !n || (max > 0 && !out)) return PHG_ERR_ARG;
+    std::unique_lock<std::mutex> lk(s->mu);
+    if (s->done.empty() && wait_s > 0)
+        s->done_cv.wait_for(lk, std::chrono::duration<double>(wait_s), [&] { return !s->done.empty(); });
+    int k = 0;
+    while (k < max && !s->done.empty()) {
+        out[k++] = s->done.front();
+        s->done.pop_front();
+    }
+    *n = k;
+    return PHG_OK;
+}
+
+extern "C" int phg_serve_stats(phg_serve s, double *bytes_in_use, int *lanes_open, long long *completed) {
+    if (!s) return PHG_ERR_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    int open = 0;
+    for (auto &kv : s->lanes) open += !kv.second->closed;
+    if (bytes_in_use) *bytes_in_use = (double)s->in_use;
+    if (lanes_open) *lanes_open = open;
+    if (completed) *completed = s->ndone;
+    return PHG_OK;
+}
+
+extern "C" void phg_serve_destroy(phg_serve s) {
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->shutting = true;
+        for (auto &L : s->all) {
+            L->stop = true;
+            L->cv.notify_all();
+        }
+        s->mem_cv.notify_all();
+    }
+    for (auto &L : s->all)
+        if (L->th.joinable()) L->th.join();
+    for (auto &kv : s->meshes) phg_mesh_destroy(kv.second);
+    delete s;
+}

@@ -18,7 +18,8 @@ from . import build as _build
 
 PHG_FP64, PHG_MIXED = 0, 1
 _ERRORS = {1: "bad argument", 2: "CUDA error", 3: "solve did not converge", 4: "device wait timed out",
-           5: "mesh I/O error"}
+           5: "mesh I/O error", 6: "over the HBM budget"}
+PHG_REQ_LAPLACE_SOLVE, PHG_REQ_BARVORTEX = 0, 1
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -38,6 +39,22 @@ class BvConf(C.Structure):
 class BcConf(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("tau", "sigma", "mu", "sigma1", "mu1", "alpha")] + [
         ("picard_iters", C.c_int), ("picard_tol", C.c_double)]
+
+
+class ServeConf(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_double), ("precision", C.c_int), ("max_slots", C.c_int),
+                ("solve_tol", C.c_double), ("step_tol", C.c_double), ("bv", BvConf)]
+
+
+class Request(C.Structure):
+    _fields_ = [("kind", C.c_int), ("level", C.c_int), ("steps", C.c_int), ("input", _vp), ("bnd", _vp),
+                ("output", _vp), ("tag", C.c_longlong)]
+
+
+class Completion(C.Structure):
+    _fields_ = [("tag", C.c_longlong), ("status", C.c_int), ("kind", C.c_int), ("level", C.c_int),
+                ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double), ("batch", C.c_int),
+                ("error", C.c_char * 128)]
 
 
 # every symbol the header declares, with its ctypes signature
@@ -61,6 +78,10 @@ SIGNATURES = {
     "phg_laplace_calc1": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "phg_laplace_calc2": (C.c_int, [_vp, _vp, _vp, _vp]),
     "phg_laplace_solve": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "phg_laplace_solve_batch": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp]),
+    "phg_ops_check": (C.c_int, [_vp, _vp]),
+    "phg_ops_set_sms": (C.c_int, [_vp, C.c_int]),
+    "phg_device_bytes": (C.c_int, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "phg_laplace_calc2_noalloc": (C.c_int, [_vp, _vp, _vp, _vp]),
     "phg_jacobian_calc1": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "phg_jacobian_calc2": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
@@ -76,6 +97,13 @@ SIGNATURES = {
     "phg_baroclin_create": (C.c_int, [_vp, C.POINTER(BcConf), _vp, C.POINTER(_vp)]),
     "phg_baroclin_destroy": (None, [_vp]),
     "phg_baroclin_calc": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "phg_serve_create": (C.c_int, [C.POINTER(ServeConf), C.POINTER(_vp)]),
+    "phg_serve_preload": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "phg_serve_submit": (C.c_int, [_vp, C.POINTER(Request)]),
+    "phg_serve_poll": (C.c_int, [_vp, C.POINTER(Completion), C.c_int, C.c_double, _ip]),
+    "phg_serve_stats": (C.c_int, [_vp, _dp, _ip, C.POINTER(C.c_longlong)]),
+    "phg_serve_clock": (C.c_double, [_vp]),
+    "phg_serve_destroy": (None, [_vp]),
 }
 
 _lib = None
@@ -250,6 +278,14 @@ class SphereLaplace:
         _check(lib().phg_laplace_solve(self.ops._h, _ptr(out), _ptr(F), _ptr(bnd), _stream(stream)))
         return out
 
+    def solve_batch(self, F, bnd=None, out=None, stream=None):
+        """nv right-hand sides (nv x V, member-major) in one launch."""
+        nv = F.shape[0]
+        out = np.zeros((nv, self.m.size)) if out is None else out
+        F, bnd = _f8(F), _f8(bnd)
+        _check(lib().phg_laplace_solve_batch(self.ops._h, nv, _ptr(out), _ptr(F), _ptr(bnd), _stream(stream)))
+        return out
+
 
 class SphereJacobian:
     """SphereJacobian (src/sjacobian.h:65-149): calc1, calc2, calc2t."""
@@ -364,3 +400,69 @@ class Baroclin:
         _check(lib().phg_baroclin_calc(self._h, _ptr(out1), _ptr(out2), _ptr(_f8(u1)), _ptr(_f8(u2)),
                                        _ptr(_f8(bnd)), _ptr(_f8(f)), _ptr(_f8(g)), _stream(stream)))
         return out1, out2
+
+
+def device_bytes():
+    """(total, this thread) device bytes the library holds."""
+    t, m = C.c_longlong(), C.c_longlong()
+    _check(lib().phg_device_bytes(C.byref(t), C.byref(m)))
+    return t.value, m.value
+
+
+class Server:
+    """Request loop with continuous batching (phg_serve_*).
+
+    ``submit`` takes host numpy arrays; they are kept alive here until the
+    request's completion has been polled, and ``poll`` returns dicts with the
+    completion fields plus ``output`` (the array the result was written to).
+    """
+
+    def __init__(self, precision=PHG_MIXED, hbm_budget_bytes=150e9, max_slots=64, solve_tol=1e-10,
+                 step_tol=1e-12, tau=1e-3, sigma=1.6e-2, mu=8e-5, k1=1.0, k2=1.0, theta=0.5, picard_iters=3):
+        bv = BvConf(tau, sigma, mu, k1, k2, theta, picard_iters)
+        c = ServeConf(hbm_budget_bytes, precision, max_slots, solve_tol, step_tol, bv)
+        h = C.c_void_p()
+        _check(lib().phg_serve_create(C.byref(c), C.byref(h)))
+        self._h = h
+        self._live = {}
+        self._buf = (Completion * 256)()
+
+    def close(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.phg_serve_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def clock(self) -> float:
+        return lib().phg_serve_clock(self._h)
+
+    def preload(self, kind: int, level: int):
+        _check(lib().phg_serve_preload(self._h, kind, level))
+
+    def submit(self, kind: int, level: int, input, bnd=None, steps: int = 1, tag: int = 0, output=None):
+        inp = np.ascontiguousarray(input, dtype=np.float64)
+        b = None if bnd is None else np.ascontiguousarray(bnd, dtype=np.float64)
+        out = np.empty_like(inp) if output is None else output
+        r = Request(kind, level, steps, inp.ctypes.data, None if b is None else b.ctypes.data, out.ctypes.data, tag)
+        self._live[tag] = (inp, b, out)
+        _check(lib().phg_serve_submit(self._h, C.byref(r)))
+
+    def poll(self, wait: float = 0.0, max_n: int = 256):
+        n = C.c_int()
+        _check(lib().phg_serve_poll(self._h, self._buf, min(max_n, 256), wait, C.byref(n)))
+        res = []
+        for k in range(n.value):
+            c = self._buf[k]
+            keep = self._live.pop(c.tag, None)
+            res.append({"tag": c.tag, "status": c.status, "kind": c.kind, "level": c.level,
+                        "t_submit": c.t_submit, "t_admit": c.t_admit, "t_done": c.t_done, "batch": c.batch,
+                        "error": c.error.decode(errors="replace"),
+                        "output": keep[2] if keep else None})
+        return res
+
+    def stats(self):
+        b, nl, d = C.c_double(), C.c_int(), C.c_longlong()
+        _check(lib().phg_serve_stats(self._h, C.byref(b), C.byref(nl), C.byref(d)))
+        return {"bytes_in_use": b.value, "lanes": nl.value, "completed": d.value}
