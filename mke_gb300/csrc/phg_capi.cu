@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdint>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -213,7 +214,7 @@ void to_ell(const Csr &c, int W, std::vector<int> *col, std::vector<double> &val
 }
 
 struct SolveOpBufs {
-    DBuf val, as64, as32, a32, dinv;
+    DBuf val, as64, as32, a32, dinv, dinv32;
     DevSolveOp op;
 };
 
@@ -276,7 +277,53 @@ struct phg_ops_s {
 
 namespace {
 
-int build_solve_op(phg_ops_s *o, const Csr &c, SolveOpBufs &b) {
+int env_int(const char *name, int dflt);
+
+// Real interval holding the spectrum of D^-1 A, or false when it is not a
+// small one (then the solver keeps GMRES).  Upper end: Gershgorin (the rows
+// of D^-1 A have unit diagonal, so Re(lambda) <= 1 + max off-diagonal row
+// sum).  Lower end: power iteration on lmax I - D^-1 A, which approaches
+// lmax - lmin from below, so the estimate of lmin is high; 0.9 of it is used.
+bool cheb_interval(const Csr &c, const std::vector<double> &dinv, double &lmin, double &lmax) {
+    const int n = c.n;
+    if (n < 2) return false;
+    double g = 0.0;
+    for (int i = 0; i < n; ++i) {
+        double r = 0.0;
+        for (int q = c.ptr[i]; q < c.ptr[i + 1]; ++q)
+            if (c.col[q] != i) r += std::fabs(c.val[q]);
+        g = std::max(g, 1.0 + r * std::fabs(dinv[i]));
+    }
+    std::vector<double> v(n), w(n);
+    uint64_t st = 0x9e3779b97f4a7c15ULL;
+    for (int i = 0; i < n; ++i) {
+        st = st * 6364136223846793005ULL + 1442695040888963407ULL;
+        v[i] = (double)(st >> 11) / 9007199254740992.0 - 0.5;
+    }
+    double mu = 0.0;
+    for (int it = 0; it < 100; ++it) {
+        double nv = 0.0, num = 0.0;
+        for (int i = 0; i < n; ++i) {
+            double s = 0.0;
+            for (int q = c.ptr[i]; q < c.ptr[i + 1]; ++q) s += c.val[q] * v[c.col[q]];
+            w[i] = g * v[i] - dinv[i] * s;
+        }
+        for (int i = 0; i < n; ++i) { num += v[i] * w[i]; nv += v[i] * v[i]; }
+        mu = num / nv;
+        double nw = 0.0;
+        for (int i = 0; i < n; ++i) nw += w[i] * w[i];
+        nw = std::sqrt(nw);
+        if (!(nw > 0.0)) return false;
+        for (int i = 0; i < n; ++i) v[i] = w[i] / nw;
+    }
+    const double est = g - mu;
+    if (!(est > 0.05 * g)) return false;
+    lmin = 0.9 * est;
+    lmax = g;
+    return true;
+}
+
+int build_solve_op(phg_ops_s *o, const Csr &c, SolveOpBufs &b, bool try_cheb = false) {
     std::vector<double> v;
     to_ell(c, o->W, nullptr, v);
     std::vector<double> dinv(o->rs, 0.0), as64(v.size());
@@ -296,10 +343,16 @@ int build_solve_op(phg_ops_s *o, const Csr &c, SolveOpBufs &b) {
     }
     (void)n;
     CK(upload(b.val, v)); CK(upload(b.as64, as64)); CK(upload(b.as32, as32)); CK(upload(b.a32, a32));
-    CK(upload(b.dinv, dinv));
+    CK(upload(b.dinv, dinv)); CK(upload(b.dinv32, std::vector<float>(dinv.begin(), dinv.end())));
     b.op.A = o->ell(b.val);
     b.op.as64 = b.as64.as<double>(); b.op.as32 = b.as32.as<float>(); b.op.dinv = b.dinv.as<double>();
     b.op.a32 = b.a32.as<float>();
+    b.op.dinv32 = b.dinv32.as<float>();
+    b.op.cheb_lmin = b.op.cheb_lmax = 0.0;
+    if (try_cheb && o->W <= 8 && env_int("PHG_CHEB", 1)) {
+        double lo = 0.0, hi = 0.0;
+        if (cheb_interval(c, dinv, lo, hi)) { b.op.cheb_lmin = lo; b.op.cheb_lmax = hi; }
+    }
     return PHG_OK;
 }
 
@@ -459,10 +512,10 @@ extern "C" int phg_ops_create(phg_mesh h, int precision, phg_ops *out) {
     CK(upload(o->inner, m.inner)); CK(upload(o->outer, m.outer.empty() ? std::vector<int>{0} : m.outer));
     CK(upload(o->p2io, m.p2io)); CK(upload(o->isb, m.bnd));
     int r;
-    if ((r = build_solve_op(o.get(), so.idt, o->ML))) return r;
+    if ((r = build_solve_op(o.get(), so.idt, o->ML, true))) return r;
     if ((r = build_solve_op(o.get(), so.lapl, o->L))) return r;
     if ((r = build_mg_dev(o.get(), h, o->L, o->mgL, precision))) return r;
-    if ((r = build_solve_op(o.get(), so.jidt, o->MJ))) return r;
+    if ((r = build_solve_op(o.get(), so.jidt, o->MJ, true))) return r;
     if ((r = build_vals(o.get(), so.d1, o->vd1)) || (r = build_vals(o.get(), so.d2, o->vd2)) ||
         (r = build_vals(o.get(), so.d1c, o->vd1c)) || (r = build_vals(o.get(), so.d2c, o->vd2c)))
         return r;
@@ -856,7 +909,7 @@ extern "C" int phg_barvortex_create(phg_ops o, const phg_bv_conf *c, const doubl
     assemble_barvortex(o->mesh->m, c1, c2, A, Ab);
     if (!same_pattern(A, o->mesh->ops.idt)) return fail(PHG_ERR_ARG, "barvortex matrix pattern mismatch");
     int r;
-    if ((r = build_solve_op(o, A, b->A))) return r;
+    if ((r = build_solve_op(o, A, b->A, true))) return r;
     if ((r = build_cols(Ab, b->Ab))) return r;
     std::vector<double> lh(o->V, 0.0);
     if (coriolis) {

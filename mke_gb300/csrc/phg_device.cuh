@@ -71,6 +71,11 @@ struct DevSolveOp {
     DevEll cpl;
     const float *cpl32 = nullptr;
     const float *dinv32 = nullptr;
+    // Spectrum interval of D^{-1} A for well-conditioned operators (mass
+    // matrices, whose Jacobi-scaled eigenvalues lie in about [1/2, 2]): when
+    // set, the solver runs Chebyshev iterations inside the FP64 refinement
+    // loop instead of GMRES -- no inner products, one group barrier per step.
+    double cheb_lmin = 0.0, cheb_lmax = 0.0;
 };
 
 // rs x os boundary columns in CSR over rows (few nonzero rows).

@@ -31,6 +31,7 @@
 // Every wait is bounded: a barrier that spins longer than ~1 s (clock64)
 // raises a device error flag; all blocks see the flag at their next barrier
 // and return, and the host reports status 2.
+#include <cmath>
 #include <cstdio>
 #include <mutex>
 
@@ -45,6 +46,7 @@ constexpr int BLOCK = 256;
 constexpr int NWARP = BLOCK / 32;
 constexpr double INNER_RTOL = 1e-5;  // FP32 cycle: reduce the residual 1e5x, then refine
 constexpr long long SPIN_LIMIT = 2000000000LL;  // clock64 cycles (~1 s)
+constexpr int CHEB_KMAX = 64;    // most Chebyshev steps per refinement cycle
 
 struct Params {
     DevSolveOp op;
@@ -65,6 +67,11 @@ struct Params {
     long long *timers;       // optional phase cycle counters (block 0)
     double mg_row_bytes;     // algorithmic bytes of one V-cycle per fine row
     size_t group_elems;      // per-group scratch elements (V-cycle + block preconditioner)
+    double inner_rtol;       // mixed path: residual reduction of one FP32 cycle
+    // Chebyshev path: steps per refinement cycle and the recurrence
+    // coefficients d_k = ca[k] d_{k-1} + cb[k] D^-1 r_k, d_0 = c0 D^-1 r_0
+    int cheb_k;
+    double cheb_c0, cheb_ca[CHEB_KMAX], cheb_cb[CHEB_KMAX];
 };
 
 // phase cycle counters kept by block 0 when PHG_PHASE_TIMING is set
@@ -115,15 +122,23 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// block-reduce K (<= KMAX) per-thread values, result in red[off + l][0]
-template <int KMAX>
-__device__ __forceinline__ void block_reduce(const double (&acc)[KMAX], int K, double (*red)[NWARP], int off) {
+__device__ __forceinline__ float warp_sum(float v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// block-reduce K (<= KMAX) per-thread values, result in red[off + l][0].
+// The warps reduce in the type of the values (FP32 in the mixed path: FP64
+// runs at a small fraction of the FP32 rate on this part), the NWARP warp
+// sums are added in FP64.
+template <int KMAX, typename T>
+__device__ __forceinline__ void block_reduce(const T (&acc)[KMAX], int K, double (*red)[NWARP], int off) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int l = 0; l < KMAX; ++l) {
         if (l < K) {
-            double v = warp_sum(acc[l]);
-            if (lane == 0) red[off + l][warp] = v;
+            T v = warp_sum(acc[l]);
+            if (lane == 0) red[off + l][warp] = (double)v;
         }
     }
     __syncthreads();
@@ -138,18 +153,21 @@ __device__ __forceinline__ void block_reduce(const double (&acc)[KMAX], int K, d
 // group-wide sums of K values held in red[l][0] by every block: publish into
 // one of two alternating partial buffers ([value][block] layout), barrier,
 // then warp w sums value l = w, w + NWARP, ... over the G blocks
+// T: the type the partials are published and summed in (FP32 for the inner
+// Krylov scalars of the mixed path, FP64 otherwise)
+template <typename T = double>
 __device__ __forceinline__ bool group_sum(int K, double *out, double (*red)[NWARP], double *part2, int &parity,
                                           int G, int bi, unsigned *bar, int *err, long long *tm) {
-    double *part = part2 + (size_t)parity * G * (MAXM + 2);
+    T *part = (T *)(part2 + (size_t)parity * G * (MAXM + 2));
     parity ^= 1;
-    if (threadIdx.x < K) part[(size_t)threadIdx.x * G + bi] = red[threadIdx.x][0];
+    if (threadIdx.x < K) part[(size_t)threadIdx.x * G + bi] = (T)red[threadIdx.x][0];
     if (!group_sync(bar, G, err, tm)) return false;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int l = warp; l < K; l += NWARP) {
-        double s = 0.0;
+        T s = 0;
         for (int b = lane; b < G; b += 32) s += ldcg(&part[(size_t)l * G + b]);
         s = warp_sum(s);
-        if (lane == 0) out[l] = s;
+        if (lane == 0) out[l] = (double)s;
     }
     __syncthreads();
     return true;
@@ -429,6 +447,10 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
     VT *msm = (VT *)(hcol + MAXM + 2);      // redundant multigrid levels
     __shared__ double red[MAXM + 2][NWARP];
     __shared__ int flag[4];
+    // scalars computed by thread 0 and read by all (FP64 division and square
+    // roots are slow on this part; one thread does them, not every thread)
+    __shared__ double scal[4];
+    __shared__ VT vscal[1];
 
     // everything the loops need, copied out of the parameter block
     const int m = p.m, n = p.n, G = p.G, nv = p.nv, groups = p.groups, max_iter = p.max_iter;
@@ -467,7 +489,7 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
     double *Xp = p.X;
     VT *Vp = (VT *)p.V, *Zp = (VT *)p.Z, *Wp = (VT *)p.Wv;
     double *Rp = p.R;
-    const double inner_rtol = sizeof(VT) == 4 ? INNER_RTOL : 0.0;
+    const double inner_rtol = sizeof(VT) == 4 ? p.inner_rtol : 0.0;
     const double es = (double)sizeof(VT), nrows = (double)(r1 - r0);
     const double mg_row_bytes = p.mg_row_bytes;
     long long t_start = clock64(), tph = 0;
@@ -503,7 +525,9 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
         }
         block_reduce<1>(acc, 1, red, 0);
         if (!group_sum(1, hcol, red, part2, parity, G, bi, bar, err, tm)) return;
-        const double bnorm = sqrt(hcol[0]);
+        if (threadIdx.x == 0) scal[0] = sqrt(hcol[0]);
+        __syncthreads();
+        const double bnorm = scal[0];
         int iters = 0, cycles = 0, status = 1;
         double beta_prev = 0.0, rel = 0.0;
         if (bnorm == 0.0) {
@@ -527,18 +551,25 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
             }
             block_reduce<1>(acc, 1, red, 0);
             if (!group_sum(1, hcol, red, part2, parity, G, bi, bar, err, tm)) return;
-            const double beta = sqrt(hcol[0]);
+            if (threadIdx.x == 0) {
+                const double bt = sqrt(hcol[0]);
+                scal[1] = bt;
+                scal[2] = bt / bnorm;
+                scal[3] = bt > 0.0 ? 1.0 / bt : 0.0;
+            }
+            __syncthreads();
+            const double beta = scal[1];
             PHG_TICK(T_RESID);
             my_bytes += nrows * (W * 12.0 + 24.0);
-            rel = beta / bnorm;
+            rel = scal[2];
             if (rel <= tol) { status = 0; break; }
             if (iters >= max_iter) { status = 1; break; }
             if (cycles > 0 && !(beta < 0.9999 * beta_prev)) { status = 1; break; }
             beta_prev = beta;
             ++cycles;
-            const double target = fmax(tol * bnorm, inner_rtol * beta);
+            const double target = threadIdx.x == 0 ? fmax(tol * bnorm, inner_rtol * beta) : 0.0;
             {
-                const double ib = 1.0 / beta;
+                const double ib = scal[3];
                 for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) V[i] = (VT)(R[i] * ib);
             }
             if (threadIdx.x == 0) {
@@ -613,14 +644,17 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
                         t0 += q0 * s; t1 += q1 * s; t2 += q2 * s; t3 += q3 * s;
                         t4 += q4 * s; t5 += q5 * s; t6 += q6 * s; t7 += q7 * s;
                     }
-                    const double a8[8] = {(double)t0, (double)t1, (double)t2, (double)t3,
-                                          (double)t4, (double)t5, (double)t6, (double)t7};
+                    const VT a8[8] = {t0, t1, t2, t3, t4, t5, t6, t7};
                     block_reduce<8>(a8, kk, red, l0);
                 }
                 PHG_TICK(T_SPMV_DOT);
-                if (!group_sum(j + 1, hcol, red, part2, parity, G, bi, bar, err, tm)) return;
+                if (!group_sum<VT>(j + 1, hcol, red, part2, parity, G, bi, bar, err, tm)) return;
                 PHG_TICK(T_DOT_SUM);
-                // (2) w -= sum h_l v_l, ||w||^2
+                // (2) w -= sum h_l v_l, ||w||^2; the coefficients converted to
+                // the Krylov precision once (y is free until the cycle ends)
+                VT *hv = (VT *)y;
+                if (threadIdx.x <= j) hv[threadIdx.x] = (VT)hcol[threadIdx.x];
+                __syncthreads();
                 {
                     VT a2 = 0;
                     for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
@@ -636,32 +670,29 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
                             const VT q5 = kk > 5 ? Vl[(size_t)5 * n + i] : (VT)0;
                             const VT q6 = kk > 6 ? Vl[(size_t)6 * n + i] : (VT)0;
                             const VT q7 = kk > 7 ? Vl[(size_t)7 * n + i] : (VT)0;
-                            s -= (VT)hcol[l0] * q0;
-                            if (kk > 1) s -= (VT)hcol[l0 + 1] * q1;
-                            if (kk > 2) s -= (VT)hcol[l0 + 2] * q2;
-                            if (kk > 3) s -= (VT)hcol[l0 + 3] * q3;
-                            if (kk > 4) s -= (VT)hcol[l0 + 4] * q4;
-                            if (kk > 5) s -= (VT)hcol[l0 + 5] * q5;
-                            if (kk > 6) s -= (VT)hcol[l0 + 6] * q6;
-                            if (kk > 7) s -= (VT)hcol[l0 + 7] * q7;
+                            s -= hv[l0] * q0;
+                            if (kk > 1) s -= hv[l0 + 1] * q1;
+                            if (kk > 2) s -= hv[l0 + 2] * q2;
+                            if (kk > 3) s -= hv[l0 + 3] * q3;
+                            if (kk > 4) s -= hv[l0 + 4] * q4;
+                            if (kk > 5) s -= hv[l0 + 5] * q5;
+                            if (kk > 6) s -= hv[l0 + 6] * q6;
+                            if (kk > 7) s -= hv[l0 + 7] * q7;
                         }
                         w[i] = s;
                         a2 += s * s;
                     }
-                    acc[0] = (double)a2;
+                    const VT a1[1] = {a2};
+                    block_reduce<1>(a1, 1, red, 0);
                 }
-                block_reduce<1>(acc, 1, red, 0);
                 PHG_TICK(T_UPDATE);
-                if (!group_sum(1, hcol + j + 1, red, part2, parity, G, bi, bar, err, tm)) return;
+                if (!group_sum<VT>(1, hcol + j + 1, red, part2, parity, G, bi, bar, err, tm)) return;
                 PHG_TICK(T_NORM_SUM);
-                const double hn = sqrt(hcol[j + 1]);
-                // (3) v_{j+1}, Givens
-                if (hn > 0.0) {
-                    const VT inv = (VT)(1.0 / hn);
-                    VT *vn = V + (size_t)(j + 1) * n;
-                    for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) vn[i] = w[i] * inv;
-                }
+                // (3) thread 0: ||w||, the rotations and the stopping test;
+                // then every thread scales w into v_{j+1}
                 if (threadIdx.x == 0) {
+                    const double hn = sqrt(hcol[j + 1]);
+                    vscal[0] = hn > 0.0 ? (VT)(1.0 / hn) : (VT)0;
                     hcol[j + 1] = hn;
                     for (int l = 0; l < j; ++l) {
                         double a = hcol[l], c = hcol[l + 1];
@@ -679,6 +710,12 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
                     flag[0] = (fabs(g[j + 1]) <= target) || hn == 0.0;
                 }
                 __syncthreads();
+                {
+                    const VT inv = vscal[0];
+                    VT *vn = V + (size_t)(j + 1) * n;
+                    if (inv != (VT)0)
+                        for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) vn[i] = w[i] * inv;
+                }
                 PHG_TICK(T_GIVENS);
                 ++iters;
                 ++my_steps;
@@ -687,20 +724,25 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
                 if (flag[0] || iters >= max_iter) break;
             }
             // y = H^-1 g; x += D^-1 V y (Jacobi) or Z y (multigrid)
+            // The correction sum_l y_l z_l is formed in the Krylov precision
+            // (in the mixed path it only has to be as accurate as the FP32
+            // inner solve) and added to the FP64 iterate once.
+            VT *yv = (VT *)cs;   // the rotations are not needed any more
             if (threadIdx.x == 0) {
                 for (int l = jlast - 1; l >= 0; --l) {
                     double s = g[l];
                     for (int k = l + 1; k < jlast; ++k) s -= H[l * MAXM + k] * y[k];
                     y[l] = s / H[l * MAXM + l];
                 }
+                for (int l = 0; l < jlast; ++l) yv[l] = (VT)y[l];
             }
             __syncthreads();
             {
                 const VT *Bb = use_mg ? Z : V;
                 for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
-                    double s = 0.0;
-                    for (int l = 0; l < jlast; ++l) s += y[l] * (double)Bb[(size_t)l * n + i];
-                    x[i] += use_mg ? s : dinv[i] * s;
+                    VT s = 0;
+                    for (int l = 0; l < jlast; ++l) s += yv[l] * Bb[(size_t)l * n + i];
+                    x[i] += use_mg ? (double)s : dinv[i] * (double)s;
                 }
             }
             my_bytes += nrows * (jlast * es + 24.0);
@@ -720,6 +762,152 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
         atomicMax(&p.stats->cycles, my_cycles);
         atomicMax(&p.stats->status, my_status);
         // relres >= 0: max via the integer order of non-negative doubles
+        atomicMax((unsigned long long *)&p.stats->relres, (unsigned long long)__double_as_longlong(my_rel));
+    }
+}
+
+// Chebyshev iteration (Saad, Iterative Methods for Sparse Linear Systems,
+// 2nd ed., Alg. 12.1, Jacobi-preconditioned) inside the same FP64 iterative
+// refinement as the GMRES kernel: per cycle r = b - A x in FP64, then
+// cheb_k steps on A e = r / ||r|| in the Krylov precision, x += ||r|| e.
+// For operators whose Jacobi-scaled spectrum is known to lie in a small real
+// interval (mass matrices) this needs no inner products: one SpMV and one
+// group barrier per step.  Work vectors (in the V region): rv, d, e0, e1.
+template <typename VT>
+__global__ void __launch_bounds__(BLOCK, 2) cheb_kernel(const Params p) {
+    extern __shared__ double smem[];
+    double *hcol = smem;
+    VT *cf = (VT *)(smem + 4);              // ca[k], cb[k] in the Krylov precision
+    __shared__ double red[MAXM + 2][NWARP];
+    __shared__ double scal[4];
+    const int n = p.n, G = p.G, nv = p.nv, groups = p.groups, max_iter = p.max_iter, K = p.cheb_k;
+    const size_t ld = (size_t)p.ld;
+    const double tol = p.tol;
+    const int grp = blockIdx.x / G, bi = blockIdx.x % G;
+    if (grp >= groups) return;
+    if (threadIdx.x == 0) {   // constant indices: the parameter block stays in param space
+#pragma unroll
+        for (int k = 0; k < CHEB_KMAX; ++k) {
+            cf[k] = (VT)p.cheb_ca[k];
+            cf[CHEB_KMAX + k] = (VT)p.cheb_cb[k];
+        }
+    }
+    __syncthreads();
+    const VT c0 = (VT)p.cheb_c0;
+    unsigned *bar = p.bar + 2 * grp;
+    int *err = p.err;
+    double *part2 = p.part + (size_t)grp * 2 * G * (MAXM + 2);
+    int parity = 0;
+    int r0, r1;
+    own_rows(n, G, bi, r0, r1);
+    const int W = p.op.A.W;
+    const int *__restrict__ col = p.op.A.col;
+    const double *__restrict__ aval = p.op.A.val;
+    const VT *__restrict__ sval = sizeof(VT) == 8 ? (const VT *)(const void *)p.op.A.val
+                                                   : (const VT *)(const void *)p.op.a32;
+    const VT *__restrict__ dv = sizeof(VT) == 8 ? (const VT *)(const void *)p.op.dinv
+                                                 : (const VT *)(const void *)p.op.dinv32;
+    const double *Bp = p.B;
+    double *Xp = p.X;
+    VT *Vp = (VT *)p.V;
+    double *Rp = p.R;
+    const double inner_rtol = sizeof(VT) == 4 ? p.inner_rtol : 0.0;
+    const double es = (double)sizeof(VT), nrows = (double)(r1 - r0);
+    int my_iters = 0, my_cycles = 0, my_status = 0, my_steps = 0;
+    double my_rel = 0.0, my_bytes = 0.0;
+    (void)inner_rtol;
+
+    for (int v = grp; v < nv; v += groups) {
+        const double *__restrict__ b = Bp + (size_t)v * ld;
+        double *x = Xp + (size_t)v * ld;
+        VT *rv = Vp + (size_t)v * (p.m + 1) * n;
+        VT *d = rv + n, *e0 = d + n, *e1 = e0 + n;
+        double *R = Rp + (size_t)v * n;
+        {
+            double s = 0.0;
+            for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) { const double t = b[i]; s += t * t; }
+            const double a1[1] = {s};
+            block_reduce<1>(a1, 1, red, 0);
+        }
+        if (!group_sum(1, hcol, red, part2, parity, G, bi, bar, err, nullptr)) return;
+        if (threadIdx.x == 0) scal[0] = sqrt(hcol[0]);
+        __syncthreads();
+        const double bnorm = scal[0];
+        int iters = 0, cycles = 0, status = 1;
+        double beta_prev = 0.0, rel = 0.0;
+        if (bnorm == 0.0) {
+            for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) x[i] = 0.0;
+            status = 0;
+        }
+        while (bnorm != 0.0) {
+            if (!group_sync(bar, G, err, nullptr)) return;   // x complete
+            {
+                double s = 0.0;
+                for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
+                    const double q = b[i] - spmv_row<double, true>(col, aval, n, W, x, i);
+                    R[i] = q;
+                    s += q * q;
+                }
+                const double a1[1] = {s};
+                block_reduce<1>(a1, 1, red, 0);
+            }
+            if (!group_sum(1, hcol, red, part2, parity, G, bi, bar, err, nullptr)) return;
+            if (threadIdx.x == 0) {
+                const double bt = sqrt(hcol[0]);
+                scal[1] = bt;
+                scal[2] = bt / bnorm;
+                scal[3] = bt > 0.0 ? 1.0 / bt : 0.0;
+            }
+            __syncthreads();
+            const double beta = scal[1];
+            my_bytes += nrows * (W * 12.0 + 24.0);
+            rel = scal[2];
+            if (rel <= tol) { status = 0; break; }
+            if (iters >= max_iter) { status = 1; break; }
+            if (cycles > 0 && !(beta < 0.9999 * beta_prev)) { status = 1; break; }
+            beta_prev = beta;
+            ++cycles;
+            // e_1 = d_0 = c0 D^-1 r / beta
+            {
+                const double ib = scal[3];
+                for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
+                    const VT r = (VT)(R[i] * ib);
+                    const VT dd = c0 * dv[i] * r;
+                    rv[i] = r;
+                    d[i] = dd;
+                    e0[i] = dd;
+                }
+            }
+            VT *ec = e0, *en = e1;
+            for (int k = 1; k < K; ++k) {
+                if (!group_sync(bar, G, err, nullptr)) return;   // e_k complete
+                const VT ca = cf[k], cb = cf[CHEB_KMAX + k];
+                for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
+                    const VT s = spmv_row<VT, true>(col, sval, n, W, ec, i);
+                    const VT dd = ca * d[i] + cb * dv[i] * (rv[i] - s);
+                    d[i] = dd;
+                    en[i] = ec[i] + dd;
+                }
+                VT *t = ec; ec = en; en = t;
+                ++iters;
+                ++my_steps;
+                my_bytes += nrows * (W * (4.0 + es) + 7.0 * es);
+            }
+            ++iters;
+            for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) x[i] += beta * (double)ec[i];
+            my_bytes += nrows * (es + 16.0);
+        }
+        my_iters = max(my_iters, iters);
+        my_cycles = max(my_cycles, cycles);
+        my_rel = fmax(my_rel, rel);
+        my_status = max(my_status, status);
+    }
+    if (threadIdx.x == 0) atomicAdd(&p.stats->bytes, my_bytes);
+    if (threadIdx.x == 0 && bi == 0) {
+        atomicAdd(&p.stats->steps_total, my_steps);
+        atomicMax(&p.stats->iters, my_iters);
+        atomicMax(&p.stats->cycles, my_cycles);
+        atomicMax(&p.stats->status, my_status);
         atomicMax((unsigned long long *)&p.stats->relres, (unsigned long long)__double_as_longlong(my_rel));
     }
 }
@@ -809,10 +997,14 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     const int n = op.A.n;
     Params p;
     const size_t es = prec == PREC_MIXED ? 4 : 8;
-    const size_t smem = smem_gmres_bytes() + (op.mgd ? es * op.mg.red_elems : 0) + 16;
+    const bool cheb = op.cheb_lmax > 0.0 && op.cheb_lmin > 0.0 && op.cheb_lmin < op.cheb_lmax && m >= 3 &&
+                      !op.mgd && !op.block4 && op.A.W <= 8;
+    const size_t smem = cheb ? sizeof(double) * (4 + 2 * CHEB_KMAX)
+                             : smem_gmres_bytes() + (op.mgd ? es * op.mg.red_elems : 0) + 16;
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
-    void *fn = prec == PREC_MIXED ? (void *)gmres_kernel<float> : (void *)gmres_kernel<double>;
-    cudaError_t e = allow_smem(prec);
+    void *fn = cheb ? (prec == PREC_MIXED ? (void *)cheb_kernel<float> : (void *)cheb_kernel<double>)
+                    : (prec == PREC_MIXED ? (void *)gmres_kernel<float> : (void *)gmres_kernel<double>);
+    cudaError_t e = cheb ? cudaSuccess : allow_smem(prec);
     if (e != cudaSuccess) return e;
     int per = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, BLOCK, smem);
@@ -835,6 +1027,30 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     p.V = w + L.v; p.Z = w + L.z; p.Wv = w + L.w; p.R = (double *)(w + L.r);
     p.mgbuf = w + L.mg;
     p.group_elems = block_group_elems(op);
+    {
+        const char *e = getenv("PHG_INNER_RTOL");
+        p.inner_rtol = e ? atof(e) : INNER_RTOL;
+    }
+    p.cheb_k = 0;
+    if (cheb) {
+        // steps for an error reduction eps (residual: one more factor kappa)
+        const double lo = op.cheb_lmin, hi = op.cheb_lmax;
+        const double kappa = hi / lo, sq = sqrt(kappa), sigma = (sq - 1.0) / (sq + 1.0);
+        const double eps = prec == PREC_MIXED ? p.inner_rtol : fmax(0.25 * tol, 1e-15);
+        int K = (int)ceil(log(2.0 * kappa / eps) / log(1.0 / sigma)) + 1;
+        K = K < 2 ? 2 : (K > CHEB_KMAX ? CHEB_KMAX : K);
+        const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), s1 = theta / delta;
+        p.cheb_k = K;
+        p.cheb_c0 = 1.0 / theta;
+        double rho_prev = 1.0 / s1;
+        p.cheb_ca[0] = p.cheb_cb[0] = 0.0;
+        for (int k = 1; k < K; ++k) {
+            const double rho = 1.0 / (2.0 * s1 - rho_prev);
+            p.cheb_ca[k] = rho * rho_prev;
+            p.cheb_cb[k] = 2.0 * rho / delta;
+            rho_prev = rho;
+        }
+    }
     p.part = (double *)(w + L.part);
     p.bar = (unsigned *)(w + L.bar); p.err = (int *)(w + L.err); p.stats = stats_dev;
     p.groups = groups; p.G = G;
