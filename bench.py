@@ -211,6 +211,9 @@ def run_ours(args, ws, rank, local):
             row["mixed_over_fp64"] = row["mixed"]["member_steps_per_s"] / row["fp64"]["member_steps_per_s"]
             batched[f"L{lvl}x{B}"] = row
 
+    # operator apply at a streaming size (level 8, 64 FP32 vectors; one FP64 vector)
+    spmv = None if args.no_spmv else run_spmv(8, 64)
+
     # serving trace (the first --bench-serve-requests requests of the 10,000-request trace)
     served = None
     if not args.no_serve and args.bench_serve_requests > 0:
@@ -277,6 +280,7 @@ def run_ours(args, ws, rank, local):
         "state_rel_diff_mixed_vs_fp64": rel,
         "batched": batched,
         "serve": served,
+        "spmv": spmv,
         "solver": {"mixed": mixed["stats"], "fp64": fp64["stats"]},
         "roofline": {"kernel": "gmres_kernel (persistent solver)", "bound": "hbm", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -378,11 +382,83 @@ def run_serve(precision: str, n: int, rate: float, levels=(3, 4, 5, 6, 7)):
     return stats
 
 
+def run_spmv(level: int = 8, nv: int = 64, reps: int = 20):
+    """Operator apply (phelm::Solver::mult_vector) at a streaming size: the
+    Laplacian of a level-`level` mesh applied to nv FP32 vectors (the mixed
+    path's SpMV, interleaved members) and to one FP64 vector; L2 flushed
+    before every launch, CUDA events around each launch on its stream.
+    Algorithmic bytes: the matrix once (column + value per nonzero) plus every
+    vector read and written once."""
+    import torch
+    from mke_gb300 import phelm
+    saved = {k: os.environ.get(k) for k in ("PHG_MG", "PHG_CHEB")}
+    os.environ["PHG_MG"] = "0"      # no solves here: skip the multigrid setup
+    os.environ["PHG_CHEB"] = "0"
+    try:
+        m = phelm.Mesh.sphere(level)
+        ops = phelm.Operators(m, phelm.PHG_MIXED)
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    rs = m.inner_size
+    ptr, _, _ = m.csr("lapl")
+    nnz = int(ptr[-1])
+    dev = torch.device("cuda")
+    st = torch.cuda.Stream()
+    # flush: write 256 MB (> L2), then read another 256 MB so that the write-backs
+    # of the dirty lines happen here and not inside the timed launch
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    clean = torch.zeros(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    g = torch.Generator(device=dev).manual_seed(SEED)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+
+    def timed(fn):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        with torch.cuda.stream(st):
+            fn()
+            for a, b in ev:
+                flush.zero_()
+                clean.sum()
+                a.record(st)
+                fn()
+                b.record(st)
+        st.synchronize()
+        return sum(a.elapsed_time(b) for a, b in ev) / reps * 1e3   # us
+
+    x32 = torch.randn(rs, nv, dtype=torch.float32, device=dev, generator=g)   # interleaved members
+    y32 = torch.empty_like(x32)
+    us32 = timed(lambda: ops.mult32("lapl", x32, y32, stream=st))
+    b32 = nnz * 8 + nv * rs * 8
+    x64 = torch.randn(rs, dtype=torch.float64, device=dev, generator=g)
+    y64 = torch.empty_like(x64)
+    us64 = timed(lambda: ops.mult("lapl", x64, out=y64, stream=st))
+    b64 = nnz * 12 + rs * 16
+    return {"level": level, "rows": rs, "nnz": nnz,
+            "l2": "flushed before every launch (256 MB written, then 256 MB of another buffer read)",
+            "fp32_multivector": {"members": nv, "layout": "interleaved (rs x nv)", "us_per_launch": us32,
+                                 "bytes": b32, "gbs": b32 / us32 / 1e3, "frac_of_peak": b32 / us32 / 1e3 / peak},
+            "fp64_single": {"us_per_launch": us64, "bytes": b64, "gbs": b64 / us64 / 1e3,
+                            "frac_of_peak": b64 / us64 / 1e3 / peak,
+                            "fp64_gops_nonfused": 2.0 * nnz / us64 / 1e3},
+            "peak_gbs": peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"}
+
+
 def run_case(args):
     """Small fixed workloads for profilers: `solve` = Laplace solves,
     `step` = barvortex steps, at --level with --steps repetitions."""
     if args.case == "serve":
         print(json.dumps(run_serve(args.precision, args.serve_requests, args.serve_rate)))
+        return
+    if args.case == "spmv":
+        print(json.dumps(run_spmv(args.level, args.members)))
         return
     import torch
     from mke_gb300 import phelm
@@ -446,11 +522,12 @@ def main():
     ap.add_argument("--tol", type=float, default=TOL)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurements")
-    ap.add_argument("--case", choices=["solve", "step", "batch", "serve"],
+    ap.add_argument("--case", choices=["solve", "step", "batch", "serve", "spmv"],
                     help="one workload only (no bench line): profiling cases, or the serving trace")
     ap.add_argument("--serve-requests", type=int, default=10000, help="requests of --case serve")
     ap.add_argument("--bench-serve-requests", type=int, default=2000, help="requests of the bench line's serve block")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving trace")
+    ap.add_argument("--no-spmv", action="store_true", help="skip the streaming operator-apply measurement")
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--members", type=int, default=16, help="ensemble members for --case batch")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])

@@ -104,6 +104,18 @@ int phg_ops_set_solver(phg_ops o, int restart, double tol, int max_iter);
 int phg_ops_set_sms(phg_ops o, int max_sms);
 /* Statistics of the last solve on this handle (host memory). */
 int phg_ops_last_solve(phg_ops o, int *iters, int *cycles, double *relres);
+/* phelm::Solver::mult_vector (src/impl/slaplace_impl.h:109-113,
+ * src/sjacobian.cpp:160-181): y = A x for nv member-major inner vectors
+ * (nv x rs), A one of the handle's inner x inner operators: "idt" "lapl"
+ * (SphereLaplace), "jidt" "d1" "d2" "d1c" "d2c" (SphereJacobian).  FP64,
+ * ascending column order: the same bits as the CPU CSR product. */
+int phg_ops_mult(phg_ops o, const char *name, double *y, const double *x, int nv, void *stream);
+/* The FP32 operator apply of the mixed-precision path ("idt" "lapl" "jidt")
+ * on an interleaved multi-vector: x, y are rs x nv with the nv members of a
+ * point contiguous (nv = 4, 8, 16, ..., 256; 16-byte aligned device pointers),
+ * so every gathered row of x is one contiguous read.  No reference
+ * counterpart. */
+int phg_ops_mult32(phg_ops o, const char *name, float *y, const float *x, int nv, void *stream);
 /* Synchronise `stream` and judge the solves enqueued on this handle since the
  * last check (calls with device pointers do not wait for their solves):
  * PHG_ERR_NOT_CONVERGED / PHG_ERR_TIMEOUT as a host-pointer call would

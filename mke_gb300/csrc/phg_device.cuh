@@ -45,8 +45,8 @@ struct MgDev {
     MgLevelDev lev[MG_MAXLEV];
     int nc = 0;      // coarsest size; dense inverse row-major
     const double *cinv64 = nullptr; const float *cinv32 = nullptr;
-    double omega = 0.7;
-    int nu1 = 2, nu2 = 2;
+    double omega = 0.9;
+    int nu1 = 1, nu2 = 1;
     int red_off[MG_MAXLEV] = {0};  // shared-memory element offsets of levels [nred, nlev)
     size_t red_elems = 0;          // shared-memory elements of those levels (x, xt, b, r each)
     size_t group_elems = 0;        // global elements per group for levels [0, nred)

@@ -1,3 +1,4 @@
+#include <cstdint>
 // phg_kernels.cu -- operator applies and fused elementwise kernels.
 //
 // This file is compiled with -fmad=false: every product and sum below is
@@ -489,6 +490,132 @@ cudaError_t bc_commit(double *un, const double *un1, const double *nr, int *done
     k_bc_done<<<1, 32, 0, s>>>(nr, done, tol);
     g_kernel_launches += 2;
     return cudaGetLastError();
+}
+
+}  // namespace phg
+
+// ------------------------------------------------------- operator apply ---
+namespace phg {
+namespace {
+
+// y_v = A x_v for nv member-major vectors on the shared inner x inner
+// pattern.  A thread owns one row: it loads the row's columns and values once
+// (the matrix streams from memory once per launch) and applies them to every
+// member.  Ascending column order; FP64 sums round like the CPU CSR product.
+template <typename T>
+__global__ void __launch_bounds__(TB) k_spmm(const int *__restrict__ col, const T *__restrict__ val, int n, int W,
+                                             const T *__restrict__ x, int ldx, T *__restrict__ y, int ldy, int nv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int c[8];
+    T a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        if (k < W) { c[k] = __ldg(&col[(size_t)k * n + i]); a[k] = __ldg(&val[(size_t)k * n + i]); }
+    for (int v = 0; v < nv; ++v) {
+        const T *xv = x + (size_t)v * ldx;
+        T g[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < W) g[k] = __ldg(&xv[c[k]]);
+        T s = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < W) s += a[k] * g[k];
+        y[(size_t)v * ldy + i] = s;
+    }
+}
+
+// Y = A X for an interleaved FP32 multi-vector (row r of X holds the nv
+// members of point r contiguously, nv = 4 q4).  TPR = q4 / CH threads share
+// a row; thread q forms the 4-member chunks q, q + TPR, ... (CH of them), so
+// consecutive threads read consecutive 16-byte chunks of each gathered row
+// of X and every sector fetched is used in full; the row's columns and values
+// are loaded once per thread and reused for its CH chunks.  W is a
+// compile-time slot count (7 for the P1 sphere pattern).
+template <int W, int CH>
+__global__ void __launch_bounds__(TB) k_spmm_il(const int *__restrict__ col, const float *__restrict__ val, int n,
+                                                const float4 *__restrict__ x, float4 *__restrict__ y, int q4,
+                                                int tpr_log2) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;   // n * q4 / CH < 2^31 (host check)
+    const int i = (int)(t >> tpr_log2), q = (int)(t & ((1u << tpr_log2) - 1u));
+    if (i >= n) return;
+    const int tpr = 1 << tpr_log2;
+    int c[W];
+    float a[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) { c[k] = __ldg(&col[(size_t)k * n + i]); a[k] = __ldg(&val[(size_t)k * n + i]); }
+    // all CH x W gathers are issued before any arithmetic (more bytes in flight)
+    float4 g[CH][W];
+#pragma unroll
+    for (int j = 0; j < CH; ++j)
+#pragma unroll
+        for (int k = 0; k < W; ++k) g[j][k] = __ldg(&x[(size_t)c[k] * q4 + q + j * tpr]);
+#pragma unroll
+    for (int j = 0; j < CH; ++j) {
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < W; ++k) {
+            s.x = __fmaf_rn(a[k], g[j][k].x, s.x); s.y = __fmaf_rn(a[k], g[j][k].y, s.y);
+            s.z = __fmaf_rn(a[k], g[j][k].z, s.z); s.w = __fmaf_rn(a[k], g[j][k].w, s.w);
+        }
+        y[(size_t)i * q4 + q + j * tpr] = s;
+    }
+}
+
+template <int W>
+cudaError_t launch_il(const int *col, const float *val, int n, const float4 *x, float4 *y, int q4, cudaStream_t s) {
+    // Eight threads per row (fewer when the row has fewer chunks), each with
+    // q4 / 8 chunks: the best of a sweep over 1..16 chunks per thread and
+    // 256/1024-thread blocks on a level-8 Laplacian with 32 and 64 members.
+    const int tpr = q4 < 8 ? q4 : 8;
+    const int ch = q4 / tpr;
+    if (tpr * ch != q4) return cudaErrorInvalidValue;
+    int lg = 0;
+    while ((1 << lg) < tpr) ++lg;
+    if ((1 << lg) != tpr) return cudaErrorInvalidValue;
+    const long long work = (long long)n * tpr;
+    if (work >= (1LL << 31)) return cudaErrorInvalidValue;
+    const unsigned blocks = (unsigned)((work + TB - 1) / TB);
+    switch (ch) {
+    case 1: k_spmm_il<W, 1><<<blocks, TB, 0, s>>>(col, val, n, x, y, q4, lg); break;
+    case 2: k_spmm_il<W, 2><<<blocks, TB, 0, s>>>(col, val, n, x, y, q4, lg); break;
+    case 4: k_spmm_il<W, 4><<<blocks, TB, 0, s>>>(col, val, n, x, y, q4, lg); break;
+    case 8: k_spmm_il<W, 8><<<blocks, TB, 0, s>>>(col, val, n, x, y, q4, lg); break;
+    default: return cudaErrorInvalidValue;   // more than 256 members: split the call
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+template <typename T>
+cudaError_t spmm(const int *col, const T *val, int n, int W, const T *x, int ldx, T *y, int ldy, int nv,
+                 cudaStream_t s) {
+    if (W > 8 || n < 1 || nv < 1) return cudaErrorInvalidValue;
+    k_spmm<T><<<(unsigned)((n + TB - 1) / TB), TB, 0, s>>>(col, val, n, W, x, ldx, y, ldy, nv);
+    g_kernel_launches++;
+    return cudaGetLastError();
+}
+
+template cudaError_t spmm<double>(const int *, const double *, int, int, const double *, int, double *, int, int,
+                                  cudaStream_t);
+template cudaError_t spmm<float>(const int *, const float *, int, int, const float *, int, float *, int, int,
+                                 cudaStream_t);
+
+cudaError_t spmm_il32(const int *col, const float *val, int n, int W, const float *x, float *y, int nv,
+                      cudaStream_t s) {
+    if (n < 1 || nv < 4 || nv % 4 || ((uintptr_t)x & 15) || ((uintptr_t)y & 15)) return cudaErrorInvalidValue;
+    const int q4 = nv / 4;
+    cudaError_t e;
+    switch (W) {   // the ELL arrays hold exactly W slots (padding: diagonal column, zero value)
+    case 8: e = launch_il<8>(col, val, n, (const float4 *)x, (float4 *)y, q4, s); break;
+    case 7: e = launch_il<7>(col, val, n, (const float4 *)x, (float4 *)y, q4, s); break;
+    case 6: e = launch_il<6>(col, val, n, (const float4 *)x, (float4 *)y, q4, s); break;
+    default: return cudaErrorInvalidValue;
+    }
+    g_kernel_launches++;
+    return e;
 }
 
 }  // namespace phg

@@ -41,6 +41,15 @@ cudaError_t bv_commit(double *u_n, const double *u_n1, const double *nr, const d
                       int V, int nv, cudaStream_t s);
 cudaError_t gather(double *y, int ldy, const double *x, int ldx, const int *map, int n, int nv, cudaStream_t s);
 
+// y_v = A x_v, v < nv, member-major, on a slot-major ELL pattern of at most 8 slots
+template <typename T>
+cudaError_t spmm(const int *col, const T *val, int n, int W, const T *x, int ldx, T *y, int ldy, int nv,
+                 cudaStream_t s);
+// Y = A X, X and Y interleaved (n x nv, member-minor), FP32, nv = 4 * 2^k <= 256,
+// 16-byte aligned
+cudaError_t spmm_il32(const int *col, const float *val, int n, int W, const float *x, float *y, int nv,
+                      cudaStream_t s);
+
 // Baroclin step helpers (examples/baroclin.cpp:445-606)
 struct BcCoef {
     double a;       // -0.5 (1-theta) sigma

@@ -81,6 +81,8 @@ SIGNATURES = {
     "phg_laplace_solve_batch": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp]),
     "phg_ops_check": (C.c_int, [_vp, _vp]),
     "phg_ops_set_sms": (C.c_int, [_vp, C.c_int]),
+    "phg_ops_mult": (C.c_int, [_vp, C.c_char_p, _vp, _vp, C.c_int, _vp]),
+    "phg_ops_mult32": (C.c_int, [_vp, C.c_char_p, _vp, _vp, C.c_int, _vp]),
     "phg_device_bytes": (C.c_int, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "phg_laplace_calc2_noalloc": (C.c_int, [_vp, _vp, _vp, _vp]),
     "phg_jacobian_calc1": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
@@ -227,6 +229,20 @@ class Operators:
         if getattr(self, "_h", None) and _lib is not None:
             _lib.phg_ops_destroy(self._h)
             self._h = None
+
+    def mult(self, name: str, x, out=None, stream=None):
+        """phelm::Solver::mult_vector: y = A x on inner vectors (rs or nv x rs)."""
+        x = _f8(x)
+        nv = 1 if x.ndim == 1 else x.shape[0]
+        out = np.zeros_like(x) if out is None else out
+        _check(lib().phg_ops_mult(self._h, name.encode(), _ptr(out), _ptr(x), nv, _stream(stream)))
+        return out
+
+    def mult32(self, name: str, x, out, stream=None):
+        """FP32 operator apply of the mixed path on interleaved multi-vectors
+        (CUDA float32 tensors rs x nv, nv = 4 * 2^k <= 256)."""
+        _check(lib().phg_ops_mult32(self._h, name.encode(), _ptr(out), _ptr(x), x.shape[1], _stream(stream)))
+        return out
 
     def set_solver(self, restart=30, tol=1e-12, max_iter=20000):
         _check(lib().phg_ops_set_solver(self._h, restart, tol, max_iter))

@@ -117,3 +117,36 @@ def test_mixed_precision_matches_fp64():
     assert rel(s32, s64) <= 1e-9
     J64, J32 = phelm.SphereJacobian(ops), phelm.SphereJacobian(mixed)
     assert rel(J32.calc2(u, v), J64.calc2(u, v)) <= 1e-12
+
+
+@pytest.mark.parametrize("level", [3, 5])
+@pytest.mark.parametrize("name", ["idt", "lapl", "jidt", "d1", "d2", "d1c", "d2c"])
+def test_operator_apply_bit_exact(level, name):
+    """phelm::Solver::mult_vector: the CSR product in ascending column order,
+    the same bits as the sequential CPU sum (oracle rounding, no FMA)."""
+    m, ops, *_ = setup(level)
+    ptr, col, val = m.csr(name)
+    n = len(ptr) - 1
+    rng = np.random.default_rng(level)
+    X = rng.standard_normal((3, n))
+    got = ops.mult(name, X)
+    W = int(np.diff(ptr).max())
+    ref = np.zeros_like(X)
+    for k in range(W):   # slot k of every row; rows shorter than k add nothing
+        has = np.diff(ptr) > k
+        idx = ptr[:-1][has] + k
+        ref[:, has] = ref[:, has] + val[idx] * X[:, col[idx]]
+    assert np.array_equal(got.view(np.uint64), ref.view(np.uint64))
+
+
+def test_operator_apply_fp32():
+    torch = pytest.importorskip("torch")
+    m, ops, *_ = setup(5, phelm.PHG_MIXED)
+    rng = np.random.default_rng(3)
+    X = rng.standard_normal((8, m.inner_size))
+    ref = ops.mult("lapl", X)
+    x = torch.tensor(X.T.copy(), dtype=torch.float32, device="cuda")   # interleaved: rs x nv
+    y = torch.empty_like(x)
+    ops.mult32("lapl", x, y)
+    torch.cuda.synchronize()
+    assert rel(y.cpu().numpy().T, ref) <= 1e-5
