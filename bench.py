@@ -211,6 +211,9 @@ def run_ours(args, ws, rank, local):
             row["mixed_over_fp64"] = row["mixed"]["member_steps_per_s"] / row["fp64"]["member_steps_per_s"]
             batched[f"L{lvl}x{B}"] = row
 
+    # two-layer baroclinic steps, level 6 (the reference's baroclin configuration)
+    baroclin = None if args.no_baroclin else run_baroclin(args.level, 20)
+
     # operator apply at a streaming size (level 8, 64 FP32 vectors; one FP64 vector)
     spmv = None if args.no_spmv else run_spmv(8, 64)
 
@@ -281,6 +284,7 @@ def run_ours(args, ws, rank, local):
         "batched": batched,
         "serve": served,
         "spmv": spmv,
+        "baroclin": baroclin,
         "solver": {"mixed": mixed["stats"], "fp64": fp64["stats"]},
         "roofline": {"kernel": "gmres_kernel (persistent solver)", "bound": "hbm", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -451,6 +455,66 @@ def run_spmv(level: int = 8, nv: int = 64, reps: int = 20):
             "peak_gbs": peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"}
 
 
+BC_CONF = dict(tau=1e-3, sigma=0.05, mu=6.77e-5, sigma1=0.05, mu1=6.77e-5, alpha=0.1 ** 0.5,
+               picard_iters=20, picard_tol=1e-8)
+
+
+def baroclin_initial(lat, lon, seed=SEED):
+    """Stream functions of two independent seeded vorticity fields (l <= 12, amplitude 0.05)."""
+    from mke_gb300 import fields
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(2):
+        c = fields.random_coeffs(rng, 1, 12, 0.05)
+        out.append(fields.sh_field(fields.sh_inverse_laplacian(c), lat, lon))
+    return out
+
+
+def run_baroclin(level: int = 6, steps: int = 20, warmup: int = 2):
+    """Two-layer baroclinic steps (alpha^2 = 0.1, sigma = 0.05, mu = 6.77e-5,
+    sigma1 = sigma, mu1 = mu, tau = 1e-3, Picard up to 20 iterations / 1e-8 as
+    in the reference, GMRES(40)), FP64 and mixed; device buffers, events per
+    step on the launching stream, L2 flushed between steps."""
+    import torch
+    from mke_gb300 import phelm
+    m = phelm.Mesh.sphere(level)
+    lat, lon = m.latlon()
+    u1h, u2h = baroclin_initial(lat, lon)
+    dev = torch.device("cuda")
+    st = torch.cuda.Stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    res = {}
+    for name, prec in (("mixed", phelm.PHG_MIXED), ("fp64", phelm.PHG_FP64)):
+        ops = phelm.Operators(m, prec, restart=40, tol=TOL)
+        bc = phelm.Baroclin(ops, coriolis=np.sin(lat), **BC_CONF)
+        u1 = torch.tensor(u1h, device=dev)
+        u2 = torch.tensor(u2h, device=dev)
+        with torch.cuda.stream(st):
+            for _ in range(warmup):
+                bc.calc(u1, u2, out1=u1, out2=u2, stream=st)
+        st.synchronize()
+        u1 = torch.tensor(u1h, device=dev)
+        u2 = torch.tensor(u2h, device=dev)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        with torch.cuda.stream(st):
+            for a, b in ev:
+                flush.zero_()
+                a.record(st)
+                bc.calc(u1, u2, out1=u1, out2=u2, stream=st)
+                b.record(st)
+        st.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+        res[name] = {"steps_per_s": 1000.0 / ms, "ms_per_step": ms, "state": (u1.cpu().numpy(), u2.cpu().numpy())}
+        del bc, ops
+    (a1, a2), (b1, b2) = res["mixed"].pop("state"), res["fp64"].pop("state")
+    diff = max(float(np.linalg.norm(a1 - b1) / np.linalg.norm(b1)), float(np.linalg.norm(a2 - b2) / np.linalg.norm(b2)))
+    return {"level": level, "steps": steps, "unknowns": 4 * m.inner_size, "mixed": res["mixed"], "fp64": res["fp64"],
+            "mixed_over_fp64": res["mixed"]["steps_per_s"] / res["fp64"]["steps_per_s"],
+            f"state_rel_diff_mixed_vs_fp64_after_{steps}": diff,
+            "config": "alpha^2=0.1, sigma=sigma1=0.05, mu=mu1=6.77e-5, tau=1e-3, Picard <= 20 / 1e-8, GMRES(40), "
+                      "u1, u2 from seeded vorticity l <= 12 amplitude 0.05"}
+
+
 def run_case(args):
     """Small fixed workloads for profilers: `solve` = Laplace solves,
     `step` = barvortex steps, at --level with --steps repetitions."""
@@ -459,6 +523,9 @@ def run_case(args):
         return
     if args.case == "spmv":
         print(json.dumps(run_spmv(args.level, args.members)))
+        return
+    if args.case == "baroclin":
+        print(json.dumps(run_baroclin(args.level, args.steps)))
         return
     import torch
     from mke_gb300 import phelm
@@ -522,12 +589,13 @@ def main():
     ap.add_argument("--tol", type=float, default=TOL)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurements")
-    ap.add_argument("--case", choices=["solve", "step", "batch", "serve", "spmv"],
+    ap.add_argument("--case", choices=["solve", "step", "batch", "serve", "spmv", "baroclin"],
                     help="one workload only (no bench line): profiling cases, or the serving trace")
     ap.add_argument("--serve-requests", type=int, default=10000, help="requests of --case serve")
     ap.add_argument("--bench-serve-requests", type=int, default=2000, help="requests of the bench line's serve block")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving trace")
     ap.add_argument("--no-spmv", action="store_true", help="skip the streaming operator-apply measurement")
+    ap.add_argument("--no-baroclin", action="store_true", help="skip the two-layer baroclinic steps")
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--members", type=int, default=16, help="ensemble members for --case batch")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])

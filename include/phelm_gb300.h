@@ -214,7 +214,9 @@ typedef struct {
 int phg_baroclin_create(phg_ops o, const phg_bc_conf *conf, const double *coriolis, phg_baroclin *out);
 void phg_baroclin_destroy(phg_baroclin b);
 /* Baroclin::calc(u11, u21, u1, u2, bnd, t) (examples/baroclin.cpp:445-606);
- * f, g: forcing fields at time t (V each, NULL = none). */
+ * f, g: forcing fields at time t (V each, NULL = none).  The call reads the
+ * Picard stop flag after each iteration (one stream synchronisation per
+ * iteration), so it returns after the last iteration's work is done. */
 int phg_baroclin_calc(phg_baroclin b, double *u11, double *u21, const double *u1, const double *u2,
                       const double *bnd, const double *f, const double *g, void *stream);
 

@@ -1125,6 +1125,8 @@ struct phg_baroclin_s {
     DBuf U, w, dw, FC, un, wn, un1, ju, jv, jsol, jac, FG, MFG, rp, x, xi, nr, done;
     GmresStats each[64];
     int nslots = 0;
+    int *hdone = nullptr;   // pinned copy of the Picard stop flag
+    ~phg_baroclin_s() { if (hdone) cudaFreeHost(hdone); }
 };
 
 extern "C" int phg_baroclin_create(phg_ops o, const phg_bc_conf *c, const double *coriolis, phg_baroclin *out) {
@@ -1211,6 +1213,7 @@ extern "C" int phg_baroclin_create(phg_ops o, const phg_bc_conf *c, const double
     CK(b->FG.ensure(8 * 2 * (size_t)rs)); CK(b->MFG.ensure(8 * 2 * (size_t)rs)); CK(b->xi.ensure(8 * 2 * (size_t)rs));
     CK(b->rp.ensure(8 * (size_t)n)); CK(b->x.ensure(8 * (size_t)n));
     CK(b->nr.ensure(16)); CK(b->done.ensure(4));
+    CK(cudaHostAlloc(&b->hdone, sizeof(int), cudaHostAllocDefault));
     o->refs++;
     *out = b.release();
     return PHG_OK;
@@ -1281,6 +1284,13 @@ int bc_step_dev(phg_baroclin_s *b, double *u11, double *u21, const double *u1, c
         // nr = max(dist(u1_n1, u1_n), dist(u2_n1, u2_n)); commit unless stopped
         if ((r = norm_dev(o, un1, un, 2, b->nr.as<double>(), true, true, s))) return r;
         CK(bc_commit(un, un1, b->nr.as<double>(), b->done.as<int>(), c.picard_tol, 2 * V, s));
+        // the reference leaves the loop once max(nr) < tol (examples/baroclin.cpp:600): read the
+        // flag so that converged steps do not run the remaining iterations
+        if (it + 1 < c.picard_iters) {
+            CK(cudaMemcpyAsync(b->hdone, b->done.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            if (*b->hdone) break;
+        }
     }
     CK(cudaMemcpyAsync(u11, un, 8 * (size_t)V, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(u21, un + V, 8 * (size_t)V, cudaMemcpyDeviceToDevice, s));

@@ -158,3 +158,29 @@ def test_handles_destroyed_in_any_order():
     a2, b2 = bc.calc(u1, u2)
     assert np.array_equal(a, a2) and np.array_equal(b, b2)
     del bc
+
+
+def test_level6_mixed_tracks_fp64_over_100_steps():
+    """The reference's baroclin configuration on level 6 (Picard up to 20
+    iterations / 1e-8, GMRES(40)): after 100 steps the mixed-precision state
+    stays within 1e-8 relative L2 of the FP64 state."""
+    torch = pytest.importorskip("torch")
+    m = phelm.Mesh.sphere(6)
+    lat, lon = m.latlon()
+    rng = np.random.default_rng(2024)
+    u = [fields.sh_field(fields.sh_inverse_laplacian(fields.random_coeffs(rng, 1, 12, 0.05)), lat, lon)
+         for _ in range(2)]
+    out = {}
+    s = torch.cuda.Stream()
+    for prec in (phelm.PHG_FP64, phelm.PHG_MIXED):
+        ops = phelm.Operators(m, prec, restart=40, tol=1e-12)
+        bc = phelm.Baroclin(ops, picard_iters=20, picard_tol=1e-8, coriolis=np.sin(lat))
+        a = torch.tensor(u[0], device="cuda")
+        b = torch.tensor(u[1], device="cuda")
+        for _ in range(100):
+            bc.calc(a, b, out1=a, out2=b, stream=s)
+        s.synchronize()
+        out[prec] = (a.cpu().numpy(), b.cpu().numpy())
+        assert np.all(np.isfinite(out[prec][0])) and np.all(np.isfinite(out[prec][1]))
+    (f1, f2), (m1, m2) = out[phelm.PHG_FP64], out[phelm.PHG_MIXED]
+    assert rel(m1, f1) <= 1e-8 and rel(m2, f2) <= 1e-8
