@@ -47,6 +47,7 @@ constexpr int NWARP = BLOCK / 32;
 constexpr double INNER_RTOL = 1e-5;  // FP32 cycle: reduce the residual 1e5x, then refine
 constexpr long long SPIN_LIMIT = 2000000000LL;  // clock64 cycles (~1 s)
 constexpr int CHEB_KMAX = 64;    // most Chebyshev steps per refinement cycle
+constexpr int LS_MIN_RHS = 32;   // right-hand sides from which the lockstep path runs
 
 struct Params {
     DevSolveOp op;
@@ -950,6 +951,250 @@ Layout layout(const DevSolveOp &op, int nv, int m, Precision prec) {
     return L;
 }
 
+// ------------------------------------------------- lockstep Chebyshev ---
+// Many right-hand sides of one mass-like operator (the Jacobian's 8 x members
+// solves of an ensemble step) in lockstep: the FP32 Chebyshev vectors are
+// kept interleaved (row i holds the nvp members contiguously), so every step
+// is one pass of an SpMM that reads each matrix row once for all members and
+// gathers whole 16-byte member chunks, fused with the recurrence update.
+// The FP64 residual, the norms and the stopping test run between cycles in
+// separate launches; a device flag ends the remaining launches once every
+// member has converged (no host synchronisation).
+constexpr int LS_MAXC = 6;     // refinement cycles at most
+constexpr int LS_MG = 16;      // members per thread in the FP64 residual
+
+template <int W>
+__global__ void __launch_bounds__(256) k_ls_resid(const int *__restrict__ col, const double *__restrict__ val, int n,
+                                                  const double *__restrict__ B, const double *__restrict__ X, int ld,
+                                                  double *__restrict__ R, int nv, const int *done) {
+    if (*(volatile const int *)done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int c[W];
+    double a[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) { c[k] = __ldg(&col[(size_t)k * n + i]); a[k] = __ldg(&val[(size_t)k * n + i]); }
+    const int v0 = blockIdx.y * LS_MG, v1 = min(nv, v0 + LS_MG);
+    for (int v = v0; v < v1; ++v) {
+        const double *x = X + (size_t)v * ld;
+        double sum = 0.0;
+#pragma unroll
+        for (int k = 0; k < W; ++k) sum += a[k] * x[c[k]];
+        R[(size_t)v * n + i] = B[(size_t)v * ld + i] - sum;
+    }
+}
+
+// out[v] = sum_i A[v * ld + i]^2 (one block per member, fixed order)
+__global__ void __launch_bounds__(256) k_ls_norm2(const double *__restrict__ A, int n, int ld, double *out,
+                                                  const int *done) {
+    if (done && *(volatile const int *)done) return;
+    __shared__ double red[NWARP];
+    const double *a = A + (size_t)blockIdx.x * ld;
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += a[i] * a[i];
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < NWARP; ++w) t += red[w];
+        out[blockIdx.x] = t;
+    }
+}
+
+// per-member scales 1/||r|| (0 once converged), the stopping test and the stats
+__global__ void __launch_bounds__(256) k_ls_scale(const double *nrm, const double *bn2, int nv, int nvp, double tol,
+                                                  double *beta, double *sc, int *done, GmresStats *st, int cycle,
+                                                  int K, double bytes) {
+    if (*(volatile int *)done) return;
+    __shared__ double rmax[NWARP];
+    __shared__ int open[NWARP];
+    double mx = 0.0;
+    int op = 0;
+    for (int v = threadIdx.x; v < nvp; v += blockDim.x) {
+        if (v >= nv) { sc[v] = 0.0; beta[v] = 0.0; continue; }
+        const double bt = sqrt(nrm[v]), bn = sqrt(bn2[v]);
+        const double rel = bn > 0.0 ? bt / bn : 0.0;
+        const bool conv = rel <= tol || bt == 0.0;
+        beta[v] = bt;
+        sc[v] = conv ? 0.0 : 1.0 / bt;
+        mx = fmax(mx, rel);
+        if (!(rel == rel)) mx = rel;   // NaN propagates into the stats
+        op += conv ? 0 : 1;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        op += __shfl_xor_sync(0xffffffffu, op, o);
+    }
+    if ((threadIdx.x & 31) == 0) { rmax[threadIdx.x >> 5] = mx; open[threadIdx.x >> 5] = op; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0.0;
+        int o = 0;
+        for (int w = 0; w < NWARP; ++w) { m = fmax(m, rmax[w]); o += open[w]; }
+        st->relres = m;
+        st->cycles = cycle;
+        st->iters = cycle * K;
+        st->steps_total = cycle * K;
+        st->status = o ? 1 : 0;
+        st->bytes += bytes;
+        *done = o ? 0 : 1;
+    }
+}
+
+// rv = (float)(r * scale), d = e0 = c0 D^-1 rv: member-major FP64 -> interleaved FP32 (tiled transpose)
+__global__ void __launch_bounds__(256) k_ls_init(const double *__restrict__ R, int n, int nv, int nvp,
+                                                 const double *__restrict__ sc, const float *__restrict__ dinv, float c0,
+                                                 float *rv, float *d, float *e0, const int *done) {
+    if (*(volatile const int *)done) return;
+    __shared__ float t[32][33];
+    const int i0 = blockIdx.x * 32, v0 = blockIdx.y * 32, tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int j = ty; j < 32; j += 8) {
+        const int v = v0 + j, i = i0 + tx;
+        t[j][tx] = (v < nv && i < n) ? (float)(R[(size_t)v * n + i] * sc[v]) : 0.f;
+    }
+    __syncthreads();
+    for (int j = ty; j < 32; j += 8) {
+        const int i = i0 + j, v = v0 + tx;
+        if (i >= n) continue;
+        const float r = t[tx][j];
+        const float dd = c0 * dinv[i] * r;
+        const size_t q = (size_t)i * nvp + v;
+        rv[q] = r;
+        d[q] = dd;
+        e0[q] = dd;
+    }
+}
+
+// one step for every member: s = A e_c, d = ca d + cb D^-1 (rv - s), e_n = e_c + d
+template <int W>
+__global__ void __launch_bounds__(256) k_ls_step(const int *__restrict__ col, const float *__restrict__ a32,
+                                                 const float *__restrict__ dinv, int n, int q4,
+                                                 const float4 *__restrict__ ec, const float4 *__restrict__ rv,
+                                                 float4 *__restrict__ d, float4 *__restrict__ en, float ca, float cb,
+                                                 const int *done) {
+    if (*(volatile const int *)done) return;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = (int)(t / (unsigned)q4), q = (int)(t - (unsigned)i * (unsigned)q4);
+    if (i >= n) return;
+    int c[W];
+    float a[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) { c[k] = __ldg(&col[(size_t)k * n + i]); a[k] = __ldg(&a32[(size_t)k * n + i]); }
+    float4 g[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) g[k] = ec[(size_t)c[k] * q4 + q];
+    float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+        sum.x = fmaf(a[k], g[k].x, sum.x); sum.y = fmaf(a[k], g[k].y, sum.y);
+        sum.z = fmaf(a[k], g[k].z, sum.z); sum.w = fmaf(a[k], g[k].w, sum.w);
+    }
+    const size_t idx = (size_t)i * q4 + q;
+    const float di = cb * __ldg(&dinv[i]);
+    const float4 r = rv[idx], dd = d[idx], e = ec[idx];
+    float4 dn;
+    dn.x = ca * dd.x + di * (r.x - sum.x); dn.y = ca * dd.y + di * (r.y - sum.y);
+    dn.z = ca * dd.z + di * (r.z - sum.z); dn.w = ca * dd.w + di * (r.w - sum.w);
+    d[idx] = dn;
+    en[idx] = make_float4(e.x + dn.x, e.y + dn.y, e.z + dn.z, e.w + dn.w);
+}
+
+// x += beta * e: interleaved FP32 -> member-major FP64 (tiled transpose)
+__global__ void __launch_bounds__(256) k_ls_update(double *X, int ld, int n, int nv, int nvp,
+                                                   const double *__restrict__ beta, const float *__restrict__ e,
+                                                   const int *done) {
+    if (*(volatile const int *)done) return;
+    __shared__ float t[32][33];
+    const int i0 = blockIdx.x * 32, v0 = blockIdx.y * 32, tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int j = ty; j < 32; j += 8) {
+        const int i = i0 + j, v = v0 + tx;
+        t[j][tx] = i < n ? e[(size_t)i * nvp + v] : 0.f;
+    }
+    __syncthreads();
+    for (int j = ty; j < 32; j += 8) {
+        const int v = v0 + j, i = i0 + tx;
+        if (v < nv && i < n) X[(size_t)v * ld + i] += beta[v] * (double)t[tx][j];
+    }
+}
+
+template <int W>
+cudaError_t ls_steps(const DevSolveOp &op, int n, int q4, float *&ec, float *&en, const float *rv, float *d,
+                     const double *ca, const double *cb, int K, const int *done, cudaStream_t s) {
+    const long long work = (long long)n * q4;
+    const unsigned blocks = (unsigned)((work + 255) / 256);
+    for (int k = 1; k < K; ++k) {
+        k_ls_step<W><<<blocks, 256, 0, s>>>(op.A.col, op.a32, op.dinv32, n, q4, (const float4 *)ec,
+                                            (const float4 *)rv, (float4 *)d, (float4 *)en, (float)ca[k],
+                                            (float)cb[k], done);
+        float *t = ec; ec = en; en = t;
+    }
+    return cudaGetLastError();
+}
+
+// returns cudaErrorNotSupported when this path does not apply (the caller
+// then runs the per-member kernels)
+cudaError_t cheb_lockstep(const DevSolveOp &op, const double *B, double *X, int nv, int ld, double tol,
+                          double inner_rtol, char *w, const Layout &L, GmresStats *st, cudaStream_t s) {
+    const int n = op.A.n, W = op.A.W;
+    if (W < 6 || W > 8 || !op.a32 || !op.dinv32) return cudaErrorNotSupported;
+    const int nvp = (nv + 31) / 32 * 32, q4 = nvp / 4;
+    if ((long long)n * q4 >= (1LL << 31)) return cudaErrorNotSupported;
+    const size_t vec = ((size_t)n * nvp * 4 + 255) & ~size_t(255);
+    if (4 * vec > L.r - L.v) return cudaErrorNotSupported;
+    if ((size_t)(4 * nvp + 64) * 8 > L.bar - L.part) return cudaErrorNotSupported;
+    float *rv = (float *)(w + L.v), *d = (float *)(w + L.v + vec), *e0 = (float *)(w + L.v + 2 * vec),
+          *e1 = (float *)(w + L.v + 3 * vec);
+    double *R = (double *)(w + L.r);
+    double *bn2 = (double *)(w + L.part), *nrm = bn2 + nvp, *beta = nrm + nvp, *sc = beta + nvp;
+    int *done = (int *)(sc + nvp);
+    // coefficients (as the per-member Chebyshev kernel)
+    const double lo = op.cheb_lmin, hi = op.cheb_lmax;
+    const double kappa = hi / lo, sq = sqrt(kappa), sigma = (sq - 1.0) / (sq + 1.0);
+    int K = (int)ceil(log(2.0 * kappa / inner_rtol) / log(1.0 / sigma)) + 1;
+    K = K < 2 ? 2 : (K > CHEB_KMAX ? CHEB_KMAX : K);
+    const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), s1 = theta / delta;
+    double ca[CHEB_KMAX], cb[CHEB_KMAX], rho_prev = 1.0 / s1;
+    ca[0] = cb[0] = 0.0;
+    for (int k = 1; k < K; ++k) {
+        const double rho = 1.0 / (2.0 * s1 - rho_prev);
+        ca[k] = rho * rho_prev;
+        cb[k] = 2.0 * rho / delta;
+        rho_prev = rho;
+    }
+    // algorithmic bytes of one cycle: FP64 residual, init, K - 1 steps, update
+    const double rowsb = (double)n;
+    const double cyc = rowsb * nv * (8.0 * 3 + 8.0) + rowsb * W * 12.0 +
+                       rowsb * nvp * (8.0 + 12.0) + (K - 1) * (rowsb * W * 8.0 + rowsb * nvp * 4.0 * 6.0) +
+                       rowsb * nvp * 4.0 + rowsb * nv * 16.0;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(done, 0, sizeof(int), s)) != cudaSuccess) return e;
+    k_ls_norm2<<<nv, 256, 0, s>>>(B, n, ld, bn2, nullptr);
+    const dim3 rgrid((unsigned)((n + 255) / 256), (unsigned)((nv + LS_MG - 1) / LS_MG));
+    const dim3 tgrid((unsigned)((n + 31) / 32), (unsigned)(nvp / 32));
+    for (int c = 0; c <= LS_MAXC; ++c) {
+        switch (W) {
+        case 6: k_ls_resid<6><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, R, nv, done); break;
+        case 7: k_ls_resid<7><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, R, nv, done); break;
+        default: k_ls_resid<8><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, R, nv, done); break;
+        }
+        k_ls_norm2<<<nv, 256, 0, s>>>(R, n, n, nrm, done);
+        k_ls_scale<<<1, 256, 0, s>>>(nrm, bn2, nv, nvp, tol, beta, sc, done, st, c, K, c ? cyc : 0.0);
+        if (c == LS_MAXC) break;
+        k_ls_init<<<tgrid, 256, 0, s>>>(R, n, nv, nvp, sc, op.dinv32, (float)(1.0 / theta), rv, d, e0, done);
+        float *ec = e0, *en = e1;
+        switch (W) {
+        case 6: e = ls_steps<6>(op, n, q4, ec, en, rv, d, ca, cb, K, done, s); break;
+        case 7: e = ls_steps<7>(op, n, q4, ec, en, rv, d, ca, cb, K, done, s); break;
+        default: e = ls_steps<8>(op, n, q4, ec, en, rv, d, ca, cb, K, done, s); break;
+        }
+        if (e != cudaSuccess) return e;
+        k_ls_update<<<tgrid, 256, 0, s>>>(X, ld, n, nv, nvp, beta, ec, done);
+    }
+    g_kernel_launches += 1 + (LS_MAXC + 1) * 3 + LS_MAXC * (K + 1);
+    return cudaGetLastError();
+}
+
 int g_sms = 0;
 
 int sm_count() {
@@ -999,6 +1244,15 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     const size_t es = prec == PREC_MIXED ? 4 : 8;
     const bool cheb = op.cheb_lmax > 0.0 && op.cheb_lmin > 0.0 && op.cheb_lmin < op.cheb_lmax && m >= 3 &&
                       !op.mgd && !op.block4 && op.A.W <= 8;
+    // ensembles in the mixed path: all right-hand sides in lockstep
+    if (cheb && prec == PREC_MIXED && nv >= LS_MIN_RHS && !no_alloc && env_int("PHG_CHEB_LOCKSTEP", 1)) {
+        const char *ev = getenv("PHG_INNER_RTOL");
+        cudaError_t e0 = cudaMemsetAsync(stats_dev, 0, sizeof(GmresStats), s);
+        if (e0 != cudaSuccess) return e0;
+        e0 = cheb_lockstep(op, B, X, nv, ld, tol, ev ? atof(ev) : INNER_RTOL, (char *)work,
+                           layout(op, nv, m, prec), stats_dev, s);
+        if (e0 != cudaErrorNotSupported) return e0;
+    }
     const size_t smem = cheb ? sizeof(double) * (4 + 2 * CHEB_KMAX)
                              : smem_gmres_bytes() + (op.mgd ? es * op.mg.red_elems : 0) + 16;
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
