@@ -157,12 +157,15 @@ int orc_bv_init(orc_barvortex *bv, orc_ops *o, const orc_bv_conf *c, const doubl
 	bv->lh = VEC(V);
 	if (coriolis) memcpy(bv->lh, coriolis, sizeof(double) * (size_t)V);
 	orc_gen_bv(&bv->A, &bv->bndA, o->m, 1.0 / c->tau + c->sigma * c->theta, -c->theta * c->mu);
+	/* backward matrix Ab_ / bndb_ (examples/barvortex_impl.h:84-105, 150-151) */
+	orc_gen_bv(&bv->Ab, &bv->bndAb, o->m, 1.0 / c->tau - c->sigma * (1.0 - c->theta), (1.0 - c->theta) * c->mu);
 	return 0;
 }
 
 void orc_bv_free(orc_barvortex *bv)
 {
-	orc_csr_free(&bv->A); orc_csr_free(&bv->bndA); free(bv->lh);
+	orc_csr_free(&bv->A); orc_csr_free(&bv->bndA);
+	orc_csr_free(&bv->Ab); orc_csr_free(&bv->bndAb); free(bv->lh);
 	memset(bv, 0, sizeof(*bv));
 }
 
@@ -209,6 +212,137 @@ void orc_bv_step(orc_barvortex *bv, double *u1, const double *u,
 	memcpy(u1, u_n, sizeof(double) * (size_t)sz);
 	free(w); free(dw); free(FC); free(u_n); free(w_n); free(u_n1);
 	free(tmp1); free(tmp2); free(jac); free(F); free(rp); free(x);
+}
+
+/* ------------------------------------------- linearised / adjoint steps --- */
+/* J^T(u, v) on the full vector: -J(u, v) with boundary values bnd
+ * (src/sjacobian.cpp:404-408, 463-468) */
+static void jac_calc1t(orc_ops *o, double *ans, const double *u, const double *v, const double *bnd)
+{
+	orc_jacobian_calc1(o, ans, u, v, NULL);
+	double *p = VEC(o->m->rs);
+	orc_u2p(o->m, p, ans);
+	for (int i = 0; i < o->m->rs; ++i) p[i] = -1.0 * p[i];
+	orc_p2u(o->m, ans, p, bnd);
+	free(p);
+}
+
+/* rp = idt u2p(u) (+ B bnd_w); x = M^-1 rp; ans = p2u(x, bnd_w)
+ * (phelm::solve, src/mesh.h:720-746, with the right-hand side of
+ * examples/barvortex_impl.h:379-390) */
+static void bv_solve(orc_barvortex *bv, double *ans, const double *u, const orc_csr *M, const orc_csr *B,
+                     const double *bnd_w)
+{
+	orc_ops *o = bv->o;
+	const orc_mesh *m = o->m;
+	int rs = m->rs;
+	double *tmp = VEC(rs), *rp = VEC(rs), *x = VEC(rs);
+	orc_u2p(m, tmp, u);
+	orc_csr_mult(&o->idt, rp, tmp);
+	if (bnd_w) {
+		orc_csr_mult(B, tmp, bnd_w);
+		for (int i = 0; i < rs; ++i) rp[i] = rp[i] + tmp[i];
+	}
+	orc_csr_solve((orc_csr *)M, x, rp);
+	orc_p2u(m, ans, x, bnd_w);
+	free(tmp); free(rp); free(x);
+}
+
+/* the shared first part of calc_L / calc_L_1 (examples/barvortex_impl.h:343-362) */
+static void bv_lin_parts(orc_barvortex *bv, const double *u, const double *z, const double *bnd_w,
+                         double *pt1, double *pt3)
+{
+	orc_ops *o = bv->o;
+	int sz = o->m->V;
+	double k1 = bv->c.k1, k2 = bv->c.k2;
+	double *z_lapl = VEC(sz), *jac1 = VEC(sz), *jac2 = VEC(sz), *jac3 = VEC(sz);
+	orc_laplace_calc1(o, z_lapl, z, bnd_w);
+	orc_laplace_calc1(o, pt1, u, bnd_w);
+	orc_jacobian_calc1(o, jac1, u, bv->lh, NULL);
+	orc_jacobian_calc1(o, jac2, z, pt1, NULL);
+	orc_jacobian_calc1(o, jac3, u, z_lapl, NULL);
+	for (int i = 0; i < sz; ++i) pt3[i] = 0.0;
+	for (int i = 0; i < sz; ++i) pt3[i] = pt3[i] + k2 * jac1[i];
+	for (int i = 0; i < sz; ++i) pt3[i] = pt3[i] + k1 * jac2[i];
+	for (int i = 0; i < sz; ++i) pt3[i] = pt3[i] + k1 * jac3[i];
+	free(z_lapl); free(jac1); free(jac2); free(jac3);
+}
+
+/* BarVortex::calc_L (examples/barvortex_impl.h:326-400) */
+void orc_bv_calc_L(orc_barvortex *bv, double *u1, const double *u, const double *z,
+                   const double *bnd_u, const double *bnd_w)
+{
+	orc_ops *o = bv->o;
+	int sz = o->m->V;
+	double theta = bv->c.theta, mu = bv->c.mu, sigma = bv->c.sigma, tau = bv->c.tau;
+	double *pt1 = VEC(sz), *pt2 = VEC(sz), *pt3 = VEC(sz);
+	bv_lin_parts(bv, u, z, bnd_w, pt1, pt3);
+	for (int i = 0; i < sz; ++i) pt3[i] = -1.0 * pt3[i];
+	orc_laplace_calc1(o, pt2, pt1, NULL);
+	for (int i = 0; i < sz; ++i) pt2[i] = (1. - theta) * mu * pt2[i];
+	for (int i = 0; i < sz; ++i) pt1[i] = (1.0 / tau - (1. - theta) * sigma) * pt1[i];
+	for (int i = 0; i < sz; ++i) u1[i] = 0.0;
+	for (int i = 0; i < sz; ++i) u1[i] = u1[i] + pt1[i];
+	for (int i = 0; i < sz; ++i) u1[i] = u1[i] + pt2[i];
+	for (int i = 0; i < sz; ++i) u1[i] = u1[i] + pt3[i];
+	bv_solve(bv, u1, u1, &bv->A, &bv->bndA, bnd_w);
+	orc_laplace_solve(o, u1, u1, bnd_u);
+	free(pt1); free(pt2); free(pt3);
+}
+
+/* BarVortex::calc_L_1 (examples/barvortex_impl.h:402-467); adds into u1 as
+ * the reference does (it does not clear u1 first) */
+void orc_bv_calc_L1(orc_barvortex *bv, double *u1, const double *u, const double *z,
+                    const double *bnd_u, const double *bnd_w)
+{
+	orc_ops *o = bv->o;
+	int sz = o->m->V;
+	double theta = bv->c.theta, mu = bv->c.mu, sigma = bv->c.sigma, tau = bv->c.tau;
+	double *pt1 = VEC(sz), *pt2 = VEC(sz), *pt3 = VEC(sz);
+	bv_lin_parts(bv, u, z, bnd_w, pt1, pt3);
+	orc_laplace_calc1(o, pt2, pt1, NULL);
+	for (int i = 0; i < sz; ++i) pt2[i] = -theta * mu * pt2[i];
+	for (int i = 0; i < sz; ++i) pt1[i] = (1.0 / tau + theta * sigma) * pt1[i];
+	for (int i = 0; i < sz; ++i) u1[i] = u1[i] + pt1[i];
+	for (int i = 0; i < sz; ++i) u1[i] = u1[i] + pt2[i];
+	for (int i = 0; i < sz; ++i) u1[i] = u1[i] + pt3[i];
+	bv_solve(bv, u1, u1, &bv->Ab, &bv->bndAb, bnd_w);
+	orc_laplace_solve(o, u1, u1, bnd_u);
+	free(pt1); free(pt2); free(pt3);
+}
+
+/* BarVortex::calc_LT (examples/barvortex_impl.h:469-536) */
+void orc_bv_calc_LT(orc_barvortex *bv, double *v1, const double *v, const double *z,
+                    const double *bnd_u, const double *bnd_w)
+{
+	orc_ops *o = bv->o;
+	const orc_mesh *m = o->m;
+	int sz = m->V;
+	double k1 = bv->c.k1, k2 = bv->c.k2;
+	double theta = bv->c.theta, mu = bv->c.mu, sigma = bv->c.sigma, tau = bv->c.tau;
+	double *lz = VEC(sz), *pt1 = VEC(sz), *pt2 = VEC(sz), *h1 = VEC(sz), *p_lapl = VEC(sz), *tmp = VEC(sz);
+	orc_laplace_calc1(o, lz, z, bnd_w);
+	orc_laplace_solve(o, v1, v, bnd_u);
+	bv_solve(bv, v1, v1, &bv->A, &bv->bndA, bnd_w);
+	orc_laplace_calc1(o, pt1, v1, bnd_w);
+	for (int i = 0; i < sz; ++i) pt1[i] = (1.0 / tau - (1.0 - theta) * sigma) * pt1[i];
+	orc_laplace_calc1(o, pt2, v1, bnd_w);
+	orc_laplace_calc1(o, pt2, pt2, NULL);
+	for (int i = 0; i < sz; ++i) pt2[i] = (1.0 - theta) * mu * pt2[i];
+	jac_calc1t(o, tmp, v1, bv->lh, NULL);
+	jac_calc1t(o, p_lapl, z, v1, NULL);
+	orc_laplace_calc1(o, p_lapl, p_lapl, NULL);
+	jac_calc1t(o, h1, v1, lz, NULL);
+	for (int i = 0; i < sz; ++i) h1[i] = k1 * h1[i] + k1 * p_lapl[i];
+	for (int i = 0; i < sz; ++i) h1[i] = h1[i] + k2 * tmp[i];
+	for (int i = 0; i < sz; ++i) h1[i] = -1.0 * h1[i];
+	for (int i = 0; i < sz; ++i) v1[i] = 0.0;
+	for (int i = 0; i < sz; ++i) v1[i] = v1[i] + pt1[i];
+	for (int i = 0; i < sz; ++i) v1[i] = v1[i] + pt2[i];
+	for (int i = 0; i < sz; ++i) v1[i] = v1[i] + h1[i];
+	for (int p = 0; p < sz; ++p)   /* set_bnd (src/proj.cpp:110-133) */
+		if (m->bnd[p]) v1[p] = bnd_u ? bnd_u[m->p2io[p]] : 0.0;
+	free(lz); free(pt1); free(pt2); free(h1); free(p_lapl); free(tmp);
 }
 
 /* ------------------------------------------------------------- baroclin --- */

@@ -129,6 +129,7 @@ typedef struct {
 	orc_ops *o;
 	orc_bv_conf c;
 	orc_csr A, bndA;     /* forward CN matrix and its boundary columns */
+	orc_csr Ab, bndAb;   /* backward matrix Ab_ and bndb_ (linearised inverse step) */
 	double *lh;          /* l + h at every point */
 	int last_iters;
 } orc_barvortex;
@@ -141,6 +142,14 @@ void orc_bv_free(orc_barvortex *bv);
  * rp[V] is the forcing f already evaluated at time t (NULL = none). */
 void orc_bv_step(orc_barvortex *bv, double *u1, const double *u,
                  const double *bnd_u, const double *bnd_w, const double *rp);
+/* Linearised step around the background z, its inverse and its adjoint
+ * (BarVortex::calc_L / calc_L_1 / calc_LT).  calc_L1 adds into u1. */
+void orc_bv_calc_L(orc_barvortex *bv, double *u1, const double *u, const double *z,
+                   const double *bnd_u, const double *bnd_w);
+void orc_bv_calc_L1(orc_barvortex *bv, double *u1, const double *u, const double *z,
+                    const double *bnd_u, const double *bnd_w);
+void orc_bv_calc_LT(orc_barvortex *bv, double *v1, const double *v, const double *z,
+                    const double *bnd_u, const double *bnd_w);
 
 typedef struct {
 	double tau, sigma, mu, sigma1, mu1, alpha, theta;

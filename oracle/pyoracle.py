@@ -50,7 +50,7 @@ class BvConf(C.Structure):
 
 
 class BarVortex(C.Structure):
-    _fields_ = [("o", C.POINTER(Ops)), ("c", BvConf), ("A", Csr), ("bndA", Csr),
+    _fields_ = [("o", C.POINTER(Ops)), ("c", BvConf), ("A", Csr), ("bndA", Csr), ("Ab", Csr), ("bndAb", Csr),
                 ("lh", _dp), ("last_iters", C.c_int)]
 
 
@@ -94,6 +94,8 @@ def lib():
             getattr(L, f).restype = C.c_double
         L.orc_bv_init.argtypes = [C.POINTER(BarVortex), C.POINTER(Ops), C.POINTER(BvConf), _dp]
         L.orc_bv_step.argtypes = [C.POINTER(BarVortex), _dp, _dp, _dp, _dp, _dp]
+        for f in ("orc_bv_calc_L", "orc_bv_calc_L1", "orc_bv_calc_LT"):
+            getattr(L, f).argtypes = [C.POINTER(BarVortex), _dp, _dp, _dp, _dp, _dp]
         L.orc_bc_init.argtypes = [C.POINTER(Baroclin), C.POINTER(Ops), C.POINTER(BcConf), _dp]
         L.orc_bc_step.argtypes = [C.POINTER(Baroclin), _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         L.orc_set_solver.argtypes = [C.c_double, C.c_int, C.c_int]
@@ -201,6 +203,14 @@ class Oracle:
                           _p(None if bnd_u is None else _f8(bnd_u)),
                           _p(None if bnd_w is None else _f8(bnd_w)),
                           _p(None if rp is None else _f8(rp)))
+        return out
+
+    def bv_linear(self, bv, which, u, z, bnd_u=None, bnd_w=None, u1=None):
+        """BarVortex::calc_L ("L"), calc_L_1 ("L1", adds into u1) or calc_LT ("LT")."""
+        out = np.zeros(self.V) if u1 is None else np.array(u1, dtype=np.float64)
+        fn = {"L": "orc_bv_calc_L", "L1": "orc_bv_calc_L1", "LT": "orc_bv_calc_LT"}[which]
+        getattr(lib(), fn)(C.byref(bv), _p(out), _p(_f8(u)), _p(_f8(z)),
+                           _p(None if bnd_u is None else _f8(bnd_u)), _p(None if bnd_w is None else _f8(bnd_w)))
         return out
 
     def baroclin(self, tau=1e-3, sigma=0.05, mu=6.77e-5, sigma1=0.05, mu1=6.77e-5,

@@ -8,7 +8,7 @@
  *
  * Usage: ref_driver MESH.txt OUTDIR [key=value ...]
  *   reads optional inputs OUTDIR/in_u.npy, in_v.npy, in_bnd.npy (f8)
- *   keys: bv_steps, bv_iters, bc_steps, bc_iters, coriolis (0 zero, 1 sin(phi))
+ *   keys: bv_steps, bv_iters, bv_lin, bc_steps, bc_iters, coriolis (0 zero, 1 sin(phi))
  */
 #include <cstdio>
 #include <cstdlib>
@@ -222,6 +222,15 @@ int main(int argc, char **argv)
 			if (s == 0) wf8(dir, "out_bv_step1", st);
 		}
 		wf8(dir, "out_bv_final", st);
+		if (have_v && get("bv_lin", 0)) {
+			// linearised step around z = u, its inverse and its adjoint, applied to v
+			std::vector<double> r(sz, 0.0);
+			bv.calc_L(&r[0], &v[0], &u[0], &bu[0], &bw[0], 0.0); wf8(dir, "out_bv_L", r);
+			std::fill(r.begin(), r.end(), 0.0);
+			bv.calc_L_1(&r[0], &v[0], &u[0], &bu[0], &bw[0], 0.0); wf8(dir, "out_bv_L1", r);
+			std::fill(r.begin(), r.end(), 0.0);
+			bv.calc_LT(&r[0], &v[0], &u[0], &bu[0], &bw[0], 0.0); wf8(dir, "out_bv_LT", r);
+		}
 	}
 
 	int bc_steps = (int)get("bc_steps", 0);

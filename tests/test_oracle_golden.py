@@ -130,3 +130,18 @@ def test_kat_gauss_kronrod():
     L = po.lib()
     assert abs(L.orc_gauss_kronrod15(0.0, 1.0, C.cast(f1, C.c_void_p), None) - 1.0 / 3.0) <= 1e-14
     assert abs(L.orc_gauss_kronrod15(-1.0, 1.0, C.cast(f2, C.c_void_p), None)) <= 1e-14
+
+
+@pytest.mark.parametrize("level", [1, 2, 3, 4])
+def test_barvortex_linear_steps(golden, level):
+    """BarVortex::calc_L / calc_L_1 / calc_LT around z = in_u applied to in_v
+    (zero boundary, coriolis sin(lat)): the restatement returns the
+    reference's bits."""
+    g = golden(f"ref_L{level}.npz")
+    o = po.Oracle(level)
+    lat = o.mesh_arrays()["uv"].reshape(-1, 4, 2)[:, 0, 0]
+    bv = o.barvortex(max_iter=3, coriolis=np.sin(lat))
+    z = np.zeros(o.os)
+    for which, key in (("L", "out_bv_L"), ("L1", "out_bv_L1"), ("LT", "out_bv_LT")):
+        got = o.bv_linear(bv, which, g["in_v"], g["in_u"], z, z)
+        assert np.array_equal(bits(got), bits(g[key])), which
