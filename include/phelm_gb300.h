@@ -193,6 +193,20 @@ int phg_barvortex_calc(phg_barvortex b, double *u1, const double *u, const doubl
  * within the solve tolerance.  No reference counterpart (ensemble mode). */
 int phg_barvortex_calc_batch(phg_barvortex b, int nmembers, double *u1, const double *u,
                              const double *bnd_u, const double *bnd_w, const double *forcing, void *stream);
+/* BarVortex::calc_L (examples/barvortex_impl.h:326-400): the step
+ * linearised around the background z, applied to u (u1 = L_z u).  Outputs
+ * may alias inputs. */
+int phg_barvortex_calc_L(phg_barvortex b, double *u1, const double *u, const double *z, const double *bnd_u,
+                         const double *bnd_w, void *stream);
+/* BarVortex::calc_L_1 (examples/barvortex_impl.h:402-467): the inverse of the
+ * linearised step, with the backward matrix Ab_ (built on the first call).
+ * Like the reference it ADDS into u1 (u1 is read and written). */
+int phg_barvortex_calc_L_1(phg_barvortex b, double *u1, const double *u, const double *z, const double *bnd_u,
+                           const double *bnd_w, void *stream);
+/* BarVortex::calc_LT (examples/barvortex_impl.h:469-536): the adjoint of the
+ * linearised step around z applied to v. */
+int phg_barvortex_calc_LT(phg_barvortex b, double *v1, const double *v, const double *z, const double *bnd_u,
+                          const double *bnd_w, void *stream);
 /* Totals of the last calc on this handle: GMRES iterations of each solve
  * kind (L, A, mass J, mass L) summed over the step, and the worst relative
  * residual of any solve. */

@@ -938,6 +938,12 @@ struct phg_barvortex_s {
     GmresStats each[64];
     int nslots = 0;
     cudaStream_t last_stream = nullptr;   // stream of the last step (its stats live there)
+    // linearised / adjoint steps: the backward matrix Ab_ and its boundary
+    // columns bndb_ (built on first use), and their scratch vectors
+    bool have_back = false;
+    SolveOpBufs Aback;
+    ColsBufs Abackb;
+    DBuf lz, lp1, lp2, lp3, lju, ljv, ljac, ljf, lx, lrp, lin;
 };
 
 extern "C" int phg_barvortex_create(phg_ops o, const phg_bv_conf *c, const double *coriolis, phg_barvortex *out) {
@@ -1078,6 +1084,198 @@ extern "C" int phg_barvortex_calc_batch(phg_barvortex b, int nmembers, double *u
                                         const double *bnd_u, const double *bnd_w, const double *forcing,
                                         void *stream) {
     return bv_calc(b, nmembers, u1, u, bnd_u, bnd_w, forcing, stream);
+}
+
+// ------------------------------------------- linearised / adjoint steps ---
+namespace {
+
+// full vector out = p2u(M_L^-1 (L F + B3 bnd), bnd): SphereLaplace::calc1
+int lin_calc1(phg_barvortex_s *b, double *out, const double *F, const double *bnd, int &slot, cudaStream_t s) {
+    phg_ops_s *o = b->o;
+    int r = laplace_calc2_dev(o, b->lx.as<double>(), o->rs, F, o->V, 1, slot++, s, mass_tol(o));
+    if (r) return r;
+    CK(p2u(out, o->V, b->lx.as<double>(), o->rs, bnd, o->os, o->p2io.as<int>(), o->isb.as<int>(), o->V, 1, s));
+    return PHG_OK;
+}
+
+// full vector out = SphereLaplace::solve(F, bnd)
+int lin_lsolve(phg_barvortex_s *b, double *out, const double *F, const double *bnd, int &slot, cudaStream_t s) {
+    phg_ops_s *o = b->o;
+    double *rp = b->lrp.as<double>(), *x = b->lx.as<double>();
+    CK(apply_op(o->ML.op.A, o->bnd2.c, F, o->V, o->imap(), bnd, o->os, nullptr, rp, o->rs, 1, s));
+    CK(cudaMemsetAsync(x, 0, 8 * (size_t)o->rs, s));
+    int r = solve(o, o->L.op, rp, x, 1, o->rs, o->tol, slot++, s);
+    if (r) return r;
+    CK(p2u(out, o->V, x, o->rs, bnd, o->os, o->p2io.as<int>(), o->isb.as<int>(), o->V, 1, s));
+    return PHG_OK;
+}
+
+// out = p2u(M^-1 (idt u2p(F) + Bc bnd_w), bnd_w): phelm::solve with the step's
+// right-hand side (src/mesh.h:720-746, examples/barvortex_impl.h:379-390)
+int lin_msolve(phg_barvortex_s *b, double *out, const double *F, const DevSolveOp &M, const DevCols &Bc,
+               const double *bnd_w, int &slot, cudaStream_t s) {
+    phg_ops_s *o = b->o;
+    double *rp = b->lrp.as<double>(), *x = b->lx.as<double>();
+    CK(apply_op(o->ML.op.A, Bc, F, o->V, o->imap(), bnd_w, o->os, nullptr, rp, o->rs, 1, s));
+    CK(cudaMemsetAsync(x, 0, 8 * (size_t)o->rs, s));
+    int r = solve(o, M, rp, x, 1, o->rs, o->tol, slot++, s);
+    if (r) return r;
+    CK(p2u(out, o->V, x, o->rs, bnd_w, o->os, o->p2io.as<int>(), o->isb.as<int>(), o->V, 1, s));
+    return PHG_OK;
+}
+
+// three Jacobians in one batched solve, as full vectors with zero boundary:
+// jf[k] = sign * J(u_k, v_k) (SphereJacobian::calc1 / calc1t with bnd = 0)
+int lin_jac3(phg_barvortex_s *b, const double *const u[3], const double *const v[3], double sign, int &slot,
+             cudaStream_t s) {
+    phg_ops_s *o = b->o;
+    const int V = o->V, rs = o->rs;
+    double *ju = b->lju.as<double>(), *jv = b->ljv.as<double>(), *jac = b->ljac.as<double>();
+    for (int k = 0; k < 3; ++k) {
+        CK(cudaMemcpyAsync(ju + (size_t)k * V, u[k], 8 * (size_t)V, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(jv + (size_t)k * V, v[k], 8 * (size_t)V, cudaMemcpyDeviceToDevice, s));
+    }
+    int r = jacobian_derivs_dev(o, ju, jv, V, o->s_e.as<double>(), 3, slot++, s, mass_tol(o));
+    if (r) return r;
+    CK(jac_combine(o->s_e.as<double>(), rs, rs, jac, rs, nullptr, 0, nullptr, 3, s));
+    if (sign != 1.0) CK(axpbz(jac, jac, sign, jac, 0.0, 3LL * rs, s));
+    CK(p2u(b->ljf.as<double>(), V, jac, rs, nullptr, o->os, o->p2io.as<int>(), o->isb.as<int>(), V, 3, s));
+    return PHG_OK;
+}
+
+int lin_reserve(phg_barvortex_s *b) {
+    phg_ops_s *o = b->o;
+    const size_t V = o->V, rs = o->rs;
+    DBuf *full[] = {&b->lz, &b->lp1, &b->lp2, &b->lp3, &b->lin};
+    for (DBuf *d : full) CK(d->ensure(8 * V));
+    CK(b->lju.ensure(8 * 3 * V)); CK(b->ljv.ensure(8 * 3 * V)); CK(b->ljf.ensure(8 * 3 * V));
+    CK(b->ljac.ensure(8 * 3 * rs)); CK(b->lx.ensure(8 * rs)); CK(b->lrp.ensure(8 * rs));
+    CK(o->s_e.ensure(8 * rs * 8 * 3));
+    return PHG_OK;
+}
+
+int lin_backward(phg_barvortex_s *b) {
+    if (b->have_back) return PHG_OK;
+    phg_ops_s *o = b->o;
+    const phg_bv_conf &c = b->c;
+    Csr A, Ab;
+    // Ab_ = (1/tau - sigma (1 - theta)) M + (1 - theta) mu L (examples/barvortex_impl.h:84-105)
+    assemble_barvortex(o->mesh->m, 1.0 / c.tau - c.sigma * (1.0 - c.theta), (1.0 - c.theta) * c.mu, A, Ab);
+    if (!same_pattern(A, o->mesh->ops.idt)) return fail(PHG_ERR_ARG, "backward matrix pattern mismatch");
+    int r;
+    if ((r = build_solve_op(o, A, b->Aback, true))) return r;
+    if ((r = build_cols(Ab, b->Abackb))) return r;
+    b->have_back = true;
+    return PHG_OK;
+}
+
+// kind 0: calc_L, 1: calc_L_1 (adds into u1), 2: calc_LT; device pointers
+int lin_dev(phg_barvortex_s *b, int kind, double *u1, const double *u, const double *z, const double *bnd_u,
+            const double *bnd_w, cudaStream_t s) {
+    phg_ops_s *o = b->o;
+    const int V = o->V;
+    const long long NV = V;
+    const phg_bv_conf &c = b->c;
+    const double k1 = c.k1, k2 = c.k2, th = c.theta, mu = c.mu, sg = c.sigma, tau = c.tau;
+    int r, slot = 0;
+    if ((r = lin_reserve(b))) return r;
+    if (kind == 1 && (r = lin_backward(b))) return r;
+    double *zl = b->lz.as<double>(), *pt1 = b->lp1.as<double>(), *pt2 = b->lp2.as<double>(),
+           *pt3 = b->lp3.as<double>(), *jf = b->ljf.as<double>(), *in = b->lin.as<double>();
+    const double *lh = b->lh.as<double>();
+    if (kind < 2) {
+        // examples/barvortex_impl.h:343-362 (calc_L) and 421-440 (calc_L_1)
+        CK(cudaMemcpyAsync(in, u, 8 * NV, cudaMemcpyDeviceToDevice, s));   // u1 may alias u
+        if ((r = lin_calc1(b, zl, z, bnd_w, slot, s))) return r;
+        if ((r = lin_calc1(b, pt1, in, bnd_w, slot, s))) return r;
+        const double *ju[3] = {in, z, in}, *jv[3] = {lh, pt1, zl};
+        if ((r = lin_jac3(b, ju, jv, 1.0, slot, s))) return r;
+        CK(axpbz(pt3, jf, k2, jf, 0.0, NV, s));
+        CK(axpbz(pt3, pt3, 1.0, jf + V, k1, NV, s));
+        CK(axpbz(pt3, pt3, 1.0, jf + 2 * (size_t)V, k1, NV, s));
+        if (kind == 0) CK(axpbz(pt3, pt3, -1.0, pt3, 0.0, NV, s));
+        if ((r = lin_calc1(b, pt2, pt1, nullptr, slot, s))) return r;
+        if (kind == 0) {
+            CK(axpbz(pt2, pt2, (1. - th) * mu, pt2, 0.0, NV, s));
+            CK(axpbz(pt1, pt1, 1.0 / tau - (1. - th) * sg, pt1, 0.0, NV, s));
+            CK(axpbz(u1, pt1, 1.0, pt1, 0.0, NV, s));
+        } else {
+            CK(axpbz(pt2, pt2, -th * mu, pt2, 0.0, NV, s));
+            CK(axpbz(pt1, pt1, 1.0 / tau + th * sg, pt1, 0.0, NV, s));
+            CK(axpbz(u1, u1, 1.0, pt1, 1.0, NV, s));
+        }
+        CK(axpbz(u1, u1, 1.0, pt2, 1.0, NV, s));
+        CK(axpbz(u1, u1, 1.0, pt3, 1.0, NV, s));
+        const DevSolveOp &M = kind == 0 ? b->A.op : b->Aback.op;
+        const DevCols &Bc = kind == 0 ? b->Ab.c : b->Abackb.c;
+        if ((r = lin_msolve(b, u1, u1, M, Bc, bnd_w, slot, s))) return r;
+        if ((r = lin_lsolve(b, u1, u1, bnd_u, slot, s))) return r;
+    } else {
+        // examples/barvortex_impl.h:485-535
+        CK(cudaMemcpyAsync(in, z, 8 * NV, cudaMemcpyDeviceToDevice, s));   // v1 may alias z
+        if ((r = lin_calc1(b, zl, in, bnd_w, slot, s))) return r;
+        if ((r = lin_lsolve(b, u1, u, bnd_u, slot, s))) return r;
+        if ((r = lin_msolve(b, u1, u1, b->A.op, b->Ab.c, bnd_w, slot, s))) return r;
+        if ((r = lin_calc1(b, pt1, u1, bnd_w, slot, s))) return r;
+        CK(axpbz(pt1, pt1, 1.0 / tau - (1.0 - th) * sg, pt1, 0.0, NV, s));
+        if ((r = lin_calc1(b, pt2, u1, bnd_w, slot, s))) return r;
+        if ((r = lin_calc1(b, pt2, pt2, nullptr, slot, s))) return r;
+        CK(axpbz(pt2, pt2, (1.0 - th) * mu, pt2, 0.0, NV, s));
+        // tmp = J^T(v1, l), p = J^T(z, v1), h1 = J^T(v1, lz)
+        const double *ju[3] = {u1, in, u1}, *jv[3] = {lh, u1, zl};
+        if ((r = lin_jac3(b, ju, jv, -1.0, slot, s))) return r;
+        double *tmp = jf, *pl = jf + V, *h1 = jf + 2 * (size_t)V;
+        if ((r = lin_calc1(b, pl, pl, nullptr, slot, s))) return r;
+        CK(axpbz(h1, h1, k1, pl, k1, NV, s));
+        CK(axpbz(h1, h1, 1.0, tmp, k2, NV, s));
+        CK(axpbz(h1, h1, -1.0, h1, 0.0, NV, s));
+        CK(axpbz(u1, pt1, 1.0, pt1, 0.0, NV, s));
+        CK(axpbz(u1, u1, 1.0, pt2, 1.0, NV, s));
+        CK(axpbz(u1, u1, 1.0, h1, 1.0, NV, s));
+        // set_bnd (src/proj.cpp:110-133): inner values kept, boundary = bnd_u
+        CK(gather(b->lx.as<double>(), o->rs, u1, V, o->imap(), o->rs, 1, s));
+        CK(p2u(u1, V, b->lx.as<double>(), o->rs, bnd_u, o->os, o->p2io.as<int>(), o->isb.as<int>(), V, 1, s));
+    }
+    b->nslots = slot;
+    b->last_stream = s;
+    return PHG_OK;
+}
+
+}  // namespace
+
+static int bv_linear(phg_barvortex b, int kind, double *u1, const double *u, const double *z, const double *bnd_u,
+                     const double *bnd_w, void *stream) {
+    if (!b || !u1 || !u || !z) return fail(PHG_ERR_ARG, "NULL argument");
+    phg_ops_s *o = b->o;
+    cudaStream_t s = o->str(stream);
+    Stage st(o, s);
+    const double *du, *dz, *dbu, *dbw, *dacc = nullptr; double *d1;
+    CK(st.in(u, o->V, &du)); CK(st.in(z, o->V, &dz));
+    CK(st.in(bnd_u, o->os, &dbu)); CK(st.in(bnd_w, o->os, &dbw));
+    if (kind == 1) CK(st.in(u1, o->V, &dacc));   // calc_L_1 adds into u1
+    CK(st.out(u1, o->V, &d1));
+    if (kind == 1 && dacc != d1) CK(cudaMemcpyAsync(d1, dacc, 8 * (size_t)o->V, cudaMemcpyDeviceToDevice, s));
+    if (o->os == 0) { dbu = nullptr; dbw = nullptr; }
+    int r = lin_dev(b, kind, d1, du, dz, dbu, dbw, s);
+    if (r) return r;
+    CK(st.finish());
+    if (!st.host) return PHG_OK;
+    return check_stats(o, b->nslots, s, nullptr, b->each);
+}
+
+extern "C" int phg_barvortex_calc_L(phg_barvortex b, double *u1, const double *u, const double *z,
+                                    const double *bnd_u, const double *bnd_w, void *stream) {
+    return bv_linear(b, 0, u1, u, z, bnd_u, bnd_w, stream);
+}
+
+extern "C" int phg_barvortex_calc_L_1(phg_barvortex b, double *u1, const double *u, const double *z,
+                                      const double *bnd_u, const double *bnd_w, void *stream) {
+    return bv_linear(b, 1, u1, u, z, bnd_u, bnd_w, stream);
+}
+
+extern "C" int phg_barvortex_calc_LT(phg_barvortex b, double *v1, const double *v, const double *z,
+                                     const double *bnd_u, const double *bnd_w, void *stream) {
+    return bv_linear(b, 2, v1, v, z, bnd_u, bnd_w, stream);
 }
 
 extern "C" int phg_barvortex_last_stats(phg_barvortex b, int *il, int *ia, int *imj, int *iml, double *worst) {

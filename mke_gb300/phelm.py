@@ -96,6 +96,9 @@ SIGNATURES = {
     "phg_barvortex_calc": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "phg_barvortex_calc_batch": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "phg_barvortex_last_stats": (C.c_int, [_vp, _ip, _ip, _ip, _ip, _dp]),
+    "phg_barvortex_calc_L": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "phg_barvortex_calc_L_1": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "phg_barvortex_calc_LT": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "phg_baroclin_create": (C.c_int, [_vp, C.POINTER(BcConf), _vp, C.POINTER(_vp)]),
     "phg_baroclin_destroy": (None, [_vp]),
     "phg_baroclin_calc": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
@@ -384,6 +387,25 @@ class BarVortex:
         _check(lib().phg_barvortex_calc_batch(self._h, nm, _ptr(out), _ptr(u), _ptr(bnd_u), _ptr(bnd_w),
                                               _ptr(forcing), _stream(stream)))
         return out
+
+    def _linear(self, fn, u, z, bnd_u, bnd_w, out, stream):
+        out = np.zeros(self.m.size) if out is None else out
+        u, z = _f8(u), _f8(z)
+        _check(getattr(lib(), fn)(self._h, _ptr(out), _ptr(u), _ptr(z), _ptr(_f8(bnd_u)), _ptr(_f8(bnd_w)),
+                                  _stream(stream)))
+        return out
+
+    def calc_L(self, u, z, bnd_u=None, bnd_w=None, out=None, stream=None):
+        """BarVortex::calc_L: the step linearised around z, applied to u."""
+        return self._linear("phg_barvortex_calc_L", u, z, bnd_u, bnd_w, out, stream)
+
+    def calc_L_1(self, u, z, bnd_u=None, bnd_w=None, out=None, stream=None):
+        """BarVortex::calc_L_1: inverse linearised step; adds into ``out`` (zeros when None)."""
+        return self._linear("phg_barvortex_calc_L_1", u, z, bnd_u, bnd_w, out, stream)
+
+    def calc_LT(self, v, z, bnd_u=None, bnd_w=None, out=None, stream=None):
+        """BarVortex::calc_LT: adjoint of the linearised step around z, applied to v."""
+        return self._linear("phg_barvortex_calc_LT", v, z, bnd_u, bnd_w, out, stream)
 
     def last_stats(self):
         a = [C.c_int() for _ in range(4)]

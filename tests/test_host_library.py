@@ -17,7 +17,7 @@ OPS = ["idt", "lapl", "bnd2", "bnd3", "jidt", "d1", "d2", "d1c", "d2c", "d1b", "
 def header_symbols():
     txt = open(os.path.join(REPO, "include", "phelm_gb300.h")).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    return sorted(set(re.findall(r"\b(phg_[a-z0-9_]+)\s*\(", txt)))
+    return sorted(set(re.findall(r"\b(phg_[A-Za-z0-9_]+)\s*\(", txt)))
 
 
 def test_exports_every_declared_symbol():
