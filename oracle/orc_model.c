@@ -362,18 +362,35 @@ static void bc_elements(const orc_bc_conf *c, double a, double b, double e[9])
 	e[7] = a;
 	e[8] = -b;
 }
+/* the backward (inverse linearised step) entries, examples/baroclin.cpp:182-243 */
+static void bc_elements_back(const orc_bc_conf *c, double a, double b, double e[9])
+{
+	double tau = c->tau, mu = c->mu, mu1 = c->mu1, sigma = c->sigma, sigma1 = c->sigma1;
+	double alpha = c->alpha, theta = c->theta;
+	e[0] = a * (1.0 / tau - 0.5 * (1.0 - theta) * sigma) + (1.0 - theta) * mu * b;
+	e[1] = 0.5 * a * sigma * (1.0 - theta);
+	e[2] = -0.5 * (1.0 - theta) * sigma * a;
+	e[3] = a * (1.0 / tau - 0.5 * (1.0 - theta) * sigma - alpha * alpha * (1.0 - theta) * mu1)
+	       + (1.0 - theta) * mu * b;
+	e[4] = a * (-alpha * alpha / tau + alpha * alpha * (1.0 - theta) * sigma1);
+	e[5] = a;
+	e[6] = -b;
+	e[7] = a;
+	e[8] = -b;
+}
+static void bc_entries(const orc_bc_conf *c, int backward, double a, double b, double e[9])
+{
+	if (backward) bc_elements_back(c, a, b, e);
+	else bc_elements(c, a, b, e);
+}
 /* element (row block, column block) for e[0..8] (examples/baroclin.cpp:157-177) */
 static const int bc_ri[9] = { 0, 0, 1, 1, 1, 2, 2, 3, 3 };
 static const int bc_cj[9] = { 0, 1, 0, 1, 3, 0, 2, 1, 3 };
 
-int orc_bc_init(orc_baroclin *bc, orc_ops *o, const orc_bc_conf *c, const double *coriolis)
+static void bc_assemble(orc_baroclin *bc, int backward, orc_csr *M)
 {
-	memset(bc, 0, sizeof(*bc));
-	bc->o = o; bc->c = *c;
-	const orc_mesh *m = o->m;
+	const orc_mesh *m = bc->o->m;
 	int rs = m->rs;
-	bc->lh = VEC(m->V);
-	if (coriolis) memcpy(bc->lh, coriolis, sizeof(double) * (size_t)m->V);
 	orc_builder *b = orc_builder_new(4 * rs, 4 * rs);
 	#pragma omp parallel for schedule(dynamic, 64)
 	for (int i = 0; i < rs; ++i) {
@@ -390,25 +407,36 @@ int orc_bc_init(orc_baroclin *bc, orc_ops *o, const orc_bc_conf *c, const double
 				double a = orc_mass_cos(pi, &phi[i0], m, t, zone);
 				double bb = orc_slaplace(&phi[i0], pi, m, t, zone);
 				double e[9];
-				bc_elements(c, a, bb, e);
+				bc_entries(&bc->c, backward, a, bb, e);
 				for (int q = 0; q < 9; ++q)
 					orc_builder_add(b, i + bc_ri[q] * rs, j + bc_cj[q] * rs, e[q]);
 			}
 		}
 	}
-	orc_builder_finish(b, &bc->A);
+	orc_builder_finish(b, M);
+}
+
+int orc_bc_init(orc_baroclin *bc, orc_ops *o, const orc_bc_conf *c, const double *coriolis)
+{
+	memset(bc, 0, sizeof(*bc));
+	bc->o = o; bc->c = *c;
+	bc->lh = VEC(o->m->V);
+	if (coriolis) memcpy(bc->lh, coriolis, sizeof(double) * (size_t)o->m->V);
+	bc_assemble(bc, 0, &bc->A);
+	bc_assemble(bc, 1, &bc->Ab);   /* Ab_ (examples/baroclin.cpp:69-106, 182-243) */
 	return 0;
 }
 
 void orc_bc_free(orc_baroclin *bc)
 {
-	orc_csr_free(&bc->A); free(bc->lh);
+	orc_csr_free(&bc->A); orc_csr_free(&bc->Ab); free(bc->lh);
 	memset(bc, 0, sizeof(*bc));
 }
 
 /* generate_right_part with right_part_cb (examples/baroclin.cpp:245-339,
  * src/generators.h:236-276): rp = mass * [F; G] - boundary columns * bnd */
-static void bc_rhs(orc_baroclin *bc, double *rp, const double *F, const double *G, const double *bnd)
+static void bc_rhs(orc_baroclin *bc, double *rp, const double *F, const double *G, const double *bnd,
+                   int backward)
 {
 	const orc_mesh *m = bc->o->m;
 	int rs = m->rs;
@@ -429,7 +457,7 @@ static void bc_rhs(orc_baroclin *bc, double *rp, const double *F, const double *
 					double a = orc_mass_cos(pi, &phi[i0], m, t, zone);
 					double bb = orc_slaplace(&phi[i0], pi, m, t, zone);
 					double e[9], acc[4] = { 0, 0, 0, 0 };
-					bc_elements(&bc->c, a, bb, e);
+					bc_entries(&bc->c, backward, a, bb, e);
 					for (int q = 0; q < 9; ++q)
 						if (bnd) acc[bc_ri[q]] += -bnd[j0] * e[q];
 					for (int q = 0; q < 4; ++q) rp[i + q * rs] += acc[q];
@@ -508,7 +536,7 @@ void orc_bc_step(orc_baroclin *bc, double *u11, double *u21,
 			F[i] += FC[point];
 			G[i] += GC[point];
 		}
-		bc_rhs(bc, rp, F, G, bnd);
+		bc_rhs(bc, rp, F, G, bnd, 0);
 		orc_csr_solve(&bc->A, ans, rp);
 		orc_p2u(m, w1_n, ans, bnd);
 		orc_p2u(m, w2_n, ans + rs, bnd);
@@ -526,6 +554,138 @@ void orc_bc_step(orc_baroclin *bc, double *u11, double *u21,
 	free(w1); free(w2); free(dw1); free(dw2); free(FC); free(GC);
 	free(u1_n); free(u2_n); free(w1_n); free(w2_n); free(u1_n1); free(u2_n1);
 	free(tmp1); free(tmp2); free(jac1); free(jac2); free(jac3); free(F); free(G); free(rp); free(ans);
+}
+
+/* Baroclin::calc_L (kind 0, examples/baroclin.cpp:620-802: one iteration,
+ * forward matrix) and calc_L_1 (kind 1, :804-986: up to 10 iterations,
+ * backward matrix Ab_), linearised around (z1, z2). */
+static void bc_linear(orc_baroclin *bc, int kind, double *u11, double *u21,
+                      const double *u1, const double *u2, const double *z1, const double *z2,
+                      const double *bnd)
+{
+	orc_ops *o = bc->o;
+	const orc_mesh *m = o->m;
+	int rs = m->rs, sz = m->V;
+	double th = bc->c.theta, sigma = bc->c.sigma, mu = bc->c.mu, tau = bc->c.tau;
+	double alpha = bc->c.alpha, mu1 = bc->c.mu1, sigma1 = bc->c.sigma1;
+	double *w1 = VEC(sz), *w2 = VEC(sz), *dw1 = VEC(sz), *dw2 = VEC(sz), *dz1 = VEC(sz), *dz2 = VEC(sz);
+	double *FC = VEC(sz), *GC = VEC(sz);
+	double *u1_n = VEC(sz), *u2_n = VEC(sz), *w1_n = VEC(sz), *w2_n = VEC(sz);
+	double *u1_n1 = VEC(sz), *u2_n1 = VEC(sz), *tmp1 = VEC(sz), *tmp2 = VEC(sz);
+	double *jac1 = VEC(rs), *jac2 = VEC(rs), *F = VEC(rs), *G = VEC(rs);
+	double *rp = VEC(4 * rs), *ans = VEC(4 * rs);
+	/* weights of the input and of the iterate in the Jacobian arguments */
+	double wa = kind == 0 ? 1.0 - th : th, wb = kind == 0 ? th : 1.0 - th;
+	double sgn = kind == 0 ? -1.0 : 1.0;
+
+	orc_laplace_calc1(o, w1, u1, bnd);
+	orc_laplace_calc1(o, w2, u2, bnd);
+	orc_laplace_calc1(o, dw1, w1, bnd);
+	orc_laplace_calc1(o, dw2, w2, bnd);
+	orc_laplace_calc1(o, dz1, z1, bnd);
+	orc_laplace_calc1(o, dz2, z2, bnd);
+	if (kind == 0) {
+		for (int i = 0; i < sz; ++i) FC[i] = -0.5 * (1.0 - th) * sigma * w1[i] + 0.5 * (1.0 - th) * sigma * w2[i];
+		for (int i = 0; i < sz; ++i) FC[i] = 1.0 * FC[i] + mu * (1.0 - th) * dw1[i];
+		for (int i = 0; i < sz; ++i) FC[i] = 1.0 * FC[i] + 1.0 / tau * w1[i];
+		for (int i = 0; i < sz; ++i) GC[i] = -0.5 * (1.0 - th) * sigma * w1[i] + -0.5 * (1.0 - th) * sigma * w2[i];
+		for (int i = 0; i < sz; ++i) GC[i] = 1.0 * GC[i] + mu * (1.0 - th) * dw2[i];
+		for (int i = 0; i < sz; ++i) GC[i] = 1.0 * GC[i] + 1.0 / tau * w2[i];
+		for (int i = 0; i < sz; ++i) GC[i] = 1.0 * GC[i] + -alpha * alpha / tau * u2[i];
+		for (int i = 0; i < sz; ++i) GC[i] = 1.0 * GC[i] + -alpha * alpha * mu1 * (1 - th) * w2[i];
+		for (int i = 0; i < sz; ++i) GC[i] = 1.0 * GC[i] + alpha * alpha * sigma1 * (1 - th) * u2[i];
+	} else {
+		for (int i = 0; i < sz; ++i) FC[i] = 0.5 * th * sigma * w1[i] + -0.5 * th * sigma * w2[i];
+		for (int i = 0; i < sz; ++i) FC[i] = 1.0 * FC[i] + -mu * th * dw1[i];
+		for (int i = 0; i < sz; ++i) FC[i] = 1.0 * FC[i] + 1.0 / tau * w1[i];
+		for (int i = 0; i < sz; ++i) GC[i] = 0.5 * th * sigma * w1[i] + 0.5 * th * sigma * w2[i];
+		for (int i = 0; i < sz; ++i) GC[i] = 1.0 * GC[i] + -mu * th * dw2[i];
+		for (int i = 0; i < sz; ++i) GC[i] = 1.0 * GC[i] + 1.0 / tau * w2[i];
+		for (int i = 0; i < sz; ++i) GC[i] = 1.0 * GC[i] + -alpha * alpha / tau * u2[i];
+		for (int i = 0; i < sz; ++i) GC[i] = 1.0 * GC[i] + alpha * alpha * mu1 * th * w2[i];
+		for (int i = 0; i < sz; ++i) GC[i] = 1.0 * GC[i] + -alpha * alpha * sigma1 * th * u2[i];
+	}
+	memcpy(u1_n, u1, sizeof(double) * (size_t)sz);
+	memcpy(u2_n, u2, sizeof(double) * (size_t)sz);
+	memcpy(w1_n, w1, sizeof(double) * (size_t)sz);
+	memcpy(w2_n, w2, sizeof(double) * (size_t)sz);
+	int iters = kind == 0 ? 1 : 10;
+	for (int it = 0; it < iters; ++it) {
+#define MIX(d, a, b) for (int i = 0; i < sz; ++i) d[i] = wa * a[i] + wb * b[i]
+		/* F */
+		MIX(tmp1, u1, u1_n);
+		for (int i = 0; i < sz; ++i) tmp2[i] = dz1[i] + bc->lh[i];
+		orc_jacobian_calc2(o, jac1, tmp1, tmp2);
+		MIX(tmp1, w1, w1_n);
+		orc_jacobian_calc2(o, jac2, z1, tmp1);
+		if (kind == 0) for (int i = 0; i < rs; ++i) F[i] = -1.0 * jac1[i] + -1.0 * jac2[i];
+		else for (int i = 0; i < rs; ++i) F[i] = jac1[i] + jac2[i];
+		MIX(tmp1, w2, w2_n);
+		orc_jacobian_calc2(o, jac1, z2, tmp1);
+		if (kind == 0) for (int i = 0; i < rs; ++i) F[i] = 1.0 * F[i] + -1.0 * jac1[i];
+		else for (int i = 0; i < rs; ++i) F[i] = F[i] + jac1[i];
+		MIX(tmp1, u2, u2_n);
+		orc_jacobian_calc2(o, jac1, tmp1, dz2);
+		if (kind == 0) for (int i = 0; i < rs; ++i) F[i] = 1.0 * F[i] + -1.0 * jac1[i];
+		else for (int i = 0; i < rs; ++i) F[i] = F[i] + jac1[i];
+		/* G (the reference's J(z1, .) uses L(z1) here) */
+		MIX(tmp1, w2, w2_n);
+		orc_jacobian_calc2(o, jac1, dz1, tmp1);
+		MIX(tmp1, u1, u1_n);
+		orc_jacobian_calc2(o, jac2, dz2, tmp1);
+		if (kind == 0) for (int i = 0; i < rs; ++i) G[i] = -1.0 * jac1[i] + -1.0 * jac2[i];
+		else for (int i = 0; i < rs; ++i) G[i] = jac1[i] + jac2[i];
+		MIX(tmp1, u2, u2_n);
+		for (int i = 0; i < sz; ++i) tmp2[i] = dz1[i] + bc->lh[i];
+		orc_jacobian_calc2(o, jac1, tmp1, tmp2);
+		if (kind == 0) for (int i = 0; i < rs; ++i) G[i] = 1.0 * G[i] + -1.0 * jac1[i];
+		else for (int i = 0; i < rs; ++i) G[i] = G[i] + jac1[i];
+		MIX(tmp1, w1, w1_n);
+		orc_jacobian_calc2(o, jac1, z2, tmp1);
+		if (kind == 0) for (int i = 0; i < rs; ++i) G[i] = 1.0 * G[i] + -1.0 * jac1[i];
+		else for (int i = 0; i < rs; ++i) G[i] = G[i] + jac1[i];
+		MIX(tmp1, u2, u2_n);
+		orc_jacobian_calc2(o, jac1, z1, tmp1);
+		for (int i = 0; i < rs; ++i) G[i] = 1.0 * G[i] + -sgn * alpha * alpha * jac1[i];
+		MIX(tmp1, u1, u1_n);
+		orc_jacobian_calc2(o, jac1, tmp1, z2);
+		for (int i = 0; i < rs; ++i) G[i] = 1.0 * G[i] + -sgn * alpha * alpha * jac1[i];
+#undef MIX
+		for (int i = 0; i < rs; ++i) {
+			int point = m->inner[i];
+			F[i] += FC[point];
+			G[i] += GC[point];
+		}
+		bc_rhs(bc, rp, F, G, bnd, kind);
+		orc_csr_solve(kind == 0 ? &bc->A : &bc->Ab, ans, rp);
+		orc_p2u(m, w1_n, ans, bnd);
+		orc_p2u(m, w2_n, ans + rs, bnd);
+		orc_p2u(m, u1_n1, ans + 2 * rs, bnd);
+		orc_p2u(m, u2_n1, ans + 3 * rs, bnd);
+		double nr1 = orc_dist(o, u1_n1, u1_n), nr2 = orc_dist(o, u2_n1, u2_n);
+		double nr = nr1 > nr2 ? nr1 : nr2;
+		double *s = u1_n1; u1_n1 = u1_n; u1_n = s;
+		s = u2_n1; u2_n1 = u2_n; u2_n = s;
+		bc->last_iters = it + 1;
+		if (nr < 1e-8) break;
+	}
+	memcpy(u11, u1_n, sizeof(double) * (size_t)sz);
+	memcpy(u21, u2_n, sizeof(double) * (size_t)sz);
+	free(w1); free(w2); free(dw1); free(dw2); free(dz1); free(dz2); free(FC); free(GC);
+	free(u1_n); free(u2_n); free(w1_n); free(w2_n); free(u1_n1); free(u2_n1); free(tmp1); free(tmp2);
+	free(jac1); free(jac2); free(F); free(G); free(rp); free(ans);
+}
+
+void orc_bc_calc_L(orc_baroclin *bc, double *u11, double *u21, const double *u1, const double *u2,
+                   const double *z1, const double *z2, const double *bnd)
+{
+	bc_linear(bc, 0, u11, u21, u1, u2, z1, z2, bnd);
+}
+
+void orc_bc_calc_L1(orc_baroclin *bc, double *u11, double *u21, const double *u1, const double *u2,
+                    const double *z1, const double *z2, const double *bnd)
+{
+	bc_linear(bc, 1, u11, u21, u1, u2, z1, z2, bnd);
 }
 
 /* ------------------------------------------------- known-answer helpers --- */

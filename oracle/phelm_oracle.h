@@ -161,6 +161,7 @@ typedef struct {
 	orc_ops *o;
 	orc_bc_conf c;
 	orc_csr A;           /* 4 rs x 4 rs block matrix [w1 | w2 | u1 | u2] */
+	orc_csr Ab;          /* the backward matrix Ab_ (inverse linearised step) */
 	double *lh;
 	int last_iters;
 } orc_baroclin;
@@ -172,6 +173,11 @@ void orc_bc_free(orc_baroclin *bc);
 void orc_bc_step(orc_baroclin *bc, double *u11, double *u21,
                  const double *u1, const double *u2, const double *bnd,
                  const double *f, const double *g);
+/* Baroclin::calc_L / calc_L_1 linearised around (z1, z2). */
+void orc_bc_calc_L(orc_baroclin *bc, double *u11, double *u21, const double *u1, const double *u2,
+                   const double *z1, const double *z2, const double *bnd);
+void orc_bc_calc_L1(orc_baroclin *bc, double *u11, double *u21, const double *u1, const double *u2,
+                    const double *z1, const double *z2, const double *bnd);
 
 #ifdef __cplusplus
 }

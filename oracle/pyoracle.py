@@ -60,7 +60,7 @@ class BcConf(C.Structure):
 
 
 class Baroclin(C.Structure):
-    _fields_ = [("o", C.POINTER(Ops)), ("c", BcConf), ("A", Csr), ("lh", _dp),
+    _fields_ = [("o", C.POINTER(Ops)), ("c", BcConf), ("A", Csr), ("Ab", Csr), ("lh", _dp),
                 ("last_iters", C.c_int)]
 
 
@@ -98,6 +98,8 @@ def lib():
             getattr(L, f).argtypes = [C.POINTER(BarVortex), _dp, _dp, _dp, _dp, _dp]
         L.orc_bc_init.argtypes = [C.POINTER(Baroclin), C.POINTER(Ops), C.POINTER(BcConf), _dp]
         L.orc_bc_step.argtypes = [C.POINTER(Baroclin), _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        for f in ("orc_bc_calc_L", "orc_bc_calc_L1"):
+            getattr(L, f).argtypes = [C.POINTER(Baroclin), _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         L.orc_set_solver.argtypes = [C.c_double, C.c_int, C.c_int]
         L.orc_last_residual.restype = C.c_double
         L.orc_gauss_kronrod15.restype = C.c_double
@@ -221,6 +223,14 @@ class Oracle:
         lib().orc_bc_init(C.byref(bc), C.byref(self.ops), C.byref(c), _p(cor))
         bc._keep = (self, cor)
         return bc
+
+    def bc_linear(self, bc, which, u1, u2, z1, z2, bnd=None):
+        """Baroclin::calc_L ("L") or calc_L_1 ("L1") around (z1, z2)."""
+        o1, o2 = np.zeros(self.V), np.zeros(self.V)
+        fn = {"L": "orc_bc_calc_L", "L1": "orc_bc_calc_L1"}[which]
+        getattr(lib(), fn)(C.byref(bc), _p(o1), _p(o2), _p(_f8(u1)), _p(_f8(u2)), _p(_f8(z1)), _p(_f8(z2)),
+                           _p(None if bnd is None else _f8(bnd)))
+        return o1, o2
 
     def bc_step(self, bc, u1, u2, bnd=None, f=None, g=None):
         o1, o2 = np.zeros(self.V), np.zeros(self.V)

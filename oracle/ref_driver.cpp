@@ -247,6 +247,14 @@ int main(int argc, char **argv)
 		}
 		wf8(dir, "out_bc_final_u1", u1);
 		wf8(dir, "out_bc_final_u2", u2);
+		if (get("bc_lin", 0)) {
+			// linearised step around (z1, z2) = (u, v) and its inverse, applied to (v, u)
+			std::vector<double> a1(sz), a2(sz);
+			bc.calc_L(&a1[0], &a2[0], &v[0], &u[0], &u[0], &v[0], &z[0], 0.0);
+			wf8(dir, "out_bc_L_u1", a1); wf8(dir, "out_bc_L_u2", a2);
+			bc.calc_L_1(&a1[0], &a2[0], &v[0], &u[0], &u[0], &v[0], &z[0], 0.0);
+			wf8(dir, "out_bc_L1_u1", a1); wf8(dir, "out_bc_L1_u2", a2);
+		}
 	}
 	return 0;
 }

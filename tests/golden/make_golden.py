@@ -64,7 +64,7 @@ def run_level(ref_bin, level, work, bv_steps=0, bc_steps=0, seed=1234, extra=())
     np.save(os.path.join(out, "in_v.npy"), v)
     np.save(os.path.join(out, "in_bnd.npy"), u[bnd == 1].copy())
     args = [os.path.join(ref_bin, "ref_driver"), mesh_txt, out,
-            f"bv_steps={bv_steps}", f"bc_steps={bc_steps}", "bv_iters=3", "bc_iters=3", "bv_lin=1", *extra]
+            f"bv_steps={bv_steps}", f"bc_steps={bc_steps}", "bv_iters=3", "bc_iters=3", "bv_lin=1", "bc_lin=1", *extra]
     subprocess.run(args, check=True, stderr=subprocess.DEVNULL)
     return out
 

@@ -145,3 +145,18 @@ def test_barvortex_linear_steps(golden, level):
     for which, key in (("L", "out_bv_L"), ("L1", "out_bv_L1"), ("LT", "out_bv_LT")):
         got = o.bv_linear(bv, which, g["in_v"], g["in_u"], z, z)
         assert np.array_equal(bits(got), bits(g[key])), which
+
+
+@pytest.mark.parametrize("level", [1, 2, 3])
+def test_baroclin_linear_steps(golden, level):
+    """Baroclin::calc_L / calc_L_1 around (z1, z2) = (in_u, in_v) applied to
+    (in_v, in_u), zero boundary: the restatement returns the reference's bits."""
+    g = golden(f"ref_L{level}.npz")
+    o = po.Oracle(level)
+    lat = o.mesh_arrays()["uv"].reshape(-1, 4, 2)[:, 0, 0]
+    bc = o.baroclin(max_iter=3, coriolis=np.sin(lat))
+    z = np.zeros(o.os)
+    for which in ("L", "L1"):
+        a, b = o.bc_linear(bc, which, g["in_v"], g["in_u"], g["in_u"], g["in_v"], z)
+        assert np.array_equal(bits(a), bits(g[f"out_bc_{which}_u1"])), which
+        assert np.array_equal(bits(b), bits(g[f"out_bc_{which}_u2"])), which
