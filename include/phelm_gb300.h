@@ -233,6 +233,15 @@ void phg_baroclin_destroy(phg_baroclin b);
  * iteration), so it returns after the last iteration's work is done. */
 int phg_baroclin_calc(phg_baroclin b, double *u11, double *u21, const double *u1, const double *u2,
                       const double *bnd, const double *f, const double *g, void *stream);
+/* Baroclin::calc_L (examples/baroclin.cpp:620-802): the step linearised around
+ * (z1, z2) applied to (u1, u2), one iteration.  Outputs may alias inputs. */
+int phg_baroclin_calc_L(phg_baroclin b, double *u11, double *u21, const double *u1, const double *u2,
+                        const double *z1, const double *z2, const double *bnd, void *stream);
+/* Baroclin::calc_L_1 (examples/baroclin.cpp:804-986): the inverse linearised
+ * step with the backward block matrix Ab_ (built on the first call), up to 10
+ * iterations with the reference's 1e-8 stop test. */
+int phg_baroclin_calc_L_1(phg_baroclin b, double *u11, double *u21, const double *u1, const double *u2,
+                          const double *z1, const double *z2, const double *bnd, void *stream);
 
 /* --------------------------------------------------------------- serving --
  * Request loop with continuous batching; no reference counterpart (the

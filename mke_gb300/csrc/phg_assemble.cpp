@@ -324,6 +324,19 @@ namespace {
 void baroclin_blocks(const BaroclinParams &c, double a, double b, double e[9]) {
     const double tau = c.tau, mu = c.mu, mu1 = c.mu1, sigma = c.sigma, sigma1 = c.sigma1;
     const double alpha = c.alpha, theta = c.theta;
+    if (c.backward) {   // examples/baroclin.cpp:214-241
+        e[0] = a * (1.0 / tau - 0.5 * (1.0 - theta) * sigma) + (1.0 - theta) * mu * b;
+        e[1] = 0.5 * a * sigma * (1.0 - theta);
+        e[2] = -0.5 * (1.0 - theta) * sigma * a;
+        e[3] = a * (1.0 / tau - 0.5 * (1.0 - theta) * sigma - alpha * alpha * (1.0 - theta) * mu1) +
+               (1.0 - theta) * mu * b;
+        e[4] = a * (-alpha * alpha / tau + alpha * alpha * (1.0 - theta) * sigma1);
+        e[5] = a;
+        e[6] = -b;
+        e[7] = a;
+        e[8] = -b;
+        return;
+    }
     e[0] = a * (1.0 / tau + 0.5 * theta * sigma) - theta * mu * b;
     e[1] = -0.5 * a * sigma * theta;
     e[2] = 0.5 * theta * sigma * a;

@@ -1310,16 +1310,27 @@ extern "C" int phg_barvortex_last_stats(phg_barvortex b, int *il, int *ia, int *
 // rows 1/tau times less accurate: the u rows and the u unknowns are scaled
 // by su, the power of two nearest 1/tau (exact scaling; the solution is the
 // same).
+namespace {
+// one interleaved 4rs block system (A_ of the step or Ab_ of the inverse
+// linearised step) with its block preconditioner and boundary columns
+struct BcSystem {
+    DBuf col, val, a32, dinv, as64, as32, cpl64, cpl32;
+    DevSolveOp op;
+    ColsBufs bc[4];
+    BcCols bcols;
+};
+}  // namespace
+
 struct phg_baroclin_s {
     phg_ops_s *o = nullptr;
     phg_bc_conf c{};
     double theta = 0.5;
     double su = 1.0;
-    DBuf col, val, a32, dinv, as64, as32, cpl64, cpl32;
-    DevSolveOp op;
-    ColsBufs bc[4];
-    BcCols bcols;
+    BcSystem fwd, back;
+    bool have_back = false;
     DBuf lh;
+    // linearised steps: background fields, their Laplacians, 10 Jacobian pairs
+    DBuf Z, dZ, lju, ljv, ljsol, ljac;
     DBuf U, w, dw, FC, un, wn, un1, ju, jv, jsol, jac, FG, MFG, rp, x, xi, nr, done;
     GmresStats each[64];
     int nslots = 0;
@@ -1327,27 +1338,27 @@ struct phg_baroclin_s {
     ~phg_baroclin_s() { if (hdone) cudaFreeHost(hdone); }
 };
 
-extern "C" int phg_baroclin_create(phg_ops o, const phg_bc_conf *c, const double *coriolis, phg_baroclin *out) {
-    if (!o || !c || !out) return fail(PHG_ERR_ARG, "NULL argument");
-    if (!(c->tau > 0) || c->picard_iters < 1 || c->picard_iters > 30) return fail(PHG_ERR_ARG, "bad configuration");
-    auto b = std::make_unique<phg_baroclin_s>();
-    b->o = o;
-    b->c = *c;
-    const Mesh &m = o->mesh->m;
-    const int rs = o->rs, n = 4 * rs;
+namespace {
+
+BaroclinParams bc_params(const phg_bc_conf &c, double theta, bool backward) {
     BaroclinParams bp;
-    bp.tau = c->tau; bp.sigma = c->sigma; bp.mu = c->mu; bp.sigma1 = c->sigma1; bp.mu1 = c->mu1;
-    bp.alpha = c->alpha; bp.theta = b->theta;
+    bp.tau = c.tau; bp.sigma = c.sigma; bp.mu = c.mu; bp.sigma1 = c.sigma1; bp.mu1 = c.mu1;
+    bp.alpha = c.alpha; bp.theta = theta; bp.backward = backward;
+    return bp;
+}
+
+// assemble one 4rs block system, interleave it (unknown q*rs + i -> 4i + q),
+// scale the u rows and u unknowns by su and set up its preconditioner
+int build_bc_system(phg_ops_s *o, const BaroclinParams &bp, double su, BcSystem &S) {
+    const int rs = o->rs, n = 4 * rs;
     Csr A, bcol[4];
-    assemble_baroclin(m, bp, A, bcol);
+    assemble_baroclin(o->mesh->m, bp, A, bcol);
     // interleave: block-order row/column q*rs + i -> 4i + q, columns ascending
     std::vector<std::vector<std::pair<int, double>>> rows(n);
     for (int r = 0; r < A.n; ++r) {
         const int nr_ = 4 * (r % rs) + r / rs;
         for (int k = A.ptr[r]; k < A.ptr[r + 1]; ++k) rows[nr_].push_back({4 * (A.col[k] % rs) + A.col[k] / rs, A.val[k]});
     }
-    b->su = std::ldexp(1.0, (int)std::lround(std::log2(1.0 / c->tau)));
-    const double su = b->su;
     int W = 0;
     for (int i = 0; i < n; ++i) {
         auto &row = rows[i];
@@ -1372,10 +1383,10 @@ extern "C" int phg_baroclin_create(phg_ops o, const phg_bc_conf *c, const double
         for (; k < W; ++k) col[(size_t)k * n + i] = i;
         if (!(dinv[i] != 0.0) || !std::isfinite(dinv[i])) return fail(PHG_ERR_ARG, "zero diagonal in row %d", i);
     }
-    CK(upload(b->col, col)); CK(upload(b->val, val)); CK(upload(b->a32, to_f32(val))); CK(upload(b->dinv, dinv));
-    DevSolveOp &op = b->op;
-    op.A.n = n; op.A.W = W; op.A.col = b->col.as<int>(); op.A.val = b->val.as<double>();
-    op.a32 = b->a32.as<float>(); op.dinv = b->dinv.as<double>();
+    CK(upload(S.col, col)); CK(upload(S.val, val)); CK(upload(S.a32, to_f32(val))); CK(upload(S.dinv, dinv));
+    DevSolveOp &op = S.op;
+    op.A.n = n; op.A.W = W; op.A.col = S.col.as<int>(); op.A.val = S.val.as<double>();
+    op.a32 = S.a32.as<float>(); op.dinv = S.dinv.as<double>();
     if (o->L.op.mgd) {
         // w rows: Jacobi; u rows: -L u = r_u - M w with the Laplacian's multigrid
         op.mg = o->L.op.mg; op.mgd = o->L.op.mgd;
@@ -1383,20 +1394,35 @@ extern "C" int phg_baroclin_create(phg_ops o, const phg_bc_conf *c, const double
         std::vector<double> mv;
         to_ell(o->mesh->ops.idt, o->W, nullptr, mv);
         for (auto &x : mv) x *= su;
-        CK(upload(b->cpl64, mv)); CK(upload(b->cpl32, to_f32(mv)));
-        op.cpl = o->ell(b->cpl64); op.cpl32 = b->cpl32.as<float>();
+        CK(upload(S.cpl64, mv)); CK(upload(S.cpl32, to_f32(mv)));
+        op.cpl = o->ell(S.cpl64); op.cpl32 = S.cpl32.as<float>();
     } else {
         // small meshes (no multigrid hierarchy): Jacobi-scaled GMRES
         std::vector<double> as64(val.size());
         for (size_t e = 0; e < val.size(); ++e) as64[e] = val[e] * dinv[col[e]];
-        CK(upload(b->as64, as64)); CK(upload(b->as32, to_f32(as64)));
-        op.as64 = b->as64.as<double>(); op.as32 = b->as32.as<float>();
+        CK(upload(S.as64, as64)); CK(upload(S.as32, to_f32(as64)));
+        op.as64 = S.as64.as<double>(); op.as32 = S.as32.as<float>();
     }
     int r;
     for (int q = 0; q < 4; ++q) {
-        if ((r = build_cols(bcol[q], b->bc[q]))) return r;
-        b->bcols.c[q] = b->bc[q].c;
+        if ((r = build_cols(bcol[q], S.bc[q]))) return r;
+        S.bcols.c[q] = S.bc[q].c;
     }
+    return PHG_OK;
+}
+
+}  // namespace
+
+extern "C" int phg_baroclin_create(phg_ops o, const phg_bc_conf *c, const double *coriolis, phg_baroclin *out) {
+    if (!o || !c || !out) return fail(PHG_ERR_ARG, "NULL argument");
+    if (!(c->tau > 0) || c->picard_iters < 1 || c->picard_iters > 30) return fail(PHG_ERR_ARG, "bad configuration");
+    auto b = std::make_unique<phg_baroclin_s>();
+    b->o = o;
+    b->c = *c;
+    const int rs = o->rs, n = 4 * rs;
+    b->su = std::ldexp(1.0, (int)std::lround(std::log2(1.0 / c->tau)));
+    int r;
+    if ((r = build_bc_system(o, bc_params(*c, b->theta, false), b->su, b->fwd))) return r;
     std::vector<double> lh(o->V, 0.0);
     if (coriolis) {
         if (is_device_ptr(coriolis)) CK(cudaMemcpy(lh.data(), coriolis, 8 * lh.size(), cudaMemcpyDeviceToHost));
@@ -1458,6 +1484,7 @@ int bc_step_dev(phg_baroclin_s *b, double *u11, double *u21, const double *u1, c
     k.g_w2 = -c.alpha * c.alpha * c.mu1 * (1 - th);
     k.g_u2b = c.alpha * c.alpha * c.sigma1 * (1 - th);
     k.alpha2 = c.alpha * c.alpha;
+    k.ga = k.gb = k.a;
     CK(bc_fcgc(FC, GC, w, w + V, dw, dw + V, U + V, f, g, k, V, s));
     CK(cudaMemcpyAsync(un, U, 16 * (size_t)V, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(wn, w, 16 * (size_t)V, cudaMemcpyDeviceToDevice, s));
@@ -1474,10 +1501,10 @@ int bc_step_dev(phg_baroclin_s *b, double *u11, double *u21, const double *u1, c
         CK(bc_fg(F, G, b->jac.as<double>(), FC, GC, o->imap(), k.alpha2, rs, s));
         // rp = [M F, M G, 0, 0] - boundary columns * bnd, interleaved
         CK(apply_op(o->ML.op.A, DevCols(), F, rs, nullptr, nullptr, 0, nullptr, MF, rs, 2, s));
-        CK(bc_rhs(rp, MF, MG, b->bcols, os ? bnd : nullptr, b->su, rs, s));
+        CK(bc_rhs(rp, MF, MG, b->fwd.bcols, os ? bnd : nullptr, b->su, rs, s));
         // warm start from the current iterate
         CK(bc_pack(x, wn, wn + V, un, un + V, o->imap(), b->su, rs, s));
-        if ((r = solve(o, b->op, rp, x, 1, 4 * rs, o->tol, slot++, s))) return r;
+        if ((r = solve(o, b->fwd.op, rp, x, 1, 4 * rs, o->tol, slot++, s))) return r;
         CK(bc_unpack(wn, wn + V, un1, un1 + V, x, os ? bnd : nullptr, p2io, isb, 1.0 / b->su, V, s));
         // nr = max(dist(u1_n1, u1_n), dist(u2_n1, u2_n)); commit unless stopped
         if ((r = norm_dev(o, un1, un, 2, b->nr.as<double>(), true, true, s))) return r;
@@ -1497,6 +1524,120 @@ int bc_step_dev(phg_baroclin_s *b, double *u11, double *u21, const double *u1, c
 }
 
 }  // namespace
+
+namespace {
+
+// Baroclin::calc_L (kind 0: one iteration, forward matrix A_,
+// examples/baroclin.cpp:620-802) and calc_L_1 (kind 1: up to 10 iterations,
+// backward matrix Ab_, :804-986), linearised around (z1, z2); device pointers
+int bc_lin_dev(phg_baroclin_s *b, int kind, double *u11, double *u21, const double *u1, const double *u2,
+               const double *z1, const double *z2, const double *bnd, cudaStream_t s) {
+    phg_ops_s *o = b->o;
+    const int V = o->V, rs = o->rs, os = o->os;
+    const phg_bc_conf &c = b->c;
+    const double th = b->theta, sg = c.sigma, mu = c.mu, tau = c.tau, al = c.alpha;
+    int r, slot = 0;
+    if (kind == 1 && !b->have_back) {
+        if ((r = build_bc_system(o, bc_params(c, th, true), b->su, b->back))) return r;
+        b->have_back = true;
+    }
+    const BcSystem &S = kind == 0 ? b->fwd : b->back;
+    CK(b->Z.ensure(16 * (size_t)V)); CK(b->dZ.ensure(16 * (size_t)V));
+    CK(b->lju.ensure(80 * (size_t)V)); CK(b->ljv.ensure(80 * (size_t)V));
+    CK(b->ljsol.ensure(8 * 80 * (size_t)rs)); CK(b->ljac.ensure(80 * (size_t)rs));
+    double *U = b->U.as<double>(), *w = b->w.as<double>(), *dw = b->dw.as<double>();
+    double *FC = b->FC.as<double>(), *GC = FC + V, *Z = b->Z.as<double>(), *dZ = b->dZ.as<double>();
+    double *un = b->un.as<double>(), *wn = b->wn.as<double>(), *un1 = b->un1.as<double>();
+    double *xi = b->xi.as<double>(), *x = b->x.as<double>(), *rp = b->rp.as<double>();
+    const int *p2io = o->p2io.as<int>(), *isb = o->isb.as<int>();
+    // inputs first: the outputs may alias them
+    CK(cudaMemcpyAsync(U, u1, 8 * (size_t)V, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(U + V, u2, 8 * (size_t)V, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(Z, z1, 8 * (size_t)V, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(Z + V, z2, 8 * (size_t)V, cudaMemcpyDeviceToDevice, s));
+    // w = L(u), dw = L(w), dz = L(z), all with the boundary values bnd
+    const double *src[3] = {U, w, Z};
+    double *dst[3] = {w, dw, dZ};
+    for (int k = 0; k < 3; ++k) {
+        if ((r = laplace_calc2_dev(o, xi, rs, src[k], V, 2, slot++, s, o->tol))) return r;
+        CK(p2u(dst[k], V, xi, rs, bnd, 0, p2io, isb, V, 2, s));
+    }
+    BcCoef k;
+    if (kind == 0) {
+        k.a = -0.5 * (1.0 - th) * sg; k.b = 0.5 * (1.0 - th) * sg; k.ga = k.gb = k.a;
+        k.mu1t = mu * (1.0 - th);
+        k.g_w2 = -al * al * c.mu1 * (1 - th); k.g_u2b = al * al * c.sigma1 * (1 - th);
+    } else {
+        k.a = 0.5 * th * sg; k.b = -0.5 * th * sg; k.ga = k.gb = 0.5 * th * sg;
+        k.mu1t = -mu * th;
+        k.g_w2 = al * al * c.mu1 * th; k.g_u2b = -al * al * c.sigma1 * th;
+    }
+    k.itau = 1.0 / tau;
+    k.g_u2 = -al * al / tau;
+    k.alpha2 = 0.0;
+    CK(bc_fcgc(FC, GC, w, w + V, dw, dw + V, U + V, nullptr, nullptr, k, V, s));
+    CK(cudaMemcpyAsync(un, U, 16 * (size_t)V, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(wn, w, 16 * (size_t)V, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemsetAsync(b->done.p, 0, 4, s));
+    double *F = b->FG.as<double>(), *G = F + rs, *MF = b->MFG.as<double>(), *MG = MF + rs;
+    const double wa = kind == 0 ? 1.0 - th : th, wb = kind == 0 ? th : 1.0 - th;
+    const double ka2 = kind == 0 ? al * al : -al * al;
+    const int iters = kind == 0 ? 1 : 10;
+    for (int it = 0; it < iters; ++it) {
+        CK(bc_lin_jin(b->lju.as<double>(), b->ljv.as<double>(), U, w, un, wn, Z, dZ, b->lh.as<double>(), wa, wb, V, s));
+        if ((r = jacobian_derivs_dev(o, b->lju.as<double>(), b->ljv.as<double>(), V, b->ljsol.as<double>(), 10, slot++,
+                                     s, o->tol)))
+            return r;
+        CK(jac_combine(b->ljsol.as<double>(), rs, rs, b->ljac.as<double>(), rs, nullptr, 0, nullptr, 10, s));
+        CK(bc_lin_fg(F, G, b->ljac.as<double>(), FC, GC, o->imap(), kind, ka2, rs, s));
+        CK(apply_op(o->ML.op.A, DevCols(), F, rs, nullptr, nullptr, 0, nullptr, MF, rs, 2, s));
+        CK(bc_rhs(rp, MF, MG, S.bcols, os ? bnd : nullptr, b->su, rs, s));
+        CK(bc_pack(x, wn, wn + V, un, un + V, o->imap(), b->su, rs, s));
+        if ((r = solve(o, S.op, rp, x, 1, 4 * rs, o->tol, slot++, s))) return r;
+        CK(bc_unpack(wn, wn + V, un1, un1 + V, x, os ? bnd : nullptr, p2io, isb, 1.0 / b->su, V, s));
+        if ((r = norm_dev(o, un1, un, 2, b->nr.as<double>(), true, true, s))) return r;
+        CK(bc_commit(un, un1, b->nr.as<double>(), b->done.as<int>(), 1e-8, 2 * V, s));   // :797, :981
+        if (it + 1 < iters) {
+            CK(cudaMemcpyAsync(b->hdone, b->done.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            if (*b->hdone) break;
+        }
+    }
+    CK(cudaMemcpyAsync(u11, un, 8 * (size_t)V, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(u21, un + V, 8 * (size_t)V, cudaMemcpyDeviceToDevice, s));
+    b->nslots = slot;
+    return PHG_OK;
+}
+
+}  // namespace
+
+static int bc_linear(phg_baroclin b, int kind, double *u11, double *u21, const double *u1, const double *u2,
+                     const double *z1, const double *z2, const double *bnd, void *stream) {
+    if (!b || !u11 || !u21 || !u1 || !u2 || !z1 || !z2) return fail(PHG_ERR_ARG, "NULL argument");
+    phg_ops_s *o = b->o;
+    cudaStream_t s = o->str(stream);
+    Stage st(o, s);
+    const double *d1, *d2, *dz1, *dz2, *db; double *o1, *o2;
+    CK(st.in(u1, o->V, &d1)); CK(st.in(u2, o->V, &d2)); CK(st.in(z1, o->V, &dz1)); CK(st.in(z2, o->V, &dz2));
+    CK(st.in(bnd, o->os, &db));
+    CK(st.out(u11, o->V, &o1)); CK(st.out(u21, o->V, &o2));
+    if (o->os == 0) db = nullptr;
+    int r = bc_lin_dev(b, kind, o1, o2, d1, d2, dz1, dz2, db, s);
+    if (r) return r;
+    CK(st.finish());
+    if (!st.host) return PHG_OK;
+    return check_stats(o, b->nslots, s, nullptr, b->each);
+}
+
+extern "C" int phg_baroclin_calc_L(phg_baroclin b, double *u11, double *u21, const double *u1, const double *u2,
+                                   const double *z1, const double *z2, const double *bnd, void *stream) {
+    return bc_linear(b, 0, u11, u21, u1, u2, z1, z2, bnd, stream);
+}
+
+extern "C" int phg_baroclin_calc_L_1(phg_baroclin b, double *u11, double *u21, const double *u1, const double *u2,
+                                     const double *z1, const double *z2, const double *bnd, void *stream) {
+    return bc_linear(b, 1, u11, u21, u1, u2, z1, z2, bnd, stream);
+}
 
 extern "C" int phg_baroclin_calc(phg_baroclin b, double *u11, double *u21, const double *u1, const double *u2,
                                  const double *bnd, const double *f, const double *g, void *stream) {

@@ -96,7 +96,9 @@ void assemble_barvortex(const Mesh &m, double c1, double c2, Csr &A, Csr &Abnd);
 // per-boundary-point columns its right-hand side uses, integrated in the row
 // point's chart (examples/baroclin.cpp:245-339): bcol[q] is rs x os for the
 // row block q = 0..3 and carries the summed coefficient of bnd[j].
-struct BaroclinParams { double tau, sigma, mu, sigma1, mu1, alpha, theta; };
+// backward: the entries of Ab_, the matrix of the inverse linearised step
+// (examples/baroclin.cpp:182-243) instead of A_ (:119-180)
+struct BaroclinParams { double tau, sigma, mu, sigma1, mu1, alpha, theta; bool backward = false; };
 void assemble_baroclin(const Mesh &m, const BaroclinParams &p, Csr &A, Csr bcol[4]);
 
 }  // namespace phg

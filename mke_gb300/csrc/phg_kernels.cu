@@ -336,7 +336,7 @@ __global__ void k_bc_fcgc(double *FC, double *GC, const double *w1, const double
         double fc = c.a * w1[t] + c.b * w2[t];
         fc = 1.0 * fc + c.mu1t * dw1[t];
         fc = 1.0 * fc + c.itau * w1[t];
-        double gc = c.a * w1[t] + c.a * w2[t];
+        double gc = c.ga * w1[t] + c.gb * w2[t];
         gc = 1.0 * gc + c.mu1t * dw2[t];
         gc = 1.0 * gc + c.itau * w2[t];
         gc = 1.0 * gc + c.g_u2 * u2[t];
@@ -346,6 +346,58 @@ __global__ void k_bc_fcgc(double *FC, double *GC, const double *w1, const double
         if (g) gc += c.alpha2 * g[t];
         FC[t] = fc;
         GC[t] = gc;
+    }
+}
+
+// Jacobian argument pairs of the linearised steps, in the reference's order
+// (examples/baroclin.cpp:717-776): U = wa u + wb u_n, W = wa w + wb w_n
+//   0 (U1, dz1 + l)  1 (z1, W1)  2 (z2, W2)  3 (U2, dz2)  4 (dz1, W2)
+//   5 (dz2, U1)      6 (U2, dz1 + l)  7 (z2, W1)  8 (z1, U2)  9 (U1, z2)
+__global__ void k_bc_lin_jin(double *ju, double *jv, const double *U, const double *Wv, const double *Un,
+                             const double *Wn, const double *Z, const double *dZ, const double *lh, double wa,
+                             double wb, int V) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < V; t += gridDim.x * blockDim.x) {
+        const double U1 = wa * U[t] + wb * Un[t], U2 = wa * U[V + t] + wb * Un[V + t];
+        const double W1 = wa * Wv[t] + wb * Wn[t], W2 = wa * Wv[V + t] + wb * Wn[V + t];
+        const double z1 = Z[t], z2 = Z[V + t], dz1 = dZ[t], dz2 = dZ[V + t];
+        const double dzl = dz1 + lh[t];
+        const double a[10] = {U1, z1, z2, U2, dz1, dz2, U2, z2, z1, U1};
+        const double b[10] = {dzl, W1, W2, dz2, W2, U1, dzl, W1, U2, z2};
+#pragma unroll
+        for (int k = 0; k < 10; ++k) {
+            ju[(size_t)k * V + t] = a[k];
+            jv[(size_t)k * V + t] = b[k];
+        }
+    }
+}
+
+__global__ void k_bc_lin_fg(double *F, double *G, const double *jac, const double *FC, const double *GC,
+                            const int *inner, int kind, double ka2, int rs) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rs; i += gridDim.x * blockDim.x) {
+        double j[10];
+#pragma unroll
+        for (int k = 0; k < 10; ++k) j[k] = jac[(size_t)k * rs + i];
+        double f, g;
+        if (kind == 0) {
+            f = -1.0 * j[0] + -1.0 * j[1];
+            f = 1.0 * f + -1.0 * j[2];
+            f = 1.0 * f + -1.0 * j[3];
+            g = -1.0 * j[4] + -1.0 * j[5];
+            g = 1.0 * g + -1.0 * j[6];
+            g = 1.0 * g + -1.0 * j[7];
+        } else {
+            f = j[0] + j[1];
+            f = f + j[2];
+            f = f + j[3];
+            g = j[4] + j[5];
+            g = g + j[6];
+            g = g + j[7];
+        }
+        g = 1.0 * g + ka2 * j[8];
+        g = 1.0 * g + ka2 * j[9];
+        const int p = inner[i];
+        F[i] = f + FC[p];
+        G[i] = g + GC[p];
     }
 }
 
@@ -481,6 +533,21 @@ cudaError_t bc_pack(double *x, const double *a, const double *b, const double *c
 cudaError_t bc_unpack(double *a, double *b, double *c, double *d, const double *x, const double *bnd,
                       const int *p2io, const int *isb, double isu, int V, cudaStream_t s) {
     k_bc_unpack<<<grid_for(V), TB, 0, s>>>(a, b, c, d, x, bnd, p2io, isb, isu, V);
+    g_kernel_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t bc_lin_jin(double *ju, double *jv, const double *U, const double *Wv, const double *Un, const double *Wn,
+                       const double *Z, const double *dZ, const double *lh, double wa, double wb, int V,
+                       cudaStream_t s) {
+    k_bc_lin_jin<<<grid_for(V), TB, 0, s>>>(ju, jv, U, Wv, Un, Wn, Z, dZ, lh, wa, wb, V);
+    g_kernel_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t bc_lin_fg(double *F, double *G, const double *jac, const double *FC, const double *GC, const int *inner,
+                      int kind, double ka2, int rs, cudaStream_t s) {
+    k_bc_lin_fg<<<grid_for(rs), TB, 0, s>>>(F, G, jac, FC, GC, inner, kind, ka2, rs);
     g_kernel_launches++;
     return cudaGetLastError();
 }

@@ -60,6 +60,7 @@ struct BcCoef {
     double g_w2;    // -alpha^2 mu1 (1-theta)
     double g_u2b;   //  alpha^2 sigma1 (1-theta)
     double alpha2;  //  alpha^2
+    double ga, gb;  //  GC's w1, w2 coefficients (the step: a, a)
 };
 struct BcCols { DevCols c[4]; };
 cudaError_t bc_fcgc(double *FC, double *GC, const double *w1, const double *w2, const double *dw1, const double *dw2,
@@ -76,5 +77,13 @@ cudaError_t bc_pack(double *x, const double *a, const double *b, const double *c
 cudaError_t bc_unpack(double *a, double *b, double *c, double *d, const double *x, const double *bnd,
                       const int *p2io, const int *isb, double isu, int V, cudaStream_t s);
 cudaError_t bc_commit(double *un, const double *un1, const double *nr, int *done, double tol, int n, cudaStream_t s);
+// linearised steps (examples/baroclin.cpp:620-986): the 10 Jacobian argument
+// pairs (weights wa on the input, wb on the iterate) and the F, G combination
+// (kind 0: calc_L signs, 1: calc_L_1 signs; ka2 the alpha^2 coefficient)
+cudaError_t bc_lin_jin(double *ju, double *jv, const double *U, const double *Wv, const double *Un, const double *Wn,
+                       const double *Z, const double *dZ, const double *lh, double wa, double wb, int V,
+                       cudaStream_t s);
+cudaError_t bc_lin_fg(double *F, double *G, const double *jac, const double *FC, const double *GC, const int *inner,
+                      int kind, double ka2, int rs, cudaStream_t s);
 
 }  // namespace phg

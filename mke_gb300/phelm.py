@@ -102,6 +102,8 @@ SIGNATURES = {
     "phg_baroclin_create": (C.c_int, [_vp, C.POINTER(BcConf), _vp, C.POINTER(_vp)]),
     "phg_baroclin_destroy": (None, [_vp]),
     "phg_baroclin_calc": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "phg_baroclin_calc_L": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "phg_baroclin_calc_L_1": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "phg_serve_create": (C.c_int, [C.POINTER(ServeConf), C.POINTER(_vp)]),
     "phg_serve_preload": (C.c_int, [_vp, C.c_int, C.c_int]),
     "phg_serve_submit": (C.c_int, [_vp, C.POINTER(Request)]),
@@ -438,6 +440,21 @@ class Baroclin:
         _check(lib().phg_baroclin_calc(self._h, _ptr(out1), _ptr(out2), _ptr(_f8(u1)), _ptr(_f8(u2)),
                                        _ptr(_f8(bnd)), _ptr(_f8(f)), _ptr(_f8(g)), _stream(stream)))
         return out1, out2
+
+    def _linear(self, fn, u1, u2, z1, z2, bnd, out1, out2, stream):
+        out1 = np.zeros(self.m.size) if out1 is None else out1
+        out2 = np.zeros(self.m.size) if out2 is None else out2
+        _check(getattr(lib(), fn)(self._h, _ptr(out1), _ptr(out2), _ptr(_f8(u1)), _ptr(_f8(u2)), _ptr(_f8(z1)),
+                                  _ptr(_f8(z2)), _ptr(_f8(bnd)), _stream(stream)))
+        return out1, out2
+
+    def calc_L(self, u1, u2, z1, z2, bnd=None, out1=None, out2=None, stream=None):
+        """Baroclin::calc_L: the step linearised around (z1, z2)."""
+        return self._linear("phg_baroclin_calc_L", u1, u2, z1, z2, bnd, out1, out2, stream)
+
+    def calc_L_1(self, u1, u2, z1, z2, bnd=None, out1=None, out2=None, stream=None):
+        """Baroclin::calc_L_1: the inverse linearised step around (z1, z2)."""
+        return self._linear("phg_baroclin_calc_L_1", u1, u2, z1, z2, bnd, out1, out2, stream)
 
 
 def device_bytes():

@@ -57,3 +57,20 @@ def test_calc_L_1_accumulates_and_aliases(golden):
     bv.calc_L(u, zz, out=u, stream=s)
     s.synchronize()
     assert rel(u.cpu().numpy(), ref) <= 1e-12
+
+
+@pytest.mark.parametrize("precision", [phelm.PHG_FP64, phelm.PHG_MIXED])
+@pytest.mark.parametrize("level", [1, 2, 3])
+def test_baroclin_linear_steps_vs_reference(golden, level, precision):
+    """Baroclin::calc_L / calc_L_1 around (z1, z2) = (in_u, in_v) applied to
+    (in_v, in_u) (examples/baroclin.cpp:620-986), zero boundary."""
+    g = golden(f"ref_L{level}.npz")
+    m = phelm.Mesh.sphere(level)
+    ops = phelm.Operators(m, precision, tol=1e-12)
+    lat, _ = m.latlon()
+    bc = phelm.Baroclin(ops, picard_iters=3, coriolis=np.sin(lat))
+    z = np.zeros(m.outer_size)
+    for which, fn in (("L", bc.calc_L), ("L1", bc.calc_L_1)):
+        a, b = fn(g["in_v"], g["in_u"], g["in_u"], g["in_v"], z)
+        assert rel(a, g[f"out_bc_{which}_u1"]) <= TOL, which
+        assert rel(b, g[f"out_bc_{which}_u2"]) <= TOL, which
