@@ -70,6 +70,20 @@ int phg_mesh_generate(int level, phg_mesh *out);
  * the reference's text format (charts stdsphere1..4). */
 int phg_mesh_load_file(const char *path, phg_mesh *out);
 void phg_mesh_destroy(phg_mesh m);
+/* The reference's mesh text file (the output of "mke_mesh_sphere --type full
+ * --coord local", utils/icosahedron.cpp:268-457).  For a generated mesh the
+ * file equals the reference generator's byte for byte; a loaded mesh is
+ * written from its parsed coordinates. */
+int phg_mesh_save_file(phg_mesh m, const char *path);
+/* print_function / print_inner_function (src/phelm.cpp:160-321): a full
+ * vector ans[V] as text; x, y, z (host, V values each, or NULL) replace the
+ * zone-0 coordinates (u, v, 0), i.e. the values of the reference's x_t
+ * callbacks at the points.  The inner variant lists inner points and the
+ * triangles made of them.  Host memory only. */
+int phg_print_function(phg_mesh m, const char *path, const double *ans, const double *x, const double *y,
+                       const double *z);
+int phg_print_inner_function(phg_mesh m, const char *path, const double *ans, const double *x, const double *y,
+                             const double *z);
 /* Mesh::size / inner_size / outer_size / tr.size() (src/mesh.h:381-383). */
 int phg_mesh_info(phg_mesh m, int *V, int *T, int *rs, int *os);
 /* Copies of Mesh::ps (xyz: V x 3; uv: V x 4 x 2 chart coordinates), Mesh::tr

@@ -141,6 +141,39 @@ static void mesh_release(phg_mesh m) {
 
 extern "C" void phg_mesh_destroy(phg_mesh m) { mesh_release(m); }
 
+extern "C" int phg_mesh_save_file(phg_mesh h, const char *path) {
+    if (!h || !path) return fail(PHG_ERR_ARG, "NULL argument");
+    FILE *f = fopen(path, "wb");
+    if (!f) return fail(PHG_ERR_IO, "cannot open %s", path);
+    const bool ok = save_mesh_text(f, h->m);
+    const bool closed = fclose(f) == 0;
+    if (!ok) return fail(PHG_ERR_ARG, "only 4-chart sphere meshes can be written");
+    if (!closed) return fail(PHG_ERR_IO, "cannot write %s", path);
+    return PHG_OK;
+}
+
+static int print_common(phg_mesh h, const char *path, const double *ans, const double *x, const double *y,
+                        const double *z, bool inner) {
+    if (!h || !path || !ans) return fail(PHG_ERR_ARG, "NULL argument");
+    if (is_device_ptr(ans) || (x && is_device_ptr(x)) || (y && is_device_ptr(y)) || (z && is_device_ptr(z)))
+        return fail(PHG_ERR_ARG, "host arrays only");
+    FILE *f = fopen(path, "wb");
+    if (!f) return fail(PHG_ERR_IO, "cannot open %s", path);
+    print_function_text(f, h->m, ans, x, y, z, inner);
+    if (fclose(f) != 0) return fail(PHG_ERR_IO, "cannot write %s", path);
+    return PHG_OK;
+}
+
+extern "C" int phg_print_function(phg_mesh h, const char *path, const double *ans, const double *x, const double *y,
+                                  const double *z) {
+    return print_common(h, path, ans, x, y, z, false);
+}
+
+extern "C" int phg_print_inner_function(phg_mesh h, const char *path, const double *ans, const double *x,
+                                        const double *y, const double *z) {
+    return print_common(h, path, ans, x, y, z, true);
+}
+
 extern "C" int phg_mesh_info(phg_mesh h, int *V, int *T, int *rs, int *os) {
     if (!h) return fail(PHG_ERR_ARG, "NULL mesh");
     if (V) *V = h->m.V;

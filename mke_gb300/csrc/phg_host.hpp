@@ -27,6 +27,7 @@ struct Mesh {
     std::vector<int> orig;          // point -> index before the Cuthill-McKee reorder
     std::vector<int> par_a, par_b;  // pre-reorder index -> endpoints (pre-reorder, level-1
                                     // numbering) of the coarse edge it bisects; -1 for coarse points
+    std::vector<double> raw_xyz;    // point coordinates before the text round trip
 
     double u(int p, int z) const { return uv[8 * (size_t)p + 2 * z]; }
     double v(int p, int z) const { return uv[8 * (size_t)p + 2 * z + 1]; }
@@ -40,6 +41,15 @@ struct Mesh {
 bool generate_sphere(int level, Mesh &m, std::string &err);
 // Parse the reference's mesh text format (src/mesh.cpp:323-519).
 bool load_mesh_text(FILE *f, Mesh &m, std::string &err);
+// The reference's mesh text (utils/icosahedron.cpp:268-457, full sphere with
+// local charts).  Generated meshes print their coordinates before the text
+// round trip, so the file equals mke_mesh_sphere's byte for byte; loaded
+// meshes print the parsed values.
+bool save_mesh_text(FILE *f, const Mesh &m);
+// print_function / print_inner_function (src/phelm.cpp:160-321); x, y, z:
+// values at every point replacing the zone-0 (u, v, 0), or null
+void print_function_text(FILE *f, const Mesh &m, const double *ans, const double *x, const double *y,
+                         const double *z, bool inner_only);
 // Finish a mesh whose points/triangles/boundary flags are filled in:
 // inner/outer/p2io in point order and the point->triangle adjacency.
 void finish_mesh(Mesh &m);

@@ -149,6 +149,8 @@ bool generate_sphere(int level, Mesh &m, std::string &err) {
     m.xyz.resize(3 * (size_t)V); m.uv.resize(8 * (size_t)V); m.bnd.assign(V, 0);
     std::vector<P3> np(V);
     for (int i = 0; i < V; ++i) np[perm[i]] = pts[i];
+    m.raw_xyz.resize(3 * (size_t)V);
+    for (int i = 0; i < V; ++i) { m.raw_xyz[3 * i] = np[i].x; m.raw_xyz[3 * i + 1] = np[i].y; m.raw_xyz[3 * i + 2] = np[i].z; }
     for (int i = 0; i < V; ++i) {
         const double x = np[i].x, y = np[i].y, z = np[i].z;
         m.xyz[3 * i] = text16(x); m.xyz[3 * i + 1] = text16(y); m.xyz[3 * i + 2] = text16(z);
@@ -249,6 +251,76 @@ bool load_mesh_text(FILE *f, Mesh &m, std::string &err) {
     for (int i = 0; i < m.V; ++i)
         if (m.adj_ptr[i + 1] == m.adj_ptr[i]) { err = "point without triangles"; return false; }
     return true;
+}
+
+}  // namespace phg
+
+namespace phg {
+
+bool save_mesh_text(FILE *f, const Mesh &m) {
+    if (m.nz != 4) return false;
+    const bool raw = m.raw_xyz.size() == 3 * (size_t)m.V;
+    if (m.level >= 0)   // the generator's command line and build tag (utils/icosahedron.cpp:565-570)
+        std::fprintf(f, "#cmd:mke_mesh_sphere --type full --coord local --iter %d \n#build:$Id$\n", m.level);
+    std::fprintf(f, "#points:%lu\n", (unsigned long)m.V);
+    std::fprintf(f, "#triangles:%lu\n", (unsigned long)m.T);
+    std::fprintf(f, "# zone1 ; zone2 ; zone 3; ... \n");
+    std::fprintf(f, "# u = theta  [-pi/2, pi/2]\n# v = lambda [0, 2pi]\n");
+    std::fprintf(f, "#predef: zone 1 stdsphere1\n");
+    std::fprintf(f, "#predef: zone 2 stdsphere2\n");
+    std::fprintf(f, "# zone 1\n# x = cos(u)*cos(v) \n# y = cos(u)*sin(v) \n# z = sin(u) \n"
+                    "# zone 2\n# x = -cos(u)*cos(v) \n# y = -cos(u)*sin(v) \n# z = sin(u) \n");
+    std::fprintf(f, "#predef: zone 3 stdsphere3\n");
+    std::fprintf(f, "#predef: zone 4 stdsphere4\n");
+    std::fprintf(f, "# zone 3\n# x = cos(u)*cos(v) \n# y = cos(u)*sin(v) \n# z = -sin(u) \n"
+                    "# zone 4\n# x = cos(u)*cos(v) \n# y = -cos(u)*sin(v) \n# z = sin(u) \n");
+    for (int i = 0; i < m.V; ++i) {
+        const double *p = raw ? &m.raw_xyz[3 * (size_t)i] : &m.xyz[3 * (size_t)i];
+        const double x = p[0], y = p[1], z = p[2];
+        std::fprintf(f, "%.16lf %.16lf %.16lf", x, y, z);
+        if (raw) {
+            const double c[4][3] = {{x, y, z}, {-x, -y, z}, {x, -z, y}, {x, z, -y}};
+            for (int k = 0; k < 4; ++k)
+                std::fprintf(f, " ; %.16lf %.16lf ", lat_of(c[k][0], c[k][1], c[k][2]), lon_of(c[k][0], c[k][1], c[k][2]));
+        } else {
+            for (int k = 0; k < 4; ++k) std::fprintf(f, " ; %.16lf %.16lf ", m.u(i, k), m.v(i, k));
+        }
+        std::fprintf(f, "\n");
+    }
+    std::fprintf(f, "# triangles %lu \n", (unsigned long)m.T);
+    for (int t = 0; t < m.T; ++t) {
+        std::fprintf(f, "%d %d %d ", m.tri[3 * t] + 1, m.tri[3 * t + 1] + 1, m.tri[3 * t + 2] + 1);
+        if (m.tz[t] > 0) std::fprintf(f, " ; %d ", m.tz[t] + 1);
+        std::fprintf(f, "\n");
+    }
+    std::fprintf(f, "# boundary \n");
+    for (int i = 0; i < m.V; ++i)
+        if (m.bnd[i]) std::fprintf(f, "%lu \n", (unsigned long)(i + 1));
+    return true;
+}
+
+void print_function_text(FILE *f, const Mesh &m, const double *ans, const double *x, const double *y,
+                         const double *z, bool inner_only) {
+    const int n = inner_only ? m.rs : m.V;
+    std::fprintf(f, "# points %lu\n", (unsigned long)n);
+    for (int k = 0; k < n; ++k) {
+        const int p = inner_only ? m.inner[k] : k;
+        const double u = m.u(p, 0), v = m.v(p, 0);
+        std::fprintf(f, "%.16lf ", x ? x[p] : u);
+        std::fprintf(f, "%.16lf ", y ? y[p] : v);
+        std::fprintf(f, "%.16lf ", z ? z[p] : 0.0);
+        std::fprintf(f, "%.16lf %.16lf %.16lf \n", ans[p], u, v);
+    }
+    std::fprintf(f, "# triangles %lu\n", (unsigned long)m.T);
+    for (int t = 0; t < m.T; ++t) {
+        const int a = m.tri[3 * t], b = m.tri[3 * t + 1], c = m.tri[3 * t + 2];
+        if (!inner_only) std::fprintf(f, "%d %d %d\n", a + 1, b + 1, c + 1);
+        // the reference prints the triangles whose three points are all NOT
+        // regular (src/phelm.cpp:208-218), i.e. boundary triangles; kept as is
+        else if (m.bnd[a] && m.bnd[b] && m.bnd[c])
+            std::fprintf(f, "%d %d %d\n", m.p2io[a] + 1, m.p2io[b] + 1, m.p2io[c] + 1);
+    }
+    std::fprintf(f, "# end \n");
 }
 
 }  // namespace phg

@@ -65,6 +65,9 @@ SIGNATURES = {
     "phg_mesh_generate": (C.c_int, [C.c_int, C.POINTER(_vp)]),
     "phg_mesh_load_file": (C.c_int, [C.c_char_p, C.POINTER(_vp)]),
     "phg_mesh_destroy": (None, [_vp]),
+    "phg_mesh_save_file": (C.c_int, [_vp, C.c_char_p]),
+    "phg_print_function": (C.c_int, [_vp, C.c_char_p, _vp, _vp, _vp, _vp]),
+    "phg_print_inner_function": (C.c_int, [_vp, C.c_char_p, _vp, _vp, _vp, _vp]),
     "phg_mesh_info": (C.c_int, [_vp, _ip, _ip, _ip, _ip]),
     "phg_mesh_arrays": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "phg_mesh_maps": (C.c_int, [_vp, _vp, _vp, _vp]),
@@ -204,6 +207,16 @@ class Mesh:
         p2io = np.zeros(self.size, np.int32)
         _check(lib().phg_mesh_maps(self._h, _ptr(inner), _ptr(outer), _ptr(p2io)))
         return {"inner": inner, "outer": outer[: self.outer_size], "p2io": p2io}
+
+    def save(self, path: str):
+        """The reference's mesh text file (as mke_mesh_sphere writes it)."""
+        _check(lib().phg_mesh_save_file(self._h, os.fsencode(path)))
+
+    def print_function(self, path: str, ans, x=None, y=None, z=None, inner: bool = False):
+        """print_function / print_inner_function of a full vector (host arrays)."""
+        ans, x, y, z = _f8(ans), _f8(x), _f8(y), _f8(z)
+        fn = lib().phg_print_inner_function if inner else lib().phg_print_function
+        _check(fn(self._h, os.fsencode(path), _ptr(ans), _ptr(x), _ptr(y), _ptr(z)))
 
     def latlon(self):
         """Zone-0 chart coordinates (latitude, longitude) of every point."""

@@ -196,6 +196,9 @@ int main(int argc, char **argv)
 			j.calc1(&a[0], &u[0], &v[0], &bnd[0]); wf8(dir, "out_jac_calc1", a);
 		}
 		wf8(dir, "out_norms", ns);
+		// the text output routines (src/phelm.cpp:160-321), default coordinates
+		print_function((dir + "/print_function.txt").c_str(), &u[0], m);
+		print_inner_function((dir + "/print_inner_function.txt").c_str(), &u[0], m);
 	}
 
 	BarVortexConf conf;

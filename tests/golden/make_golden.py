@@ -16,6 +16,7 @@ from __future__ import annotations
 
 import argparse
 import hashlib
+import shutil
 import os
 import subprocess
 import sys
@@ -51,6 +52,7 @@ def run_level(ref_bin, level, work, bv_steps=0, bc_steps=0, seed=1234, extra=())
                         "--iter", str(level)], stdout=f, check=True)
     out = os.path.join(work, f"L{level}")
     os.makedirs(out, exist_ok=True)
+    shutil.copyfile(mesh_txt, os.path.join(out, "mesh_text.txt"))
     # first pass: mesh only, to learn the coordinates for the inputs
     subprocess.run([os.path.join(ref_bin, "ref_driver"), mesh_txt, out], check=True,
                    stderr=subprocess.DEVNULL)
@@ -74,6 +76,10 @@ def load_dir(d):
     for f in os.listdir(d):
         if f.endswith(".npy"):
             r[f[:-4]] = np.load(os.path.join(d, f))
+        elif f.endswith(".txt"):   # text outputs: their SHA-256 (and without the first line: the
+            data = open(os.path.join(d, f), "rb").read()   # generator's "#cmd:" line names its path)
+            r["out_text_sha256_" + f[:-4]] = np.array(hashlib.sha256(data).hexdigest())
+            r["out_text_sha256_" + f[:-4] + "_body"] = np.array(hashlib.sha256(data.split(b"\n", 1)[1]).hexdigest())
     return r
 
 

@@ -118,3 +118,27 @@ def test_no_gpu_fails_loudly():
     with pytest.raises(phelm.PhgError) as e:
         phelm.Operators(m)
     assert e.value.code == 2
+
+
+@pytest.mark.parametrize("level", [1, 2, 3, 4, 5])
+def test_text_outputs_match_reference(golden, level, tmp_path):
+    """The mesh file (as mke_mesh_sphere writes it, utils/icosahedron.cpp:268-457)
+    and print_function / print_inner_function (src/phelm.cpp:160-321) give the
+    reference's bytes; the mesh file's first line is the generator's command
+    line with its path, so it is compared from the second line on."""
+    import hashlib
+    g = golden(f"ref_L{level}.npz")
+    m = phelm.Mesh.sphere(level)
+    p = tmp_path / "mesh.txt"
+    m.save(str(p))
+    body = p.read_bytes().split(b"\n", 1)[1]
+    assert hashlib.sha256(body).hexdigest() == str(g["out_text_sha256_mesh_text_body"])
+    for inner, key in ((False, "print_function"), (True, "print_inner_function")):
+        q = tmp_path / f"{key}.txt"
+        m.print_function(str(q), g["in_u"], inner=inner)
+        assert hashlib.sha256(q.read_bytes()).hexdigest() == str(g["out_text_sha256_" + key]), key
+    # and the written file loads back into the same mesh
+    m2 = phelm.Mesh.load(str(p))
+    a, b = m.arrays(), m2.arrays()
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
