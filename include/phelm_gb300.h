@@ -84,6 +84,12 @@ int phg_print_function(phg_mesh m, const char *path, const double *ans, const do
                        const double *z);
 int phg_print_inner_function(phg_mesh m, const char *path, const double *ans, const double *x, const double *y,
                              const double *z);
+/* Binary checkpoints of a model state (nfields full vectors of the mesh, the
+ * model time and step count); the file records the mesh (size and a digest of
+ * its points and triangles) and loading into another mesh is refused.  No
+ * reference counterpart.  Host memory only. */
+int phg_state_save(phg_mesh m, const char *path, const double *const *fields, int nfields, double t, long long step);
+int phg_state_load(phg_mesh m, const char *path, double *const *fields, int nfields, double *t, long long *step);
 /* Mesh::size / inner_size / outer_size / tr.size() (src/mesh.h:381-383). */
 int phg_mesh_info(phg_mesh m, int *V, int *T, int *rs, int *os);
 /* Copies of Mesh::ps (xyz: V x 3; uv: V x 4 x 2 chart coordinates), Mesh::tr

@@ -164,6 +164,63 @@ static int print_common(phg_mesh h, const char *path, const double *ans, const d
     return PHG_OK;
 }
 
+// Binary state checkpoints: "PHGSTAT1", int32 V, int32 nfields, float64 t,
+// int64 step, uint64 mesh digest (FNV-1a over the point coordinates and
+// triangles), then nfields x V float64, all little-endian as in memory.
+static unsigned long long mesh_digest(const Mesh &m) {
+    unsigned long long h = 1469598103934665603ULL;
+    auto add = [&](const void *p, size_t n) {
+        const unsigned char *c = (const unsigned char *)p;
+        for (size_t i = 0; i < n; ++i) { h ^= c[i]; h *= 1099511628211ULL; }
+    };
+    add(m.xyz.data(), 8 * m.xyz.size());
+    add(m.tri.data(), 4 * m.tri.size());
+    return h;
+}
+
+extern "C" int phg_state_save(phg_mesh h, const char *path, const double *const *fields, int nfields, double t,
+                              long long step) {
+    if (!h || !path || !fields || nfields < 1) return fail(PHG_ERR_ARG, "bad argument");
+    for (int k = 0; k < nfields; ++k)
+        if (!fields[k] || is_device_ptr(fields[k])) return fail(PHG_ERR_ARG, "field %d: host array required", k);
+    FILE *f = fopen(path, "wb");
+    if (!f) return fail(PHG_ERR_IO, "cannot open %s", path);
+    const int V = h->m.V;
+    const unsigned long long dg = mesh_digest(h->m);
+    bool ok = fwrite("PHGSTAT1", 1, 8, f) == 8 && fwrite(&V, 4, 1, f) == 1 && fwrite(&nfields, 4, 1, f) == 1 &&
+              fwrite(&t, 8, 1, f) == 1 && fwrite(&step, 8, 1, f) == 1 && fwrite(&dg, 8, 1, f) == 1;
+    for (int k = 0; ok && k < nfields; ++k) ok = fwrite(fields[k], 8, (size_t)V, f) == (size_t)V;
+    ok = (fclose(f) == 0) && ok;
+    return ok ? PHG_OK : fail(PHG_ERR_IO, "cannot write %s", path);
+}
+
+extern "C" int phg_state_load(phg_mesh h, const char *path, double *const *fields, int nfields, double *t,
+                              long long *step) {
+    if (!h || !path || !fields || nfields < 1) return fail(PHG_ERR_ARG, "bad argument");
+    FILE *f = fopen(path, "rb");
+    if (!f) return fail(PHG_ERR_IO, "cannot open %s", path);
+    char magic[8];
+    int V = 0, nf = 0;
+    double tt = 0;
+    long long st = 0;
+    unsigned long long dg = 0;
+    bool ok = fread(magic, 1, 8, f) == 8 && !memcmp(magic, "PHGSTAT1", 8) && fread(&V, 4, 1, f) == 1 &&
+              fread(&nf, 4, 1, f) == 1 && fread(&tt, 8, 1, f) == 1 && fread(&st, 8, 1, f) == 1 &&
+              fread(&dg, 8, 1, f) == 1;
+    if (!ok) { fclose(f); return fail(PHG_ERR_IO, "%s: not a state checkpoint", path); }
+    if (V != h->m.V || dg != mesh_digest(h->m)) { fclose(f); return fail(PHG_ERR_ARG, "%s: written for another mesh", path); }
+    if (nf != nfields) { fclose(f); return fail(PHG_ERR_ARG, "%s: holds %d fields, %d requested", path, nf, nfields); }
+    for (int k = 0; ok && k < nfields; ++k) {
+        if (!fields[k] || is_device_ptr(fields[k])) { fclose(f); return fail(PHG_ERR_ARG, "field %d: host array required", k); }
+        ok = fread(fields[k], 8, (size_t)V, f) == (size_t)V;
+    }
+    fclose(f);
+    if (!ok) return fail(PHG_ERR_IO, "%s: truncated", path);
+    if (t) *t = tt;
+    if (step) *step = st;
+    return PHG_OK;
+}
+
 extern "C" int phg_print_function(phg_mesh h, const char *path, const double *ans, const double *x, const double *y,
                                   const double *z) {
     return print_common(h, path, ans, x, y, z, false);

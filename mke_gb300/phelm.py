@@ -68,6 +68,8 @@ SIGNATURES = {
     "phg_mesh_save_file": (C.c_int, [_vp, C.c_char_p]),
     "phg_print_function": (C.c_int, [_vp, C.c_char_p, _vp, _vp, _vp, _vp]),
     "phg_print_inner_function": (C.c_int, [_vp, C.c_char_p, _vp, _vp, _vp, _vp]),
+    "phg_state_save": (C.c_int, [_vp, C.c_char_p, C.POINTER(_vp), C.c_int, C.c_double, C.c_longlong]),
+    "phg_state_load": (C.c_int, [_vp, C.c_char_p, C.POINTER(_vp), C.c_int, _dp, C.POINTER(C.c_longlong)]),
     "phg_mesh_info": (C.c_int, [_vp, _ip, _ip, _ip, _ip]),
     "phg_mesh_arrays": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "phg_mesh_maps": (C.c_int, [_vp, _vp, _vp, _vp]),
@@ -217,6 +219,20 @@ class Mesh:
         ans, x, y, z = _f8(ans), _f8(x), _f8(y), _f8(z)
         fn = lib().phg_print_inner_function if inner else lib().phg_print_function
         _check(fn(self._h, os.fsencode(path), _ptr(ans), _ptr(x), _ptr(y), _ptr(z)))
+
+    def save_state(self, path: str, fields, t: float = 0.0, step: int = 0):
+        """Binary checkpoint of full vectors (host arrays) with the model time and step."""
+        arrs = [np.ascontiguousarray(f, dtype=np.float64) for f in fields]
+        ptrs = (C.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+        _check(lib().phg_state_save(self._h, os.fsencode(path), ptrs, len(arrs), t, step))
+
+    def load_state(self, path: str, nfields: int):
+        """(fields, t, step) from a checkpoint written for this mesh."""
+        arrs = [np.zeros(self.size) for _ in range(nfields)]
+        ptrs = (C.c_void_p * nfields)(*[a.ctypes.data for a in arrs])
+        t, st = C.c_double(), C.c_longlong()
+        _check(lib().phg_state_load(self._h, os.fsencode(path), ptrs, nfields, C.byref(t), C.byref(st)))
+        return arrs, t.value, st.value
 
     def latlon(self):
         """Zone-0 chart coordinates (latitude, longitude) of every point."""

@@ -142,3 +142,17 @@ def test_text_outputs_match_reference(golden, level, tmp_path):
     a, b = m.arrays(), m2.arrays()
     for k in a:
         assert np.array_equal(a[k], b[k]), k
+
+
+def test_state_checkpoint_round_trip(tmp_path):
+    m = phelm.Mesh.sphere(3)
+    rng = np.random.default_rng(5)
+    u1, u2 = rng.standard_normal(m.size), rng.standard_normal(m.size)
+    p = str(tmp_path / "state.bin")
+    m.save_state(p, [u1, u2], t=0.25, step=250)
+    (a, b), t, step = m.load_state(p, 2)
+    assert np.array_equal(a, u1) and np.array_equal(b, u2) and t == 0.25 and step == 250
+    with pytest.raises(phelm.PhgError):
+        phelm.Mesh.sphere(4).load_state(p, 2)      # another mesh
+    with pytest.raises(phelm.PhgError):
+        m.load_state(p, 3)                         # another field count
