@@ -213,6 +213,21 @@ int phg_barvortex_calc(phg_barvortex b, double *u1, const double *u, const doubl
  * within the solve tolerance.  No reference counterpart (ensemble mode). */
 int phg_barvortex_calc_batch(phg_barvortex b, int nmembers, double *u1, const double *u,
                              const double *bnd_u, const double *bnd_w, const double *forcing, void *stream);
+/* nsteps steps of nmembers states in place (member-major u, as in
+ * phg_barvortex_calc_batch), the same bnd_u / bnd_w / forcing every step:
+ * the loop of examples/test_barvortex.cpp:529 (calc(u, u, ...) per step).
+ * One step is captured as a CUDA graph and replayed (one graph launch per
+ * step); the graph stays on the handle and serves later calls with the same
+ * members, pointers and stream, as long as no buffer of the library was
+ * reallocated since (otherwise the first step of the call is enqueued kernel
+ * by kernel and the next one re-captured).  Results equal nsteps
+ * phg_barvortex_calc_batch calls bit for bit.  With host arrays the call
+ * returns after the copy back and judges every solve of every step; with
+ * device arrays it returns at once, and phg_barvortex_last_stats judges every
+ * step run since the previous check.  stream: a created stream or NULL (the
+ * handle's own), not the legacy default stream. */
+int phg_barvortex_run(phg_barvortex b, int nmembers, int nsteps, double *u, const double *bnd_u,
+                      const double *bnd_w, const double *forcing, void *stream);
 /* BarVortex::calc_L (examples/barvortex_impl.h:326-400): the step
  * linearised around the background z, applied to u (u1 = L_z u).  Outputs
  * may alias inputs. */

@@ -43,6 +43,9 @@ int fail(int code, const char *fmt, ...) {
 // (a serving lane creates, uses and frees its handles on its own thread)
 std::atomic<long long> g_dev_bytes{0};
 thread_local long long t_dev_bytes = 0;
+// bumped by every device (re)allocation: a captured step graph holds raw
+// buffer addresses and is re-captured when this moved since its capture
+std::atomic<long long> g_alloc_epoch{0};
 
 struct DBuf {
     void *p = nullptr;
@@ -62,6 +65,7 @@ struct DBuf {
         if (bytes <= n) return cudaSuccess;
         release();
         cudaError_t e = cudaMalloc(&p, bytes ? bytes : 1);
+        g_alloc_epoch++;
         if (e == cudaSuccess) {
             n = bytes;
             g_dev_bytes += (long long)n;
@@ -1034,6 +1038,23 @@ struct phg_barvortex_s {
     SolveOpBufs Aback;
     ColsBufs Abackb;
     DBuf lz, lp1, lp2, lp3, lju, ljv, ljac, ljf, lx, lrp, lin;
+    // phg_barvortex_run: one step captured as a CUDA graph, replayed per step;
+    // valid for the key it was captured with
+    struct GraphKey {
+        int nv = 0;
+        const double *u = nullptr, *bnd_u = nullptr, *bnd_w = nullptr, *forcing = nullptr;
+        cudaStream_t s = nullptr;
+        long long epoch = -1;
+        bool operator==(const GraphKey &k) const {
+            return nv == k.nv && u == k.u && bnd_u == k.bnd_u && bnd_w == k.bnd_w && forcing == k.forcing &&
+                   s == k.s && epoch == k.epoch;
+        }
+    } gkey;
+    cudaGraphExec_t gexec = nullptr;
+    long long g_launches = 0;   // kernels in one replay
+    DBuf agg;                   // solve records folded over the steps of runs since the last check
+    bool agg_pending = false;
+    ~phg_barvortex_s() { if (gexec) cudaGraphExecDestroy(gexec); }
 };
 
 extern "C" int phg_barvortex_create(phg_ops o, const phg_bv_conf *c, const double *coriolis, phg_barvortex *out) {
@@ -1174,6 +1195,102 @@ extern "C" int phg_barvortex_calc_batch(phg_barvortex b, int nmembers, double *u
                                         const double *bnd_u, const double *bnd_w, const double *forcing,
                                         void *stream) {
     return bv_calc(b, nmembers, u1, u, bnd_u, bnd_w, forcing, stream);
+}
+
+// judge the solves folded into b->agg since the last check
+static int bv_check_agg(phg_barvortex_s *b, cudaStream_t s) {
+    GmresStats a{};
+    CK(cudaMemcpyAsync(&a, b->agg.p, sizeof a, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    b->agg_pending = false;
+    const double tol = b->o->tol;
+    if (a.status == 2) return fail(PHG_ERR_TIMEOUT, "device barrier wait timed out");
+    if (a.status == 1 && !(a.relres <= std::max(1e3 * tol, 1e-8)))
+        return fail(PHG_ERR_NOT_CONVERGED, "GMRES stopped at relative residual %.3e", a.relres);
+    return PHG_OK;
+}
+
+// nsteps steps in place.  With a graph captured for this key every step is
+// one replay; otherwise the first step is enqueued kernel by kernel (it
+// sizes every buffer) and the next one is captured.
+static int bv_run(phg_barvortex b, int nv, int nsteps, double *u, const double *bnd_u, const double *bnd_w,
+                  const double *forcing, void *stream) {
+    if (!b || !u || nv < 1 || nsteps < 0) return fail(PHG_ERR_ARG, "bad argument");
+    if (nsteps == 0) return PHG_OK;
+    phg_ops_s *o = b->o;
+    cudaStream_t s = o->str(stream);
+    if (s == cudaStreamLegacy || s == cudaStreamPerThread)
+        return fail(PHG_ERR_ARG, "a captured step needs a created stream (pass NULL for the handle's own)");
+    int r = bv_reserve(b, nv);
+    if (r) return r;
+    CK(b->agg.ensure(sizeof(GmresStats)));
+    Stage st(o, s);
+    const double *dbu, *dbw, *df, *du;
+    CK(st.in(u, (size_t)o->V * nv, &du));
+    double *dio = const_cast<double *>(du);
+    if (st.host) st.outs.push_back({u, dio, (size_t)o->V * nv});
+    CK(st.in(bnd_u, (size_t)o->os * nv, &dbu));
+    CK(st.in(bnd_w, (size_t)o->os * nv, &dbw));
+    CK(st.in(forcing, (size_t)o->V, &df));
+    if (o->os == 0) { dbu = nullptr; dbw = nullptr; }
+    GmresStats *agg = b->agg.as<GmresStats>(), *slots = o->stats.as<GmresStats>();
+    if (!b->agg_pending) CK(cudaMemsetAsync(agg, 0, sizeof(GmresStats), s));
+    b->agg_pending = true;
+    phg_barvortex_s::GraphKey k;
+    k.nv = nv; k.u = dio; k.bnd_u = dbu; k.bnd_w = dbw; k.forcing = df; k.s = s;
+    k.epoch = g_alloc_epoch.load();
+    int left = nsteps;
+    if (!b->gexec || !(k == b->gkey)) {
+        if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; }
+        if ((r = bv_step_dev(b, nv, dio, dio, dbu, dbw, df, s))) return r;
+        CK(stats_fold(slots, b->nslots, agg, s));
+        --left;
+        k.epoch = g_alloc_epoch.load();
+        if (left > 0) {
+            const bool prof = o->prof;
+            o->prof = false;
+            const long long l0 = g_kernel_launches.load();
+            CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            r = bv_step_dev(b, nv, dio, dio, dbu, dbw, df, s);
+            cudaError_t ef = r ? cudaSuccess : stats_fold(slots, b->nslots, agg, s);
+            cudaGraph_t g = nullptr;
+            cudaError_t ec = cudaStreamEndCapture(s, &g);
+            o->prof = prof;
+            const long long nl = g_kernel_launches.load() - l0;
+            g_kernel_launches -= nl;   // captured, not run
+            if (r || ef != cudaSuccess || ec != cudaSuccess || !g) {
+                if (g) cudaGraphDestroy(g);
+                if (r) return r;
+                return fail(PHG_ERR_CUDA, "step capture: %s", cudaGetErrorString(ef != cudaSuccess ? ef : ec));
+            }
+            cudaError_t ei = cudaGraphInstantiate(&b->gexec, g, 0);
+            cudaGraphDestroy(g);
+            if (ei != cudaSuccess) {
+                b->gexec = nullptr;
+                return fail(PHG_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ei));
+            }
+            if (g_alloc_epoch.load() != k.epoch) {   // the capture itself moved a buffer
+                cudaGraphExecDestroy(b->gexec);
+                b->gexec = nullptr;
+                return fail(PHG_ERR_CUDA, "a buffer was reallocated while the step was captured");
+            }
+            b->gkey = k;
+            b->g_launches = nl;
+        }
+    }
+    for (int i = 0; i < left; ++i) CK(cudaGraphLaunch(b->gexec, s));
+    g_kernel_launches += b->g_launches * left;
+    b->last_stream = s;
+    CK(st.finish());
+    if (!st.host) return PHG_OK;   // device arguments: judged by phg_barvortex_last_stats
+    r = check_stats(o, b->nslots, s, nullptr, b->each);   // the last step, for phg_barvortex_last_stats
+    int r2 = bv_check_agg(b, s);
+    return r2 ? r2 : r;
+}
+
+extern "C" int phg_barvortex_run(phg_barvortex b, int nmembers, int nsteps, double *u, const double *bnd_u,
+                                 const double *bnd_w, const double *forcing, void *stream) {
+    return bv_run(b, nmembers, nsteps, u, bnd_u, bnd_w, forcing, stream);
 }
 
 // ------------------------------------------- linearised / adjoint steps ---
@@ -1371,7 +1488,12 @@ extern "C" int phg_barvortex_calc_LT(phg_barvortex b, double *v1, const double *
 extern "C" int phg_barvortex_last_stats(phg_barvortex b, int *il, int *ia, int *imj, int *iml, double *worst) {
     if (!b) return fail(PHG_ERR_ARG, "NULL handle");
     phg_ops_s *o = b->o;
-    int r = check_stats(o, b->nslots, b->last_stream ? b->last_stream : o->stream, nullptr, b->each);
+    cudaStream_t ls = b->last_stream ? b->last_stream : o->stream;
+    int r = check_stats(o, b->nslots, ls, nullptr, b->each);
+    if (b->agg_pending) {   // every step of the runs since the last check
+        int r2 = bv_check_agg(b, ls);
+        if (r2) r = r2;
+    }
     // slot layout: 0,1 mass L (calc1 x2); then per Picard iteration: J, A, L
     int l = 0, a = 0, mj = 0, ml = 0;
     double wr = 0.0;

@@ -1323,7 +1323,19 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     if ((e = cudaMemsetAsync(w + L.bar, 0, L.total - L.bar, s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(stats_dev, 0, sizeof(GmresStats), s)) != cudaSuccess) return e;
     void *args[] = {&p};
-    e = cudaLaunchCooperativeKernel(fn, dim3(groups * G), dim3(BLOCK), args, smem, s);
+    // cooperative (all blocks co-resident) through the attribute form, which
+    // stream capture records as a cooperative kernel node
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute coop[1];
+    coop[0].id = cudaLaunchAttributeCooperative;
+    coop[0].val.cooperative = 1;
+    cfg.gridDim = dim3(groups * G);
+    cfg.blockDim = dim3(BLOCK);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = coop;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelExC(&cfg, fn, args);
     if (e != cudaSuccess) return e;
     g_kernel_launches += 2;
     // a barrier timeout lands in stats->status (2)

@@ -234,6 +234,27 @@ __global__ void k_gather(double *y, int ldy, const double *x, int ldx, const int
 
 }  // namespace
 
+__global__ void k_stats_fold(const GmresStats *slots, int n, GmresStats *agg) {
+    if (threadIdx.x || blockIdx.x) return;
+    GmresStats a = *agg;
+    for (int k = 0; k < n; ++k) {
+        const GmresStats g = slots[k];
+        a.relres = fmax(a.relres, g.relres);
+        a.bytes += g.bytes;
+        a.iters += g.iters;
+        a.cycles += g.cycles;
+        a.status = max(a.status, g.status);
+        a.steps_total += g.steps_total;
+    }
+    *agg = a;
+}
+
+cudaError_t stats_fold(const GmresStats *slots, int n, GmresStats *agg, cudaStream_t s) {
+    k_stats_fold<<<1, 32, 0, s>>>(slots, n, agg);
+    g_kernel_launches++;
+    return cudaGetLastError();
+}
+
 cudaError_t apply_exact(const DevEll &A, const DevCols &C, const double *x_in, int ldx,
                         const double *x_bnd, int ldb, double *y, int ldy, int nv, cudaStream_t s) {
     k_apply<<<grid_for((long long)nv * A.n), TB, 0, s>>>(A, C, x_in, ldx, nullptr, x_bnd, ldb, nullptr, y, ldy, nv);

@@ -40,6 +40,8 @@ cudaError_t dot(const double *a, const double *b, int ld, int n, int nv, double 
 cudaError_t bv_commit(double *u_n, const double *u_n1, const double *nr, const double *nr0, int *done,
                       int V, int nv, cudaStream_t s);
 cudaError_t gather(double *y, int ldy, const double *x, int ldx, const int *map, int n, int nv, cudaStream_t s);
+// agg += the n solve records in slots (iterations summed; residual and status: the worst)
+cudaError_t stats_fold(const GmresStats *slots, int n, GmresStats *agg, cudaStream_t s);
 
 // y_v = A x_v, v < nv, member-major, on a slot-major ELL pattern of at most 8 slots
 template <typename T>

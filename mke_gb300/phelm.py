@@ -100,6 +100,7 @@ SIGNATURES = {
     "phg_barvortex_destroy": (None, [_vp]),
     "phg_barvortex_calc": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "phg_barvortex_calc_batch": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "phg_barvortex_run": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),
     "phg_barvortex_last_stats": (C.c_int, [_vp, _ip, _ip, _ip, _ip, _dp]),
     "phg_barvortex_calc_L": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "phg_barvortex_calc_L_1": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
@@ -418,6 +419,19 @@ class BarVortex:
         _check(lib().phg_barvortex_calc_batch(self._h, nm, _ptr(out), _ptr(u), _ptr(bnd_u), _ptr(bnd_w),
                                               _ptr(forcing), _stream(stream)))
         return out
+
+    def run(self, u, steps, bnd_u=None, bnd_w=None, forcing=None, stream=None):
+        """``steps`` steps of u in place (V values, or members x V), the same
+        boundary values and forcing every step; after the first step each
+        step is one launch of a captured CUDA graph.  Host arrays must be
+        writable float64 C-contiguous."""
+        nm = 1 if u.ndim == 1 else u.shape[0]
+        if not hasattr(u, "data_ptr") and (u.dtype != np.float64 or not u.flags.c_contiguous):
+            raise TypeError("u must be a C-contiguous float64 array (updated in place)")
+        bnd_u, bnd_w, forcing = _f8(bnd_u), _f8(bnd_w), _f8(forcing)
+        _check(lib().phg_barvortex_run(self._h, nm, int(steps), _ptr(u), _ptr(bnd_u), _ptr(bnd_w), _ptr(forcing),
+                                       _stream(stream)))
+        return u
 
     def _linear(self, fn, u, z, bnd_u, bnd_w, out, stream):
         out = np.zeros(self.m.size) if out is None else out
