@@ -97,6 +97,11 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def chosen(report: str) -> list:
+    """The "chose ..." lines of an autotuner report."""
+    return [ln[6:] for ln in report.splitlines() if ln.startswith("chose ")]
+
+
 def initial_state(mesh):
     from mke_gb300 import fields
     lat, lon = mesh.latlon()
@@ -125,8 +130,12 @@ def run_ours(args, ws, rank, local):
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > L2 (129 MB)
 
+    tuned = {}
+
     def make(prec):
         ops = phelm.Operators(mesh, prec, restart=30, tol=args.tol, max_iter=20000)
+        if not args.no_tune:
+            tuned[f"L{args.level}x1_{'mixed' if prec == phelm.PHG_MIXED else 'fp64'}"] = chosen(ops.autotune(1))
         return ops, phelm.BarVortex(ops, coriolis=cor, **CONF)
 
     results = {}
@@ -232,6 +241,8 @@ def run_ours(args, ws, rank, local):
             row = {"level": lvl, "members": B}
             for name, prec in (("mixed", phelm.PHG_MIXED), ("fp64", phelm.PHG_FP64)):
                 bops = phelm.Operators(bm, prec, restart=30, tol=args.tol)
+                if not args.no_tune:
+                    tuned[f"L{lvl}x{B}_{name}"] = chosen(bops.autotune(B))
                 bbv = phelm.BarVortex(bops, coriolis=np.sin(blat), **CONF)
                 U = torch.tensor(states, dtype=torch.float64, device=dev)
                 zB = torch.zeros((B, max(bm.outer_size, 1)), dtype=torch.float64, device=dev)
@@ -342,6 +353,7 @@ def run_ours(args, ws, rank, local):
         "spmv": spmv,
         "baroclin": baroclin,
         "solver": {"mixed": mixed["stats"], "fp64": fp64["stats"]},
+        "autotuned": tuned or None,
         "roofline": {"kernel": "gmres_kernel (persistent solver)", "bound": "hbm", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "launches_timed": prof["launches"],
@@ -589,6 +601,9 @@ def run_case(args):
     psi0, cor = initial_state(mesh)
     prec = phelm.PHG_MIXED if args.precision == "mixed" else phelm.PHG_FP64
     ops = phelm.Operators(mesh, prec, restart=30, tol=args.tol)
+    tune_report = None
+    if args.tune:
+        tune_report = chosen(ops.autotune(args.members if args.case == "batch" else 1))
     u = torch.tensor(psi0, dtype=torch.float64, device="cuda")
     out = torch.empty_like(u)
     zb = torch.zeros(max(mesh.outer_size, 1), dtype=torch.float64, device="cuda")
@@ -616,7 +631,8 @@ def run_case(args):
         torch.cuda.synchronize()
         ms = ev[0].elapsed_time(ev[1]) / args.steps
         print(json.dumps({"case": "batch", "level": args.level, "members": B, "precision": args.precision,
-                          "ms_per_step": ms, "member_steps_per_s": B * 1000.0 / ms, "stats": bv.last_stats()}))
+                          "ms_per_step": ms, "member_steps_per_s": B * 1000.0 / ms, "graph": args.graph,
+                          "tuned": tune_report, "stats": bv.last_stats()}))
         return
     if args.case == "solve":
         L = phelm.SphereLaplace(ops)
@@ -641,7 +657,7 @@ def run_case(args):
         ev[1].record(st)
     torch.cuda.synchronize()
     print(json.dumps({"case": args.case, "level": args.level, "steps": args.steps, "precision": args.precision,
-                      "ms_each": ev[0].elapsed_time(ev[1]) / args.steps,
+                      "ms_each": ev[0].elapsed_time(ev[1]) / args.steps, "graph": args.graph, "tuned": tune_report,
                       "env": {k: v for k, v in os.environ.items() if k.startswith("PHG_")}}))
 
 
@@ -666,6 +682,8 @@ def main():
     ap.add_argument("--members", type=int, default=16, help="ensemble members for --case batch")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--graph", action="store_true", help="--case step / batch: replay one captured step")
+    ap.add_argument("--tune", action="store_true", help="--case step / batch: autotune the launch shapes first")
+    ap.add_argument("--no-tune", action="store_true", help="bench line: keep the default launch shapes")
     args = ap.parse_args()
     if args.case:
         run_case(args)

@@ -136,6 +136,28 @@ int phg_ops_mult(phg_ops o, const char *name, double *y, const double *x, int nv
  * so every gathered row of x is one contiguous read.  No reference
  * counterpart. */
 int phg_ops_mult32(phg_ops o, const char *name, float *y, const float *x, int nv, void *stream);
+/* Autotuner (no reference counterpart).  Times the candidate launch shapes
+ * of the kernels a barotropic step of nmembers states runs on this handle's
+ * mesh and precision -- rows per block of the persistent solver (128, 256,
+ * 512, 1024) for the mass solves at nmembers and 8 x nmembers right-hand
+ * sides and the Laplace solve at nmembers, the lockstep path for mass solves
+ * in mixed precision (8 or more right-hand sides), and threads per row of
+ * phg_ops_mult32 at nmembers vectors -- and keeps the fastest in a
+ * process-wide table consulted by every later launch of the same kernel
+ * family, size, precision and right-hand-side bucket (powers of two).  A
+ * shape whose solve misses the tolerance is never chosen.  report (may be
+ * NULL) receives one text line per candidate timed and per choice. */
+int phg_ops_autotune(phg_ops o, int nmembers, char *report, int report_len, void *stream);
+/* The table as text: "solve <family> <rows> <precision> <bucket> <rows per
+ * block> <path>" and "spmm <rows> <bucket> <threads per row>" lines
+ * (family 0 GMRES, 1 Chebyshev, 2 multigrid, 3 baroclinic block system). */
+int phg_tune_describe(char *buf, int len);
+/* Save / load the table (a text file headed by the device model; a file
+ * from another model loads 0 entries).  Loading adds to the table. */
+int phg_tune_save(const char *path);
+int phg_tune_load(const char *path, int *entries);
+void phg_tune_clear(void);
+
 /* Synchronise `stream` and judge the solves enqueued on this handle since the
  * last check (calls with device pointers do not wait for their solves):
  * PHG_ERR_NOT_CONVERGED / PHG_ERR_TIMEOUT as a host-pointer call would

@@ -27,6 +27,7 @@ UNITS = [
     ("phg_gmres.cu", "cuda", []),
     ("phg_capi.cu", "cuda", []),
     ("phg_serve.cu", "cuda", []),
+    ("phg_tune.cu", "cuda", []),
 ]
 
 

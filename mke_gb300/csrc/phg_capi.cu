@@ -950,6 +950,171 @@ extern "C" int phg_ops_mult32(phg_ops o, const char *name, float *y, const float
     return PHG_OK;
 }
 
+// ------------------------------------------------------------- autotuner ---
+namespace {
+
+struct EvPair {
+    cudaEvent_t a = nullptr, b = nullptr;
+    ~EvPair() { if (a) cudaEventDestroy(a); if (b) cudaEventDestroy(b); }
+};
+
+struct Report {
+    std::string text;
+    void add(const char *fmt, ...) {
+        char line[256];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(line, sizeof line, fmt, ap);
+        va_end(ap);
+        text += line;
+    }
+};
+
+// device milliseconds of fn() on s: the best of `reps` runs after one warm-up
+template <typename F>
+int time_best(cudaStream_t s, int reps, F fn, float *best) {
+    EvPair e;
+    CK(cudaEventCreate(&e.a));
+    CK(cudaEventCreate(&e.b));
+    int r = fn();
+    if (r) return r;
+    *best = 1e30f;
+    for (int k = 0; k < reps; ++k) {
+        CK(cudaEventRecord(e.a, s));
+        if ((r = fn())) return r;
+        CK(cudaEventRecord(e.b, s));
+        CK(cudaEventSynchronize(e.b));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e.a, e.b));
+        *best = std::min(*best, ms);
+    }
+    return PHG_OK;
+}
+
+// the fastest launch shape of op's solves at nv right-hand sides b = A x*
+// (x* hashed), among rows per block 128..1024 and, for Chebyshev-solvable
+// operators in mixed precision with 8 or more right-hand sides, the lockstep
+// path; candidates that do not reach the tolerance are not chosen
+int tune_solve(phg_ops_s *o, const char *label, const DevSolveOp &op, int nv, cudaStream_t s, Report &rep) {
+    const int n = op.A.n;
+    const Precision pr = prec_of(o);
+    const int fam = solve_family(op);
+    const size_t len = (size_t)n * nv;
+    DBuf xs, b, x, st;
+    CK(xs.ensure(8 * len)); CK(b.ensure(8 * len)); CK(x.ensure(8 * len)); CK(st.ensure(sizeof(GmresStats)));
+    CK(fill_hash(xs.as<double>(), (long long)len, 12345u + (unsigned)nv, s));
+    CK(apply_op(op.A, DevCols(), xs.as<double>(), n, nullptr, nullptr, 0, nullptr, b.as<double>(), n, nv, s));
+    const size_t need = gmres_work_bytes(op, nv, o->restart, pr);
+    if (need > o->work.n) { CK(cudaStreamSynchronize(s)); CK(o->work.ensure(need)); }
+    std::vector<SolveShape> cand;
+    for (int rpb : {128, 256, 512, 1024}) { SolveShape c; c.rpb = rpb; c.path = 0; cand.push_back(c); }
+    if (fam == 1 && pr == PREC_MIXED && nv >= 8) { SolveShape c; c.rpb = 0; c.path = 1; cand.push_back(c); }
+    float best = 1e30f;
+    SolveShape pick;
+    bool any = false;
+    for (const SolveShape &c : cand) {
+        float ms = 0.f;
+        int r = time_best(s, 2, [&]() -> int {
+            CK(cudaMemsetAsync(x.p, 0, 8 * len, s));
+            CK(gmres_solve(op, b.as<double>(), x.as<double>(), nv, n, o->restart, o->max_iter, o->tol, pr, o->work.p,
+                           st.as<GmresStats>(), s, false, o->max_sms, &c));
+            return PHG_OK;
+        }, &ms);
+        if (r) return r;
+        GmresStats g{};
+        CK(cudaMemcpy(&g, st.p, sizeof g, cudaMemcpyDeviceToHost));
+        const bool ok = g.status == 0 || (g.status == 1 && g.relres <= std::max(1e3 * o->tol, 1e-8));
+        rep.add("solve %s family=%d rows=%d nv=%d rpb=%d path=%d ms=%.4f iters=%d relres=%.2e%s\n", label, fam, n,
+                nv, c.rpb, c.path, ms, g.iters, g.relres, ok ? "" : " (not converged)");
+        if (ok && ms < best) { best = ms; pick = c; any = true; }
+    }
+    if (!any) return fail(PHG_ERR_NOT_CONVERGED, "autotune: no launch shape reached the tolerance (%s)", label);
+    tune_set_solve(fam, n, pr, nv, pick);
+    rep.add("chose %s nv=%d rpb=%d path=%d\n", label, nv, pick.rpb, pick.path);
+    return PHG_OK;
+}
+
+// threads per row of the interleaved FP32 operator apply at nv vectors
+int tune_spmm(phg_ops_s *o, int nv, cudaStream_t s, Report &rep) {
+    const float *v32 = o->L.op.a32 ? o->L.op.a32 : o->ML.op.a32;
+    if (!v32 || nv < 4 || nv > 256 || nv % 4 || ((nv / 4) & (nv / 4 - 1))) return PHG_OK;
+    const int q4 = nv / 4;
+    const size_t len = (size_t)o->rs * nv;
+    DBuf x, y;
+    CK(x.ensure(4 * len)); CK(y.ensure(4 * len));
+    CK(fill_hash32(x.as<float>(), (long long)len, 777u, s));
+    float best = 1e30f;
+    int pick = 0;
+    for (int tpr = 1; tpr <= q4; tpr *= 2) {
+        if (q4 / tpr > 8) continue;
+        float ms = 0.f;
+        int r = time_best(s, 5, [&]() -> int {
+            CK(spmm_il32(o->pcol.as<int>(), v32, o->rs, o->W, x.as<float>(), y.as<float>(), nv, s, tpr));
+            return PHG_OK;
+        }, &ms);
+        if (r) return r;
+        rep.add("spmm rows=%d nv=%d threads_per_row=%d ms=%.4f\n", o->rs, nv, tpr, ms);
+        if (ms < best) { best = ms; pick = tpr; }
+    }
+    if (pick) {
+        tune_set_spmm(o->rs, nv, pick);
+        rep.add("chose spmm nv=%d threads_per_row=%d\n", nv, pick);
+    }
+    return PHG_OK;
+}
+
+void copy_out(const std::string &t, char *buf, int len) {
+    if (!buf || len <= 0) return;
+    const size_t k = std::min(t.size(), (size_t)len - 1);
+    memcpy(buf, t.data(), k);
+    buf[k] = 0;
+}
+
+}  // namespace
+
+extern "C" int phg_ops_autotune(phg_ops o, int nmembers, char *report, int report_len, void *stream) {
+    if (!o || nmembers < 1) return fail(PHG_ERR_ARG, "bad argument");
+    cudaStream_t s = o->str(stream);
+    Report rep;
+    int r;
+    // the solves of a barotropic step of nmembers states: mass (and the step
+    // matrix, same family and size) at nmembers, the Jacobian's mass solves
+    // at 8 x nmembers, the Laplace inverse at nmembers
+    if ((r = tune_solve(o, "mass", o->ML.op, nmembers, s, rep))) return r;
+    if ((r = tune_solve(o, "mass_jacobian", o->MJ.op, 8 * nmembers, s, rep))) return r;
+    if ((r = tune_solve(o, "laplace", o->L.op, nmembers, s, rep))) return r;
+    if ((r = tune_spmm(o, nmembers, s, rep))) return r;
+    CK(cudaStreamSynchronize(s));
+    g_alloc_epoch++;   // captured steps pick up the new shapes
+    copy_out(rep.text, report, report_len);
+    return PHG_OK;
+}
+
+extern "C" int phg_tune_describe(char *buf, int len) {
+    if (!buf || len <= 0) return fail(PHG_ERR_ARG, "bad argument");
+    copy_out(tune_describe(), buf, len);
+    return PHG_OK;
+}
+
+extern "C" int phg_tune_save(const char *path) {
+    if (!path) return fail(PHG_ERR_ARG, "NULL path");
+    return tune_save(path) ? fail(PHG_ERR_IO, "cannot write %s", path) : PHG_OK;
+}
+
+extern "C" int phg_tune_load(const char *path, int *entries) {
+    if (!path) return fail(PHG_ERR_ARG, "NULL path");
+    const int k = tune_load(path);
+    g_alloc_epoch++;   // captured steps pick up the new shapes
+    if (k < 0) return fail(PHG_ERR_IO, "cannot read %s (missing or malformed)", path);
+    if (entries) *entries = k;
+    return PHG_OK;
+}
+
+extern "C" void phg_tune_clear(void) {
+    tune_clear();
+    g_alloc_epoch++;
+}
+
 extern "C" int phg_ops_check(phg_ops o, void *stream) {
     if (!o) return fail(PHG_ERR_ARG, "NULL handle");
     cudaStream_t s = o->str(stream);

@@ -12,6 +12,7 @@
 // Vectors of several members (ensemble members, right-hand sides) are stored
 // member-major: x[v * ld + i].
 #pragma once
+#include <string>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -105,13 +106,38 @@ struct GmresStats {
 // `work` must hold gmres_work_bytes(...) bytes; `stats_dev` receives a
 // GmresStats on the device.
 size_t gmres_work_bytes(const DevSolveOp &op, int nv, int m, Precision p);
+
+// Launch shape of a solve.  rpb: rows per block of the persistent kernels
+// (no block gets fewer rows; 0 = 256).  path, for Chebyshev-solvable
+// operators in mixed precision: 1 = lockstep launches over an interleaved
+// FP32 multi-vector (8 or more right-hand sides), 0 = per-member persistent
+// kernels, -1 = the built-in rule (lockstep from 32 right-hand sides).
+struct SolveShape {
+    int rpb = 0;
+    int path = -1;
+};
+// the autotuner's table (phg_tune.cu); family: 0 plain GMRES, 1 Chebyshev,
+// 2 multigrid-preconditioned, 3 4-field block system
+int nv_bucket(int nv);
+int solve_family(const DevSolveOp &op);
+bool tune_get_solve(int family, int n, Precision p, int nv, SolveShape *out);
+void tune_set_solve(int family, int n, Precision p, int nv, const SolveShape &s);
+bool tune_get_spmm(int n, int nv, int *tpr);
+void tune_set_spmm(int n, int nv, int tpr);
+void tune_clear();
+std::string tune_describe();
+int tune_save(const char *path);
+int tune_load(const char *path);
 // no_alloc: never allocate (the optional debug phase timers stay off)
 // max_sms: use at most this many SMs' worth of co-resident blocks (0 = all);
 // callers that run several persistent launches at once partition the SMs
+// shape: the launch shape to use (null = the tuned one for this operator,
+// else the defaults); the environment variables PHG_ROWS_PER_BLOCK and
+// PHG_CHEB_LOCKSTEP override both
 cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv, int ld,
                         int m, int max_iter, double tol, Precision p,
                         void *work, GmresStats *stats_dev, cudaStream_t s, bool no_alloc = false,
-                        int max_sms = 0);
+                        int max_sms = 0, const SolveShape *shape = nullptr);
 
 // y[v] = A x_in[v] + C x_bnd[v] with every row summed in ascending column
 // order from 0.0 and no fused multiply-add (same rounding as a CPU CSR

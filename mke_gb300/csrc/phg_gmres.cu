@@ -48,6 +48,7 @@ constexpr double INNER_RTOL = 1e-5;  // FP32 cycle: reduce the residual 1e5x, th
 constexpr long long SPIN_LIMIT = 2000000000LL;  // clock64 cycles (~1 s)
 constexpr int CHEB_KMAX = 64;    // most Chebyshev steps per refinement cycle
 constexpr int LS_MIN_RHS = 32;   // right-hand sides from which the lockstep path runs
+constexpr int LS_MIN_TUNED = 8;  // the fewest for which the autotuner may choose it
 
 struct Params {
     DevSolveOp op;
@@ -1237,15 +1238,22 @@ size_t gmres_work_bytes(const DevSolveOp &op, int nv, int m, Precision p) { retu
 
 cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv, int ld,
                         int m, int max_iter, double tol, Precision prec,
-                        void *work, GmresStats *stats_dev, cudaStream_t s, bool no_alloc, int max_sms) {
+                        void *work, GmresStats *stats_dev, cudaStream_t s, bool no_alloc, int max_sms,
+                        const SolveShape *shape) {
     if (m < 1 || m > MAXM || nv < 1) return cudaErrorInvalidValue;
     const int n = op.A.n;
     Params p;
     const size_t es = prec == PREC_MIXED ? 4 : 8;
     const bool cheb = op.cheb_lmax > 0.0 && op.cheb_lmin > 0.0 && op.cheb_lmin < op.cheb_lmax && m >= 3 &&
                       !op.mgd && !op.block4 && op.A.W <= 8;
+    SolveShape sh;
+    if (shape) sh = *shape;
+    else tune_get_solve(solve_family(op), n, prec, nv, &sh);
+    if (getenv("PHG_ROWS_PER_BLOCK")) sh.rpb = env_int("PHG_ROWS_PER_BLOCK", 256);
+    if (getenv("PHG_CHEB_LOCKSTEP") && !env_int("PHG_CHEB_LOCKSTEP", 1)) sh.path = 0;
+    const bool lockstep = sh.path == 1 ? nv >= LS_MIN_TUNED : (sh.path == 0 ? false : nv >= LS_MIN_RHS);
     // ensembles in the mixed path: all right-hand sides in lockstep
-    if (cheb && prec == PREC_MIXED && nv >= LS_MIN_RHS && !no_alloc && env_int("PHG_CHEB_LOCKSTEP", 1)) {
+    if (cheb && prec == PREC_MIXED && lockstep && !no_alloc) {
         const char *ev = getenv("PHG_INNER_RTOL");
         cudaError_t e0 = cudaMemsetAsync(stats_dev, 0, sizeof(GmresStats), s);
         if (e0 != cudaSuccess) return e0;
@@ -1268,7 +1276,7 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     const int cap = sms * per;
     // as many right-hand sides in flight as there are blocks; the blocks are
     // shared out evenly, but no block gets fewer than `rpb` rows
-    const int rpb = env_int("PHG_ROWS_PER_BLOCK", 256);
+    const int rpb = sh.rpb > 0 ? sh.rpb : 256;
     int groups = nv < cap ? nv : cap;
     if (groups > GROUPS_CAP) groups = GROUPS_CAP;
     int G = cap / groups;

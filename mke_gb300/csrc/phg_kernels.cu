@@ -234,6 +234,37 @@ __global__ void k_gather(double *y, int ldy, const double *x, int ldx, const int
 
 }  // namespace
 
+__device__ __forceinline__ double hash_unit(unsigned long long i, unsigned seed) {
+    // splitmix64 finaliser of (i, seed), top 53 bits -> [-1, 1)
+    unsigned long long z = i + 0x9E3779B97F4A7C15ull * (seed + 1ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+}
+
+__global__ void k_fill_hash(double *x, long long n, unsigned seed) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        x[i] = hash_unit((unsigned long long)i, seed);
+}
+
+__global__ void k_fill_hash32(float *x, long long n, unsigned seed) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        x[i] = (float)hash_unit((unsigned long long)i, seed);
+}
+
+cudaError_t fill_hash(double *x, long long n, unsigned seed, cudaStream_t s) {
+    k_fill_hash<<<grid_for(n), TB, 0, s>>>(x, n, seed);
+    g_kernel_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t fill_hash32(float *x, long long n, unsigned seed, cudaStream_t s) {
+    k_fill_hash32<<<grid_for(n), TB, 0, s>>>(x, n, seed);
+    g_kernel_launches++;
+    return cudaGetLastError();
+}
+
 __global__ void k_stats_fold(const GmresStats *slots, int n, GmresStats *agg) {
     if (threadIdx.x || blockIdx.x) return;
     GmresStats a = *agg;
@@ -652,11 +683,13 @@ __global__ void __launch_bounds__(TB) k_spmm_il(const int *__restrict__ col, con
 }
 
 template <int W>
-cudaError_t launch_il(const int *col, const float *val, int n, const float4 *x, float4 *y, int q4, cudaStream_t s) {
-    // Eight threads per row (fewer when the row has fewer chunks), each with
-    // q4 / 8 chunks: the best of a sweep over 1..16 chunks per thread and
-    // 256/1024-thread blocks on a level-8 Laplacian with 32 and 64 members.
-    const int tpr = q4 < 8 ? q4 : 8;
+cudaError_t launch_il(const int *col, const float *val, int n, const float4 *x, float4 *y, int q4, int tpr,
+                      cudaStream_t s) {
+    // Default: eight threads per row (fewer when the row has fewer chunks),
+    // each with q4 / 8 chunks -- the best of a sweep over 1..16 chunks per
+    // thread and 256/1024-thread blocks on a level-8 Laplacian with 32 and 64
+    // members.  The autotuner may choose another power of two.
+    if (tpr <= 0 || tpr > q4 || q4 % tpr || q4 / tpr > 8) tpr = q4 < 8 ? q4 : 8;
     const int ch = q4 / tpr;
     if (tpr * ch != q4) return cudaErrorInvalidValue;
     int lg = 0;
@@ -692,14 +725,15 @@ template cudaError_t spmm<float>(const int *, const float *, int, int, const flo
                                  cudaStream_t);
 
 cudaError_t spmm_il32(const int *col, const float *val, int n, int W, const float *x, float *y, int nv,
-                      cudaStream_t s) {
+                      cudaStream_t s, int tpr) {
     if (n < 1 || nv < 4 || nv % 4 || ((uintptr_t)x & 15) || ((uintptr_t)y & 15)) return cudaErrorInvalidValue;
     const int q4 = nv / 4;
+    if (tpr <= 0) tune_get_spmm(n, nv, &tpr);
     cudaError_t e;
     switch (W) {   // the ELL arrays hold exactly W slots (padding: diagonal column, zero value)
-    case 8: e = launch_il<8>(col, val, n, (const float4 *)x, (float4 *)y, q4, s); break;
-    case 7: e = launch_il<7>(col, val, n, (const float4 *)x, (float4 *)y, q4, s); break;
-    case 6: e = launch_il<6>(col, val, n, (const float4 *)x, (float4 *)y, q4, s); break;
+    case 8: e = launch_il<8>(col, val, n, (const float4 *)x, (float4 *)y, q4, tpr, s); break;
+    case 7: e = launch_il<7>(col, val, n, (const float4 *)x, (float4 *)y, q4, tpr, s); break;
+    case 6: e = launch_il<6>(col, val, n, (const float4 *)x, (float4 *)y, q4, tpr, s); break;
     default: return cudaErrorInvalidValue;
     }
     g_kernel_launches++;

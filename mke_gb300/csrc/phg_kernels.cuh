@@ -48,9 +48,13 @@ template <typename T>
 cudaError_t spmm(const int *col, const T *val, int n, int W, const T *x, int ldx, T *y, int ldy, int nv,
                  cudaStream_t s);
 // Y = A X, X and Y interleaved (n x nv, member-minor), FP32, nv = 4 * 2^k <= 256,
-// 16-byte aligned
+// 16-byte aligned; tpr: threads per row (a power of two with nv / 4 / tpr
+// in 1..8; 0 = the tuned value, else 8)
 cudaError_t spmm_il32(const int *col, const float *val, int n, int W, const float *x, float *y, int nv,
-                      cudaStream_t s);
+                      cudaStream_t s, int tpr = 0);
+// deterministic test data: x[i] = a hash of (i, seed) in [-1, 1)
+cudaError_t fill_hash(double *x, long long n, unsigned seed, cudaStream_t s);
+cudaError_t fill_hash32(float *x, long long n, unsigned seed, cudaStream_t s);
 
 // Baroclin step helpers (examples/baroclin.cpp:445-606)
 struct BcCoef {

@@ -101,6 +101,11 @@ SIGNATURES = {
     "phg_barvortex_calc": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "phg_barvortex_calc_batch": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "phg_barvortex_run": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),
+    "phg_ops_autotune": (C.c_int, [_vp, C.c_int, C.c_char_p, C.c_int, _vp]),
+    "phg_tune_describe": (C.c_int, [C.c_char_p, C.c_int]),
+    "phg_tune_save": (C.c_int, [C.c_char_p]),
+    "phg_tune_load": (C.c_int, [C.c_char_p, _ip]),
+    "phg_tune_clear": (None, []),
     "phg_barvortex_last_stats": (C.c_int, [_vp, _ip, _ip, _ip, _ip, _dp]),
     "phg_barvortex_calc_L": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "phg_barvortex_calc_L_1": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
@@ -138,6 +143,37 @@ def lib(build_if_missing: bool = True):
             f.argtypes = args
         _lib = L
     return _lib
+
+
+def tune_table() -> list:
+    """The autotuner's table: dicts with kind "solve" (family, rows,
+    precision, bucket, rows_per_block, path) or "spmm" (rows, bucket,
+    threads_per_row)."""
+    buf = C.create_string_buffer(1 << 16)
+    _check(lib().phg_tune_describe(buf, len(buf)))
+    out = []
+    for line in buf.value.decode().splitlines():
+        f = line.split()
+        if f[0] == "solve":
+            out.append(dict(kind="solve", family=int(f[1]), rows=int(f[2]), precision=int(f[3]), bucket=int(f[4]),
+                            rows_per_block=int(f[5]), path=int(f[6])))
+        elif f[0] == "spmm":
+            out.append(dict(kind="spmm", rows=int(f[1]), bucket=int(f[2]), threads_per_row=int(f[3])))
+    return out
+
+
+def tune_save(path: str) -> None:
+    _check(lib().phg_tune_save(path.encode()))
+
+
+def tune_load(path: str) -> int:
+    k = C.c_int()
+    _check(lib().phg_tune_load(path.encode(), C.byref(k)))
+    return k.value
+
+
+def tune_clear() -> None:
+    lib().phg_tune_clear()
 
 
 def kernel_launches() -> int:
@@ -278,6 +314,13 @@ class Operators:
         (CUDA float32 tensors rs x nv, nv = 4 * 2^k <= 256)."""
         _check(lib().phg_ops_mult32(self._h, name.encode(), _ptr(out), _ptr(x), x.shape[1], _stream(stream)))
         return out
+
+    def autotune(self, members: int = 1, stream=None) -> str:
+        """Time the candidate launch shapes of a ``members``-state step's
+        kernels and keep the fastest (phg_ops_autotune); returns the report."""
+        buf = C.create_string_buffer(1 << 16)
+        _check(lib().phg_ops_autotune(self._h, int(members), buf, len(buf), _stream(stream)))
+        return buf.value.decode()
 
     def set_solver(self, restart=30, tol=1e-12, max_iter=20000):
         _check(lib().phg_ops_set_solver(self._h, restart, tol, max_iter))
