@@ -964,49 +964,89 @@ Layout layout(const DevSolveOp &op, int nv, int m, Precision prec) {
 constexpr int LS_MAXC = 6;     // refinement cycles at most
 constexpr int LS_MG = 16;      // members per thread in the FP64 residual
 
+// R = B - A X for LS_MG members per block row (FP64, ascending slot order),
+// and each member's sum of R^2 over the block's rows into part[v][block]
+// (fixed order: the norms are reproducible)
 template <int W>
 __global__ void __launch_bounds__(256) k_ls_resid(const int *__restrict__ col, const double *__restrict__ val, int n,
                                                   const double *__restrict__ B, const double *__restrict__ X, int ld,
-                                                  double *__restrict__ R, int nv, const int *done) {
+                                                  double *__restrict__ R, int nv, double *__restrict__ part,
+                                                  const int *done) {
     if (*(volatile const int *)done) return;
+    __shared__ double sq[LS_MG][256];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const bool row = i < n;
+    const int v0 = blockIdx.y * LS_MG, v1 = min(nv, v0 + LS_MG);
     int c[W];
     double a[W];
 #pragma unroll
-    for (int k = 0; k < W; ++k) { c[k] = __ldg(&col[(size_t)k * n + i]); a[k] = __ldg(&val[(size_t)k * n + i]); }
-    const int v0 = blockIdx.y * LS_MG, v1 = min(nv, v0 + LS_MG);
+    for (int k = 0; k < W; ++k) {
+        c[k] = row ? __ldg(&col[(size_t)k * n + i]) : 0;
+        a[k] = row ? __ldg(&val[(size_t)k * n + i]) : 0.0;
+    }
     for (int v = v0; v < v1; ++v) {
-        const double *x = X + (size_t)v * ld;
-        double sum = 0.0;
+        double r = 0.0;
+        if (row) {
+            const double *x = X + (size_t)v * ld;
+            double sum = 0.0;
 #pragma unroll
-        for (int k = 0; k < W; ++k) sum += a[k] * x[c[k]];
-        R[(size_t)v * n + i] = B[(size_t)v * ld + i] - sum;
+            for (int k = 0; k < W; ++k) sum += a[k] * x[c[k]];
+            r = B[(size_t)v * ld + i] - sum;
+            R[(size_t)v * n + i] = r;
+        }
+        sq[v - v0][threadIdx.x] = r * r;
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int j = warp; j < v1 - v0; j += NWARP) {
+        double t = 0.0;
+        for (int q = lane; q < 256; q += 32) t += sq[j][q];
+        t = warp_sum(t);
+        if (lane == 0) part[(size_t)(v0 + j) * gridDim.x + blockIdx.x] = t;
     }
 }
 
-// out[v] = sum_i A[v * ld + i]^2 (one block per member, fixed order)
-__global__ void __launch_bounds__(256) k_ls_norm2(const double *__restrict__ A, int n, int ld, double *out,
-                                                  const int *done) {
-    if (done && *(volatile const int *)done) return;
-    __shared__ double red[NWARP];
-    const double *a = A + (size_t)blockIdx.x * ld;
-    double s = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) s += a[i] * a[i];
-    s = warp_sum(s);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < NWARP; ++w) t += red[w];
-        out[blockIdx.x] = t;
+// each member's sum of A^2 over block rows into part[v][block] (as k_ls_resid)
+__global__ void __launch_bounds__(256) k_ls_sq(const double *__restrict__ A, int n, int ld, int nv,
+                                               double *__restrict__ part) {
+    __shared__ double sq[LS_MG][256];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int v0 = blockIdx.y * LS_MG, v1 = min(nv, v0 + LS_MG);
+    for (int v = v0; v < v1; ++v) {
+        const double x = i < n ? A[(size_t)v * ld + i] : 0.0;
+        sq[v - v0][threadIdx.x] = x * x;
     }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int j = warp; j < v1 - v0; j += NWARP) {
+        double t = 0.0;
+        for (int q = lane; q < 256; q += 32) t += sq[j][q];
+        t = warp_sum(t);
+        if (lane == 0) part[(size_t)(v0 + j) * gridDim.x + blockIdx.x] = t;
+    }
+}
+
+// ||r||^2 and ||b||^2 of every member: the sums of its nbx block partials
+// (one warp per member, fixed order)
+__global__ void __launch_bounds__(256) k_ls_nrm(const double *rpart, const double *bpart, int nbx, double *nrm,
+                                                int nv, const int *done) {
+    if (*(volatile const int *)done) return;
+    const int v = blockIdx.x * NWARP + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (v >= nv) return;
+    double tr = 0.0, tb = 0.0;
+    for (int q = lane; q < nbx; q += 32) {
+        tr += rpart[(size_t)v * nbx + q];
+        tb += bpart[(size_t)v * nbx + q];
+    }
+    tr = warp_sum(tr);
+    tb = warp_sum(tb);
+    if (lane == 0) { nrm[2 * v] = tr; nrm[2 * v + 1] = tb; }
 }
 
 // per-member scales 1/||r|| (0 once converged), the stopping test and the stats
-__global__ void __launch_bounds__(256) k_ls_scale(const double *nrm, const double *bn2, int nv, int nvp, double tol,
-                                                  double *beta, double *sc, int *done, GmresStats *st, int cycle,
-                                                  int K, double bytes) {
+__global__ void __launch_bounds__(256) k_ls_scale(const double *nrm, int nv, int nvp, double tol, double *beta,
+                                                  double *sc, int *done, GmresStats *st, int cycle, int K,
+                                                  double bytes) {
     if (*(volatile int *)done) return;
     __shared__ double rmax[NWARP];
     __shared__ int open[NWARP];
@@ -1014,7 +1054,7 @@ __global__ void __launch_bounds__(256) k_ls_scale(const double *nrm, const doubl
     int op = 0;
     for (int v = threadIdx.x; v < nvp; v += blockDim.x) {
         if (v >= nv) { sc[v] = 0.0; beta[v] = 0.0; continue; }
-        const double bt = sqrt(nrm[v]), bn = sqrt(bn2[v]);
+        const double bt = sqrt(nrm[2 * v]), bn = sqrt(nrm[2 * v + 1]);
         const double rel = bn > 0.0 ? bt / bn : 0.0;
         const bool conv = rel <= tol || bt == 0.0;
         beta[v] = bt;
@@ -1142,12 +1182,14 @@ cudaError_t cheb_lockstep(const DevSolveOp &op, const double *B, double *X, int 
     const int nvp = (nv + 31) / 32 * 32, q4 = nvp / 4;
     if ((long long)n * q4 >= (1LL << 31)) return cudaErrorNotSupported;
     const size_t vec = ((size_t)n * nvp * 4 + 255) & ~size_t(255);
-    if (4 * vec > L.r - L.v) return cudaErrorNotSupported;
+    const int nbx = (n + 255) / 256;   // row blocks of the residual: one norm partial each
+    if (4 * vec + (size_t)16 * nv * nbx > L.r - L.v) return cudaErrorNotSupported;
     if ((size_t)(4 * nvp + 64) * 8 > L.bar - L.part) return cudaErrorNotSupported;
     float *rv = (float *)(w + L.v), *d = (float *)(w + L.v + vec), *e0 = (float *)(w + L.v + 2 * vec),
           *e1 = (float *)(w + L.v + 3 * vec);
+    double *rpart = (double *)(w + L.v + 4 * vec), *bpart = rpart + (size_t)nv * nbx;
     double *R = (double *)(w + L.r);
-    double *bn2 = (double *)(w + L.part), *nrm = bn2 + nvp, *beta = nrm + nvp, *sc = beta + nvp;
+    double *nrm = (double *)(w + L.part), *beta = nrm + 2 * nvp, *sc = beta + nvp;
     int *done = (int *)(sc + nvp);
     // coefficients (as the per-member Chebyshev kernel)
     const double lo = op.cheb_lmin, hi = op.cheb_lmax;
@@ -1165,22 +1207,22 @@ cudaError_t cheb_lockstep(const DevSolveOp &op, const double *B, double *X, int 
     }
     // algorithmic bytes of one cycle: FP64 residual, init, K - 1 steps, update
     const double rowsb = (double)n;
-    const double cyc = rowsb * nv * (8.0 * 3 + 8.0) + rowsb * W * 12.0 +
+    const double cyc = rowsb * nv * (8.0 * 3) + rowsb * W * 12.0 +
                        rowsb * nvp * (8.0 + 12.0) + (K - 1) * (rowsb * W * 8.0 + rowsb * nvp * 4.0 * 6.0) +
                        rowsb * nvp * 4.0 + rowsb * nv * 16.0;
     cudaError_t e;
     if ((e = cudaMemsetAsync(done, 0, sizeof(int), s)) != cudaSuccess) return e;
-    k_ls_norm2<<<nv, 256, 0, s>>>(B, n, ld, bn2, nullptr);
-    const dim3 rgrid((unsigned)((n + 255) / 256), (unsigned)((nv + LS_MG - 1) / LS_MG));
+    const dim3 rgrid((unsigned)nbx, (unsigned)((nv + LS_MG - 1) / LS_MG));
+    k_ls_sq<<<rgrid, 256, 0, s>>>(B, n, ld, nv, bpart);
     const dim3 tgrid((unsigned)((n + 31) / 32), (unsigned)(nvp / 32));
     for (int c = 0; c <= LS_MAXC; ++c) {
         switch (W) {
-        case 6: k_ls_resid<6><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, R, nv, done); break;
-        case 7: k_ls_resid<7><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, R, nv, done); break;
-        default: k_ls_resid<8><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, R, nv, done); break;
+        case 6: k_ls_resid<6><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, R, nv, rpart, done); break;
+        case 7: k_ls_resid<7><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, R, nv, rpart, done); break;
+        default: k_ls_resid<8><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, R, nv, rpart, done); break;
         }
-        k_ls_norm2<<<nv, 256, 0, s>>>(R, n, n, nrm, done);
-        k_ls_scale<<<1, 256, 0, s>>>(nrm, bn2, nv, nvp, tol, beta, sc, done, st, c, K, c ? cyc : 0.0);
+        k_ls_nrm<<<(nv + NWARP - 1) / NWARP, 256, 0, s>>>(rpart, bpart, nbx, nrm, nv, done);
+        k_ls_scale<<<1, 256, 0, s>>>(nrm, nv, nvp, tol, beta, sc, done, st, c, K, c ? cyc : 0.0);
         if (c == LS_MAXC) break;
         k_ls_init<<<tgrid, 256, 0, s>>>(R, n, nv, nvp, sc, op.dinv32, (float)(1.0 / theta), rv, d, e0, done);
         float *ec = e0, *en = e1;
