@@ -62,7 +62,7 @@ struct Params {
     double *R;        // nv x n (FP64 residual)
     void *mgbuf;      // groups x per-group V-cycle buffers (parallel levels)
     double *part;     // groups x 2 x (MAXM + 2) x G
-    unsigned *bar;    // groups x 2
+    unsigned *bar;    // groups x 2 (one 64-bit arrival count per group)
     int *err;
     GmresStats *stats;
     int groups, G;
@@ -84,6 +84,19 @@ __device__ __forceinline__ unsigned ld_volatile(const unsigned *p) { return *(co
 __device__ __forceinline__ int ld_volatile(const int *p) { return *(const volatile int *)p; }
 
 // Barrier over the G blocks of one group; false if the grid is aborting.
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Barrier of the G blocks of one group.  The group's 64-bit word at bar
+// counts arrivals and is never reset within a launch (nor wraps): a block
+// arriving as the k-th (0-based) waits until the count reaches the next
+// multiple of G, so the last arrival's one atomic releases everyone (no
+// reset, no second flag) and a block that runs ahead into the next barrier
+// only raises the count further.  The wait gives up after SPIN_LIMIT cycles
+// and raises the launch's error flag.
 __device__ bool group_sync(unsigned *bar, int G, int *err, long long *tm) {
     __shared__ int ok;
     long long tb = (tm && threadIdx.x == 0) ? clock64() : 0;
@@ -94,20 +107,14 @@ __device__ bool group_sync(unsigned *bar, int G, int *err, long long *tm) {
     }
     if (threadIdx.x == 0) {
         ok = 1;
-        unsigned *cnt = bar, *gen = bar + 1;
-        unsigned my = ld_volatile(gen);
+        unsigned long long *cnt = reinterpret_cast<unsigned long long *>(bar);   // 8-byte aligned
         __threadfence();
-        unsigned arrived = atomicAdd(cnt, 1u);
-        if (arrived == (unsigned)G - 1) {
-            atomicExch(cnt, 0u);
-            __threadfence();
-            atomicAdd(gen, 1u);
-        } else {
-            long long t0 = clock64();
-            while (ld_volatile(gen) == my) {
-                if (ld_volatile(err)) { ok = 0; break; }
-                if (clock64() - t0 > SPIN_LIMIT) { atomicExch(err, 1); ok = 0; break; }
-            }
+        const unsigned long long old = atomicAdd(cnt, 1ull);
+        const unsigned long long target = old - old % (unsigned long long)G + (unsigned long long)G;
+        const long long t0 = clock64();
+        while (ld_acquire(cnt) < target) {
+            if (ld_volatile(err)) { ok = 0; break; }
+            if (clock64() - t0 > SPIN_LIMIT) { atomicExch(err, 1); ok = 0; break; }
         }
         __threadfence();
         if (ld_volatile(err)) ok = 0;
