@@ -108,7 +108,9 @@ __device__ bool group_sync(unsigned *bar, int G, int *err, long long *tm) {
     if (threadIdx.x == 0) {
         ok = 1;
         unsigned long long *cnt = reinterpret_cast<unsigned long long *>(bar);   // 8-byte aligned
-        __threadfence();
+        // release: the block's writes (ordered before this thread by the
+        // __syncthreads above) are visible device-wide before the arrival
+        asm volatile("fence.acq_rel.gpu;" ::: "memory");
         const unsigned long long old = atomicAdd(cnt, 1ull);
         const unsigned long long target = old - old % (unsigned long long)G + (unsigned long long)G;
         const long long t0 = clock64();
@@ -116,7 +118,9 @@ __device__ bool group_sync(unsigned *bar, int G, int *err, long long *tm) {
             if (ld_volatile(err)) { ok = 0; break; }
             if (clock64() - t0 > SPIN_LIMIT) { atomicExch(err, 1); ok = 0; break; }
         }
-        __threadfence();
+        // acquire: the load that saw the count completes before any later
+        // access of the block (the __syncthreads below orders the others)
+        asm volatile("fence.acq_rel.gpu;" ::: "memory");
         if (ld_volatile(err)) ok = 0;
         if (tm) { tm[T_BARRIER] += clock64() - tb; tm[T_BARRIERS]++; }
     }
