@@ -35,8 +35,10 @@ def test_level6_mesh_matches_reference(golden):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("replay", [False, True], ids=["calc", "graph"])
 @pytest.mark.parametrize("precision", [phelm.PHG_FP64, phelm.PHG_MIXED])
-def test_level6_100_steps(golden, precision):
+def test_level6_100_steps(golden, precision, replay):
+    """replay: steps 2..100 as one phg_barvortex_run (a captured step replayed)."""
     import torch
     g = golden("ref_L6_barvortex100.npz")
     m = phelm.Mesh.sphere(6)
@@ -50,8 +52,11 @@ def test_level6_100_steps(golden, precision):
     bv.calc(u, z, z, out=u, stream=s)
     s.synchronize()
     assert rel(u.cpu().numpy(), g["out_bv_step1"]) <= 1e-10
-    for _ in range(99):
-        bv.calc(u, z, z, out=u, stream=s)
+    if replay:
+        bv.run(u, 99, z, z, stream=s)
+    else:
+        for _ in range(99):
+            bv.calc(u, z, z, out=u, stream=s)
     s.synchronize()
     st = bv.last_stats()
     assert st["worst_relres"] <= 1e-12
