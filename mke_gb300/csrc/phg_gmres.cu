@@ -317,11 +317,50 @@ __device__ __forceinline__ void residual_rows(const MgLevelDev &L, const VT *b, 
         r[i] = (CG ? ldcg(&b[i]) : b[i]) - spmv_row<VT, CG>(L.col, A, L.n, L.W, x, i);
 }
 
+// sum_k A[k][i] fx(col): spmv_row with the gathered values computed by fx
+// (same load grouping and summation order)
+template <typename VT, typename F>
+__device__ __forceinline__ VT spmv_row_fx(const int *__restrict__ col, const VT *__restrict__ val, int n, int W, int i,
+                                          F fx) {
+    VT s = 0;
+    if (W <= 8) {
+        int c[8];
+        VT a[8], xv[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < W) { c[k] = __ldg(&col[(size_t)k * n + i]); a[k] = __ldg(&val[(size_t)k * n + i]); }
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < W) xv[k] = fx(c[k]);
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < W) s += a[k] * xv[k];
+        return s;
+    }
+    for (int k = 0; k < W; ++k) s += __ldg(&val[(size_t)k * n + i]) * fx(__ldg(&col[(size_t)k * n + i]));
+    return s;
+}
+
+// r = b - A x1 on rows [r0, r1) where x1 = w D^-1 b is the first damped-Jacobi
+// sweep from zero, formed from b alone (b complete on every block): the
+// residual needs no barrier after the sweep
+template <typename VT>
+__device__ __forceinline__ void residual_first_rows(const MgLevelDev &L, const VT *b, VT omega, VT *r, int r0, int r1) {
+    const VT *A = Prec<VT>::la(L), *D = Prec<VT>::ld(L);
+    for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
+        const VT s = spmv_row_fx<VT>(L.col, A, L.n, L.W, i,
+                                     [&](int c) { return omega * __ldg(&D[c]) * ldcg(&b[c]); });
+        r[i] = ldcg(&b[i]) - s;
+    }
+}
+
 // Damped-Jacobi V-cycle: x0 = M^-1 b0 for the group's right-hand side.
 // Returns false if the grid is aborting.
+// b0_visible: b0 is complete on every block at entry (a barrier since it was
+// written), so the finest level's residual is formed without a barrier.
 template <typename VT>
 __device__ __noinline__ bool vcycle(const MgDev *__restrict__ mgp, const VT *b0, VT *x0, VT *gbuf, VT *sm,
-                                    unsigned *bar, int G, int bi, int *err, long long *tm) {
+                                    unsigned *bar, int G, int bi, int *err, long long *tm, bool b0_visible) {
     const int nred = mgp->nred, nlev = mgp->nlev, nu1 = mgp->nu1, nu2 = mgp->nu2;
     const VT omega = (VT)mgp->omega;
     VT *xcur[MG_MAXLEV];
@@ -342,13 +381,19 @@ __device__ __noinline__ bool vcycle(const MgDev *__restrict__ mgp, const VT *b0,
         own_rows(n, G, bi, r0, r1);
         VT *x = xa, *xo = xb;
         jacobi_rows<VT, true>(L, b, nullptr, x, omega, r0, r1, true);
-        for (int s = 1; s < nu1; ++s) {
+        // FP32 only: in FP64 the two extra multiplies per gathered entry cost
+        // more than the barrier (measured at level 6)
+        if (sizeof(VT) == 4 && l == 0 && b0_visible && nu1 == 1) {
+            residual_first_rows<VT>(L, b, omega, r, r0, r1);
+        } else {
+            for (int s = 1; s < nu1; ++s) {
+                if (!group_sync(bar, G, err, tm)) return false;
+                jacobi_rows<VT, true>(L, b, x, xo, omega, r0, r1, false);
+                VT *t = x; x = xo; xo = t;
+            }
             if (!group_sync(bar, G, err, tm)) return false;
-            jacobi_rows<VT, true>(L, b, x, xo, omega, r0, r1, false);
-            VT *t = x; x = xo; xo = t;
+            residual_rows<VT, true>(L, b, x, r, r0, r1);
         }
-        if (!group_sync(bar, G, err, tm)) return false;
-        residual_rows<VT, true>(L, b, x, r, r0, r1);
         xcur[l] = x;
         if (!group_sync(bar, G, err, tm)) return false;
         const MgLevelDev &C = mgp->lev[l + 1];
@@ -614,8 +659,8 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
                         bt3[k] = ldcg(&vj[4 * k + 2]) - s3;
                         bt4[k] = ldcg(&vj[4 * k + 3]) - s4;
                     }
-                    if (!vcycle<VT>(mgp, bt3, bu3, gbuf, msm, bar, G, bi, err, tm)) return;
-                    if (!vcycle<VT>(mgp, bt4, bu4, gbuf2, msm, bar, G, bi, err, tm)) return;
+                    if (!vcycle<VT>(mgp, bt3, bu3, gbuf, msm, bar, G, bi, err, tm, false)) return;
+                    if (!vcycle<VT>(mgp, bt4, bu4, gbuf2, msm, bar, G, bi, err, tm, false)) return;
                     if (!group_sync(bar, G, err, tm)) return;
                     for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
                         const int q = i & 3;
@@ -627,7 +672,7 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
                     my_bytes += nrows * mg_row_bytes;
                 } else if (use_mg) {
                     VT *zz = Z + (size_t)j * n;
-                    if (!vcycle<VT>(mgp, vj, zz, gbuf, msm, bar, G, bi, err, tm)) return;
+                    if (!vcycle<VT>(mgp, vj, zz, gbuf, msm, bar, G, bi, err, tm, true)) return;
                     if (!group_sync(bar, G, err, tm)) return;   // z_j complete
                     PHG_TICK(T_VCYCLE);
                     zj = zz;
