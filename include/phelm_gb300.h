@@ -174,6 +174,10 @@ int phg_device_bytes(long long *total, long long *this_thread);
  * bytes since the last enable. */
 int phg_ops_profile(phg_ops o, int enable);
 int phg_ops_profile_read(phg_ops o, int *launches, double *ms, double *bytes);
+/* The same restricted to the launches of one solver family (0 GMRES, 1
+ * Chebyshev, 2 multigrid-preconditioned GMRES, 3 baroclinic block system;
+ * -1 = all), e.g. the Laplacian solves' gmres_kernel launches alone. */
+int phg_ops_profile_read_family(phg_ops o, int family, int *launches, double *ms, double *bytes);
 
 /* SphereLaplace::calc1 (src/impl/slaplace_impl.h:176-192): ans[V] = Laplacian
  * of F[V] with boundary values bnd[os] written on the boundary. */

@@ -359,6 +359,7 @@ struct phg_ops_s {
     // solver-launch profiling
     bool prof = false;
     std::vector<cudaEvent_t> ev;
+    std::vector<int> ev_family;      // solver family of each recorded launch
     int nev = 0;
     DBuf hist;
     ~phg_ops_s() { for (auto e : ev) cudaEventDestroy(e); }
@@ -684,6 +685,7 @@ int solve(phg_ops_s *o, const DevSolveOp &op, const double *B, double *X, int nv
     CK(gmres_solve(op, B, X, nv, ld, o->restart, o->max_iter, tol, prec_of(o), o->work.p,
                    o->stats.as<GmresStats>() + slot, s, false, o->max_sms));
     if (rec) {
+        o->ev_family[o->nev / 2] = solve_family(op);
         CK(cudaEventRecord(o->ev[o->nev + 1], s));
         CK(cudaMemcpyAsync(o->hist.as<GmresStats>() + o->nev / 2, o->stats.as<GmresStats>() + slot,
                            sizeof(GmresStats), cudaMemcpyDeviceToDevice, s));
@@ -816,6 +818,7 @@ extern "C" int phg_ops_profile(phg_ops o, int enable) {
     if (!o) return fail(PHG_ERR_ARG, "NULL handle");
     if (enable && o->ev.empty()) {
         o->ev.resize(8192);
+        o->ev_family.assign(4096, -1);
         for (auto &e : o->ev) CK(cudaEventCreate(&e));
         CK(o->hist.ensure(sizeof(GmresStats) * 4096));
     }
@@ -825,25 +828,32 @@ extern "C" int phg_ops_profile(phg_ops o, int enable) {
     return PHG_OK;
 }
 
-extern "C" int phg_ops_profile_read(phg_ops o, int *launches, double *ms, double *bytes) {
+extern "C" int phg_ops_profile_read_family(phg_ops o, int family, int *launches, double *ms, double *bytes) {
     if (!o) return fail(PHG_ERR_ARG, "NULL handle");
     const int n = o->nev / 2;
     double t = 0.0, b = 0.0;
+    int cnt = 0;
     if (n > 0) {
         CK(cudaEventSynchronize(o->ev[o->nev - 1]));
         std::vector<GmresStats> h(n);
         CK(cudaMemcpy(h.data(), o->hist.p, sizeof(GmresStats) * n, cudaMemcpyDeviceToHost));
         for (int k = 0; k < n; ++k) {
+            if (family >= 0 && o->ev_family[k] != family) continue;
             float dt = 0.f;
             CK(cudaEventElapsedTime(&dt, o->ev[2 * k], o->ev[2 * k + 1]));
             t += dt;
             b += h[k].bytes;
+            ++cnt;
         }
     }
-    if (launches) *launches = n;
+    if (launches) *launches = cnt;
     if (ms) *ms = t;
     if (bytes) *bytes = b;
     return PHG_OK;
+}
+
+extern "C" int phg_ops_profile_read(phg_ops o, int *launches, double *ms, double *bytes) {
+    return phg_ops_profile_read_family(o, -1, launches, ms, bytes);
 }
 
 extern "C" int phg_laplace_calc2(phg_ops o, double *ans, const double *F, void *stream) {

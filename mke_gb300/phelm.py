@@ -80,6 +80,7 @@ SIGNATURES = {
     "phg_ops_last_solve": (C.c_int, [_vp, _ip, _ip, _dp]),
     "phg_ops_profile": (C.c_int, [_vp, C.c_int]),
     "phg_ops_profile_read": (C.c_int, [_vp, _ip, _dp, _dp]),
+    "phg_ops_profile_read_family": (C.c_int, [_vp, C.c_int, _ip, _dp, _dp]),
     "phg_laplace_calc1": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "phg_laplace_calc2": (C.c_int, [_vp, _vp, _vp, _vp]),
     "phg_laplace_solve": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
@@ -328,9 +329,12 @@ class Operators:
     def profile(self, enable=True):
         _check(lib().phg_ops_profile(self._h, 1 if enable else 0))
 
-    def profile_read(self):
+    def profile_read(self, family: int = -1):
+        """Solver launches recorded since profile(True): count, event-timed ms
+        and algorithmic bytes; family restricts to one solver family
+        (0 GMRES, 1 Chebyshev, 2 multigrid GMRES, 3 baroclinic block system)."""
         n, ms, b = C.c_int(), C.c_double(), C.c_double()
-        _check(lib().phg_ops_profile_read(self._h, C.byref(n), C.byref(ms), C.byref(b)))
+        _check(lib().phg_ops_profile_read_family(self._h, int(family), C.byref(n), C.byref(ms), C.byref(b)))
         return {"launches": n.value, "ms": ms.value, "bytes": b.value}
 
     @property
