@@ -1018,7 +1018,7 @@ int tune_solve(phg_ops_s *o, const char *label, const DevSolveOp &op, int nv, cu
     if (need > o->work.n) { CK(cudaStreamSynchronize(s)); CK(o->work.ensure(need)); }
     std::vector<SolveShape> cand;
     for (int rpb : {128, 256, 512, 1024}) { SolveShape c; c.rpb = rpb; c.path = 0; cand.push_back(c); }
-    if (fam == 1 && pr == PREC_MIXED && nv >= 8) { SolveShape c; c.rpb = 0; c.path = 1; cand.push_back(c); }
+    if ((fam == 1 || fam == 2) && pr == PREC_MIXED && nv >= 8) { SolveShape c; c.rpb = 0; c.path = 1; cand.push_back(c); }
     float best = 1e30f;
     SolveShape pick;
     bool any = false;

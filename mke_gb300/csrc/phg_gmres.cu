@@ -49,6 +49,9 @@ constexpr long long SPIN_LIMIT = 2000000000LL;  // clock64 cycles (~1 s)
 constexpr int CHEB_KMAX = 64;    // most Chebyshev steps per refinement cycle
 constexpr int LS_MIN_RHS = 32;   // right-hand sides from which the lockstep path runs
 constexpr int LS_MIN_TUNED = 8;  // the fewest for which the autotuner may choose it
+// right-hand sides from which the multigrid Laplacian runs in lockstep by
+// default (below: only when the autotuner chose it)
+constexpr int LSG_DEFAULT_RHS = 1 << 30;
 
 struct Params {
     DevSolveOp op;
@@ -1310,6 +1313,644 @@ int env_int(const char *name, int dflt) {
     return e ? atoi(e) : dflt;
 }
 
+// ------------------------------------------------ lockstep multigrid FGMRES ---
+// Many right-hand sides of the multigrid-preconditioned Laplacian solve in
+// lockstep (the Laplace solves of an ensemble step).  The algorithm is the one
+// gmres_kernel runs for each member -- restarted FGMRES, right-preconditioned
+// by a V-cycle with one damped-Jacobi sweep down and one up and a dense
+// coarsest solve, FP32 inner cycles inside an FP64 refinement loop with the
+// same stopping tests -- but the Krylov and multigrid vectors of all members
+// are interleaved FP32 multi-vectors (row i holds the nvp members
+// contiguously) and every phase is one short kernel over all members: a
+// gathered row is read once as whole 16-byte member chunks, and no block
+// waits on another.  Per-member state (Hessenberg factor, rotations,
+// stopping tests) lives in device arrays.  Device flags end the remaining
+// launches of a cycle once every member has met its inner target and of the
+// solve once every member has stopped, without a host synchronisation, so
+// the whole solve can sit in a captured step graph; every kernel walks its
+// index range with a grid-stride loop over a grid capped at a few blocks per
+// SM, so a launch that finds its flag set costs little.
+constexpr int LSG_M = 8;        // Arnoldi steps per refinement cycle
+constexpr int LSG_MAXC = 4;     // refinement cycles at most
+constexpr int LSG_MINRHS = 8;   // fewest right-hand sides the path accepts
+
+struct LsgLevel {               // one multigrid level; buffers n x nvp FP32
+    int n, W, Wr;
+    const int *col; const float *a; const float *d;
+    const int *pc; const float *pw;      // prolongation from level + 1
+    const int *rf; const float *rw;      // restriction to level + 1
+    float *x, *xo, *r, *b;
+};
+
+struct LsgParams {
+    int n, nv, nvp, q4, m, nlev, W, RB, nbx, ld, max_iter;
+    double tol, inner_rtol, step_row_bytes, resid_row_bytes;
+    float omega;
+    const int *col; const float *a32;    // fine operator, FP32 (w = A z)
+    LsgLevel lev[MG_MAXLEV];
+    int nc; const float *cinv;           // coarsest level, dense inverse
+    const double *B; double *X;          // member-major FP64, leading dimension ld
+    float *V, *Z, *w;                    // (m + 1), m and 1 interleaved vectors
+    double *R, *rpart, *bpart, *nrm;     // FP64 residual, norm partials, norms (2 per member)
+    double *dpart, *npart;               // RB x (m + 1) x nvp dot partials; RB x nvp norm partials
+    double *hcol, *H, *cs, *sn, *g;      // per member: column (m + 1), R factor (m + 1) x m, rotations, rhs
+    float *hv, *yv;                      // per member: FP32 column, FP32 solution
+    double *bnorm, *beta_prev, *target, *relv;
+    float *scale, *vscale;
+    int *stt, *arn, *jl, *iters, *cycles, *zerox, *cnt, *done;
+    GmresStats *st;
+};
+
+__device__ __forceinline__ unsigned lsg_grid_stride() { return gridDim.x * blockDim.x; }
+
+// per member: the refinement test on ||b - A x|| (norms from k_ls_nrm) and the
+// start of the next cycle; 0 members left sets the solve's done flag
+__global__ void __launch_bounds__(256) k_lsg_begin(LsgParams P, int c) {
+    if (*(volatile int *)P.done) return;
+    __shared__ double rmax[NWARP];
+    __shared__ int open[NWARP], bad[NWARP], itm[NWARP], cym[NWARP], its[NWARP];
+    double mx = 0.0;
+    int nopen = 0, nbad = 0, imax = 0, cmax = 0, isum = 0;
+    const int m = P.m;
+    for (int v = threadIdx.x; v < P.nvp; v += blockDim.x) {
+        P.jl[v] = 0;
+        P.vscale[v] = 0.f;
+        if (v >= P.nv) { P.scale[v] = 0.f; P.arn[v] = 0; continue; }
+        if (c == 0) {
+            P.bnorm[v] = sqrt(P.nrm[2 * v + 1]);
+            P.stt[v] = 0; P.iters[v] = 0; P.cycles[v] = 0; P.beta_prev[v] = 0.0; P.relv[v] = 0.0;
+            P.zerox[v] = P.bnorm[v] == 0.0;
+        }
+        int s = P.stt[v];
+        if (s == 0) {
+            const double bn = P.bnorm[v];
+            if (bn == 0.0) { s = 1; P.relv[v] = 0.0; }
+            else {
+                const double beta = sqrt(P.nrm[2 * v]), rel = beta / bn;
+                P.relv[v] = rel;
+                if (rel <= P.tol) s = 1;
+                else if (P.iters[v] >= P.max_iter) s = 2;
+                else if (P.cycles[v] > 0 && !(beta < 0.9999 * P.beta_prev[v])) s = 2;
+                else if (c == LSG_MAXC) s = 2;   // out of cycles
+                if (s == 0) {
+                    P.beta_prev[v] = beta;
+                    P.cycles[v] += 1;
+                    P.target[v] = fmax(P.tol * bn, P.inner_rtol * beta);
+                    double *g = P.g + (size_t)v * (m + 1);
+                    g[0] = beta;
+                    for (int l = 1; l <= m; ++l) g[l] = 0.0;
+                    P.scale[v] = (float)(1.0 / beta);
+                    P.arn[v] = 1;
+                    ++nopen;
+                }
+            }
+            P.stt[v] = s;
+        }
+        if (s != 0) { P.scale[v] = 0.f; P.arn[v] = 0; }
+        const double rel = P.relv[v];
+        mx = fmax(mx, rel);
+        if (!(rel == rel)) mx = rel;
+        nbad += s == 2 ? 1 : 0;
+        imax = max(imax, P.iters[v]);
+        cmax = max(cmax, P.cycles[v]);
+        isum += P.iters[v];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        nopen += __shfl_xor_sync(0xffffffffu, nopen, o);
+        nbad += __shfl_xor_sync(0xffffffffu, nbad, o);
+        imax = max(imax, __shfl_xor_sync(0xffffffffu, imax, o));
+        cmax = max(cmax, __shfl_xor_sync(0xffffffffu, cmax, o));
+        isum += __shfl_xor_sync(0xffffffffu, isum, o);
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) { rmax[w] = mx; open[w] = nopen; bad[w] = nbad; itm[w] = imax; cym[w] = cmax; its[w] = isum; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = 0.0;
+        int o = 0, b = 0, im = 0, cm = 0, is = 0;
+        for (int k = 0; k < NWARP; ++k) {
+            r = fmax(r, rmax[k]); o += open[k]; b += bad[k]; im = max(im, itm[k]); cm = max(cm, cym[k]); is += its[k];
+        }
+        P.st->relres = r;
+        P.st->status = (o || b) ? 1 : 0;
+        P.st->iters = im;
+        P.st->cycles = cm;
+        P.st->steps_total = is;
+        P.st->bytes += P.resid_row_bytes * P.n * (double)P.nv;
+        P.cnt[0] = o;
+        for (int l = 1; l <= m; ++l) P.cnt[l] = 0;
+        if (!o) *P.done = 1;
+    }
+}
+
+// x = 0 for members whose right-hand side is zero (as the per-member solver)
+__global__ void __launch_bounds__(256) k_lsg_zero(LsgParams P) {
+    const long long total = (long long)P.nv * P.n;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += lsg_grid_stride()) {
+        const int v = (int)(t / P.n), i = (int)(t - (long long)v * P.n);
+        if (P.zerox[v]) P.X[(size_t)v * P.ld + i] = 0.0;
+    }
+}
+
+// V_0 = (float)(R * scale): member-major FP64 -> interleaved FP32 (tiled transpose)
+__global__ void __launch_bounds__(256) k_lsg_v0(LsgParams P) {
+    if (*(volatile int *)P.done) return;
+    __shared__ float t[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int ntile = (P.n + 31) / 32, mtile = P.nvp / 32;
+    for (int tile = blockIdx.x; tile < ntile * mtile; tile += gridDim.x) {
+        const int i0 = (tile % ntile) * 32, v0 = (tile / ntile) * 32;
+        for (int j = ty; j < 32; j += 8) {
+            const int v = v0 + j, i = i0 + tx;
+            t[j][tx] = (v < P.nv && i < P.n) ? (float)(P.R[(size_t)v * P.n + i] * (double)P.scale[v]) : 0.f;
+        }
+        __syncthreads();
+        for (int j = ty; j < 32; j += 8) {
+            const int i = i0 + j;
+            if (i < P.n) P.V[(size_t)i * P.nvp + v0 + tx] = t[tx][j];
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ float4 f4fma(float a, float4 x, float4 s) {
+    return make_float4(fmaf(a, x.x, s.x), fmaf(a, x.y, s.y), fmaf(a, x.z, s.z), fmaf(a, x.w, s.w));
+}
+
+__device__ __forceinline__ bool lsg_skip(const LsgParams &P, int j) {
+    return *(volatile const int *)P.done || (j >= 0 && *(volatile const int *)&P.cnt[j] == 0);
+}
+
+// down sweep at level l: x = w D^-1 b, r = b - A x (from b alone)
+__global__ void __launch_bounds__(256) k_mg_down(LsgParams P, LsgLevel L, const float *src, int j) {
+    if (lsg_skip(P, j)) return;
+    const int q4 = P.q4;
+    const float4 *b = (const float4 *)src;
+    float4 *x = (float4 *)L.x, *r = (float4 *)L.r;
+    const float om = P.omega;
+    const long long total = (long long)L.n * q4;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += lsg_grid_stride()) {
+        const int i = (int)(t / q4), q = (int)(t - (long long)i * q4);
+        int c[8];
+        float a[8];
+        float4 g[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < L.W) { c[k] = __ldg(&L.col[(size_t)k * L.n + i]); a[k] = __ldg(&L.a[(size_t)k * L.n + i]); }
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < L.W) g[k] = b[(size_t)c[k] * q4 + q];
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < L.W) s = f4fma(a[k] * (om * __ldg(&L.d[c[k]])), g[k], s);
+        const float4 bi = b[(size_t)i * q4 + q];
+        const float di = om * __ldg(&L.d[i]);
+        x[(size_t)i * q4 + q] = make_float4(di * bi.x, di * bi.y, di * bi.z, di * bi.w);
+        r[(size_t)i * q4 + q] = make_float4(bi.x - s.x, bi.y - s.y, bi.z - s.z, bi.w - s.w);
+    }
+}
+
+// b_{l+1} = R r_l
+__global__ void __launch_bounds__(256) k_mg_restrict(LsgParams P, LsgLevel L, LsgLevel C, int j) {
+    if (lsg_skip(P, j)) return;
+    const int q4 = P.q4, nc = C.n;
+    const float4 *r = (const float4 *)L.r;
+    float4 *bc = (float4 *)C.b;
+    const long long total = (long long)nc * q4;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += lsg_grid_stride()) {
+        const int cc = (int)(t / q4), q = (int)(t - (long long)cc * q4);
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int k = 0; k < L.Wr; ++k) {
+            const int f = __ldg(&L.rf[(size_t)k * nc + cc]);
+            if (f >= 0) s = f4fma(__ldg(&L.rw[(size_t)k * nc + cc]), r[(size_t)f * q4 + q], s);
+        }
+        bc[(size_t)cc * q4 + q] = s;
+    }
+}
+
+// coarsest level: x = C^-1 b (dense)
+__global__ void __launch_bounds__(256) k_mg_coarse(LsgParams P, LsgLevel C, int j) {
+    if (lsg_skip(P, j)) return;
+    const int n = P.nc, q4 = P.q4;
+    const float4 *b = (const float4 *)C.b;
+    float4 *x = (float4 *)C.x;
+    const long long total = (long long)n * q4;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += lsg_grid_stride()) {
+        const int i = (int)(t / q4), q = (int)(t - (long long)i * q4);
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int k = 0; k < n; ++k) s = f4fma(__ldg(&P.cinv[(size_t)i * n + k]), b[(size_t)k * q4 + q], s);
+        x[(size_t)i * q4 + q] = s;
+    }
+}
+
+// x_l += P x_{l+1}
+__global__ void __launch_bounds__(256) k_mg_prolong(LsgParams P, LsgLevel L, const float *xcoarse, int j) {
+    if (lsg_skip(P, j)) return;
+    const int q4 = P.q4;
+    const float4 *xc = (const float4 *)xcoarse;
+    float4 *x = (float4 *)L.x;
+    const long long total = (long long)L.n * q4;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += lsg_grid_stride()) {
+        const int i = (int)(t / q4), q = (int)(t - (long long)i * q4);
+        const int c0 = __ldg(&L.pc[2 * i]), c1 = __ldg(&L.pc[2 * i + 1]);
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (c0 >= 0) s = f4fma(__ldg(&L.pw[2 * i]), xc[(size_t)c0 * q4 + q], s);
+        if (c1 >= 0) s = f4fma(__ldg(&L.pw[2 * i + 1]), xc[(size_t)c1 * q4 + q], s);
+        float4 xi = x[(size_t)i * q4 + q];
+        x[(size_t)i * q4 + q] = make_float4(xi.x + s.x, xi.y + s.y, xi.z + s.z, xi.w + s.w);
+    }
+}
+
+// post-smoothing at level l: out = x + w D^-1 (b - A x)
+__global__ void __launch_bounds__(256) k_mg_smooth(LsgParams P, LsgLevel L, const float *bsrc, float *out, int j) {
+    if (lsg_skip(P, j)) return;
+    const int q4 = P.q4;
+    const float4 *b = (const float4 *)bsrc, *x = (const float4 *)L.x;
+    float4 *o = (float4 *)out;
+    const float om = P.omega;
+    const long long total = (long long)L.n * q4;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += lsg_grid_stride()) {
+        const int i = (int)(t / q4), q = (int)(t - (long long)i * q4);
+        int c[8];
+        float a[8];
+        float4 g[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < L.W) { c[k] = __ldg(&L.col[(size_t)k * L.n + i]); a[k] = __ldg(&L.a[(size_t)k * L.n + i]); }
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < L.W) g[k] = x[(size_t)c[k] * q4 + q];
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < L.W) s = f4fma(a[k], g[k], s);
+        const float4 bi = b[(size_t)i * q4 + q], xi = x[(size_t)i * q4 + q];
+        const float di = om * __ldg(&L.d[i]);
+        o[(size_t)i * q4 + q] = make_float4(xi.x + di * (bi.x - s.x), xi.y + di * (bi.y - s.y),
+                                            xi.z + di * (bi.z - s.z), xi.w + di * (bi.w - s.w));
+    }
+}
+
+// w = A z_j (fine operator, FP32)
+__global__ void __launch_bounds__(256) k_lsg_spmm(LsgParams P, int j) {
+    if (lsg_skip(P, j)) return;
+    const int q4 = P.q4, n = P.n, W = P.W;
+    const float4 *z = (const float4 *)(P.Z + (size_t)j * n * P.nvp);
+    float4 *w = (float4 *)P.w;
+    const long long total = (long long)n * q4;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += lsg_grid_stride()) {
+        const int i = (int)(t / q4), q = (int)(t - (long long)i * q4);
+        int c[8];
+        float a[8];
+        float4 g[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < W) { c[k] = __ldg(&P.col[(size_t)k * n + i]); a[k] = __ldg(&P.a32[(size_t)k * n + i]); }
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < W) g[k] = z[(size_t)c[k] * q4 + q];
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < W) s = f4fma(a[k], g[k], s);
+        w[(size_t)i * q4 + q] = s;
+    }
+}
+
+// dot partials: dpart[rb][l][v] = sum over the block's rows of V_l[r][v] w[r][v], l <= j
+// (grid RB x nvp/32; lane = member, warps stride the rows; eight vectors per pass)
+__global__ void __launch_bounds__(256) k_lsg_dot(LsgParams P, int j) {
+    if (lsg_skip(P, j)) return;
+    __shared__ double red[NWARP][8][32];
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const int v = blockIdx.y * 32 + lane, nvp = P.nvp, n = P.n;
+    const int rpr = (n + P.RB - 1) / P.RB;
+    const int r0 = min(n, (int)blockIdx.x * rpr), r1 = min(n, r0 + rpr);
+    const size_t vs = (size_t)n * nvp;
+    for (int l0 = 0; l0 <= j; l0 += 8) {
+        const int kk = min(8, j + 1 - l0);
+        float t[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        for (int r = r0 + wp; r < r1; r += NWARP) {
+            const float s = P.w[(size_t)r * nvp + v];
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (k < kk) t[k] += P.V[(size_t)(l0 + k) * vs + (size_t)r * nvp + v] * s;
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) red[wp][k][lane] = (double)t[k];
+        __syncthreads();
+        for (int e = threadIdx.x; e < kk * 32; e += blockDim.x) {
+            const int k = e >> 5, ln = e & 31;
+            double s = 0.0;
+            for (int q = 0; q < NWARP; ++q) s += red[q][k][ln];
+            P.dpart[((size_t)blockIdx.x * (P.m + 1) + l0 + k) * nvp + blockIdx.y * 32 + ln] = s;
+        }
+        __syncthreads();
+    }
+}
+
+// h[v][l] = sum over row blocks of the partials (one warp per (member, l), fixed order)
+__global__ void __launch_bounds__(256) k_lsg_hsum(LsgParams P, int j) {
+    if (lsg_skip(P, j)) return;
+    const int pair = blockIdx.x * NWARP + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (pair >= P.nv * (j + 1)) return;
+    const int v = pair / (j + 1), l = pair - v * (j + 1);
+    double s = 0.0;
+    for (int rb = lane; rb < P.RB; rb += 32) s += P.dpart[((size_t)rb * (P.m + 1) + l) * P.nvp + v];
+    s = warp_sum(s);
+    if (lane == 0) {
+        P.hcol[(size_t)v * (P.m + 1) + l] = s;
+        P.hv[(size_t)v * (P.m + 1) + l] = (float)s;
+    }
+}
+
+// w -= sum_l h_l V_l; ||w||^2 partials per row block
+__global__ void __launch_bounds__(256) k_lsg_update(LsgParams P, int j) {
+    if (lsg_skip(P, j)) return;
+    __shared__ double red[NWARP][32];
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const int v = blockIdx.y * 32 + lane, nvp = P.nvp, n = P.n;
+    const int rpr = (n + P.RB - 1) / P.RB;
+    const int r0 = min(n, (int)blockIdx.x * rpr), r1 = min(n, r0 + rpr);
+    const size_t vs = (size_t)n * nvp;
+    float h[LSG_M];
+#pragma unroll
+    for (int l = 0; l < LSG_M; ++l) h[l] = (l <= j && v < P.nv) ? P.hv[(size_t)v * (P.m + 1) + l] : 0.f;
+    float a2 = 0.f;
+    for (int r = r0 + wp; r < r1; r += NWARP) {
+        float s = P.w[(size_t)r * nvp + v];
+#pragma unroll
+        for (int l = 0; l < LSG_M; ++l)
+            if (l <= j) s -= h[l] * P.V[(size_t)l * vs + (size_t)r * nvp + v];
+        P.w[(size_t)r * nvp + v] = s;
+        a2 += s * s;
+    }
+    red[wp][lane] = (double)a2;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double s = 0.0;
+        for (int q = 0; q < NWARP; ++q) s += red[q][threadIdx.x];
+        P.npart[(size_t)blockIdx.x * nvp + blockIdx.y * 32 + threadIdx.x] = s;
+    }
+}
+
+// ||w||, the rotations, the stopping test (one warp per member)
+__global__ void __launch_bounds__(256) k_lsg_givens(LsgParams P, int j) {
+    if (lsg_skip(P, j)) return;
+    const int v = blockIdx.x * NWARP + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (v >= P.nv) return;
+    double s = 0.0;
+    for (int rb = lane; rb < P.RB; rb += 32) s += P.npart[(size_t)rb * P.nvp + v];
+    s = warp_sum(s);
+    if (lane != 0) return;
+    if (!P.arn[v]) { P.vscale[v] = 0.f; return; }
+    const int m = P.m;
+    double *hc = P.hcol + (size_t)v * (m + 1), *H = P.H + (size_t)v * (m + 1) * m;
+    double *cs = P.cs + (size_t)v * m, *sn = P.sn + (size_t)v * m, *g = P.g + (size_t)v * (m + 1);
+    const double hn = sqrt(s);
+    hc[j + 1] = hn;
+    for (int l = 0; l < j; ++l) {
+        const double a = hc[l], c = hc[l + 1];
+        hc[l] = cs[l] * a + sn[l] * c;
+        hc[l + 1] = -sn[l] * a + cs[l] * c;
+    }
+    const double a = hc[j], c = hc[j + 1];
+    const double r = hypot(a, c);
+    cs[j] = r > 0.0 ? a / r : 1.0;
+    sn[j] = r > 0.0 ? c / r : 0.0;
+    for (int l = 0; l < j; ++l) H[(size_t)l * m + j] = hc[l];
+    H[(size_t)j * m + j] = r;
+    g[j + 1] = -sn[j] * g[j];
+    g[j] = cs[j] * g[j];
+    P.iters[v] += 1;
+    P.jl[v] = j + 1;
+    atomicAdd(&P.st->bytes, P.step_row_bytes * P.n + 8.0 * (j + 1) * P.n);
+    const bool stop = fabs(g[j + 1]) <= P.target[v] || hn == 0.0 || P.iters[v] >= P.max_iter || j + 1 == m;
+    if (stop) { P.arn[v] = 0; P.vscale[v] = 0.f; }
+    else { P.vscale[v] = (float)(1.0 / hn); atomicAdd(&P.cnt[j + 1], 1); }
+}
+
+// V_{j+1} = w * vscale (0 for members out of the Arnoldi loop)
+__global__ void __launch_bounds__(256) k_lsg_norm(LsgParams P, int j) {
+    if (lsg_skip(P, j + 1)) return;
+    const int q4 = P.q4;
+    const float4 *w = (const float4 *)P.w, *vs4 = (const float4 *)P.vscale;
+    float4 *vn = (float4 *)(P.V + (size_t)(j + 1) * P.n * P.nvp);
+    const long long total = (long long)P.n * q4;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += lsg_grid_stride()) {
+        const int i = (int)(t / q4), q = (int)(t - (long long)i * q4);
+        const float4 a = w[(size_t)i * q4 + q], sc = vs4[q];
+        vn[(size_t)i * q4 + q] = make_float4(a.x * sc.x, a.y * sc.y, a.z * sc.z, a.w * sc.w);
+    }
+}
+
+// y = H^-1 g over each member's jl columns (FP64), FP32 copy for the correction
+__global__ void __launch_bounds__(256) k_lsg_solve(LsgParams P) {
+    if (*(volatile int *)P.done) return;
+    const int m = P.m;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < P.nvp; v += lsg_grid_stride()) {
+        float *yv = P.yv + (size_t)v * m;
+        const int jl = v < P.nv ? P.jl[v] : 0;
+        double y[LSG_M];
+        const double *H = P.H + (size_t)v * (m + 1) * m, *g = P.g + (size_t)v * (m + 1);
+        for (int l = jl - 1; l >= 0; --l) {
+            double s = g[l];
+            for (int k = l + 1; k < jl; ++k) s -= H[(size_t)l * m + k] * y[k];
+            y[l] = s / H[(size_t)l * m + l];
+        }
+        for (int l = 0; l < m; ++l) yv[l] = l < jl ? (float)y[l] : 0.f;
+    }
+}
+
+// x += sum_l y_l z_l: interleaved FP32 -> member-major FP64 (tiled transpose)
+__global__ void __launch_bounds__(256) k_lsg_correct(LsgParams P) {
+    if (*(volatile int *)P.done) return;
+    __shared__ float t[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, m = P.m, n = P.n, nvp = P.nvp;
+    const int ntile = (n + 31) / 32, mtile = nvp / 32;
+    const size_t vs = (size_t)n * nvp;
+    for (int tile = blockIdx.x; tile < ntile * mtile; tile += gridDim.x) {
+        const int i0 = (tile % ntile) * 32, v0 = (tile / ntile) * 32;
+        const int v = v0 + tx;
+        // only the member's own Arnoldi columns: later ones were not written this cycle
+        const int jv = v < P.nv ? P.jl[v] : 0;
+        float y[LSG_M];
+#pragma unroll
+        for (int l = 0; l < LSG_M; ++l) y[l] = l < jv ? P.yv[(size_t)v * m + l] : 0.f;
+        for (int jj = ty; jj < 32; jj += 8) {
+            const int i = i0 + jj;
+            float s = 0.f;
+            if (i < n)
+#pragma unroll
+                for (int l = 0; l < LSG_M; ++l)
+                    if (l < jv) s += y[l] * P.Z[(size_t)l * vs + (size_t)i * nvp + v];
+            t[jj][tx] = s;
+        }
+        __syncthreads();
+        for (int jj = ty; jj < 32; jj += 8) {
+            const int vv = v0 + jj, i = i0 + tx;
+            if (vv < P.nv && i < n && P.jl[vv] > 0) P.X[(size_t)vv * P.ld + i] += (double)t[tx][jj];
+        }
+        __syncthreads();
+    }
+}
+
+struct LsgLayout {
+    size_t V, Z, w, R, lev[MG_MAXLEV], rpart, bpart, nrm, dpart, npart, hcol, H, cs, sn, g, hv, yv;
+    size_t bnorm, beta_prev, target, relv, scale, vscale, ints, total;
+    int nvp, m, RB, nbx;
+};
+
+LsgLayout lsg_layout(const DevSolveOp &op, int nv, int restart) {
+    LsgLayout L;
+    const size_t n = (size_t)op.A.n;
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    L.nvp = (nv + 31) / 32 * 32;
+    L.m = restart < LSG_M ? restart : LSG_M;
+    L.nbx = (int)((n + 255) / 256);
+    int rb = 4 * sm_count() / (L.nvp / 32);
+    const int rbmax = (int)((n + 63) / 64);
+    L.RB = rb < 1 ? 1 : (rb > rbmax ? rbmax : rb);
+    const size_t nvp = (size_t)L.nvp, m = (size_t)L.m, vec = al(4 * n * nvp);
+    size_t o = 0;
+    L.V = o; o += (m + 1) * vec;
+    L.Z = o; o += m * vec;
+    L.w = o; o += vec;
+    L.R = o; o += al(8 * n * (size_t)nv);
+    for (int l = 0; l < op.mg.nlev && l < MG_MAXLEV; ++l) { L.lev[l] = o; o += 4 * al(4 * (size_t)op.mg.lev[l].n * nvp); }
+    L.rpart = o; o += al(8 * (size_t)nv * L.nbx);
+    L.bpart = o; o += al(8 * (size_t)nv * L.nbx);
+    L.nrm = o; o += al(16 * nvp);
+    L.dpart = o; o += al(8 * (size_t)L.RB * (m + 1) * nvp);
+    L.npart = o; o += al(8 * (size_t)L.RB * nvp);
+    L.hcol = o; o += al(8 * nvp * (m + 1));
+    L.H = o; o += al(8 * nvp * (m + 1) * m);
+    L.cs = o; o += al(8 * nvp * m);
+    L.sn = o; o += al(8 * nvp * m);
+    L.g = o; o += al(8 * nvp * (m + 1));
+    L.hv = o; o += al(4 * nvp * (m + 1));
+    L.yv = o; o += al(4 * nvp * m);
+    L.bnorm = o; o += al(8 * nvp);
+    L.beta_prev = o; o += al(8 * nvp);
+    L.target = o; o += al(8 * nvp);
+    L.relv = o; o += al(8 * nvp);
+    L.scale = o; o += al(4 * nvp);
+    L.vscale = o; o += al(4 * nvp);
+    L.ints = o; o += al(4 * (6 * nvp + m + 2 + 1));
+    L.total = o;
+    return L;
+}
+
+bool lsg_applicable(const DevSolveOp &op, int nv, Precision p, int restart) {
+    if (p != PREC_MIXED || !op.mgd || op.block4 || op.A.W > 8 || !op.a32 || nv < LSG_MINRHS || restart < 2) return false;
+    if (op.mg.nu1 != 1 || op.mg.nu2 != 1 || op.mg.nlev < 2 || op.mg.nlev > MG_MAXLEV || !op.mg.cinv32) return false;
+    for (int l = 0; l < op.mg.nlev; ++l) {
+        const MgLevelDev &D = op.mg.lev[l];
+        if (D.W > 8 || !D.a32 || !D.d32) return false;
+        if (l + 1 < op.mg.nlev && (!D.pc || !D.pw32 || !D.rf || !D.rw32)) return false;
+    }
+    return (long long)op.A.n * ((nv + 31) / 32 * 8) < (1LL << 31);
+}
+
+unsigned lsg_blocks(long long work) {
+    long long b = (work + 255) / 256;
+    const long long cap = 4LL * sm_count();
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+
+cudaError_t lsg_solve(const DevSolveOp &op, const double *B, double *X, int nv, int ld, int restart, int max_iter,
+                      double tol, double inner_rtol, char *w, GmresStats *st, double mg_row_bytes, cudaStream_t s) {
+    const LsgLayout Lo = lsg_layout(op, nv, restart);
+    const int n = op.A.n, W = op.A.W, nvp = Lo.nvp, m = Lo.m, nlev = op.mg.nlev, last = nlev - 1;
+    LsgParams P;
+    memset(&P, 0, sizeof P);
+    P.n = n; P.nv = nv; P.nvp = nvp; P.q4 = nvp / 4; P.m = m; P.nlev = nlev; P.W = W; P.RB = Lo.RB; P.nbx = Lo.nbx;
+    P.ld = ld; P.max_iter = max_iter; P.tol = tol; P.inner_rtol = inner_rtol;
+    // algorithmic bytes per member and row (the per-member solver's model, FP32 vectors)
+    P.step_row_bytes = W * 8.0 + 4.0 * 6.0 + mg_row_bytes;
+    P.resid_row_bytes = W * 12.0 + 24.0;
+    P.omega = (float)op.mg.omega;
+    P.col = op.A.col; P.a32 = op.a32;
+    for (int l = 0; l < nlev; ++l) {
+        const MgLevelDev &D = op.mg.lev[l];
+        LsgLevel &E = P.lev[l];
+        E.n = D.n; E.W = D.W; E.Wr = D.Wr; E.col = D.col; E.a = D.a32; E.d = D.d32;
+        E.pc = D.pc; E.pw = D.pw32; E.rf = D.rf; E.rw = D.rw32;
+        const size_t lv = (((size_t)D.n * nvp * 4) + 255) & ~size_t(255);
+        E.x = (float *)(w + Lo.lev[l]); E.xo = (float *)(w + Lo.lev[l] + lv);
+        E.r = (float *)(w + Lo.lev[l] + 2 * lv); E.b = (float *)(w + Lo.lev[l] + 3 * lv);
+    }
+    P.nc = op.mg.nc; P.cinv = op.mg.cinv32;
+    P.B = B; P.X = X;
+    P.V = (float *)(w + Lo.V); P.Z = (float *)(w + Lo.Z); P.w = (float *)(w + Lo.w);
+    P.R = (double *)(w + Lo.R); P.rpart = (double *)(w + Lo.rpart); P.bpart = (double *)(w + Lo.bpart);
+    P.nrm = (double *)(w + Lo.nrm); P.dpart = (double *)(w + Lo.dpart); P.npart = (double *)(w + Lo.npart);
+    P.hcol = (double *)(w + Lo.hcol); P.H = (double *)(w + Lo.H); P.cs = (double *)(w + Lo.cs);
+    P.sn = (double *)(w + Lo.sn); P.g = (double *)(w + Lo.g); P.hv = (float *)(w + Lo.hv); P.yv = (float *)(w + Lo.yv);
+    P.bnorm = (double *)(w + Lo.bnorm); P.beta_prev = (double *)(w + Lo.beta_prev);
+    P.target = (double *)(w + Lo.target); P.relv = (double *)(w + Lo.relv);
+    P.scale = (float *)(w + Lo.scale); P.vscale = (float *)(w + Lo.vscale);
+    int *ip = (int *)(w + Lo.ints);
+    P.stt = ip; P.arn = ip + nvp; P.jl = ip + 2 * nvp; P.iters = ip + 3 * nvp; P.cycles = ip + 4 * nvp;
+    P.zerox = ip + 5 * nvp; P.cnt = ip + 6 * nvp; P.done = P.cnt + m + 1;
+    P.st = st;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(st, 0, sizeof(GmresStats), s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(P.done, 0, sizeof(int), s)) != cudaSuccess) return e;
+    long long launches = 0;
+    const dim3 rgrid((unsigned)Lo.nbx, (unsigned)((nv + LS_MG - 1) / LS_MG));
+    k_ls_sq<<<rgrid, 256, 0, s>>>(B, n, ld, nv, P.bpart);
+    ++launches;
+    const unsigned gn = lsg_blocks((long long)n * P.q4);
+    const dim3 red_grid((unsigned)Lo.RB, (unsigned)(nvp / 32));
+    const unsigned tiles = lsg_blocks((long long)((n + 31) / 32) * (nvp / 32) * 256);
+    for (int c = 0; c <= LSG_MAXC; ++c) {
+        switch (W) {
+        case 6: k_ls_resid<6><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, P.R, nv, P.rpart, P.done); break;
+        case 7: k_ls_resid<7><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, P.R, nv, P.rpart, P.done); break;
+        default: k_ls_resid<8><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, P.R, nv, P.rpart, P.done); break;
+        }
+        k_ls_nrm<<<(nv + NWARP - 1) / NWARP, 256, 0, s>>>(P.rpart, P.bpart, Lo.nbx, P.nrm, nv, P.done);
+        k_lsg_begin<<<1, 256, 0, s>>>(P, c);
+        launches += 3;
+        if (c == 0) { k_lsg_zero<<<lsg_blocks((long long)nv * n), 256, 0, s>>>(P); ++launches; }
+        if (c == LSG_MAXC) break;
+        k_lsg_v0<<<tiles, 256, 0, s>>>(P);
+        ++launches;
+        for (int j = 0; j < m; ++j) {
+            const float *vj = P.V + (size_t)j * n * nvp;
+            for (int l = 0; l < last; ++l) {
+                k_mg_down<<<lsg_blocks((long long)P.lev[l].n * P.q4), 256, 0, s>>>(P, P.lev[l], l == 0 ? vj : P.lev[l].b, j);
+                k_mg_restrict<<<lsg_blocks((long long)P.lev[l + 1].n * P.q4), 256, 0, s>>>(P, P.lev[l], P.lev[l + 1], j);
+            }
+            k_mg_coarse<<<lsg_blocks((long long)P.nc * P.q4), 256, 0, s>>>(P, P.lev[last], j);
+            for (int l = last - 1; l >= 0; --l) {
+                const float *xc = (l + 1 == last) ? P.lev[last].x : P.lev[l + 1].xo;
+                k_mg_prolong<<<lsg_blocks((long long)P.lev[l].n * P.q4), 256, 0, s>>>(P, P.lev[l], xc, j);
+                float *out = l == 0 ? P.Z + (size_t)j * n * nvp : P.lev[l].xo;
+                k_mg_smooth<<<lsg_blocks((long long)P.lev[l].n * P.q4), 256, 0, s>>>(P, P.lev[l], l == 0 ? vj : P.lev[l].b,
+                                                                                  out, j);
+            }
+            k_lsg_spmm<<<gn, 256, 0, s>>>(P, j);
+            k_lsg_dot<<<red_grid, 256, 0, s>>>(P, j);
+            k_lsg_hsum<<<(unsigned)((nv * (j + 1) + NWARP - 1) / NWARP), 256, 0, s>>>(P, j);
+            k_lsg_update<<<red_grid, 256, 0, s>>>(P, j);
+            k_lsg_givens<<<(unsigned)((nv + NWARP - 1) / NWARP), 256, 0, s>>>(P, j);
+            launches += 4 * last + 1 + 5;
+            if (j + 1 < m) { k_lsg_norm<<<gn, 256, 0, s>>>(P, j); ++launches; }
+        }
+        k_lsg_solve<<<lsg_blocks(nvp), 256, 0, s>>>(P);
+        k_lsg_correct<<<tiles, 256, 0, s>>>(P);
+        launches += 2;
+    }
+    g_kernel_launches += launches;
+    return cudaGetLastError();
+}
+
 }  // namespace
 
 // The kernels may use all the opt-in shared memory; set once per kernel, so
@@ -1332,7 +1973,11 @@ static cudaError_t allow_smem(Precision prec) {
     return err[k];
 }
 
-size_t gmres_work_bytes(const DevSolveOp &op, int nv, int m, Precision p) { return layout(op, nv, m, p).total; }
+size_t gmres_work_bytes(const DevSolveOp &op, int nv, int m, Precision p) {
+    size_t t = layout(op, nv, m, p).total;
+    if (lsg_applicable(op, nv, p, m)) t = std::max(t, lsg_layout(op, nv, m).total);
+    return t;
+}
 
 cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv, int ld,
                         int m, int max_iter, double tol, Precision prec,
@@ -1350,6 +1995,18 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     if (getenv("PHG_ROWS_PER_BLOCK")) sh.rpb = env_int("PHG_ROWS_PER_BLOCK", 256);
     if (getenv("PHG_CHEB_LOCKSTEP") && !env_int("PHG_CHEB_LOCKSTEP", 1)) sh.path = 0;
     const bool lockstep = sh.path == 1 ? nv >= LS_MIN_TUNED : (sh.path == 0 ? false : nv >= LS_MIN_RHS);
+    // ensembles of the multigrid Laplacian in the mixed path: lockstep launches
+    if (!cheb && !no_alloc && lsg_applicable(op, nv, prec, m) &&
+        (sh.path == 1 || (sh.path == -1 && nv >= LSG_DEFAULT_RHS))) {
+        const char *ev = getenv("PHG_INNER_RTOL");
+        double rowb = 0.0;
+        for (int l = 0; l < op.mg.nlev; ++l) {
+            const MgLevelDev &Lv = op.mg.lev[l];
+            rowb += (double)Lv.n / (double)n * ((op.mg.nu1 + op.mg.nu2 + 1) * (Lv.W * 8.0 + 16.0) + 16.0);
+        }
+        return lsg_solve(op, B, X, nv, ld, m, max_iter, tol, ev ? atof(ev) : INNER_RTOL, (char *)work, stats_dev,
+                         rowb, s);
+    }
     // ensembles in the mixed path: all right-hand sides in lockstep
     if (cheb && prec == PREC_MIXED && lockstep && !no_alloc) {
         const char *ev = getenv("PHG_INNER_RTOL");
