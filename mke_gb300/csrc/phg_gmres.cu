@@ -49,9 +49,12 @@ constexpr long long SPIN_LIMIT = 2000000000LL;  // clock64 cycles (~1 s)
 constexpr int CHEB_KMAX = 64;    // most Chebyshev steps per refinement cycle
 constexpr int LS_MIN_RHS = 32;   // right-hand sides from which the lockstep path runs
 constexpr int LS_MIN_TUNED = 8;  // the fewest for which the autotuner may choose it
-// right-hand sides from which the multigrid Laplacian runs in lockstep by
-// default (below: only when the autotuner chose it)
-constexpr int LSG_DEFAULT_RHS = 1 << 30;
+// the multigrid Laplacian runs in lockstep by default from this many
+// right-hand sides on meshes of at least LSG_DEFAULT_ROWS rows (measured,
+// graph-replayed ensemble steps: L5 x 256 -15 %, L6 x 32 -14 %, L7 x 16 -5 %,
+// but L4 x 64 +9 %); elsewhere only when the autotuner chose it
+constexpr int LSG_DEFAULT_RHS = 16;
+constexpr int LSG_DEFAULT_ROWS = 10000;
 
 struct Params {
     DevSolveOp op;
@@ -1331,8 +1334,13 @@ int env_int(const char *name, int dflt) {
 // index range with a grid-stride loop over a grid capped at a few blocks per
 // SM, so a launch that finds its flag set costs little.
 constexpr int LSG_M = 8;        // Arnoldi steps per refinement cycle
-constexpr int LSG_MAXC = 4;     // refinement cycles at most
+// refinement cycles at most: three cycles of an 1e-5 inner reduction reach
+// 1e-12 from a zero start; a fourth only added skipped launches (L6 x 32
+// ensemble step 22.5 -> 21.9 ms without it)
+constexpr int LSG_MAXC = 3;
 constexpr int LSG_MINRHS = 8;   // fewest right-hand sides the path accepts
+constexpr int LSG_SMALL = 700;  // levels of at most this many rows run in one shared-memory kernel
+constexpr size_t LSG_SMALL_SMEM = 160 * 1024;
 
 struct LsgLevel {               // one multigrid level; buffers n x nvp FP32
     int n, W, Wr;
@@ -1343,12 +1351,14 @@ struct LsgLevel {               // one multigrid level; buffers n x nvp FP32
 };
 
 struct LsgParams {
-    int n, nv, nvp, q4, m, nlev, W, RB, nbx, ld, max_iter;
+    int n, nv, nvp, q4, m, nlev, W, RB, nbx, ld, max_iter, maxc;
     double tol, inner_rtol, step_row_bytes, resid_row_bytes;
     float omega;
     const int *col; const float *a32;    // fine operator, FP32 (w = A z)
     LsgLevel lev[MG_MAXLEV];
     int nc; const float *cinv;           // coarsest level, dense inverse
+    int lc;                              // levels [lc, nlev) run in one kernel, in shared memory
+    LsgLevel *levs;                      // device copy of lev[] (indexed at run time by that kernel)
     const double *B; double *X;          // member-major FP64, leading dimension ld
     float *V, *Z, *w;                    // (m + 1), m and 1 interleaved vectors
     double *R, *rpart, *bpart, *nrm;     // FP64 residual, norm partials, norms (2 per member)
@@ -1391,7 +1401,7 @@ __global__ void __launch_bounds__(256) k_lsg_begin(LsgParams P, int c) {
                 if (rel <= P.tol) s = 1;
                 else if (P.iters[v] >= P.max_iter) s = 2;
                 else if (P.cycles[v] > 0 && !(beta < 0.9999 * P.beta_prev[v])) s = 2;
-                else if (c == LSG_MAXC) s = 2;   // out of cycles
+                else if (c == P.maxc) s = 2;   // out of cycles
                 if (s == 0) {
                     P.beta_prev[v] = beta;
                     P.cycles[v] += 1;
@@ -1482,8 +1492,12 @@ __device__ __forceinline__ bool lsg_skip(const LsgParams &P, int j) {
     return *(volatile const int *)P.done || (j >= 0 && *(volatile const int *)&P.cnt[j] == 0);
 }
 
-// down sweep at level l: x = w D^-1 b, r = b - A x (from b alone)
-__global__ void __launch_bounds__(256) k_mg_down(LsgParams P, LsgLevel L, const float *src, int j) {
+__device__ __forceinline__ float4 f4mul(float4 a, float4 b) { return make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
+
+// down sweep at level l: x = w D^-1 b, r = b - A x (from b alone).  With
+// vout set, b = src * vscale (the Krylov vector v_j = w / ||w|| formed on the
+// fly from the previous step's w) and the block's own rows of v_j are stored.
+__global__ void __launch_bounds__(256) k_mg_down(LsgParams P, LsgLevel L, const float *src, float *vout, int j) {
     if (lsg_skip(P, j)) return;
     const int q4 = P.q4;
     const float4 *b = (const float4 *)src;
@@ -1492,6 +1506,7 @@ __global__ void __launch_bounds__(256) k_mg_down(LsgParams P, LsgLevel L, const 
     const long long total = (long long)L.n * q4;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += lsg_grid_stride()) {
         const int i = (int)(t / q4), q = (int)(t - (long long)i * q4);
+        const float4 sc = vout ? ((const float4 *)P.vscale)[q] : make_float4(1.f, 1.f, 1.f, 1.f);
         int c[8];
         float a[8];
         float4 g[8];
@@ -1500,12 +1515,13 @@ __global__ void __launch_bounds__(256) k_mg_down(LsgParams P, LsgLevel L, const 
             if (k < L.W) { c[k] = __ldg(&L.col[(size_t)k * L.n + i]); a[k] = __ldg(&L.a[(size_t)k * L.n + i]); }
 #pragma unroll
         for (int k = 0; k < 8; ++k)
-            if (k < L.W) g[k] = b[(size_t)c[k] * q4 + q];
+            if (k < L.W) g[k] = f4mul(b[(size_t)c[k] * q4 + q], sc);
         float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int k = 0; k < 8; ++k)
             if (k < L.W) s = f4fma(a[k] * (om * __ldg(&L.d[c[k]])), g[k], s);
-        const float4 bi = b[(size_t)i * q4 + q];
+        const float4 bi = f4mul(b[(size_t)i * q4 + q], sc);
+        if (vout) ((float4 *)vout)[(size_t)i * q4 + q] = bi;
         const float di = om * __ldg(&L.d[i]);
         x[(size_t)i * q4 + q] = make_float4(di * bi.x, di * bi.y, di * bi.z, di * bi.w);
         r[(size_t)i * q4 + q] = make_float4(bi.x - s.x, bi.y - s.y, bi.z - s.z, bi.w - s.w);
@@ -1530,19 +1546,127 @@ __global__ void __launch_bounds__(256) k_mg_restrict(LsgParams P, LsgLevel L, Ls
     }
 }
 
-// coarsest level: x = C^-1 b (dense)
-__global__ void __launch_bounds__(256) k_mg_coarse(LsgParams P, LsgLevel C, int j) {
+// Levels [lc, nlev) for one 4-member chunk per block, in shared memory (four
+// float4 vectors per level: x, t, b, r): b_lc = R r_{lc-1} (or the input when
+// lc = 0), down sweeps and restrictions, the dense coarsest solve, the
+// prolongations and up sweeps; x_lc is written to out (the coarse correction
+// of level lc - 1, or the V-cycle's output when lc = 0).  Replaces one launch
+// per small level and phase by a single launch.
+__global__ void __launch_bounds__(256) k_mg_small(LsgParams P, const float *src, float *vout, float *out, int j) {
     if (lsg_skip(P, j)) return;
-    const int n = P.nc, q4 = P.q4;
-    const float4 *b = (const float4 *)C.b;
-    float4 *x = (float4 *)C.x;
-    const long long total = (long long)n * q4;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += lsg_grid_stride()) {
-        const int i = (int)(t / q4), q = (int)(t - (long long)i * q4);
-        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int k = 0; k < n; ++k) s = f4fma(__ldg(&P.cinv[(size_t)i * n + k]), b[(size_t)k * q4 + q], s);
-        x[(size_t)i * q4 + q] = s;
+    extern __shared__ float4 sm4[];
+    const int q4 = P.q4, lc = P.lc, last = P.nlev - 1;
+    const float om = P.omega;
+    const LsgLevel *LV = P.levs;
+    for (int q = blockIdx.x; q < q4; q += gridDim.x) {
+        // shared-memory offsets of the levels
+        int off[MG_MAXLEV];
+        int o = 0;
+        for (int l = lc; l <= last; ++l) { off[l] = o; o += 4 * LV[l].n; }
+        // b at level lc
+        {
+            const LsgLevel L = LV[lc];
+            float4 *b = sm4 + off[lc] + 2 * L.n;
+            if (lc == 0) {
+                const float4 sc = vout ? ((const float4 *)P.vscale)[q] : make_float4(1.f, 1.f, 1.f, 1.f);
+                for (int i = threadIdx.x; i < L.n; i += blockDim.x) {
+                    const float4 v = f4mul(((const float4 *)src)[(size_t)i * q4 + q], sc);
+                    b[i] = v;
+                    if (vout) ((float4 *)vout)[(size_t)i * q4 + q] = v;
+                }
+            } else {
+                const LsgLevel F = LV[lc - 1];
+                const float4 *r = (const float4 *)F.r;
+                for (int c = threadIdx.x; c < L.n; c += blockDim.x) {
+                    float4 sacc = make_float4(0.f, 0.f, 0.f, 0.f);
+                    for (int k = 0; k < F.Wr; ++k) {
+                        const int f = __ldg(&F.rf[(size_t)k * L.n + c]);
+                        if (f >= 0) sacc = f4fma(__ldg(&F.rw[(size_t)k * L.n + c]), r[(size_t)f * q4 + q], sacc);
+                    }
+                    b[c] = sacc;
+                }
+            }
+        }
+        __syncthreads();
+        // down: x = w D^-1 b, r = b - A x, b_{l+1} = R r
+        for (int l = lc; l < last; ++l) {
+            const LsgLevel L = LV[l];
+            float4 *x = sm4 + off[l], *b = x + 2 * L.n, *r = x + 3 * L.n;
+            for (int i = threadIdx.x; i < L.n; i += blockDim.x) {
+                const float di = om * __ldg(&L.d[i]);
+                x[i] = make_float4(di * b[i].x, di * b[i].y, di * b[i].z, di * b[i].w);
+            }
+            __syncthreads();
+            for (int i = threadIdx.x; i < L.n; i += blockDim.x) {
+                float4 sacc = make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int k = 0; k < L.W; ++k)
+                    sacc = f4fma(__ldg(&L.a[(size_t)k * L.n + i]), x[__ldg(&L.col[(size_t)k * L.n + i])], sacc);
+                r[i] = make_float4(b[i].x - sacc.x, b[i].y - sacc.y, b[i].z - sacc.z, b[i].w - sacc.w);
+            }
+            __syncthreads();
+            const LsgLevel C = LV[l + 1];
+            float4 *bc = sm4 + off[l + 1] + 2 * C.n;
+            for (int c = threadIdx.x; c < C.n; c += blockDim.x) {
+                float4 sacc = make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int k = 0; k < L.Wr; ++k) {
+                    const int f = __ldg(&L.rf[(size_t)k * C.n + c]);
+                    if (f >= 0) sacc = f4fma(__ldg(&L.rw[(size_t)k * C.n + c]), r[f], sacc);
+                }
+                bc[c] = sacc;
+            }
+            __syncthreads();
+        }
+        // coarsest: x = C^-1 b
+        {
+            const int n = P.nc;
+            float4 *x = sm4 + off[last], *b = x + 2 * n;
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                float4 sacc = make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int k = 0; k < n; ++k) sacc = f4fma(__ldg(&P.cinv[(size_t)i * n + k]), b[k], sacc);
+                x[i] = sacc;
+            }
+            __syncthreads();
+        }
+        // up: x += P x_{l+1}; x = x + w D^-1 (b - A x)
+        for (int l = last - 1; l >= lc; --l) {
+            const LsgLevel L = LV[l];
+            float4 *x = sm4 + off[l], *t = x + L.n, *b = x + 2 * L.n;
+            const float4 *xc = sm4 + off[l + 1];
+            for (int i = threadIdx.x; i < L.n; i += blockDim.x) {
+                const int c0 = __ldg(&L.pc[2 * i]), c1 = __ldg(&L.pc[2 * i + 1]);
+                float4 sacc = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (c0 >= 0) sacc = f4fma(__ldg(&L.pw[2 * i]), xc[c0], sacc);
+                if (c1 >= 0) sacc = f4fma(__ldg(&L.pw[2 * i + 1]), xc[c1], sacc);
+                x[i] = make_float4(x[i].x + sacc.x, x[i].y + sacc.y, x[i].z + sacc.z, x[i].w + sacc.w);
+            }
+            __syncthreads();
+            for (int i = threadIdx.x; i < L.n; i += blockDim.x) {
+                float4 sacc = make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int k = 0; k < L.W; ++k)
+                    sacc = f4fma(__ldg(&L.a[(size_t)k * L.n + i]), x[__ldg(&L.col[(size_t)k * L.n + i])], sacc);
+                const float di = om * __ldg(&L.d[i]);
+                t[i] = make_float4(x[i].x + di * (b[i].x - sacc.x), x[i].y + di * (b[i].y - sacc.y),
+                                   x[i].z + di * (b[i].z - sacc.z), x[i].w + di * (b[i].w - sacc.w));
+            }
+            __syncthreads();
+            float4 *dst = l == lc ? (float4 *)out : x;
+            if (l == lc)
+                for (int i = threadIdx.x; i < L.n; i += blockDim.x) dst[(size_t)i * q4 + q] = t[i];
+            else
+                for (int i = threadIdx.x; i < L.n; i += blockDim.x) x[i] = t[i];
+            __syncthreads();
+        }
+        if (lc == last)   // the whole cycle is the dense solve
+            for (int i = threadIdx.x; i < P.nc; i += blockDim.x) ((float4 *)out)[(size_t)i * q4 + q] = sm4[off[last] + i];
+        __syncthreads();
     }
+}
+
+// copy of the level descriptors into device memory (static indices only)
+__global__ void k_lsg_levels(LsgParams P) {
+    if (threadIdx.x || blockIdx.x) return;
+#pragma unroll
+    for (int k = 0; k < MG_MAXLEV; ++k) P.levs[k] = P.lev[k];
 }
 
 // x_l += P x_{l+1}
@@ -1732,20 +1856,6 @@ __global__ void __launch_bounds__(256) k_lsg_givens(LsgParams P, int j) {
     else { P.vscale[v] = (float)(1.0 / hn); atomicAdd(&P.cnt[j + 1], 1); }
 }
 
-// V_{j+1} = w * vscale (0 for members out of the Arnoldi loop)
-__global__ void __launch_bounds__(256) k_lsg_norm(LsgParams P, int j) {
-    if (lsg_skip(P, j + 1)) return;
-    const int q4 = P.q4;
-    const float4 *w = (const float4 *)P.w, *vs4 = (const float4 *)P.vscale;
-    float4 *vn = (float4 *)(P.V + (size_t)(j + 1) * P.n * P.nvp);
-    const long long total = (long long)P.n * q4;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += lsg_grid_stride()) {
-        const int i = (int)(t / q4), q = (int)(t - (long long)i * q4);
-        const float4 a = w[(size_t)i * q4 + q], sc = vs4[q];
-        vn[(size_t)i * q4 + q] = make_float4(a.x * sc.x, a.y * sc.y, a.z * sc.z, a.w * sc.w);
-    }
-}
-
 // y = H^-1 g over each member's jl columns (FP64), FP32 copy for the correction
 __global__ void __launch_bounds__(256) k_lsg_solve(LsgParams P) {
     if (*(volatile int *)P.done) return;
@@ -1799,7 +1909,7 @@ __global__ void __launch_bounds__(256) k_lsg_correct(LsgParams P) {
 
 struct LsgLayout {
     size_t V, Z, w, R, lev[MG_MAXLEV], rpart, bpart, nrm, dpart, npart, hcol, H, cs, sn, g, hv, yv;
-    size_t bnorm, beta_prev, target, relv, scale, vscale, ints, total;
+    size_t bnorm, beta_prev, target, relv, scale, vscale, ints, levs, total;
     int nvp, m, RB, nbx;
 };
 
@@ -1839,6 +1949,7 @@ LsgLayout lsg_layout(const DevSolveOp &op, int nv, int restart) {
     L.scale = o; o += al(4 * nvp);
     L.vscale = o; o += al(4 * nvp);
     L.ints = o; o += al(4 * (6 * nvp + m + 2 + 1));
+    L.levs = o; o += al(sizeof(LsgLevel) * MG_MAXLEV);
     L.total = o;
     return L;
 }
@@ -1864,6 +1975,7 @@ unsigned lsg_blocks(long long work) {
 
 cudaError_t lsg_solve(const DevSolveOp &op, const double *B, double *X, int nv, int ld, int restart, int max_iter,
                       double tol, double inner_rtol, char *w, GmresStats *st, double mg_row_bytes, cudaStream_t s) {
+    const int lsg_maxc = LSG_MAXC;
     const LsgLayout Lo = lsg_layout(op, nv, restart);
     const int n = op.A.n, W = op.A.W, nvp = Lo.nvp, m = Lo.m, nlev = op.mg.nlev, last = nlev - 1;
     LsgParams P;
@@ -1885,6 +1997,19 @@ cudaError_t lsg_solve(const DevSolveOp &op, const double *B, double *X, int nv, 
         E.r = (float *)(w + Lo.lev[l] + 2 * lv); E.b = (float *)(w + Lo.lev[l] + 3 * lv);
     }
     P.nc = op.mg.nc; P.cinv = op.mg.cinv32;
+    // the small levels: from the first with <= LSG_SMALL rows whose levels fit in shared memory
+    int lc = last;
+    for (int l = last; l >= 0; --l) {
+        size_t rows = 0;
+        for (int k = l; k <= last; ++k) rows += (size_t)op.mg.lev[k].n;
+        if (op.mg.lev[l].n > LSG_SMALL || 64 * rows > LSG_SMALL_SMEM) break;
+        lc = l;
+    }
+    size_t small_rows = 0;
+    for (int k = lc; k <= last; ++k) small_rows += (size_t)op.mg.lev[k].n;
+    const size_t small_smem = 64 * small_rows;
+    P.lc = lc;
+    P.levs = (LsgLevel *)(w + Lo.levs);
     P.B = B; P.X = X;
     P.V = (float *)(w + Lo.V); P.Z = (float *)(w + Lo.Z); P.w = (float *)(w + Lo.w);
     P.R = (double *)(w + Lo.R); P.rpart = (double *)(w + Lo.rpart); P.bpart = (double *)(w + Lo.bpart);
@@ -1901,14 +2026,25 @@ cudaError_t lsg_solve(const DevSolveOp &op, const double *B, double *X, int nv, 
     cudaError_t e;
     if ((e = cudaMemsetAsync(st, 0, sizeof(GmresStats), s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(P.done, 0, sizeof(int), s)) != cudaSuccess) return e;
+    static std::once_flag smem_once;
+    static cudaError_t smem_err = cudaSuccess;
+    std::call_once(smem_once, [] {
+        smem_err = cudaFuncSetAttribute((const void *)k_mg_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)LSG_SMALL_SMEM);
+    });
+    if (smem_err != cudaSuccess) return smem_err;
+    if (small_smem > LSG_SMALL_SMEM) return cudaErrorInvalidValue;
     long long launches = 0;
     const dim3 rgrid((unsigned)Lo.nbx, (unsigned)((nv + LS_MG - 1) / LS_MG));
+    k_lsg_levels<<<1, 32, 0, s>>>(P);
     k_ls_sq<<<rgrid, 256, 0, s>>>(B, n, ld, nv, P.bpart);
-    ++launches;
+    launches += 2;
+    const unsigned gsmall = (unsigned)std::min(P.q4, 4 * sm_count());
     const unsigned gn = lsg_blocks((long long)n * P.q4);
     const dim3 red_grid((unsigned)Lo.RB, (unsigned)(nvp / 32));
     const unsigned tiles = lsg_blocks((long long)((n + 31) / 32) * (nvp / 32) * 256);
-    for (int c = 0; c <= LSG_MAXC; ++c) {
+    P.maxc = lsg_maxc;
+    for (int c = 0; c <= lsg_maxc; ++c) {
         switch (W) {
         case 6: k_ls_resid<6><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, P.R, nv, P.rpart, P.done); break;
         case 7: k_ls_resid<7><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, P.R, nv, P.rpart, P.done); break;
@@ -1918,30 +2054,39 @@ cudaError_t lsg_solve(const DevSolveOp &op, const double *B, double *X, int nv, 
         k_lsg_begin<<<1, 256, 0, s>>>(P, c);
         launches += 3;
         if (c == 0) { k_lsg_zero<<<lsg_blocks((long long)nv * n), 256, 0, s>>>(P); ++launches; }
-        if (c == LSG_MAXC) break;
+        if (c == lsg_maxc) break;
         k_lsg_v0<<<tiles, 256, 0, s>>>(P);
         ++launches;
         for (int j = 0; j < m; ++j) {
-            const float *vj = P.V + (size_t)j * n * nvp;
-            for (int l = 0; l < last; ++l) {
-                k_mg_down<<<lsg_blocks((long long)P.lev[l].n * P.q4), 256, 0, s>>>(P, P.lev[l], l == 0 ? vj : P.lev[l].b, j);
-                k_mg_restrict<<<lsg_blocks((long long)P.lev[l + 1].n * P.q4), 256, 0, s>>>(P, P.lev[l], P.lev[l + 1], j);
+            // v_0 comes from k_lsg_v0; v_j (j > 0) = w / ||w|| is formed by the
+            // first kernel of the V-cycle, which stores it
+            float *vj = P.V + (size_t)j * n * nvp;
+            const float *src0 = j == 0 ? vj : P.w;
+            float *vout0 = j == 0 ? nullptr : vj;
+            float *zj = P.Z + (size_t)j * n * nvp;
+            for (int l = 0; l < lc; ++l) {
+                k_mg_down<<<lsg_blocks((long long)P.lev[l].n * P.q4), 256, 0, s>>>(
+                    P, P.lev[l], l == 0 ? src0 : P.lev[l].b, l == 0 ? vout0 : nullptr, j);
+                if (l + 1 < lc)
+                    k_mg_restrict<<<lsg_blocks((long long)P.lev[l + 1].n * P.q4), 256, 0, s>>>(P, P.lev[l], P.lev[l + 1], j);
+                launches += l + 1 < lc ? 2 : 1;
             }
-            k_mg_coarse<<<lsg_blocks((long long)P.nc * P.q4), 256, 0, s>>>(P, P.lev[last], j);
-            for (int l = last - 1; l >= 0; --l) {
-                const float *xc = (l + 1 == last) ? P.lev[last].x : P.lev[l + 1].xo;
+            k_mg_small<<<gsmall, 256, small_smem, s>>>(P, src0, lc == 0 ? vout0 : nullptr, lc == 0 ? zj : P.lev[lc].x, j);
+            ++launches;
+            for (int l = lc - 1; l >= 0; --l) {
+                const float *xc = (l + 1 == lc) ? P.lev[lc].x : P.lev[l + 1].xo;
                 k_mg_prolong<<<lsg_blocks((long long)P.lev[l].n * P.q4), 256, 0, s>>>(P, P.lev[l], xc, j);
-                float *out = l == 0 ? P.Z + (size_t)j * n * nvp : P.lev[l].xo;
+                float *out = l == 0 ? zj : P.lev[l].xo;
                 k_mg_smooth<<<lsg_blocks((long long)P.lev[l].n * P.q4), 256, 0, s>>>(P, P.lev[l], l == 0 ? vj : P.lev[l].b,
                                                                                   out, j);
+                launches += 2;
             }
             k_lsg_spmm<<<gn, 256, 0, s>>>(P, j);
             k_lsg_dot<<<red_grid, 256, 0, s>>>(P, j);
             k_lsg_hsum<<<(unsigned)((nv * (j + 1) + NWARP - 1) / NWARP), 256, 0, s>>>(P, j);
             k_lsg_update<<<red_grid, 256, 0, s>>>(P, j);
             k_lsg_givens<<<(unsigned)((nv + NWARP - 1) / NWARP), 256, 0, s>>>(P, j);
-            launches += 4 * last + 1 + 5;
-            if (j + 1 < m) { k_lsg_norm<<<gn, 256, 0, s>>>(P, j); ++launches; }
+            launches += 5;
         }
         k_lsg_solve<<<lsg_blocks(nvp), 256, 0, s>>>(P);
         k_lsg_correct<<<tiles, 256, 0, s>>>(P);
@@ -1997,7 +2142,7 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     const bool lockstep = sh.path == 1 ? nv >= LS_MIN_TUNED : (sh.path == 0 ? false : nv >= LS_MIN_RHS);
     // ensembles of the multigrid Laplacian in the mixed path: lockstep launches
     if (!cheb && !no_alloc && lsg_applicable(op, nv, prec, m) &&
-        (sh.path == 1 || (sh.path == -1 && nv >= LSG_DEFAULT_RHS))) {
+        (sh.path == 1 || (sh.path == -1 && nv >= LSG_DEFAULT_RHS && n >= LSG_DEFAULT_ROWS))) {
         const char *ev = getenv("PHG_INNER_RTOL");
         double rowb = 0.0;
         for (int l = 0; l < op.mg.nlev; ++l) {
