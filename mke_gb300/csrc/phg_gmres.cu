@@ -1145,10 +1145,10 @@ __global__ void __launch_bounds__(256) k_ls_scale(const double *nrm, int nv, int
     }
 }
 
-// rv = (float)(r * scale), d = e0 = c0 D^-1 rv: member-major FP64 -> interleaved FP32 (tiled transpose)
+// rv = (float)(r * scale), e_1 = c0 D^-1 rv, e_0 = 0: member-major FP64 -> interleaved FP32 (tiled transpose)
 __global__ void __launch_bounds__(256) k_ls_init(const double *__restrict__ R, int n, int nv, int nvp,
                                                  const double *__restrict__ sc, const float *__restrict__ dinv, float c0,
-                                                 float *rv, float *d, float *e0, const int *done) {
+                                                 float *rv, float *e0, float *e1, const int *done) {
     if (*(volatile const int *)done) return;
     __shared__ float t[32][33];
     const int i0 = blockIdx.x * 32, v0 = blockIdx.y * 32, tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
@@ -1161,21 +1161,23 @@ __global__ void __launch_bounds__(256) k_ls_init(const double *__restrict__ R, i
         const int i = i0 + j, v = v0 + tx;
         if (i >= n) continue;
         const float r = t[tx][j];
-        const float dd = c0 * dinv[i] * r;
         const size_t q = (size_t)i * nvp + v;
         rv[q] = r;
-        d[q] = dd;
-        e0[q] = dd;
+        e0[q] = 0.f;
+        e1[q] = c0 * dinv[i] * r;
     }
 }
 
-// one step for every member: s = A e_c, d = ca d + cb D^-1 (rv - s), e_n = e_c + d
+// one step for every member, three-term form of the Chebyshev recurrence
+// (d_{k-1} = e_k - e_{k-1}): s = A e_k,
+// e_{k+1} = e_k + ca (e_k - e_{k-1}) + cb D^-1 (rv - s), written over e_{k-1}
+// (each element is read and then written by the same thread; other threads
+// gather only e_k) -- four vectors touched per step instead of five
 template <int W>
 __global__ void __launch_bounds__(256) k_ls_step(const int *__restrict__ col, const float *__restrict__ a32,
                                                  const float *__restrict__ dinv, int n, int q4,
                                                  const float4 *__restrict__ ec, const float4 *__restrict__ rv,
-                                                 float4 *__restrict__ d, float4 *__restrict__ en, float ca, float cb,
-                                                 const int *done) {
+                                                 float4 *ep, float ca, float cb, const int *done) {
     if (*(volatile const int *)done) return;
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = (int)(t / (unsigned)q4), q = (int)(t - (unsigned)i * (unsigned)q4);
@@ -1195,12 +1197,11 @@ __global__ void __launch_bounds__(256) k_ls_step(const int *__restrict__ col, co
     }
     const size_t idx = (size_t)i * q4 + q;
     const float di = cb * __ldg(&dinv[i]);
-    const float4 r = rv[idx], dd = d[idx], e = ec[idx];
+    const float4 r = rv[idx], e = ec[idx], eo = ep[idx];
     float4 dn;
-    dn.x = ca * dd.x + di * (r.x - sum.x); dn.y = ca * dd.y + di * (r.y - sum.y);
-    dn.z = ca * dd.z + di * (r.z - sum.z); dn.w = ca * dd.w + di * (r.w - sum.w);
-    d[idx] = dn;
-    en[idx] = make_float4(e.x + dn.x, e.y + dn.y, e.z + dn.z, e.w + dn.w);
+    dn.x = ca * (e.x - eo.x) + di * (r.x - sum.x); dn.y = ca * (e.y - eo.y) + di * (r.y - sum.y);
+    dn.z = ca * (e.z - eo.z) + di * (r.z - sum.z); dn.w = ca * (e.w - eo.w) + di * (r.w - sum.w);
+    ep[idx] = make_float4(e.x + dn.x, e.y + dn.y, e.z + dn.z, e.w + dn.w);
 }
 
 // x += beta * e: interleaved FP32 -> member-major FP64 (tiled transpose)
@@ -1222,15 +1223,14 @@ __global__ void __launch_bounds__(256) k_ls_update(double *X, int ld, int n, int
 }
 
 template <int W>
-cudaError_t ls_steps(const DevSolveOp &op, int n, int q4, float *&ec, float *&en, const float *rv, float *d,
+cudaError_t ls_steps(const DevSolveOp &op, int n, int q4, float *&ec, float *&ep, const float *rv,
                      const double *ca, const double *cb, int K, const int *done, cudaStream_t s) {
     const long long work = (long long)n * q4;
     const unsigned blocks = (unsigned)((work + 255) / 256);
     for (int k = 1; k < K; ++k) {
         k_ls_step<W><<<blocks, 256, 0, s>>>(op.A.col, op.a32, op.dinv32, n, q4, (const float4 *)ec,
-                                            (const float4 *)rv, (float4 *)d, (float4 *)en, (float)ca[k],
-                                            (float)cb[k], done);
-        float *t = ec; ec = en; en = t;
+                                            (const float4 *)rv, (float4 *)ep, (float)ca[k], (float)cb[k], done);
+        float *t = ec; ec = ep; ep = t;   // e_{k+1} is in the old e_{k-1} buffer
     }
     return cudaGetLastError();
 }
@@ -1245,11 +1245,10 @@ cudaError_t cheb_lockstep(const DevSolveOp &op, const double *B, double *X, int 
     if ((long long)n * q4 >= (1LL << 31)) return cudaErrorNotSupported;
     const size_t vec = ((size_t)n * nvp * 4 + 255) & ~size_t(255);
     const int nbx = (n + 255) / 256;   // row blocks of the residual: one norm partial each
-    if (4 * vec + (size_t)16 * nv * nbx > L.r - L.v) return cudaErrorNotSupported;
+    if (3 * vec + (size_t)16 * nv * nbx > L.r - L.v) return cudaErrorNotSupported;
     if ((size_t)(4 * nvp + 64) * 8 > L.bar - L.part) return cudaErrorNotSupported;
-    float *rv = (float *)(w + L.v), *d = (float *)(w + L.v + vec), *e0 = (float *)(w + L.v + 2 * vec),
-          *e1 = (float *)(w + L.v + 3 * vec);
-    double *rpart = (double *)(w + L.v + 4 * vec), *bpart = rpart + (size_t)nv * nbx;
+    float *rv = (float *)(w + L.v), *e0 = (float *)(w + L.v + vec), *e1 = (float *)(w + L.v + 2 * vec);
+    double *rpart = (double *)(w + L.v + 3 * vec), *bpart = rpart + (size_t)nv * nbx;
     double *R = (double *)(w + L.r);
     double *nrm = (double *)(w + L.part), *beta = nrm + 2 * nvp, *sc = beta + nvp;
     int *done = (int *)(sc + nvp);
@@ -1270,7 +1269,7 @@ cudaError_t cheb_lockstep(const DevSolveOp &op, const double *B, double *X, int 
     // algorithmic bytes of one cycle: FP64 residual, init, K - 1 steps, update
     const double rowsb = (double)n;
     const double cyc = rowsb * nv * (8.0 * 3) + rowsb * W * 12.0 +
-                       rowsb * nvp * (8.0 + 12.0) + (K - 1) * (rowsb * W * 8.0 + rowsb * nvp * 4.0 * 6.0) +
+                       rowsb * nvp * (8.0 + 12.0) + (K - 1) * (rowsb * W * 8.0 + rowsb * nvp * 4.0 * 4.0) +
                        rowsb * nvp * 4.0 + rowsb * nv * 16.0;
     cudaError_t e;
     if ((e = cudaMemsetAsync(done, 0, sizeof(int), s)) != cudaSuccess) return e;
@@ -1286,12 +1285,12 @@ cudaError_t cheb_lockstep(const DevSolveOp &op, const double *B, double *X, int 
         k_ls_nrm<<<(nv + NWARP - 1) / NWARP, 256, 0, s>>>(rpart, bpart, nbx, nrm, nv, done);
         k_ls_scale<<<1, 256, 0, s>>>(nrm, nv, nvp, tol, beta, sc, done, st, c, K, c ? cyc : 0.0);
         if (c == LS_MAXC) break;
-        k_ls_init<<<tgrid, 256, 0, s>>>(R, n, nv, nvp, sc, op.dinv32, (float)(1.0 / theta), rv, d, e0, done);
-        float *ec = e0, *en = e1;
+        k_ls_init<<<tgrid, 256, 0, s>>>(R, n, nv, nvp, sc, op.dinv32, (float)(1.0 / theta), rv, e0, e1, done);
+        float *ec = e1, *ep = e0;
         switch (W) {
-        case 6: e = ls_steps<6>(op, n, q4, ec, en, rv, d, ca, cb, K, done, s); break;
-        case 7: e = ls_steps<7>(op, n, q4, ec, en, rv, d, ca, cb, K, done, s); break;
-        default: e = ls_steps<8>(op, n, q4, ec, en, rv, d, ca, cb, K, done, s); break;
+        case 6: e = ls_steps<6>(op, n, q4, ec, ep, rv, ca, cb, K, done, s); break;
+        case 7: e = ls_steps<7>(op, n, q4, ec, ep, rv, ca, cb, K, done, s); break;
+        default: e = ls_steps<8>(op, n, q4, ec, ep, rv, ca, cb, K, done, s); break;
         }
         if (e != cudaSuccess) return e;
         k_ls_update<<<tgrid, 256, 0, s>>>(X, ld, n, nv, nvp, beta, ec, done);
