@@ -38,10 +38,8 @@ TOL = 1e-12  # every solve: relative residual <= 1e-12 (within the 1e-10 bound)
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from mke_gb300 import replicas
+    return replicas.env()
 
 
 class ClockSampler:
@@ -113,16 +111,11 @@ def run_ours(args, ws, rank, local):
     import torch
     from mke_gb300 import phelm
 
+    from mke_gb300 import replicas
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=dev)
-
-    def barrier():
-        if ws > 1:
-            import torch.distributed as dist
-            dist.barrier()
+    replicas.init("nccl", device=dev)   # replicas only: a collective for the timings, none on the data path
+    barrier = replicas.barrier
 
     mesh = phelm.Mesh.sphere(args.level)
     psi0, cor = initial_state(mesh)
@@ -292,19 +285,20 @@ def run_ours(args, ws, rank, local):
         for name in ("mixed", "fp64"):
             served[name] = run_serve(name, args.bench_serve_requests, args.serve_rate)
 
-    # max over ranks
-    ms = results["mixed"]["ms_per_step"]
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms, results["fp64"]["ms_per_step"], results["mixed"]["e2e_s"]], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms, ms64, e2e = t.tolist()
-    else:
-        ms64, e2e = results["fp64"]["ms_per_step"], results["mixed"]["e2e_s"]
+    # max over ranks: whole-job rates = every rank's units / the slowest rank's time
+    keys = sorted(batched)
+    mx = replicas.max_over_ranks([results["mixed"]["ms_per_step"], results["fp64"]["ms_per_step"],
+                                  results["mixed"]["e2e_s"]]
+                                 + [batched[k][p]["ms_per_step"] for k in keys for p in ("mixed", "fp64")], dev)
+    ms, ms64, e2e = mx[:3]
+    for i, k in enumerate(keys):
+        for j, p in enumerate(("mixed", "fp64")):
+            bms = mx[3 + 2 * i + j]
+            batched[k][p]["ms_per_step_max_over_ranks"] = bms
+            batched[k][p]["member_steps_per_s"] = replicas.whole_job_rate(batched[k]["members"], bms * 1e-3, ws)
+        batched[k]["mixed_over_fp64"] = batched[k]["mixed"]["member_steps_per_s"] / batched[k]["fp64"]["member_steps_per_s"]
     if rank != 0:
-        if ws > 1:
-            import torch.distributed as dist
-            dist.destroy_process_group()
+        replicas.finish()
         return None
 
     mixed, fp64 = results["mixed"], results["fp64"]
@@ -370,16 +364,14 @@ def run_ours(args, ws, rank, local):
                      "note": "L2-resident working set (level-6 operators ~30 MB < 129 MB L2): the solve is bound by "
                              "group-barrier and gather latency, not HBM; traffic = DRAM bytes per launch from ncu",
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s"},
-        "e2e": {"value": args.steps / mixed["e2e_s"], "unit": "steps/s",
+        "e2e": {"value": replicas.whole_job_rate(args.steps, e2e, ws), "unit": "steps/s",
                 "h2d_bytes_per_step": 8 * (V + 2 * max(os_, 1)), "d2h_bytes_per_step": 8 * V},
         "gpu_launches": mixed["launches"],
         "clocks": mixed["clocks"],
         "cpu_baseline": cpu,
     }
     print(json.dumps(line))
-    if ws > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+    replicas.finish()
     return line
 
 
