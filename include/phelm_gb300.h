@@ -136,6 +136,13 @@ int phg_ops_mult(phg_ops o, const char *name, double *y, const double *x, int nv
  * so every gathered row of x is one contiguous read.  No reference
  * counterpart. */
 int phg_ops_mult32(phg_ops o, const char *name, float *y, const float *x, int nv, void *stream);
+/* Index validation (debug aid, no reference counterpart): counts the entries
+ * of the handle's device index arrays outside their valid range -- the shared
+ * ELL pattern, the inner / outer / p2io maps, the norm pattern, the boundary
+ * column lists and the multigrid hierarchy (columns, prolongation and
+ * restriction lists).  Only the indices are read.  Synchronises the stream. */
+int phg_ops_validate(phg_ops o, long long *bad_entries, void *stream);
+
 /* Autotuner (no reference counterpart).  Times the candidate launch shapes
  * of the kernels a barotropic step of nmembers states runs on this handle's
  * mesh and precision -- rows per block of the persistent solver (128, 256,

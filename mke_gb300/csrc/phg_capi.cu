@@ -14,6 +14,7 @@
 
 #include "../../include/phelm_gb300.h"
 #include "phg_host.hpp"
+#include <nvtx3/nvToolsExt.h>
 #include "phg_kernels.cuh"
 
 using namespace phg;
@@ -37,6 +38,14 @@ int fail(int code, const char *fmt, ...) {
         cudaError_t e_ = (call);                                                          \
         if (e_ != cudaSuccess) return fail(PHG_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
     } while (0)
+
+// NVTX range for profiler timelines (a no-op without a tool attached)
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // owning device allocation
 // device bytes held by the library: in total, and allocated by this thread
@@ -675,6 +684,7 @@ Precision prec_of(const phg_ops_s *o) { return o->prec == PHG_MIXED ? PREC_MIXED
 // enqueue one solve; stats go to slot `slot` of the handle's device stats array
 int solve(phg_ops_s *o, const DevSolveOp &op, const double *B, double *X, int nv, int ld, double tol,
           int slot, cudaStream_t s) {
+    NvtxRange nvtx("phg:solve");
     size_t need = gmres_work_bytes(op, nv, o->restart, prec_of(o));
     if (need > o->work.n) {
         CK(cudaStreamSynchronize(s));
@@ -696,6 +706,9 @@ int solve(phg_ops_s *o, const DevSolveOp &op, const double *B, double *X, int nv
     return PHG_OK;
 }
 
+// maximum that keeps a NaN (std::max drops one on the right)
+double max_keep_nan(double a, double b) { return a != a ? a : (b != b ? b : std::max(a, b)); }
+
 // read back and judge the stats of slots [0, nslots)
 int check_stats(phg_ops_s *o, int nslots, cudaStream_t s, GmresStats *agg = nullptr, GmresStats *each = nullptr) {
     std::vector<GmresStats> st(nslots);
@@ -704,7 +717,7 @@ int check_stats(phg_ops_s *o, int nslots, cudaStream_t s, GmresStats *agg = null
     GmresStats a{0.0, 0.0, 0, 0, 0, 0};
     for (auto &x : st) {
         a.iters += x.iters; a.cycles += x.cycles;
-        a.relres = std::max(a.relres, x.relres);
+        a.relres = max_keep_nan(a.relres, x.relres);
         a.status = std::max(a.status, x.status);
     }
     if (each) memcpy(each, st.data(), sizeof(GmresStats) * nslots);
@@ -713,7 +726,7 @@ int check_stats(phg_ops_s *o, int nslots, cudaStream_t s, GmresStats *agg = null
     o->pending_slots = 0;
     if (agg) *agg = a;
     if (a.status == 2) return fail(PHG_ERR_TIMEOUT, "device barrier wait timed out");
-    if (a.status == 1 && !(a.relres <= std::max(1e3 * o->tol, 1e-8)))
+    if (!std::isfinite(a.relres) || (a.status == 1 && !(a.relres <= std::max(1e3 * o->tol, 1e-8))))
         return fail(PHG_ERR_NOT_CONVERGED, "GMRES stopped at relative residual %.3e", a.relres);
     return PHG_OK;
 }
@@ -960,6 +973,50 @@ extern "C" int phg_ops_mult32(phg_ops o, const char *name, float *y, const float
     return PHG_OK;
 }
 
+// --------------------------------------------------------- validation ---
+extern "C" int phg_ops_validate(phg_ops o, long long *bad_entries, void *stream) {
+    if (!o || !bad_entries) return fail(PHG_ERR_ARG, "NULL argument");
+    cudaStream_t s = o->str(stream);
+    DBuf cnt;
+    CK(cnt.ensure(sizeof(unsigned long long)));
+    unsigned long long *bad = cnt.as<unsigned long long>();
+    CK(cudaMemsetAsync(bad, 0, sizeof(unsigned long long), s));
+    const int V = o->V, rs = o->rs, os = o->os;
+    // the shared inner pattern and the index maps
+    CK(check_range(o->pcol.as<int>(), (long long)o->W * rs, 0, rs, bad, s));
+    CK(check_range(o->inner.as<int>(), rs, 0, V, bad, s));
+    if (os > 0) CK(check_range(o->outer.as<int>(), os, 0, V, bad, s));
+    CK(check_p2io(o->p2io.as<int>(), o->isb.as<int>(), V, rs, os, bad, s));
+    // the norm matrix's own pattern
+    CK(check_range(o->norm.col, (long long)o->norm.W * o->norm.n, 0, V, bad, s));
+    // boundary columns (CSR over the inner rows, columns in [0, os))
+    const ColsBufs *cols[] = {&o->bnd2, &o->bnd3, &o->d1b, &o->d2b, &o->d1cb, &o->d2cb};
+    for (const ColsBufs *c : cols) {
+        if (c->c.n <= 0 || !c->c.ptr) continue;
+        int nnz = 0;
+        CK(cudaMemcpyAsync(&nnz, c->c.ptr + c->c.n, sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        CK(check_ptr(c->c.ptr, c->c.n, nnz, bad, s));
+        if (nnz > 0) CK(check_range(c->c.col, nnz, 0, std::max(os, 1), bad, s));
+    }
+    // the multigrid hierarchy of the Laplacian
+    const MgDev &mg = o->L.op.mg;
+    for (int l = 0; l < mg.nlev; ++l) {
+        const MgLevelDev &D = mg.lev[l];
+        CK(check_range(D.col, (long long)D.W * D.n, 0, D.n, bad, s));
+        if (l + 1 < mg.nlev) {
+            const int nc = mg.lev[l + 1].n;
+            CK(check_range(D.pc, 2LL * D.n, -1, nc, bad, s));
+            CK(check_range(D.rf, (long long)D.Wr * nc, -1, D.n, bad, s));
+        }
+    }
+    unsigned long long h = 0;
+    CK(cudaMemcpyAsync(&h, bad, sizeof h, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    *bad_entries = (long long)h;
+    return PHG_OK;
+}
+
 // ------------------------------------------------------------- autotuner ---
 namespace {
 
@@ -1033,7 +1090,8 @@ int tune_solve(phg_ops_s *o, const char *label, const DevSolveOp &op, int nv, cu
         if (r) return r;
         GmresStats g{};
         CK(cudaMemcpy(&g, st.p, sizeof g, cudaMemcpyDeviceToHost));
-        const bool ok = g.status == 0 || (g.status == 1 && g.relres <= std::max(1e3 * o->tol, 1e-8));
+        const bool ok = std::isfinite(g.relres) &&
+                        (g.status == 0 || (g.status == 1 && g.relres <= std::max(1e3 * o->tol, 1e-8)));
         rep.add("solve %s family=%d rows=%d nv=%d rpb=%d path=%d ms=%.4f iters=%d relres=%.2e%s\n", label, fam, n,
                 nv, c.rpb, c.path, ms, g.iters, g.relres, ok ? "" : " (not converged)");
         if (ok && ms < best) { best = ms; pick = c; any = true; }
@@ -1285,6 +1343,7 @@ int bv_reserve(phg_barvortex_s *b, int nv) {
 // device (examples/barvortex_impl.h:171-310).
 int bv_step_dev(phg_barvortex_s *b, int nv, double *u1, const double *u, const double *bnd_u,
                 const double *bnd_w, const double *forcing, cudaStream_t s) {
+    NvtxRange nvtx("phg:barvortex_step");
     phg_ops_s *o = b->o;
     const int V = o->V, rs = o->rs, os = o->os;
     const long long NV = (long long)V * nv;
@@ -1380,7 +1439,7 @@ static int bv_check_agg(phg_barvortex_s *b, cudaStream_t s) {
     b->agg_pending = false;
     const double tol = b->o->tol;
     if (a.status == 2) return fail(PHG_ERR_TIMEOUT, "device barrier wait timed out");
-    if (a.status == 1 && !(a.relres <= std::max(1e3 * tol, 1e-8)))
+    if (!std::isfinite(a.relres) || (a.status == 1 && !(a.relres <= std::max(1e3 * tol, 1e-8))))
         return fail(PHG_ERR_NOT_CONVERGED, "GMRES stopped at relative residual %.3e", a.relres);
     return PHG_OK;
 }
@@ -1392,6 +1451,7 @@ static int bv_run(phg_barvortex b, int nv, int nsteps, double *u, const double *
                   const double *forcing, void *stream) {
     if (!b || !u || nv < 1 || nsteps < 0) return fail(PHG_ERR_ARG, "bad argument");
     if (nsteps == 0) return PHG_OK;
+    NvtxRange nvtx("phg:barvortex_run");
     phg_ops_s *o = b->o;
     cudaStream_t s = o->str(stream);
     if (s == cudaStreamLegacy || s == cudaStreamPerThread)
@@ -1674,7 +1734,7 @@ extern "C" int phg_barvortex_last_stats(phg_barvortex b, int *il, int *ia, int *
     double wr = 0.0;
     for (int k = 0; k < b->nslots; ++k) {
         const GmresStats &g = b->each[k];
-        wr = std::max(wr, g.relres);
+        wr = max_keep_nan(wr, g.relres);
         if (k < 2) ml += g.iters;
         else if ((k - 2) % 3 == 0) mj += g.iters;
         else if ((k - 2) % 3 == 1) a += g.iters;
@@ -1844,6 +1904,7 @@ namespace {
 // arguments on the device.
 int bc_step_dev(phg_baroclin_s *b, double *u11, double *u21, const double *u1, const double *u2,
                 const double *bnd, const double *f, const double *g, cudaStream_t s) {
+    NvtxRange nvtx("phg:baroclin_step");
     phg_ops_s *o = b->o;
     const int V = o->V, rs = o->rs, os = o->os;
     const phg_bc_conf &c = b->c;

@@ -141,6 +141,10 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+// maximum that keeps a NaN (fmax drops it): a non-finite residual must reach
+// the host as such, never as the other operand
+__device__ __forceinline__ double max_nan(double a, double b) { return a != a ? a : (b != b ? b : fmax(a, b)); }
+
 __device__ __forceinline__ float warp_sum(float v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
@@ -814,7 +818,7 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
         }
         my_iters = max(my_iters, iters);
         my_cycles = max(my_cycles, cycles);
-        my_rel = fmax(my_rel, rel);
+        my_rel = max_nan(my_rel, rel);
         my_status = max(my_status, status);
     }
 #undef PHG_TICK
@@ -963,7 +967,7 @@ __global__ void __launch_bounds__(BLOCK, 2) cheb_kernel(const Params p) {
         }
         my_iters = max(my_iters, iters);
         my_cycles = max(my_cycles, cycles);
-        my_rel = fmax(my_rel, rel);
+        my_rel = max_nan(my_rel, rel);
         my_status = max(my_status, status);
     }
     if (threadIdx.x == 0) atomicAdd(&p.stats->bytes, my_bytes);
@@ -1121,12 +1125,12 @@ __global__ void __launch_bounds__(256) k_ls_scale(const double *nrm, int nv, int
         const bool conv = rel <= tol || bt == 0.0;
         beta[v] = bt;
         sc[v] = conv ? 0.0 : 1.0 / bt;
-        mx = fmax(mx, rel);
+        mx = max_nan(mx, rel);
         if (!(rel == rel)) mx = rel;   // NaN propagates into the stats
         op += conv ? 0 : 1;
     }
     for (int o = 16; o > 0; o >>= 1) {
-        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        mx = max_nan(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         op += __shfl_xor_sync(0xffffffffu, op, o);
     }
     if ((threadIdx.x & 31) == 0) { rmax[threadIdx.x >> 5] = mx; open[threadIdx.x >> 5] = op; }
@@ -1134,7 +1138,7 @@ __global__ void __launch_bounds__(256) k_ls_scale(const double *nrm, int nv, int
     if (threadIdx.x == 0) {
         double m = 0.0;
         int o = 0;
-        for (int w = 0; w < NWARP; ++w) { m = fmax(m, rmax[w]); o += open[w]; }
+        for (int w = 0; w < NWARP; ++w) { m = max_nan(m, rmax[w]); o += open[w]; }
         st->relres = m;
         st->cycles = cycle;
         st->iters = cycle * K;
@@ -1417,7 +1421,7 @@ __global__ void __launch_bounds__(256) k_lsg_begin(LsgParams P, int c) {
         }
         if (s != 0) { P.scale[v] = 0.f; P.arn[v] = 0; }
         const double rel = P.relv[v];
-        mx = fmax(mx, rel);
+        mx = max_nan(mx, rel);
         if (!(rel == rel)) mx = rel;
         nbad += s == 2 ? 1 : 0;
         imax = max(imax, P.iters[v]);
@@ -1425,7 +1429,7 @@ __global__ void __launch_bounds__(256) k_lsg_begin(LsgParams P, int c) {
         isum += P.iters[v];
     }
     for (int o = 16; o > 0; o >>= 1) {
-        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        mx = max_nan(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         nopen += __shfl_xor_sync(0xffffffffu, nopen, o);
         nbad += __shfl_xor_sync(0xffffffffu, nbad, o);
         imax = max(imax, __shfl_xor_sync(0xffffffffu, imax, o));
@@ -1439,7 +1443,7 @@ __global__ void __launch_bounds__(256) k_lsg_begin(LsgParams P, int c) {
         double r = 0.0;
         int o = 0, b = 0, im = 0, cm = 0, is = 0;
         for (int k = 0; k < NWARP; ++k) {
-            r = fmax(r, rmax[k]); o += open[k]; b += bad[k]; im = max(im, itm[k]); cm = max(cm, cym[k]); is += its[k];
+            r = max_nan(r, rmax[k]); o += open[k]; b += bad[k]; im = max(im, itm[k]); cm = max(cm, cym[k]); is += its[k];
         }
         P.st->relres = r;
         P.st->status = (o || b) ? 1 : 0;

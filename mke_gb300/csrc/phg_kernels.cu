@@ -265,6 +265,57 @@ cudaError_t fill_hash32(float *x, long long n, unsigned seed, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// Index validation (debug aid): count the entries of an index array outside
+// [lo, hi); only the indices themselves are read, never what they point to.
+__global__ void k_check_range(const int *a, long long n, int lo, int hi, unsigned long long *bad) {
+    unsigned long long cnt = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int v = a[i];
+        cnt += (v < lo || v >= hi) ? 1ull : 0ull;
+    }
+    if (cnt) atomicAdd(bad, cnt);
+}
+
+// p2io: inner points map into [0, rs), boundary points (isb) into [0, os)
+__global__ void k_check_p2io(const int *p2io, const int *isb, int V, int rs, int os, unsigned long long *bad) {
+    unsigned long long cnt = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < V; i += gridDim.x * blockDim.x) {
+        const int v = p2io[i], b = isb[i];
+        cnt += (b != 0 && b != 1) || v < 0 || v >= (b ? os : rs) ? 1ull : 0ull;
+    }
+    if (cnt) atomicAdd(bad, cnt);
+}
+
+// CSR row pointers: ptr[0] = 0, non-decreasing, ptr[n] = nnz
+__global__ void k_check_ptr(const int *ptr, int n, int nnz, unsigned long long *bad) {
+    unsigned long long cnt = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        cnt += ptr[i + 1] < ptr[i] ? 1ull : 0ull;
+    if (blockIdx.x == 0 && threadIdx.x == 0) cnt += (ptr[0] != 0) + (ptr[n] != nnz);
+    if (cnt) atomicAdd(bad, cnt);
+}
+
+cudaError_t check_range(const int *a, long long n, int lo, int hi, unsigned long long *bad, cudaStream_t s) {
+    if (!a || n <= 0) return cudaSuccess;
+    k_check_range<<<grid_for(n), TB, 0, s>>>(a, n, lo, hi, bad);
+    g_kernel_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t check_p2io(const int *p2io, const int *isb, int V, int rs, int os, unsigned long long *bad,
+                       cudaStream_t s) {
+    k_check_p2io<<<grid_for(V), TB, 0, s>>>(p2io, isb, V, rs, os, bad);
+    g_kernel_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t check_ptr(const int *ptr, int n, int nnz, unsigned long long *bad, cudaStream_t s) {
+    if (!ptr || n <= 0) return cudaSuccess;
+    k_check_ptr<<<grid_for(n), TB, 0, s>>>(ptr, n, nnz, bad);
+    g_kernel_launches++;
+    return cudaGetLastError();
+}
+
 __global__ void k_stats_fold(const GmresStats *slots, int n, GmresStats *agg) {
     if (threadIdx.x || blockIdx.x) return;
     GmresStats a = *agg;

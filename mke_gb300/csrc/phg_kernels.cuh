@@ -40,6 +40,11 @@ cudaError_t dot(const double *a, const double *b, int ld, int n, int nv, double 
 cudaError_t bv_commit(double *u_n, const double *u_n1, const double *nr, const double *nr0, int *done,
                       int V, int nv, cudaStream_t s);
 cudaError_t gather(double *y, int ldy, const double *x, int ldx, const int *map, int n, int nv, cudaStream_t s);
+// index validation: add to *bad the entries outside their valid range
+cudaError_t check_range(const int *a, long long n, int lo, int hi, unsigned long long *bad, cudaStream_t s);
+cudaError_t check_p2io(const int *p2io, const int *isb, int V, int rs, int os, unsigned long long *bad,
+                       cudaStream_t s);
+cudaError_t check_ptr(const int *ptr, int n, int nnz, unsigned long long *bad, cudaStream_t s);
 // agg += the n solve records in slots (iterations summed; residual and status: the worst)
 cudaError_t stats_fold(const GmresStats *slots, int n, GmresStats *agg, cudaStream_t s);
 

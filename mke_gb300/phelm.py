@@ -103,6 +103,7 @@ SIGNATURES = {
     "phg_barvortex_calc_batch": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "phg_barvortex_run": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),
     "phg_ops_autotune": (C.c_int, [_vp, C.c_int, C.c_char_p, C.c_int, _vp]),
+    "phg_ops_validate": (C.c_int, [_vp, C.POINTER(C.c_longlong), _vp]),
     "phg_tune_describe": (C.c_int, [C.c_char_p, C.c_int]),
     "phg_tune_save": (C.c_int, [C.c_char_p]),
     "phg_tune_load": (C.c_int, [C.c_char_p, _ip]),
@@ -315,6 +316,12 @@ class Operators:
         (CUDA float32 tensors rs x nv, nv = 4 * 2^k <= 256)."""
         _check(lib().phg_ops_mult32(self._h, name.encode(), _ptr(out), _ptr(x), x.shape[1], _stream(stream)))
         return out
+
+    def validate(self, stream=None) -> int:
+        """Entries of the handle's device index arrays outside their valid range (0 = all fine)."""
+        n = C.c_longlong()
+        _check(lib().phg_ops_validate(self._h, C.byref(n), _stream(stream)))
+        return n.value
 
     def autotune(self, members: int = 1, stream=None) -> str:
         """Time the candidate launch shapes of a ``members``-state step's
