@@ -95,6 +95,41 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def tune_in_child(level: int, precision: str, members: int) -> list:
+    """Autotune (phg_ops_autotune) for a level / precision / ensemble size in a
+    child process and load the saved shape table here.  Tuning in this
+    process would leave its freed scratch behind the later allocations, which
+    measurably moved the step's buffers (L6 x 32 ensemble step 22.0 -> 23.0 ms
+    with identical shapes); a table tuned elsewhere and loaded does not.
+    Returns the "chose ..." lines of the tuner's report."""
+    import subprocess
+    import tempfile
+    from mke_gb300 import phelm
+    fd, path = tempfile.mkstemp(suffix=".tune")
+    os.close(fd)
+    code = ("import json, sys; sys.path.insert(0, %r); from mke_gb300 import phelm; import bench; "
+            "m = phelm.Mesh.sphere(%d); "
+            "o = phelm.Operators(m, phelm.PHG_MIXED if %r == 'mixed' else phelm.PHG_FP64, restart=30, tol=%r); "
+            "rep = o.autotune(%d); phelm.tune_save(%r); print(json.dumps(bench.chosen(rep)))"
+            % (HERE, level, precision, TOL, members, path))
+    # the child tunes on this rank's GPU, outside the process group
+    env = dict(os.environ)
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    vis = [d for d in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if d.strip()]
+    env["CUDA_VISIBLE_DEVICES"] = vis[local] if local < len(vis) else (vis[0] if vis else str(local))
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "LOCAL_WORLD_SIZE", "MASTER_ADDR", "MASTER_PORT"):
+        env.pop(k, None)
+    try:
+        r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd=HERE, timeout=600,
+                           env=env)
+        if r.returncode != 0:
+            raise RuntimeError(f"autotune child failed: {r.stderr[-2000:]}")
+        phelm.tune_load(path)
+        return json.loads(r.stdout.strip().splitlines()[-1])
+    finally:
+        os.unlink(path)
+
+
 def chosen(report: str) -> list:
     """The "chose ..." lines of an autotuner report."""
     return [ln[6:] for ln in report.splitlines() if ln.startswith("chose ")]
@@ -128,7 +163,8 @@ def run_ours(args, ws, rank, local):
     def make(prec):
         ops = phelm.Operators(mesh, prec, restart=30, tol=args.tol, max_iter=20000)
         if not args.no_tune:
-            tuned[f"L{args.level}x1_{'mixed' if prec == phelm.PHG_MIXED else 'fp64'}"] = chosen(ops.autotune(1))
+            pname = 'mixed' if prec == phelm.PHG_MIXED else 'fp64'
+            tuned[f"L{args.level}x1_{pname}"] = tune_in_child(args.level, pname, 1)
         return ops, phelm.BarVortex(ops, coriolis=cor, **CONF)
 
     results = {}
@@ -237,7 +273,7 @@ def run_ours(args, ws, rank, local):
             for name, prec in (("mixed", phelm.PHG_MIXED), ("fp64", phelm.PHG_FP64)):
                 bops = phelm.Operators(bm, prec, restart=30, tol=args.tol)
                 if not args.no_tune:
-                    tuned[f"L{lvl}x{B}_{name}"] = chosen(bops.autotune(B))
+                    tuned[f"L{lvl}x{B}_{name}"] = tune_in_child(lvl, name, B)
                 bbv = phelm.BarVortex(bops, coriolis=np.sin(blat), **CONF)
                 U = torch.tensor(states, dtype=torch.float64, device=dev)
                 zB = torch.zeros((B, max(bm.outer_size, 1)), dtype=torch.float64, device=dev)
@@ -604,7 +640,7 @@ def run_case(args):
     ops = phelm.Operators(mesh, prec, restart=30, tol=args.tol)
     tune_report = None
     if args.tune:
-        tune_report = chosen(ops.autotune(args.members if args.case == "batch" else 1))
+        tune_report = tune_in_child(args.level, args.precision, args.members if args.case == "batch" else 1)
     u = torch.tensor(psi0, dtype=torch.float64, device="cuda")
     out = torch.empty_like(u)
     zb = torch.zeros(max(mesh.outer_size, 1), dtype=torch.float64, device="cuda")

@@ -152,7 +152,9 @@ int phg_ops_validate(phg_ops o, long long *bad_entries, void *stream);
  * phg_ops_mult32 at nmembers vectors -- and keeps the fastest in a
  * process-wide table consulted by every later launch of the same kernel
  * family, size, precision and right-hand-side bucket (powers of two).  A
- * shape whose solve misses the tolerance is never chosen.  report (may be
+ * shape whose solve misses the tolerance is never chosen.  Solves are timed
+ * captured in a CUDA graph and replayed (as the steps of phg_barvortex_run
+ * run them); on the legacy or per-thread default stream, enqueued directly.  report (may be
  * NULL) receives one text line per candidate timed and per choice. */
 int phg_ops_autotune(phg_ops o, int nmembers, char *report, int report_len, void *stream);
 /* The table as text: "solve <family> <rows> <precision> <bucket> <rows per

@@ -1079,14 +1079,48 @@ int tune_solve(phg_ops_s *o, const char *label, const DevSolveOp &op, int nv, cu
     float best = 1e30f;
     SolveShape pick;
     bool any = false;
+    // Candidates are timed as a captured and replayed solve: ensemble and
+    // single-trajectory steps run from step graphs (phg_barvortex_run), where
+    // a shape's many short launches cost far less than when enqueued one by one.
+    const bool graphs = s != cudaStreamLegacy && s != cudaStreamPerThread;
     for (const SolveShape &c : cand) {
-        float ms = 0.f;
-        int r = time_best(s, 2, [&]() -> int {
+        auto enqueue = [&]() -> int {
             CK(cudaMemsetAsync(x.p, 0, 8 * len, s));
             CK(gmres_solve(op, b.as<double>(), x.as<double>(), nv, n, o->restart, o->max_iter, o->tol, pr, o->work.p,
                            st.as<GmresStats>(), s, false, o->max_sms, &c));
             return PHG_OK;
-        }, &ms);
+        };
+        float ms = 0.f;
+        int r;
+        if (graphs) {
+            // one direct run first (function attributes, first-use set-up), then the capture
+            if ((r = enqueue())) return r;
+            CK(cudaStreamSynchronize(s));
+            const long long l0 = g_kernel_launches.load();
+            CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            r = enqueue();
+            cudaGraph_t g = nullptr;
+            cudaError_t ec = cudaStreamEndCapture(s, &g);
+            const long long per = g_kernel_launches.load() - l0;
+            g_kernel_launches -= per;   // captured, not run
+            if (r || ec != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                if (r) return r;
+                return fail(PHG_ERR_CUDA, "autotune capture: %s", cudaGetErrorString(ec));
+            }
+            cudaGraphExec_t ge = nullptr;
+            cudaError_t ei = cudaGraphInstantiate(&ge, g, 0);
+            cudaGraphDestroy(g);
+            if (ei != cudaSuccess) return fail(PHG_ERR_CUDA, "autotune instantiate: %s", cudaGetErrorString(ei));
+            r = time_best(s, 2, [&]() -> int {
+                CK(cudaGraphLaunch(ge, s));
+                g_kernel_launches += per;
+                return PHG_OK;
+            }, &ms);
+            cudaGraphExecDestroy(ge);
+        } else {
+            r = time_best(s, 2, enqueue, &ms);
+        }
         if (r) return r;
         GmresStats g{};
         CK(cudaMemcpy(&g, st.p, sizeof g, cudaMemcpyDeviceToHost));
