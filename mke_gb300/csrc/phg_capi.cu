@@ -506,7 +506,12 @@ int build_mg_dev(phg_ops_s *o, phg_mesh_s *mh, SolveOpBufs &Lb, MgBufs &mb, int 
     mg.nu1 = env_int("PHG_MG_NU", 1);
     mg.nu2 = mg.nu1;
     const size_t es = prec == PHG_MIXED ? 4 : 8;
-    const int red_max = env_int("PHG_MG_REDUNDANT", 700);
+    // levels of at most red_max points run redundantly per block in shared
+    // memory, the larger ones with group barriers; with the arrival-count
+    // barrier the 641-point level is cheaper in parallel (L6 step mixed
+    // 5.30 -> 5.20 ms, FP64 6.35 -> 6.06 ms, baroclin +5 %), so only the
+    // 161-point level and the dense coarsest one stay redundant
+    const int red_max = env_int("PHG_MG_REDUNDANT", 200);
     // shared memory: the solver's own ~21 KB plus 4 vectors per redundant level
     const size_t smem_cap = 200 * 1024;
     int nred = nlev - 1;
