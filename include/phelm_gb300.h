@@ -66,6 +66,15 @@ long long phg_kernel_launches(void);
  * (utils/icosahedron.cpp:481-624, utils/mesh_builder.cpp:52-585) and then
  * Mesh::load (src/mesh.cpp:323-519); the result is identical. */
 int phg_mesh_generate(int level, phg_mesh *out);
+/* Host-side level cache (no reference counterpart).  Mesh handles of the same
+ * generated level share one copy of the mesh, its assembled operators and its
+ * multigrid hierarchy while any of them is alive.  With a cache directory
+ * (this call, or the environment variable PHG_CACHE_DIR) a generated level is
+ * read from <dir>/phelm_level<n>.cache when present and valid, else generated,
+ * fully assembled and written there (atomically, best effort), so later
+ * processes skip generation and assembly; the data are stored byte for byte.
+ * NULL or "" disables the directory. */
+int phg_cache_dir(const char *path);
 /* Mesh::load(FILE*) (src/mesh.h:411, src/mesh.cpp:323-519) from a file in
  * the reference's text format (charts stdsphere1..4). */
 int phg_mesh_load_file(const char *path, phg_mesh *out);

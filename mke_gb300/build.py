@@ -23,6 +23,7 @@ HOST = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-fopenmp", "-std
 UNITS = [
     ("phg_mesh.cpp", "host", []),
     ("phg_assemble.cpp", "host", []),
+    ("phg_cache.cpp", "host", []),
     ("phg_kernels.cu", "cuda", ["-fmad=false"]),
     ("phg_gmres.cu", "cuda", []),
     ("phg_capi.cu", "cuda", []),

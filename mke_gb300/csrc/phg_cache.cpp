@@ -1,0 +1,196 @@
+// phg_cache.cpp -- the on-disk cache of a generated mesh level: the mesh, every
+// assembled operator and the multigrid hierarchy, written once and read back
+// by later processes instead of regenerating and reassembling them.  The
+// data are stored byte for byte, so a cached level is bit-identical to a
+// freshly built one.
+//
+// File: "PHGLVL01", int32 level, then the payload (every array as a uint64
+// count followed by its raw elements), then a uint64 FNV-1a hash of the
+// payload.  A file with another magic, level, a short payload or a hash
+// mismatch is rejected (the caller rebuilds the level and rewrites it).
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "phg_host.hpp"
+
+namespace phg {
+
+namespace {
+
+const char kMagic[8] = {'P', 'H', 'G', 'L', 'V', 'L', '0', '1'};
+
+struct Writer {
+    std::vector<unsigned char> buf;
+    void raw(const void *p, size_t n) {
+        const unsigned char *c = static_cast<const unsigned char *>(p);
+        buf.insert(buf.end(), c, c + n);
+    }
+    template <typename T> void scalar(T v) { raw(&v, sizeof v); }
+    template <typename T> void vec(const std::vector<T> &v) {
+        scalar<uint64_t>(v.size());
+        if (!v.empty()) raw(v.data(), sizeof(T) * v.size());
+    }
+};
+
+struct Reader {
+    const unsigned char *p, *end;
+    bool ok = true;
+    bool raw(void *dst, size_t n) {
+        if (!ok || (size_t)(end - p) < n) return ok = false;
+        std::memcpy(dst, p, n);
+        p += n;
+        return true;
+    }
+    template <typename T> bool scalar(T &v) { return raw(&v, sizeof v); }
+    template <typename T> bool vec(std::vector<T> &v) {
+        uint64_t n = 0;
+        if (!scalar(n) || n > (uint64_t)(end - p) / sizeof(T)) return ok = false;
+        v.resize((size_t)n);
+        return n == 0 || raw(v.data(), sizeof(T) * (size_t)n);
+    }
+};
+
+uint64_t fnv1a(const unsigned char *p, size_t n) {
+    uint64_t h = 1469598103934665603ull;
+    for (size_t i = 0; i < n; ++i) { h ^= p[i]; h *= 1099511628211ull; }
+    return h;
+}
+
+void put_mesh(Writer &w, const Mesh &m) {
+    w.scalar<int32_t>(m.level); w.scalar<int32_t>(m.V); w.scalar<int32_t>(m.T);
+    w.scalar<int32_t>(m.rs); w.scalar<int32_t>(m.os); w.scalar<int32_t>(m.nz);
+    w.vec(m.xyz); w.vec(m.uv); w.vec(m.tri); w.vec(m.tz); w.vec(m.bnd);
+    w.vec(m.inner); w.vec(m.outer); w.vec(m.p2io); w.vec(m.adj_ptr); w.vec(m.adj);
+    w.vec(m.orig); w.vec(m.par_a); w.vec(m.par_b); w.vec(m.raw_xyz);
+}
+
+bool get_mesh(Reader &r, Mesh &m, bool allow_empty = false) {
+    int32_t lv, V, T, rs, os, nz;
+    r.scalar(lv); r.scalar(V); r.scalar(T); r.scalar(rs); r.scalar(os); r.scalar(nz);
+    m.level = lv; m.V = V; m.T = T; m.rs = rs; m.os = os; m.nz = nz;
+    r.vec(m.xyz); r.vec(m.uv); r.vec(m.tri); r.vec(m.tz); r.vec(m.bnd);
+    r.vec(m.inner); r.vec(m.outer); r.vec(m.p2io); r.vec(m.adj_ptr); r.vec(m.adj);
+    r.vec(m.orig); r.vec(m.par_a); r.vec(m.par_b); r.vec(m.raw_xyz);
+    if (!r.ok) return false;
+    if (allow_empty && V == 0 && T == 0 && m.xyz.empty() && m.tri.empty()) return true;   // an unused slot
+    // the sizes the rest of the library relies on
+    return V > 0 && T > 0 && rs >= 0 && os >= 0 && rs + os == V && m.xyz.size() == 3 * (size_t)V &&
+           m.uv.size() == 8 * (size_t)V && m.tri.size() == 3 * (size_t)T && m.tz.size() == (size_t)T &&
+           m.bnd.size() == (size_t)V && m.inner.size() == (size_t)rs && m.outer.size() == (size_t)os &&
+           m.p2io.size() == (size_t)V && m.adj_ptr.size() == (size_t)V + 1 &&
+           m.adj.size() == (size_t)m.adj_ptr[V];
+}
+
+void put_csr(Writer &w, const Csr &a) {
+    w.scalar<int32_t>(a.n); w.scalar<int32_t>(a.m);
+    w.vec(a.ptr); w.vec(a.col); w.vec(a.val);
+}
+
+bool get_csr(Reader &r, Csr &a) {
+    int32_t n, m;
+    r.scalar(n); r.scalar(m);
+    a.n = n; a.m = m;
+    r.vec(a.ptr); r.vec(a.col); r.vec(a.val);
+    if (r.ok && n == 0 && a.ptr.empty() && a.col.empty() && a.val.empty()) return true;   // an unused slot
+    if (!r.ok || n < 0 || a.ptr.size() != (size_t)n + 1 || a.ptr[0] != 0) return false;
+    for (int i = 0; i < n; ++i)
+        if (a.ptr[i + 1] < a.ptr[i]) return false;
+    const size_t nnz = (size_t)a.ptr[n];
+    if (a.col.size() != nnz || a.val.size() != nnz) return false;
+    for (int c : a.col)
+        if (c < 0 || c >= m) return false;
+    return true;
+}
+
+}  // namespace
+
+bool save_level_cache(const char *path, const Mesh &m, const SphereOps &ops, const MgHierarchy *mg) {
+    Writer w;
+    put_mesh(w, m);
+    const Csr *all[] = {&ops.idt, &ops.lapl, &ops.jidt, &ops.d1, &ops.d2, &ops.d1c, &ops.d2c,
+                        &ops.bnd2, &ops.bnd3, &ops.d1b, &ops.d2b, &ops.d1cb, &ops.d2cb, &ops.norm};
+    for (const Csr *a : all) put_csr(w, *a);
+    w.scalar<int32_t>(mg ? 1 : 0);
+    if (mg) {
+        w.scalar<uint64_t>(mg->mesh.size());
+        for (const Mesh &x : mg->mesh) put_mesh(w, x);
+        const std::vector<Csr> *lists[] = {&mg->A, &mg->P, &mg->R};
+        for (const auto *l : lists) {
+            w.scalar<uint64_t>(l->size());
+            for (const Csr &a : *l) put_csr(w, a);
+        }
+        w.vec(mg->coarse_inv);
+    }
+    // write to a temporary name and rename: readers never see a partial file
+    const std::string tmp = std::string(path) + ".tmp";
+    FILE *f = std::fopen(tmp.c_str(), "wb");
+    if (!f) return false;
+    const int32_t level = m.level;
+    const uint64_t h = fnv1a(w.buf.data(), w.buf.size());
+    bool ok = std::fwrite(kMagic, 1, 8, f) == 8 && std::fwrite(&level, sizeof level, 1, f) == 1 &&
+              std::fwrite(w.buf.data(), 1, w.buf.size(), f) == w.buf.size() && std::fwrite(&h, sizeof h, 1, f) == 1;
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok || std::rename(tmp.c_str(), path) != 0) {
+        std::remove(tmp.c_str());
+        return false;
+    }
+    return true;
+}
+
+bool load_level_cache(const char *path, int level, Mesh &m, SphereOps &ops, MgHierarchy &mg, bool &has_mg,
+                      std::string &err) {
+    FILE *f = std::fopen(path, "rb");
+    if (!f) { err = "no cache file"; return false; }
+    std::vector<unsigned char> all;
+    unsigned char chunk[1 << 16];
+    size_t k;
+    while ((k = std::fread(chunk, 1, sizeof chunk, f)) > 0) all.insert(all.end(), chunk, chunk + k);
+    std::fclose(f);
+    if (all.size() < 8 + 4 + 8 || std::memcmp(all.data(), kMagic, 8) != 0) { err = "not a level cache"; return false; }
+    int32_t lv;
+    std::memcpy(&lv, all.data() + 8, sizeof lv);
+    if (lv != level) { err = "cached level differs"; return false; }
+    const unsigned char *pay = all.data() + 12;
+    const size_t npay = all.size() - 12 - 8;
+    uint64_t h;
+    std::memcpy(&h, pay + npay, sizeof h);
+    if (fnv1a(pay, npay) != h) { err = "cache checksum mismatch"; return false; }
+    Reader r{pay, pay + npay};
+    Mesh mm;
+    SphereOps oo;
+    if (!get_mesh(r, mm) || mm.level != level) { err = "bad mesh record"; return false; }
+    Csr *all_ops[] = {&oo.idt, &oo.lapl, &oo.jidt, &oo.d1, &oo.d2, &oo.d1c, &oo.d2c,
+                      &oo.bnd2, &oo.bnd3, &oo.d1b, &oo.d2b, &oo.d1cb, &oo.d2cb, &oo.norm};
+    for (Csr *a : all_ops)
+        if (!get_csr(r, *a)) { err = "bad operator record"; return false; }
+    int32_t flag = 0;
+    MgHierarchy hh;
+    if (!r.scalar(flag)) { err = "truncated"; return false; }
+    if (flag) {
+        uint64_t nm = 0;
+        if (!r.scalar(nm) || nm > 64) { err = "bad hierarchy record"; return false; }
+        hh.mesh.resize((size_t)nm);
+        for (Mesh &x : hh.mesh)
+            if (!get_mesh(r, x, true)) { err = "bad hierarchy mesh"; return false; }
+        std::vector<Csr> *lists[] = {&hh.A, &hh.P, &hh.R};
+        for (auto *l : lists) {
+            uint64_t nl = 0;
+            if (!r.scalar(nl) || nl > 64) { err = "bad hierarchy record"; return false; }
+            l->resize((size_t)nl);
+            for (Csr &a : *l)
+                if (!get_csr(r, a)) { err = "bad hierarchy operator"; return false; }
+        }
+        if (!r.vec(hh.coarse_inv)) { err = "bad coarse inverse"; return false; }
+    }
+    if (r.p != r.end) { err = "trailing bytes"; return false; }
+    m = std::move(mm);
+    ops = std::move(oo);
+    has_mg = flag != 0;
+    if (has_mg) mg = std::move(hh);
+    return true;
+}
+
+}  // namespace phg

@@ -7,6 +7,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -104,23 +105,88 @@ bool is_device_ptr(const void *p) {
 }  // namespace
 
 // ----------------------------------------------------------------- mesh ---
-struct phg_mesh_s {
-    std::atomic<int> refs{1};   // the caller's, plus one per operator set
+// A level's host data -- the mesh, its assembled operators and the multigrid
+// hierarchy -- shared by every mesh handle of that level in the process (and,
+// with a cache directory, read from / written to disk once per level).
+struct LevelData {
     Mesh m;
     std::once_flag assembled;
     SphereOps ops;
-    void assemble() { std::call_once(assembled, [this] { assemble_sphere(m, ops); }); }
-    // multigrid hierarchy of the Laplacian, built once per mesh
+    bool ops_ready = false;          // filled from the disk cache
+    void assemble() { std::call_once(assembled, [this] { if (!ops_ready) assemble_sphere(m, ops); }); }
     std::once_flag mg_once;
     MgHierarchy mg;
+    bool mg_ready = false;           // filled from the disk cache
     bool mg_ok = false;
     std::string mg_err;
     const MgHierarchy *hierarchy(std::string &err) {
-        std::call_once(mg_once, [this] { mg_ok = build_mg(m, 1, mg, mg_err); });
+        std::call_once(mg_once, [this] { mg_ok = mg_ready || build_mg(m, 1, mg, mg_err); });
         if (!mg_ok) err = mg_err;
         return mg_ok ? &mg : nullptr;
     }
 };
+
+struct phg_mesh_s {
+    std::atomic<int> refs{1};   // the caller's, plus one per operator set
+    std::shared_ptr<LevelData> d;
+    Mesh &m;
+    SphereOps &ops;
+    explicit phg_mesh_s(std::shared_ptr<LevelData> dd) : d(std::move(dd)), m(d->m), ops(d->ops) {}
+    void assemble() { d->assemble(); }
+    const MgHierarchy *hierarchy(std::string &err) { return d->hierarchy(err); }
+};
+
+namespace {
+
+// generated levels alive in the process, and the optional cache directory
+std::mutex g_level_mu;
+std::map<int, std::weak_ptr<LevelData>> g_levels;
+std::string g_cache_dir = [] {
+    const char *e = getenv("PHG_CACHE_DIR");
+    return std::string(e ? e : "");
+}();
+
+std::string cache_path(int level) { return g_cache_dir + "/phelm_level" + std::to_string(level) + ".cache"; }
+
+// the shared data of a generated level: a live one, else the disk cache, else
+// generate (and, with a cache directory, assemble everything and save it)
+int level_data(int level, std::shared_ptr<LevelData> &out) {
+    std::lock_guard<std::mutex> g(g_level_mu);
+    auto it = g_levels.find(level);
+    if (it != g_levels.end())
+        if ((out = it->second.lock())) return PHG_OK;
+    auto d = std::make_shared<LevelData>();
+    std::string err;
+    bool loaded = false;
+    if (!g_cache_dir.empty()) {
+        bool has_mg = false;
+        if (load_level_cache(cache_path(level).c_str(), level, d->m, d->ops, d->mg, has_mg, err)) {
+            loaded = true;
+            d->ops_ready = true;
+            d->mg_ready = has_mg;
+        }
+    }
+    if (!loaded) {
+        if (!generate_sphere(level, d->m, err)) return fail(PHG_ERR_ARG, "%s", err.c_str());
+        if (!g_cache_dir.empty()) {
+            d->assemble();
+            std::string mg_err;
+            const MgHierarchy *h = level >= 2 ? d->hierarchy(mg_err) : nullptr;
+            save_level_cache(cache_path(level).c_str(), d->m, d->ops, h);   // best effort: a read-only dir is fine
+        }
+    }
+    g_levels[level] = d;
+    out = std::move(d);
+    return PHG_OK;
+}
+
+}  // namespace
+
+extern "C" int phg_cache_dir(const char *path) {
+    std::lock_guard<std::mutex> g(g_level_mu);
+    g_cache_dir = path ? path : "";
+    return PHG_OK;
+}
 
 extern "C" const char *phg_last_error(void) { return g_err.c_str(); }
 extern "C" const char *phg_version(void) { return "phelm-gb300 0.1 (sm_103a)"; }
@@ -128,10 +194,10 @@ extern "C" long long phg_kernel_launches(void) { return g_kernel_launches.load()
 
 extern "C" int phg_mesh_generate(int level, phg_mesh *out) {
     if (!out) return fail(PHG_ERR_ARG, "out is NULL");
-    auto h = std::make_unique<phg_mesh_s>();
-    std::string err;
-    if (!generate_sphere(level, h->m, err)) return fail(PHG_ERR_ARG, "%s", err.c_str());
-    *out = h.release();
+    std::shared_ptr<LevelData> d;
+    int r = level_data(level, d);
+    if (r) return r;
+    *out = new phg_mesh_s(std::move(d));
     return PHG_OK;
 }
 
@@ -139,12 +205,12 @@ extern "C" int phg_mesh_load_file(const char *path, phg_mesh *out) {
     if (!path || !out) return fail(PHG_ERR_ARG, "NULL argument");
     FILE *f = fopen(path, "rb");
     if (!f) return fail(PHG_ERR_IO, "cannot open %s", path);
-    auto h = std::make_unique<phg_mesh_s>();
+    auto d = std::make_shared<LevelData>();   // a loaded mesh keeps its own data
     std::string err;
-    bool ok = load_mesh_text(f, h->m, err);
+    bool ok = load_mesh_text(f, d->m, err);
     fclose(f);
     if (!ok) return fail(PHG_ERR_IO, "%s: %s", path, err.c_str());
-    *out = h.release();
+    *out = new phg_mesh_s(std::move(d));
     return PHG_OK;
 }
 

@@ -111,4 +111,12 @@ void assemble_barvortex(const Mesh &m, double c1, double c2, Csr &A, Csr &Abnd);
 struct BaroclinParams { double tau, sigma, mu, sigma1, mu1, alpha, theta; bool backward = false; };
 void assemble_baroclin(const Mesh &m, const BaroclinParams &p, Csr &A, Csr bcol[4]);
 
+// On-disk cache of a generated level (phg_cache.cpp): the mesh, the operators
+// and, when built, the multigrid hierarchy, stored byte for byte.  load
+// rejects files of another format or level, truncated files and checksum
+// mismatches (err says why).
+bool save_level_cache(const char *path, const Mesh &m, const SphereOps &ops, const MgHierarchy *mg);
+bool load_level_cache(const char *path, int level, Mesh &m, SphereOps &ops, MgHierarchy &mg, bool &has_mg,
+                      std::string &err);
+
 }  // namespace phg

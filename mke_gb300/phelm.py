@@ -65,6 +65,7 @@ SIGNATURES = {
     "phg_mesh_generate": (C.c_int, [C.c_int, C.POINTER(_vp)]),
     "phg_mesh_load_file": (C.c_int, [C.c_char_p, C.POINTER(_vp)]),
     "phg_mesh_destroy": (None, [_vp]),
+    "phg_cache_dir": (C.c_int, [C.c_char_p]),
     "phg_mesh_save_file": (C.c_int, [_vp, C.c_char_p]),
     "phg_print_function": (C.c_int, [_vp, C.c_char_p, _vp, _vp, _vp, _vp]),
     "phg_print_inner_function": (C.c_int, [_vp, C.c_char_p, _vp, _vp, _vp, _vp]),
@@ -145,6 +146,11 @@ def lib(build_if_missing: bool = True):
             f.argtypes = args
         _lib = L
     return _lib
+
+
+def cache_dir(path=None) -> None:
+    """Directory of the on-disk level cache (phg_cache_dir); None disables it."""
+    _check(lib().phg_cache_dir(path.encode() if path else None))
 
 
 def tune_table() -> list:

@@ -1,0 +1,122 @@
+"""The host-side level cache (phg_cache_dir): a generated level is written to
+disk once with its mesh, operators and multigrid hierarchy, read back byte for
+byte by later generations, and a damaged file is rejected and rebuilt.  No GPU
+needed (mesh arrays and assembled operators are host data)."""
+import gc
+import os
+import struct
+
+import numpy as np
+import pytest
+
+from mke_gb300 import phelm
+
+OPS = ["idt", "lapl", "jidt", "d1", "d2", "d1c", "d2c", "bnd2", "bnd3", "d1b", "d2b", "d1cb", "d2cb", "norm"]
+
+
+def snapshot(level):
+    m = phelm.Mesh.sphere(level)
+    out = {k: v.copy() for k, v in m.arrays().items()}
+    for name in OPS:
+        p, c, v = m.csr(name)
+        out[name] = (p.copy(), c.copy(), v.copy())
+    del m
+    gc.collect()
+    return out
+
+
+def same(a, b):
+    for k in a:
+        if isinstance(a[k], tuple):
+            if not all(np.array_equal(x, y) for x, y in zip(a[k], b[k])):
+                return False
+        elif not np.array_equal(a[k], b[k], equal_nan=True):
+            return False
+    return True
+
+
+def fnv1a(data: bytes) -> int:
+    h = 1469598103934665603
+    for byte in data:
+        h = ((h ^ byte) * 1099511628211) & 0xFFFFFFFFFFFFFFFF
+    return h
+
+
+@pytest.fixture
+def cache(tmp_path):
+    phelm.cache_dir(str(tmp_path))
+    yield tmp_path
+    phelm.cache_dir(None)
+    gc.collect()
+
+
+def test_written_then_read_back_identical(cache):
+    phelm.cache_dir(None)
+    fresh = snapshot(3)
+    phelm.cache_dir(str(cache))
+    first = snapshot(3)                      # generated, assembled and saved
+    path = cache / "phelm_level3.cache"
+    assert path.exists() and path.read_bytes()[:8] == b"PHGLVL01"
+    second = snapshot(3)                     # read from the file
+    assert same(fresh, first) and same(fresh, second)
+
+
+def test_data_come_from_the_file(cache):
+    snapshot(3)
+    path = cache / "phelm_level3.cache"
+    raw = bytearray(path.read_bytes())
+    # payload: 6 int32 mesh scalars, then xyz as uint64 count + doubles
+    off = 12 + 24 + 8
+    x0 = struct.unpack_from("<d", raw, off)[0]
+    struct.pack_into("<d", raw, off, x0 + 1.0)
+    struct.pack_into("<Q", raw, len(raw) - 8, fnv1a(bytes(raw[12:-8])))
+    path.write_bytes(bytes(raw))
+    m = phelm.Mesh.sphere(3)
+    assert m.arrays()["xyz"][0] == x0 + 1.0   # the edited (but well-formed) file was used
+    del m
+    gc.collect()
+
+
+@pytest.mark.parametrize("damage", ["flip", "truncate", "level", "magic"])
+def test_damaged_file_is_rebuilt(cache, damage):
+    phelm.cache_dir(None)
+    fresh = snapshot(3)
+    phelm.cache_dir(str(cache))
+    snapshot(3)
+    path = cache / "phelm_level3.cache"
+    raw = bytearray(path.read_bytes())
+    if damage == "flip":
+        raw[len(raw) // 2] ^= 0x40
+    elif damage == "truncate":
+        raw = raw[: len(raw) // 3]
+    elif damage == "level":
+        struct.pack_into("<i", raw, 8, 4)
+    else:
+        raw[0:8] = b"NOTACASH"
+    path.write_bytes(bytes(raw))
+    assert same(fresh, snapshot(3))           # rebuilt from scratch
+    assert path.read_bytes()[:8] == b"PHGLVL01"
+    assert same(fresh, snapshot(3))           # and the rewritten file reads back
+
+
+def test_unwritable_directory_is_not_an_error(tmp_path):
+    missing = tmp_path / "does" / "not" / "exist"
+    phelm.cache_dir(str(missing))
+    try:
+        m = phelm.Mesh.sphere(2)
+        assert m.size == 162
+        del m
+    finally:
+        phelm.cache_dir(None)
+        gc.collect()
+
+
+def test_handles_of_one_level_share_data():
+    a = phelm.Mesh.sphere(3)
+    b = phelm.Mesh.sphere(3)
+    pa, _, _ = a.csr("lapl")
+    pb, _, _ = b.csr("lapl")
+    assert np.array_equal(pa, pb)
+    del a
+    gc.collect()
+    assert b.csr("lapl")[0].size == pb.size  # b's data survives a's destruction
