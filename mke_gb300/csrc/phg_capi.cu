@@ -154,7 +154,21 @@ int level_data(int level, std::shared_ptr<LevelData> &out) {
     std::lock_guard<std::mutex> g(g_level_mu);
     auto it = g_levels.find(level);
     if (it != g_levels.end())
-        if ((out = it->second.lock())) return PHG_OK;
+        if ((out = it->second.lock())) {
+            // a live level and a cache directory without its file (the
+            // directory was set after the level was built): write it now
+            if (!g_cache_dir.empty()) {
+                const std::string path = cache_path(level);
+                if (FILE *f = fopen(path.c_str(), "rb")) fclose(f);
+                else {
+                    out->assemble();
+                    std::string mg_err;
+                    const MgHierarchy *h = level >= 2 ? out->hierarchy(mg_err) : nullptr;
+                    save_level_cache(path.c_str(), out->m, out->ops, h);
+                }
+            }
+            return PHG_OK;
+        }
     auto d = std::make_shared<LevelData>();
     std::string err;
     bool loaded = false;
@@ -384,6 +398,7 @@ void to_ell(const Csr &c, int W, std::vector<int> *col, std::vector<double> &val
 
 struct SolveOpBufs {
     DBuf val, as64, as32, a32, dinv, dinv32;
+    DBuf pk;   // FP32 row records for the interleaved apply: 8 (column, value) pairs per row
     DevSolveOp op;
 };
 
@@ -511,13 +526,26 @@ int build_solve_op(phg_ops_s *o, const Csr &c, SolveOpBufs &b, bool try_cheb = f
         as32[e] = (float)as64[e];
         a32[e] = (float)v[e];
     }
-    (void)n;
+    if (o->W <= 8) {   // row records: slot k of row i at pk[8 i + k], padding = (i, 0)
+        std::vector<unsigned> pk(16 * (size_t)n);
+        for (int i = 0; i < n; ++i)
+            for (int k = 0; k < 8; ++k) {
+                const bool real = k < o->W;
+                const float a = real ? a32[(size_t)k * n + i] : 0.0f;
+                unsigned bits;
+                memcpy(&bits, &a, sizeof bits);
+                pk[16 * (size_t)i + 2 * k] = (unsigned)(real ? col[(size_t)k * n + i] : i);
+                pk[16 * (size_t)i + 2 * k + 1] = bits;
+            }
+        CK(upload(b.pk, pk));
+    }
     CK(upload(b.val, v)); CK(upload(b.as64, as64)); CK(upload(b.as32, as32)); CK(upload(b.a32, a32));
     CK(upload(b.dinv, dinv)); CK(upload(b.dinv32, std::vector<float>(dinv.begin(), dinv.end())));
     b.op.A = o->ell(b.val);
     b.op.as64 = b.as64.as<double>(); b.op.as32 = b.as32.as<float>(); b.op.dinv = b.dinv.as<double>();
     b.op.a32 = b.a32.as<float>();
     b.op.dinv32 = b.dinv32.as<float>();
+    b.op.pk32 = b.pk.p ? b.pk.as<uint4>() : nullptr;
     b.op.cheb_lmin = b.op.cheb_lmax = 0.0;
     if (try_cheb && o->W <= 8 && env_int("PHG_CHEB", 1)) {
         double lo = 0.0, hi = 0.0;
@@ -1006,14 +1034,20 @@ extern "C" int phg_laplace_solve_batch(phg_ops o, int nv, double *ans, const dou
 
 // the handle's copy of a named inner x inner operator (FP64 values, and the
 // FP32 copy where the mixed path keeps one)
-static int named_op(phg_ops o, const char *name, const double **v64, const float **v32) {
-    struct { const char *n; const double *d; const float *f; } t[] = {
-        {"idt", o->ML.op.A.val, o->ML.op.a32}, {"lapl", o->L.op.A.val, o->L.op.a32},
-        {"jidt", o->MJ.op.A.val, o->MJ.op.a32}, {"d1", o->vd1.as<double>(), nullptr},
-        {"d2", o->vd2.as<double>(), nullptr}, {"d1c", o->vd1c.as<double>(), nullptr},
-        {"d2c", o->vd2c.as<double>(), nullptr}};
+static int named_op(phg_ops o, const char *name, const double **v64, const float **v32,
+                    const unsigned **pk = nullptr) {
+    struct { const char *n; const double *d; const float *f; const unsigned *p; } t[] = {
+        {"idt", o->ML.op.A.val, o->ML.op.a32, o->ML.pk.as<unsigned>()},
+        {"lapl", o->L.op.A.val, o->L.op.a32, o->L.pk.as<unsigned>()},
+        {"jidt", o->MJ.op.A.val, o->MJ.op.a32, o->MJ.pk.as<unsigned>()}, {"d1", o->vd1.as<double>(), nullptr, nullptr},
+        {"d2", o->vd2.as<double>(), nullptr, nullptr}, {"d1c", o->vd1c.as<double>(), nullptr, nullptr},
+        {"d2c", o->vd2c.as<double>(), nullptr, nullptr}};
     for (auto &e : t)
-        if (name && !strcmp(name, e.n)) { *v64 = e.d; *v32 = e.f; return PHG_OK; }
+        if (name && !strcmp(name, e.n)) {
+            *v64 = e.d; *v32 = e.f;
+            if (pk) *pk = e.p;
+            return PHG_OK;
+        }
     return fail(PHG_ERR_ARG, "unknown operator '%s'", name ? name : "(null)");
 }
 
@@ -1036,11 +1070,14 @@ extern "C" int phg_ops_mult32(phg_ops o, const char *name, float *y, const float
     if (!is_device_ptr(x) || !is_device_ptr(y)) return fail(PHG_ERR_ARG, "device pointers only");
     if (nv < 4 || nv > 256 || nv % 4 || ((nv / 4) & (nv / 4 - 1)) || ((uintptr_t)x & 15) || ((uintptr_t)y & 15))
         return fail(PHG_ERR_ARG, "nv must be 4 times a power of two, at most 256, and x, y 16-byte aligned");
-    const double *v64; const float *v32;
-    int r = named_op(o, name, &v64, &v32);
+    const double *v64; const float *v32; const unsigned *pk = nullptr;
+    int r = named_op(o, name, &v64, &v32, &pk);
     if (r) return r;
     if (!v32) return fail(PHG_ERR_ARG, "no FP32 copy of '%s'", name);
-    CK(spmm_il32(o->pcol.as<int>(), v32, o->rs, o->W, x, y, nv, o->str(stream)));
+    // row records where the operator has them (one matrix stream: 72 % of the HBM copy peak at level 8 x 64
+    // vs 62 % for the slot-major arrays' 14 streams); the same bits either way
+    if (pk) CK(spmm_pk32(pk, o->rs, x, y, nv, o->str(stream)));
+    else CK(spmm_il32(o->pcol.as<int>(), v32, o->rs, o->W, x, y, nv, o->str(stream)));
     return PHG_OK;
 }
 
@@ -1210,6 +1247,7 @@ int tune_solve(phg_ops_s *o, const char *label, const DevSolveOp &op, int nv, cu
 // threads per row of the interleaved FP32 operator apply at nv vectors
 int tune_spmm(phg_ops_s *o, int nv, cudaStream_t s, Report &rep) {
     const float *v32 = o->L.op.a32 ? o->L.op.a32 : o->ML.op.a32;
+    const unsigned *pk = o->L.op.a32 ? o->L.pk.as<unsigned>() : o->ML.pk.as<unsigned>();
     if (!v32 || nv < 4 || nv > 256 || nv % 4 || ((nv / 4) & (nv / 4 - 1))) return PHG_OK;
     const int q4 = nv / 4;
     const size_t len = (size_t)o->rs * nv;
@@ -1222,7 +1260,8 @@ int tune_spmm(phg_ops_s *o, int nv, cudaStream_t s, Report &rep) {
         if (q4 / tpr > 8) continue;
         float ms = 0.f;
         int r = time_best(s, 5, [&]() -> int {
-            CK(spmm_il32(o->pcol.as<int>(), v32, o->rs, o->W, x.as<float>(), y.as<float>(), nv, s, tpr));
+            if (pk) CK(spmm_pk32(pk, o->rs, x.as<float>(), y.as<float>(), nv, s, tpr));
+            else CK(spmm_il32(o->pcol.as<int>(), v32, o->rs, o->W, x.as<float>(), y.as<float>(), nv, s, tpr));
             return PHG_OK;
         }, &ms);
         if (r) return r;

@@ -77,6 +77,9 @@ struct DevSolveOp {
     // set, the solver runs Chebyshev iterations inside the FP64 refinement
     // loop instead of GMRES -- no inner products, one group barrier per step.
     double cheb_lmin = 0.0, cheb_lmax = 0.0;
+    // FP32 row records of A (8 (column, value) pairs per row, padding (i, 0)):
+    // one sequential matrix stream for the lockstep kernels; null if absent
+    const uint4 *pk32 = nullptr;
 };
 
 // rs x os boundary columns in CSR over rows (few nonzero rows).

@@ -1208,6 +1208,41 @@ __global__ void __launch_bounds__(256) k_ls_step(const int *__restrict__ col, co
     ep[idx] = make_float4(e.x + dn.x, e.y + dn.y, e.z + dn.z, e.w + dn.w);
 }
 
+// k_ls_step reading A from the 64-byte row records (one matrix stream)
+__global__ void __launch_bounds__(256) k_ls_step_pk(const uint4 *__restrict__ pk, const float *__restrict__ dinv,
+                                                    int n, int q4, const float4 *__restrict__ ec,
+                                                    const float4 *__restrict__ rv, float4 *ep, float ca, float cb,
+                                                    const int *done) {
+    if (*(volatile const int *)done) return;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = (int)(t / (unsigned)q4), q = (int)(t - (unsigned)i * (unsigned)q4);
+    if (i >= n) return;
+    int c[8];
+    float a[8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint4 e = __ldg(&pk[(size_t)i * 4 + k]);
+        c[2 * k] = (int)e.x; a[2 * k] = __uint_as_float(e.y);
+        c[2 * k + 1] = (int)e.z; a[2 * k + 1] = __uint_as_float(e.w);
+    }
+    float4 g[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) g[k] = ec[(size_t)c[k] * q4 + q];
+    float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        sum.x = fmaf(a[k], g[k].x, sum.x); sum.y = fmaf(a[k], g[k].y, sum.y);
+        sum.z = fmaf(a[k], g[k].z, sum.z); sum.w = fmaf(a[k], g[k].w, sum.w);
+    }
+    const size_t idx = (size_t)i * q4 + q;
+    const float di = cb * __ldg(&dinv[i]);
+    const float4 r = rv[idx], e = ec[idx], eo = ep[idx];
+    float4 dn;
+    dn.x = ca * (e.x - eo.x) + di * (r.x - sum.x); dn.y = ca * (e.y - eo.y) + di * (r.y - sum.y);
+    dn.z = ca * (e.z - eo.z) + di * (r.z - sum.z); dn.w = ca * (e.w - eo.w) + di * (r.w - sum.w);
+    ep[idx] = make_float4(e.x + dn.x, e.y + dn.y, e.z + dn.z, e.w + dn.w);
+}
+
 // x += beta * e: interleaved FP32 -> member-major FP64 (tiled transpose)
 __global__ void __launch_bounds__(256) k_ls_update(double *X, int ld, int n, int nv, int nvp,
                                                    const double *__restrict__ beta, const float *__restrict__ e,
@@ -1231,9 +1266,14 @@ cudaError_t ls_steps(const DevSolveOp &op, int n, int q4, float *&ec, float *&ep
                      const double *ca, const double *cb, int K, const int *done, cudaStream_t s) {
     const long long work = (long long)n * q4;
     const unsigned blocks = (unsigned)((work + 255) / 256);
+    const bool pk = op.pk32 != nullptr;   // row records: one matrix stream (ensemble steps -0.6 %)
     for (int k = 1; k < K; ++k) {
-        k_ls_step<W><<<blocks, 256, 0, s>>>(op.A.col, op.a32, op.dinv32, n, q4, (const float4 *)ec,
-                                            (const float4 *)rv, (float4 *)ep, (float)ca[k], (float)cb[k], done);
+        if (pk)
+            k_ls_step_pk<<<blocks, 256, 0, s>>>(op.pk32, op.dinv32, n, q4, (const float4 *)ec, (const float4 *)rv,
+                                                (float4 *)ep, (float)ca[k], (float)cb[k], done);
+        else
+            k_ls_step<W><<<blocks, 256, 0, s>>>(op.A.col, op.a32, op.dinv32, n, q4, (const float4 *)ec,
+                                                (const float4 *)rv, (float4 *)ep, (float)ca[k], (float)cb[k], done);
         float *t = ec; ec = ep; ep = t;   // e_{k+1} is in the old e_{k-1} buffer
     }
     return cudaGetLastError();

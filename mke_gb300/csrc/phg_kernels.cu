@@ -759,6 +759,42 @@ cudaError_t launch_il(const int *col, const float *val, int n, const float4 *x, 
     return cudaGetLastError();
 }
 
+// Y = A X as k_spmm_il, with each row's eight (column, value) pairs in one
+// 64-byte record (pk[8 i + k]; padding slots (i, 0) add an exact zero): the
+// matrix is one sequential stream instead of one per slot for the columns and
+// one per slot for the values
+template <int CH>
+__global__ void __launch_bounds__(TB) k_spmm_pk(const uint4 *__restrict__ pk, int n, const float4 *__restrict__ x,
+                                                float4 *__restrict__ y, int q4, int tpr_log2) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;   // n * q4 / CH < 2^31 (host check)
+    const int i = (int)(t >> tpr_log2), q = (int)(t & ((1u << tpr_log2) - 1u));
+    if (i >= n) return;
+    const int tpr = 1 << tpr_log2;
+    int c[8];
+    float a[8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint4 e = __ldg(&pk[(size_t)i * 4 + k]);
+        c[2 * k] = (int)e.x; a[2 * k] = __uint_as_float(e.y);
+        c[2 * k + 1] = (int)e.z; a[2 * k + 1] = __uint_as_float(e.w);
+    }
+    float4 g[CH][8];
+#pragma unroll
+    for (int j = 0; j < CH; ++j)
+#pragma unroll
+        for (int k = 0; k < 8; ++k) g[j][k] = __ldg(&x[(size_t)c[k] * q4 + q + j * tpr]);
+#pragma unroll
+    for (int j = 0; j < CH; ++j) {
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            s.x = __fmaf_rn(a[k], g[j][k].x, s.x); s.y = __fmaf_rn(a[k], g[j][k].y, s.y);
+            s.z = __fmaf_rn(a[k], g[j][k].z, s.z); s.w = __fmaf_rn(a[k], g[j][k].w, s.w);
+        }
+        y[(size_t)i * q4 + q + j * tpr] = s;
+    }
+}
+
 }  // namespace
 
 template <typename T>
@@ -774,6 +810,30 @@ template cudaError_t spmm<double>(const int *, const double *, int, int, const d
                                   cudaStream_t);
 template cudaError_t spmm<float>(const int *, const float *, int, int, const float *, int, float *, int, int,
                                  cudaStream_t);
+
+cudaError_t spmm_pk32(const unsigned *pk, int n, const float *x, float *y, int nv, cudaStream_t s, int tpr) {
+    if (n < 1 || nv < 4 || nv % 4 || ((uintptr_t)x & 15) || ((uintptr_t)y & 15) || ((uintptr_t)pk & 15))
+        return cudaErrorInvalidValue;
+    const int q4 = nv / 4;
+    if (tpr <= 0) tune_get_spmm(n, nv, &tpr);
+    if (tpr <= 0 || tpr > q4 || q4 % tpr || q4 / tpr > 8) tpr = q4 < 8 ? q4 : 8;
+    int lg = 0;
+    while ((1 << lg) < tpr) ++lg;
+    if ((1 << lg) != tpr) return cudaErrorInvalidValue;
+    const long long work = (long long)n * tpr;
+    if (work >= (1LL << 31)) return cudaErrorInvalidValue;
+    const unsigned blocks = (unsigned)((work + TB - 1) / TB);
+    const uint4 *p4 = (const uint4 *)pk;
+    switch (q4 / tpr) {
+    case 1: k_spmm_pk<1><<<blocks, TB, 0, s>>>(p4, n, (const float4 *)x, (float4 *)y, q4, lg); break;
+    case 2: k_spmm_pk<2><<<blocks, TB, 0, s>>>(p4, n, (const float4 *)x, (float4 *)y, q4, lg); break;
+    case 4: k_spmm_pk<4><<<blocks, TB, 0, s>>>(p4, n, (const float4 *)x, (float4 *)y, q4, lg); break;
+    case 8: k_spmm_pk<8><<<blocks, TB, 0, s>>>(p4, n, (const float4 *)x, (float4 *)y, q4, lg); break;
+    default: return cudaErrorInvalidValue;
+    }
+    g_kernel_launches++;
+    return cudaGetLastError();
+}
 
 cudaError_t spmm_il32(const int *col, const float *val, int n, int W, const float *x, float *y, int nv,
                       cudaStream_t s, int tpr) {

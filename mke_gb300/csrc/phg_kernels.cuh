@@ -57,6 +57,8 @@ cudaError_t spmm(const int *col, const T *val, int n, int W, const T *x, int ldx
 // in 1..8; 0 = the tuned value, else 8)
 cudaError_t spmm_il32(const int *col, const float *val, int n, int W, const float *x, float *y, int nv,
                       cudaStream_t s, int tpr = 0);
+// the same product from 64-byte row records (8 (column, value) pairs per row)
+cudaError_t spmm_pk32(const unsigned *pk, int n, const float *x, float *y, int nv, cudaStream_t s, int tpr = 0);
 // deterministic test data: x[i] = a hash of (i, seed) in [-1, 1)
 cudaError_t fill_hash(double *x, long long n, unsigned seed, cudaStream_t s);
 cudaError_t fill_hash32(float *x, long long n, unsigned seed, cudaStream_t s);

@@ -120,3 +120,17 @@ def test_handles_of_one_level_share_data():
     del a
     gc.collect()
     assert b.csr("lapl")[0].size == pb.size  # b's data survives a's destruction
+
+
+def test_live_level_written_when_directory_set_later(tmp_path):
+    phelm.cache_dir(None)
+    keep = phelm.Mesh.sphere(3)              # alive while the directory is set
+    phelm.cache_dir(str(tmp_path))
+    try:
+        other = phelm.Mesh.sphere(3)         # shares keep's data and writes the file
+        assert (tmp_path / "phelm_level3.cache").exists()
+        del other
+    finally:
+        phelm.cache_dir(None)
+    del keep
+    gc.collect()
