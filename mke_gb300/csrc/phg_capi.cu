@@ -2298,7 +2298,7 @@ extern "C" int phg_laplace_calc2_noalloc(phg_ops o, double *ans, const double *F
     if (need > NOALLOC_BYTES)
         return fail(PHG_ERR_ARG,
                     "phg_laplace_calc2_noalloc needs %zu bytes of scratch for %d inner points at restart %d; "
-                    "it holds %zu (16 MiB: up to level 6 at restart 30 in FP64)",
+                    "it holds %zu (16 MiB: a Chebyshev mass solve up to level 7 in FP64)",
                     need, o->rs, o->restart, NOALLOC_BYTES);
     unsigned char *base = nullptr;
     int r = noalloc_scratch(o->dev, &base);

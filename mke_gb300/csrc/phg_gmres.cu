@@ -62,7 +62,8 @@ struct Params {
     double *X;
     int n, nv, ld, m, max_iter;
     double tol;
-    void *V;          // nv x (m+1) x n (VT)
+    void *V;          // nv x vstride (VT): m + 1 Krylov vectors, or 4 Chebyshev vectors
+    size_t vstride;   // elements of V per right-hand side
     void *Z;          // nv x m x n (VT), multigrid path only
     void *Wv;         // nv x n (VT)
     double *R;        // nv x n (FP64 residual)
@@ -888,7 +889,7 @@ __global__ void __launch_bounds__(BLOCK, 2) cheb_kernel(const Params p) {
     for (int v = grp; v < nv; v += groups) {
         const double *__restrict__ b = Bp + (size_t)v * ld;
         double *x = Xp + (size_t)v * ld;
-        VT *rv = Vp + (size_t)v * (p.m + 1) * n;
+        VT *rv = Vp + (size_t)v * p.vstride;
         VT *d = rv + n, *e0 = d + n, *e1 = e0 + n;
         double *R = Rp + (size_t)v * n;
         {
@@ -997,14 +998,31 @@ size_t block_group_elems(const DevSolveOp &op) {
     return 2 * op.mg.group_elems + 4 * (size_t)(op.A.n / 4);
 }
 
+// whether gmres_solve runs op's solves as Chebyshev iterations (the same test)
+bool uses_cheb(const DevSolveOp &op, int m) {
+    return op.cheb_lmax > 0.0 && op.cheb_lmin > 0.0 && op.cheb_lmin < op.cheb_lmax && m >= 3 && !op.mgd &&
+           !op.block4 && op.A.W <= 8;
+}
+
 Layout layout(const DevSolveOp &op, int nv, int m, Precision prec) {
     Layout L;
     const int n = op.A.n;
     size_t es = prec == PREC_MIXED ? 4 : 8;
     auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
     const bool mg = op.mgd != nullptr;
+    // per right-hand side: the m + 1 Krylov vectors of GMRES, or the four
+    // vectors of a Chebyshev solve (rv, d, e_k, e_k+1); the lockstep Chebyshev
+    // path needs three interleaved FP32 vectors and the norm partials instead
+    size_t vregion = es * (size_t)nv * (m + 1) * n;
+    if (uses_cheb(op, m)) {
+        vregion = es * (size_t)nv * 4 * n;
+        if (prec == PREC_MIXED) {
+            const size_t nvp = (size_t)(nv + 31) / 32 * 32, nbx = ((size_t)n + 255) / 256;
+            vregion = std::max(vregion, 3 * al(4 * (size_t)n * nvp) + 16 * (size_t)nv * nbx);
+        }
+    }
     L.v = 0;
-    L.z = L.v + al(es * (size_t)nv * (m + 1) * n);
+    L.z = L.v + al(vregion);
     L.w = L.z + (mg ? al(es * (size_t)nv * m * n) : 0);
     L.r = L.w + al(es * (size_t)nv * n);
     L.mg = L.r + al(8 * (size_t)nv * n);
@@ -2175,8 +2193,7 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     const int n = op.A.n;
     Params p;
     const size_t es = prec == PREC_MIXED ? 4 : 8;
-    const bool cheb = op.cheb_lmax > 0.0 && op.cheb_lmin > 0.0 && op.cheb_lmin < op.cheb_lmax && m >= 3 &&
-                      !op.mgd && !op.block4 && op.A.W <= 8;
+    const bool cheb = uses_cheb(op, m);
     SolveShape sh;
     if (shape) sh = *shape;
     else tune_get_solve(solve_family(op), n, prec, nv, &sh);
@@ -2230,6 +2247,7 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     char *w = (char *)work;
     p.op = op; p.B = B; p.X = X; p.n = n; p.nv = nv; p.ld = ld; p.m = m; p.max_iter = max_iter; p.tol = tol;
     p.V = w + L.v; p.Z = w + L.z; p.Wv = w + L.w; p.R = (double *)(w + L.r);
+    p.vstride = (size_t)(cheb ? 4 : m + 1) * n;
     p.mgbuf = w + L.mg;
     p.group_elems = block_group_elems(op);
     {

@@ -50,11 +50,15 @@ def test_laplace_calc2_noalloc_refusals():
     assert rc == phelm.PhgError(1, "").code and "device pointers" in L.phg_last_error().decode()
 
 
-def test_laplace_calc2_noalloc_rejects_oversize():
+def test_laplace_calc2_noalloc_rejects_oversize(monkeypatch):
+    """A mass solve by GMRES(48) at level 6 needs more than the 16 MiB scratch
+    (with the default Chebyshev solve the same call fits: four vectors)."""
     import torch
     L = phelm.lib()
     m = phelm.Mesh.sphere(6)
+    monkeypatch.setenv("PHG_CHEB", "0")        # read when the operators are built
     ops = phelm.Operators(m, phelm.PHG_FP64, restart=48)
+    monkeypatch.delenv("PHG_CHEB")
     dF = torch.zeros(m.size, dtype=torch.float64, device="cuda")
     out = torch.zeros(m.inner_size, dtype=torch.float64, device="cuda")
     rc = L.phg_laplace_calc2_noalloc(ops._h, C.c_void_p(out.data_ptr()), C.c_void_p(dF.data_ptr()), None)
