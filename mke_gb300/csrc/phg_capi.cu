@@ -1179,11 +1179,12 @@ int tune_solve(phg_ops_s *o, const char *label, const DevSolveOp &op, int nv, cu
     CK(xs.ensure(8 * len)); CK(b.ensure(8 * len)); CK(x.ensure(8 * len)); CK(st.ensure(sizeof(GmresStats)));
     CK(fill_hash(xs.as<double>(), (long long)len, 12345u + (unsigned)nv, s));
     CK(apply_op(op.A, DevCols(), xs.as<double>(), n, nullptr, nullptr, 0, nullptr, b.as<double>(), n, nv, s));
-    const size_t need = gmres_work_bytes(op, nv, o->restart, pr);
-    if (need > o->work.n) { CK(cudaStreamSynchronize(s)); CK(o->work.ensure(need)); }
     std::vector<SolveShape> cand;
     for (int rpb : {128, 256, 512, 1024}) { SolveShape c; c.rpb = rpb; c.path = 0; cand.push_back(c); }
     if ((fam == 1 || fam == 2) && pr == PREC_MIXED && nv >= 8) { SolveShape c; c.rpb = 0; c.path = 1; cand.push_back(c); }
+    size_t need = 0;   // the largest workspace among the candidates' paths
+    for (const SolveShape &c : cand) need = std::max(need, gmres_work_bytes(op, nv, o->restart, pr, &c));
+    if (need > o->work.n) { CK(cudaStreamSynchronize(s)); CK(o->work.ensure(need)); }
     float best = 1e30f;
     SolveShape pick;
     bool any = false;

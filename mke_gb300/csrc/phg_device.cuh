@@ -108,7 +108,7 @@ struct GmresStats {
 // residual b - A x of every restart in FP64 (iterative refinement).
 // `work` must hold gmres_work_bytes(...) bytes; `stats_dev` receives a
 // GmresStats on the device.
-size_t gmres_work_bytes(const DevSolveOp &op, int nv, int m, Precision p);
+
 
 // Launch shape of a solve.  rpb: rows per block of the persistent kernels
 // (no block gets fewer rows; 0 = 256).  path, for Chebyshev-solvable
@@ -131,6 +131,14 @@ void tune_clear();
 std::string tune_describe();
 int tune_save(const char *path);
 int tune_load(const char *path);
+
+// launch paths of a solve: per-member persistent kernels, or lockstep
+// launches over all right-hand sides (Chebyshev / multigrid FGMRES)
+enum class SolvePath { Persistent, ChebLockstep, MgLockstep };
+SolvePath choose_path(const DevSolveOp &op, int nv, int m, Precision prec, bool no_alloc, const SolveShape *shape,
+                      SolveShape *sh_out);
+// workspace bytes of the path a solve with this shape (null = tuned/default) takes
+size_t gmres_work_bytes(const DevSolveOp &op, int nv, int m, Precision p, const SolveShape *shape = nullptr);
 // no_alloc: never allocate (the optional debug phase timers stay off)
 // max_sms: use at most this many SMs' worth of co-resident blocks (0 = all);
 // callers that run several persistent launches at once partition the SMs

@@ -2179,10 +2179,33 @@ static cudaError_t allow_smem(Precision prec) {
     return err[k];
 }
 
-size_t gmres_work_bytes(const DevSolveOp &op, int nv, int m, Precision p) {
-    size_t t = layout(op, nv, m, p).total;
-    if (lsg_applicable(op, nv, p, m)) t = std::max(t, lsg_layout(op, nv, m).total);
-    return t;
+// The launch path gmres_solve takes for these right-hand sides: the shape
+// (given, else the tuned one; environment overrides) decides between the
+// persistent kernels and the lockstep launches.  sh_out: the shape used.
+SolvePath choose_path(const DevSolveOp &op, int nv, int m, Precision prec, bool no_alloc, const SolveShape *shape,
+                      SolveShape *sh_out) {
+    SolveShape sh;
+    if (shape) sh = *shape;
+    else tune_get_solve(solve_family(op), op.A.n, prec, nv, &sh);
+    if (getenv("PHG_ROWS_PER_BLOCK")) sh.rpb = env_int("PHG_ROWS_PER_BLOCK", 256);
+    if (getenv("PHG_CHEB_LOCKSTEP") && !env_int("PHG_CHEB_LOCKSTEP", 1)) sh.path = 0;
+    if (sh_out) *sh_out = sh;
+    if (no_alloc) return SolvePath::Persistent;
+    if (uses_cheb(op, m)) {
+        const bool ls = sh.path == 1 ? nv >= LS_MIN_TUNED : (sh.path == 0 ? false : nv >= LS_MIN_RHS);
+        return prec == PREC_MIXED && ls ? SolvePath::ChebLockstep : SolvePath::Persistent;
+    }
+    if (lsg_applicable(op, nv, prec, m) &&
+        (sh.path == 1 || (sh.path == -1 && nv >= LSG_DEFAULT_RHS && op.A.n >= LSG_DEFAULT_ROWS)))
+        return SolvePath::MgLockstep;
+    return SolvePath::Persistent;
+}
+
+// workspace of the path the solve will take (the lockstep multigrid path
+// needs only its own 2m + 1 interleaved vectors; the others the layout above)
+size_t gmres_work_bytes(const DevSolveOp &op, int nv, int m, Precision p, const SolveShape *shape) {
+    if (choose_path(op, nv, m, p, false, shape, nullptr) == SolvePath::MgLockstep) return lsg_layout(op, nv, m).total;
+    return layout(op, nv, m, p).total;
 }
 
 cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv, int ld,
@@ -2195,14 +2218,10 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     const size_t es = prec == PREC_MIXED ? 4 : 8;
     const bool cheb = uses_cheb(op, m);
     SolveShape sh;
-    if (shape) sh = *shape;
-    else tune_get_solve(solve_family(op), n, prec, nv, &sh);
-    if (getenv("PHG_ROWS_PER_BLOCK")) sh.rpb = env_int("PHG_ROWS_PER_BLOCK", 256);
-    if (getenv("PHG_CHEB_LOCKSTEP") && !env_int("PHG_CHEB_LOCKSTEP", 1)) sh.path = 0;
-    const bool lockstep = sh.path == 1 ? nv >= LS_MIN_TUNED : (sh.path == 0 ? false : nv >= LS_MIN_RHS);
+    const SolvePath path = choose_path(op, nv, m, prec, no_alloc, shape, &sh);
+    const bool lockstep = path == SolvePath::ChebLockstep;
     // ensembles of the multigrid Laplacian in the mixed path: lockstep launches
-    if (!cheb && !no_alloc && lsg_applicable(op, nv, prec, m) &&
-        (sh.path == 1 || (sh.path == -1 && nv >= LSG_DEFAULT_RHS && n >= LSG_DEFAULT_ROWS))) {
+    if (path == SolvePath::MgLockstep) {
         const char *ev = getenv("PHG_INNER_RTOL");
         double rowb = 0.0;
         for (int l = 0; l < op.mg.nlev; ++l) {
