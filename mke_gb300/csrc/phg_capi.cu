@@ -138,43 +138,60 @@ struct phg_mesh_s {
 
 namespace {
 
-// generated levels alive in the process, and the optional cache directory
-std::mutex g_level_mu;
-std::map<int, std::weak_ptr<LevelData>> g_levels;
+// generated levels alive in the process (one slot per level: different levels
+// are built concurrently, one level once), and the optional cache directory
+struct LevelSlot {
+    std::mutex mu;
+    std::weak_ptr<LevelData> live;
+};
+std::mutex g_level_mu;   // guards g_levels and g_cache_dir
+std::map<int, std::shared_ptr<LevelSlot>> g_levels;
 std::string g_cache_dir = [] {
     const char *e = getenv("PHG_CACHE_DIR");
     return std::string(e ? e : "");
 }();
 
-std::string cache_path(int level) { return g_cache_dir + "/phelm_level" + std::to_string(level) + ".cache"; }
+std::string cache_path(const std::string &dir, int level) {
+    return dir + "/phelm_level" + std::to_string(level) + ".cache";
+}
+
+// write a level's data to the cache directory (best effort: a missing or
+// read-only directory is not an error)
+void save_level(const std::string &dir, int level, LevelData &d) {
+    d.assemble();
+    std::string mg_err;
+    const MgHierarchy *h = level >= 2 ? d.hierarchy(mg_err) : nullptr;
+    save_level_cache(cache_path(dir, level).c_str(), d.m, d.ops, h);
+}
 
 // the shared data of a generated level: a live one, else the disk cache, else
 // generate (and, with a cache directory, assemble everything and save it)
 int level_data(int level, std::shared_ptr<LevelData> &out) {
-    std::lock_guard<std::mutex> g(g_level_mu);
-    auto it = g_levels.find(level);
-    if (it != g_levels.end())
-        if ((out = it->second.lock())) {
-            // a live level and a cache directory without its file (the
-            // directory was set after the level was built): write it now
-            if (!g_cache_dir.empty()) {
-                const std::string path = cache_path(level);
-                if (FILE *f = fopen(path.c_str(), "rb")) fclose(f);
-                else {
-                    out->assemble();
-                    std::string mg_err;
-                    const MgHierarchy *h = level >= 2 ? out->hierarchy(mg_err) : nullptr;
-                    save_level_cache(path.c_str(), out->m, out->ops, h);
-                }
-            }
-            return PHG_OK;
+    std::shared_ptr<LevelSlot> slot;
+    std::string dir;
+    {
+        std::lock_guard<std::mutex> g(g_level_mu);
+        std::shared_ptr<LevelSlot> &e = g_levels[level];
+        if (!e) e = std::make_shared<LevelSlot>();
+        slot = e;
+        dir = g_cache_dir;
+    }
+    std::lock_guard<std::mutex> g(slot->mu);   // one level is built once; other levels proceed
+    if ((out = slot->live.lock())) {
+        // a live level and a cache directory without its file (the directory
+        // was set after the level was built): write it now
+        if (!dir.empty()) {
+            if (FILE *f = fopen(cache_path(dir, level).c_str(), "rb")) fclose(f);
+            else save_level(dir, level, *out);
         }
+        return PHG_OK;
+    }
     auto d = std::make_shared<LevelData>();
     std::string err;
     bool loaded = false;
-    if (!g_cache_dir.empty()) {
+    if (!dir.empty()) {
         bool has_mg = false;
-        if (load_level_cache(cache_path(level).c_str(), level, d->m, d->ops, d->mg, has_mg, err)) {
+        if (load_level_cache(cache_path(dir, level).c_str(), level, d->m, d->ops, d->mg, has_mg, err)) {
             loaded = true;
             d->ops_ready = true;
             d->mg_ready = has_mg;
@@ -182,14 +199,9 @@ int level_data(int level, std::shared_ptr<LevelData> &out) {
     }
     if (!loaded) {
         if (!generate_sphere(level, d->m, err)) return fail(PHG_ERR_ARG, "%s", err.c_str());
-        if (!g_cache_dir.empty()) {
-            d->assemble();
-            std::string mg_err;
-            const MgHierarchy *h = level >= 2 ? d->hierarchy(mg_err) : nullptr;
-            save_level_cache(cache_path(level).c_str(), d->m, d->ops, h);   // best effort: a read-only dir is fine
-        }
+        if (!dir.empty()) save_level(dir, level, *d);
     }
-    g_levels[level] = d;
+    slot->live = d;
     out = std::move(d);
     return PHG_OK;
 }

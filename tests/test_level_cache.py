@@ -134,3 +134,32 @@ def test_live_level_written_when_directory_set_later(tmp_path):
         phelm.cache_dir(None)
     del keep
     gc.collect()
+
+
+def test_concurrent_generation():
+    """Different levels build concurrently and one level once; every handle
+    equals a serially built one (ctypes releases the GIL during the calls)."""
+    import threading
+    phelm.cache_dir(None)
+    ref = {lv: snapshot(lv) for lv in (2, 3, 4)}
+    got = {}
+    errors = []
+
+    def work(lv, k):
+        try:
+            m = phelm.Mesh.sphere(lv)
+            p, c, v = m.csr("lapl")
+            got[(lv, k)] = (m.arrays()["xyz"].copy(), p.copy(), c.copy(), v.copy())
+        except Exception as e:   # reported below
+            errors.append(repr(e))
+
+    threads = [threading.Thread(target=work, args=(lv, k)) for lv in (2, 3, 4) for k in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(120)
+    assert not errors, errors
+    for (lv, k), (xyz, p, c, v) in got.items():
+        assert np.array_equal(xyz, ref[lv]["xyz"])
+        assert all(np.array_equal(a, b) for a, b in zip((p, c, v), ref[lv]["lapl"]))
+    gc.collect()
