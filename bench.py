@@ -249,7 +249,7 @@ def run_ours(args, ws, rank, local):
                 bv.calc(uh, zh, zh, out=out)
                 uh, out = out, uh
             e2e = time.perf_counter() - t1
-            # host arrays through the captured step: copy in, replay, copy back, judge
+            # host arrays through the captured step: copy in, replay, copy back, check
             ug = psi0.copy()
             bv.run(ug, 2, zh, zh)   # captures for the staged host arguments
             t1 = time.perf_counter()

@@ -176,7 +176,7 @@ int phg_tune_save(const char *path);
 int phg_tune_load(const char *path, int *entries);
 void phg_tune_clear(void);
 
-/* Synchronise `stream` and judge the solves enqueued on this handle since the
+/* Synchronise `stream` and check the solves enqueued on this handle since the
  * last check (calls with device pointers do not wait for their solves):
  * PHG_ERR_NOT_CONVERGED / PHG_ERR_TIMEOUT as a host-pointer call would
  * return.  No reference counterpart (the reference's calls are synchronous). */
@@ -266,8 +266,8 @@ int phg_barvortex_calc_batch(phg_barvortex b, int nmembers, double *u1, const do
  * reallocated since (otherwise the first step of the call is enqueued kernel
  * by kernel and the next one re-captured).  Results equal nsteps
  * phg_barvortex_calc_batch calls bit for bit.  With host arrays the call
- * returns after the copy back and judges every solve of every step; with
- * device arrays it returns at once, and phg_barvortex_last_stats judges every
+ * returns after the copy back and checks every solve of every step; with
+ * device arrays it returns at once, and phg_barvortex_last_stats checks every
  * step run since the previous check.  stream: a created stream or NULL (the
  * handle's own), not the legacy default stream. */
 int phg_barvortex_run(phg_barvortex b, int nmembers, int nsteps, double *u, const double *bnd_u,

@@ -820,7 +820,7 @@ int solve(phg_ops_s *o, const DevSolveOp &op, const double *B, double *X, int nv
 // maximum that keeps a NaN (std::max drops one on the right)
 double max_keep_nan(double a, double b) { return a != a ? a : (b != b ? b : std::max(a, b)); }
 
-// read back and judge the stats of slots [0, nslots)
+// read back and check the stats of slots [0, nslots)
 int check_stats(phg_ops_s *o, int nslots, cudaStream_t s, GmresStats *agg = nullptr, GmresStats *each = nullptr) {
     std::vector<GmresStats> st(nslots);
     CK(cudaMemcpyAsync(st.data(), o->stats.p, sizeof(GmresStats) * nslots, cudaMemcpyDeviceToHost, s));
@@ -1588,7 +1588,7 @@ extern "C" int phg_barvortex_calc_batch(phg_barvortex b, int nmembers, double *u
     return bv_calc(b, nmembers, u1, u, bnd_u, bnd_w, forcing, stream);
 }
 
-// judge the solves folded into b->agg since the last check
+// check the solves folded into b->agg since the last check
 static int bv_check_agg(phg_barvortex_s *b, cudaStream_t s) {
     GmresStats a{};
     CK(cudaMemcpyAsync(&a, b->agg.p, sizeof a, cudaMemcpyDeviceToHost, s));
@@ -1674,7 +1674,7 @@ static int bv_run(phg_barvortex b, int nv, int nsteps, double *u, const double *
     g_kernel_launches += b->g_launches * left;
     b->last_stream = s;
     CK(st.finish());
-    if (!st.host) return PHG_OK;   // device arguments: judged by phg_barvortex_last_stats
+    if (!st.host) return PHG_OK;   // device arguments: checked by phg_barvortex_last_stats
     r = check_stats(o, b->nslots, s, nullptr, b->each);   // the last step, for phg_barvortex_last_stats
     int r2 = bv_check_agg(b, s);
     return r2 ? r2 : r;
