@@ -42,6 +42,7 @@ extern "C" {
 #define PHG_ERR_TIMEOUT 4       /* a device-side wait ran out (kernel returned early) */
 #define PHG_ERR_IO 5            /* mesh file unreadable or malformed */
 #define PHG_ERR_BUDGET 6        /* serving: the request's lane does not fit in the HBM budget */
+#define PHG_ERR_HOST 7          /* host-side failure: host memory exhausted, a thread not started */
 
 #define PHG_FP64 0   /* every operator, vector and coefficient in double */
 #define PHG_MIXED 1  /* FP32 Krylov vectors and operator inside FP64 iterative refinement */

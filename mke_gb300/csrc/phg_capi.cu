@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/phelm_gb300.h"
+#include "phg_api.hpp"
 #include "phg_host.hpp"
 #include <nvtx3/nvToolsExt.h>
 #include "phg_kernels.cuh"
@@ -30,9 +31,28 @@ int fail(int code, const char *fmt, ...) {
     va_start(ap, fmt);
     vsnprintf(buf, sizeof buf, fmt, ap);
     va_end(ap);
-    g_err = buf;
+    try {
+        g_err = buf;
+    } catch (...) {   // no memory for the message: keep the code
+    }
     return code;
 }
+
+// a FILE closed on every exit, an exception included; close() reports fclose's result
+struct OpenFile {
+    FILE *f;
+    OpenFile(const char *path, const char *mode) : f(fopen(path, mode)) {}
+    ~OpenFile() {
+        if (f) fclose(f);
+    }
+    bool close() {
+        FILE *g = f;
+        f = nullptr;
+        return g && fclose(g) == 0;
+    }
+    OpenFile(const OpenFile &) = delete;
+    OpenFile &operator=(const OpenFile &) = delete;
+};
 
 #define CK(call)                                                                          \
     do {                                                                                  \
@@ -103,6 +123,18 @@ bool is_device_ptr(const void *p) {
 }
 
 }  // namespace
+
+int phg::api_exception() noexcept {
+    try {
+        throw;
+    } catch (const std::bad_alloc &) {
+        return fail(PHG_ERR_HOST, "host memory exhausted");
+    } catch (const std::exception &e) {
+        return fail(PHG_ERR_HOST, "host failure: %s", e.what());
+    } catch (...) {
+        return fail(PHG_ERR_HOST, "host failure");
+    }
+}
 
 // ----------------------------------------------------------------- mesh ---
 // A level's host data -- the mesh, its assembled operators and the multigrid
@@ -209,9 +241,11 @@ int level_data(int level, std::shared_ptr<LevelData> &out) {
 }  // namespace
 
 extern "C" int phg_cache_dir(const char *path) {
+    PHG_API_BEGIN
     std::lock_guard<std::mutex> g(g_level_mu);
     g_cache_dir = path ? path : "";
     return PHG_OK;
+    PHG_API_END
 }
 
 extern "C" const char *phg_last_error(void) { return g_err.c_str(); }
@@ -219,42 +253,48 @@ extern "C" const char *phg_version(void) { return "phelm-gb300 0.1 (sm_103a)"; }
 extern "C" long long phg_kernel_launches(void) { return g_kernel_launches.load(); }
 
 extern "C" int phg_mesh_generate(int level, phg_mesh *out) {
+    PHG_API_BEGIN
     if (!out) return fail(PHG_ERR_ARG, "out is NULL");
     std::shared_ptr<LevelData> d;
     int r = level_data(level, d);
     if (r) return r;
     *out = new phg_mesh_s(std::move(d));
     return PHG_OK;
+    PHG_API_END
 }
 
 extern "C" int phg_mesh_load_file(const char *path, phg_mesh *out) {
+    PHG_API_BEGIN
     if (!path || !out) return fail(PHG_ERR_ARG, "NULL argument");
-    FILE *f = fopen(path, "rb");
-    if (!f) return fail(PHG_ERR_IO, "cannot open %s", path);
+    OpenFile f(path, "rb");
+    if (!f.f) return fail(PHG_ERR_IO, "cannot open %s", path);
     auto d = std::make_shared<LevelData>();   // a loaded mesh keeps its own data
     std::string err;
-    bool ok = load_mesh_text(f, d->m, err);
-    fclose(f);
+    bool ok = load_mesh_text(f.f, d->m, err);
+    f.close();
     if (!ok) return fail(PHG_ERR_IO, "%s: %s", path, err.c_str());
     *out = new phg_mesh_s(std::move(d));
     return PHG_OK;
+    PHG_API_END
 }
 
 static void mesh_release(phg_mesh m) {
     if (m && m->refs.fetch_sub(1) == 1) delete m;
 }
 
-extern "C" void phg_mesh_destroy(phg_mesh m) { mesh_release(m); }
+extern "C" void phg_mesh_destroy(phg_mesh m) { PHG_API_BEGIN mesh_release(m); PHG_API_END_VOID }
 
 extern "C" int phg_mesh_save_file(phg_mesh h, const char *path) {
+    PHG_API_BEGIN
     if (!h || !path) return fail(PHG_ERR_ARG, "NULL argument");
-    FILE *f = fopen(path, "wb");
-    if (!f) return fail(PHG_ERR_IO, "cannot open %s", path);
-    const bool ok = save_mesh_text(f, h->m);
-    const bool closed = fclose(f) == 0;
+    OpenFile f(path, "wb");
+    if (!f.f) return fail(PHG_ERR_IO, "cannot open %s", path);
+    const bool ok = save_mesh_text(f.f, h->m);
+    const bool closed = f.close();
     if (!ok) return fail(PHG_ERR_ARG, "only 4-chart sphere meshes can be written");
     if (!closed) return fail(PHG_ERR_IO, "cannot write %s", path);
     return PHG_OK;
+    PHG_API_END
 }
 
 static int print_common(phg_mesh h, const char *path, const double *ans, const double *x, const double *y,
@@ -262,10 +302,10 @@ static int print_common(phg_mesh h, const char *path, const double *ans, const d
     if (!h || !path || !ans) return fail(PHG_ERR_ARG, "NULL argument");
     if (is_device_ptr(ans) || (x && is_device_ptr(x)) || (y && is_device_ptr(y)) || (z && is_device_ptr(z)))
         return fail(PHG_ERR_ARG, "host arrays only");
-    FILE *f = fopen(path, "wb");
-    if (!f) return fail(PHG_ERR_IO, "cannot open %s", path);
-    print_function_text(f, h->m, ans, x, y, z, inner);
-    if (fclose(f) != 0) return fail(PHG_ERR_IO, "cannot write %s", path);
+    OpenFile f(path, "wb");
+    if (!f.f) return fail(PHG_ERR_IO, "cannot open %s", path);
+    print_function_text(f.f, h->m, ans, x, y, z, inner);
+    if (!f.close()) return fail(PHG_ERR_IO, "cannot write %s", path);
     return PHG_OK;
 }
 
@@ -285,24 +325,29 @@ static unsigned long long mesh_digest(const Mesh &m) {
 
 extern "C" int phg_state_save(phg_mesh h, const char *path, const double *const *fields, int nfields, double t,
                               long long step) {
+    PHG_API_BEGIN
     if (!h || !path || !fields || nfields < 1) return fail(PHG_ERR_ARG, "bad argument");
     for (int k = 0; k < nfields; ++k)
         if (!fields[k] || is_device_ptr(fields[k])) return fail(PHG_ERR_ARG, "field %d: host array required", k);
-    FILE *f = fopen(path, "wb");
+    OpenFile of(path, "wb");
+    FILE *f = of.f;
     if (!f) return fail(PHG_ERR_IO, "cannot open %s", path);
     const int V = h->m.V;
     const unsigned long long dg = mesh_digest(h->m);
     bool ok = fwrite("PHGSTAT1", 1, 8, f) == 8 && fwrite(&V, 4, 1, f) == 1 && fwrite(&nfields, 4, 1, f) == 1 &&
               fwrite(&t, 8, 1, f) == 1 && fwrite(&step, 8, 1, f) == 1 && fwrite(&dg, 8, 1, f) == 1;
     for (int k = 0; ok && k < nfields; ++k) ok = fwrite(fields[k], 8, (size_t)V, f) == (size_t)V;
-    ok = (fclose(f) == 0) && ok;
+    ok = of.close() && ok;
     return ok ? PHG_OK : fail(PHG_ERR_IO, "cannot write %s", path);
+    PHG_API_END
 }
 
 extern "C" int phg_state_load(phg_mesh h, const char *path, double *const *fields, int nfields, double *t,
                               long long *step) {
+    PHG_API_BEGIN
     if (!h || !path || !fields || nfields < 1) return fail(PHG_ERR_ARG, "bad argument");
-    FILE *f = fopen(path, "rb");
+    OpenFile of(path, "rb");
+    FILE *f = of.f;
     if (!f) return fail(PHG_ERR_IO, "cannot open %s", path);
     char magic[8];
     int V = 0, nf = 0;
@@ -312,40 +357,47 @@ extern "C" int phg_state_load(phg_mesh h, const char *path, double *const *field
     bool ok = fread(magic, 1, 8, f) == 8 && !memcmp(magic, "PHGSTAT1", 8) && fread(&V, 4, 1, f) == 1 &&
               fread(&nf, 4, 1, f) == 1 && fread(&tt, 8, 1, f) == 1 && fread(&st, 8, 1, f) == 1 &&
               fread(&dg, 8, 1, f) == 1;
-    if (!ok) { fclose(f); return fail(PHG_ERR_IO, "%s: not a state checkpoint", path); }
-    if (V != h->m.V || dg != mesh_digest(h->m)) { fclose(f); return fail(PHG_ERR_ARG, "%s: written for another mesh", path); }
-    if (nf != nfields) { fclose(f); return fail(PHG_ERR_ARG, "%s: holds %d fields, %d requested", path, nf, nfields); }
+    if (!ok) return fail(PHG_ERR_IO, "%s: not a state checkpoint", path);
+    if (V != h->m.V || dg != mesh_digest(h->m)) return fail(PHG_ERR_ARG, "%s: written for another mesh", path);
+    if (nf != nfields) return fail(PHG_ERR_ARG, "%s: holds %d fields, %d requested", path, nf, nfields);
     for (int k = 0; ok && k < nfields; ++k) {
-        if (!fields[k] || is_device_ptr(fields[k])) { fclose(f); return fail(PHG_ERR_ARG, "field %d: host array required", k); }
+        if (!fields[k] || is_device_ptr(fields[k])) return fail(PHG_ERR_ARG, "field %d: host array required", k);
         ok = fread(fields[k], 8, (size_t)V, f) == (size_t)V;
     }
-    fclose(f);
     if (!ok) return fail(PHG_ERR_IO, "%s: truncated", path);
     if (t) *t = tt;
     if (step) *step = st;
     return PHG_OK;
+    PHG_API_END
 }
 
 extern "C" int phg_print_function(phg_mesh h, const char *path, const double *ans, const double *x, const double *y,
                                   const double *z) {
+    PHG_API_BEGIN
     return print_common(h, path, ans, x, y, z, false);
+    PHG_API_END
 }
 
 extern "C" int phg_print_inner_function(phg_mesh h, const char *path, const double *ans, const double *x,
                                         const double *y, const double *z) {
+    PHG_API_BEGIN
     return print_common(h, path, ans, x, y, z, true);
+    PHG_API_END
 }
 
 extern "C" int phg_mesh_info(phg_mesh h, int *V, int *T, int *rs, int *os) {
+    PHG_API_BEGIN
     if (!h) return fail(PHG_ERR_ARG, "NULL mesh");
     if (V) *V = h->m.V;
     if (T) *T = h->m.T;
     if (rs) *rs = h->m.rs;
     if (os) *os = h->m.os;
     return PHG_OK;
+    PHG_API_END
 }
 
 extern "C" int phg_mesh_arrays(phg_mesh h, double *xyz, double *uv, int *tri, int *tz, int *bnd) {
+    PHG_API_BEGIN
     if (!h) return fail(PHG_ERR_ARG, "NULL mesh");
     const Mesh &m = h->m;
     if (xyz) memcpy(xyz, m.xyz.data(), 8 * m.xyz.size());
@@ -354,15 +406,18 @@ extern "C" int phg_mesh_arrays(phg_mesh h, double *xyz, double *uv, int *tri, in
     if (tz) memcpy(tz, m.tz.data(), 4 * m.tz.size());
     if (bnd) memcpy(bnd, m.bnd.data(), 4 * m.bnd.size());
     return PHG_OK;
+    PHG_API_END
 }
 
 extern "C" int phg_mesh_maps(phg_mesh h, int *inner, int *outer, int *p2io) {
+    PHG_API_BEGIN
     if (!h) return fail(PHG_ERR_ARG, "NULL mesh");
     const Mesh &m = h->m;
     if (inner) memcpy(inner, m.inner.data(), 4 * m.inner.size());
     if (outer) memcpy(outer, m.outer.data(), 4 * m.outer.size());
     if (p2io) memcpy(p2io, m.p2io.data(), 4 * m.p2io.size());
     return PHG_OK;
+    PHG_API_END
 }
 
 static const Csr *find_csr(phg_mesh_s *h, const char *name) {
@@ -377,6 +432,7 @@ static const Csr *find_csr(phg_mesh_s *h, const char *name) {
 }
 
 extern "C" int phg_mesh_csr(phg_mesh h, const char *name, int *n, int *nnz, int *ptr, int *col, double *val) {
+    PHG_API_BEGIN
     if (!h || !name) return fail(PHG_ERR_ARG, "NULL argument");
     h->assemble();
     const Csr *c = find_csr(h, name);
@@ -387,6 +443,7 @@ extern "C" int phg_mesh_csr(phg_mesh h, const char *name, int *n, int *nnz, int 
     if (col) memcpy(col, c->col.data(), 4 * c->col.size());
     if (val) memcpy(val, c->val.data(), 8 * c->val.size());
     return PHG_OK;
+    PHG_API_END
 }
 
 // ------------------------------------------------------- device operators ---
@@ -700,6 +757,7 @@ int build_mg_dev(phg_ops_s *o, phg_mesh_s *mh, SolveOpBufs &Lb, MgBufs &mb, int 
 }  // namespace
 
 extern "C" int phg_ops_create(phg_mesh h, int precision, phg_ops *out) {
+    PHG_API_BEGIN
     if (!h || !out) return fail(PHG_ERR_ARG, "NULL argument");
     if (precision != PHG_FP64 && precision != PHG_MIXED) return fail(PHG_ERR_ARG, "bad precision %d", precision);
     int ndev = 0;
@@ -768,6 +826,7 @@ extern "C" int phg_ops_create(phg_mesh h, int precision, phg_ops *out) {
     h->refs++;
     *out = o.release();
     return PHG_OK;
+    PHG_API_END
 }
 
 static void ops_release(phg_ops o) {
@@ -778,14 +837,16 @@ static void ops_release(phg_ops o) {
     mesh_release(m);
 }
 
-extern "C" void phg_ops_destroy(phg_ops o) { ops_release(o); }
+extern "C" void phg_ops_destroy(phg_ops o) { PHG_API_BEGIN ops_release(o); PHG_API_END_VOID }
 
 extern "C" int phg_ops_set_solver(phg_ops o, int restart, double tol, int max_iter) {
+    PHG_API_BEGIN
     if (!o) return fail(PHG_ERR_ARG, "NULL handle");
     if (restart < 1 || restart > 48) return fail(PHG_ERR_ARG, "restart must be in 1..48");
     if (!(tol > 0) || max_iter < 1) return fail(PHG_ERR_ARG, "bad tolerance / iteration cap");
     o->restart = restart; o->tol = tol; o->max_iter = max_iter;
     return PHG_OK;
+    PHG_API_END
 }
 
 namespace {
@@ -925,20 +986,25 @@ int norm_dev(phg_ops_s *o, const double *u, const double *v, int nv, double *out
 }  // namespace
 
 extern "C" int phg_ops_set_sms(phg_ops o, int max_sms) {
+    PHG_API_BEGIN
     if (!o || max_sms < 0) return fail(PHG_ERR_ARG, "bad argument");
     o->max_sms = max_sms;
     return PHG_OK;
+    PHG_API_END
 }
 
 extern "C" int phg_ops_last_solve(phg_ops o, int *iters, int *cycles, double *relres) {
+    PHG_API_BEGIN
     if (!o) return fail(PHG_ERR_ARG, "NULL handle");
     if (iters) *iters = o->last.iters;
     if (cycles) *cycles = o->last.cycles;
     if (relres) *relres = o->last.relres;
     return PHG_OK;
+    PHG_API_END
 }
 
 extern "C" int phg_ops_profile(phg_ops o, int enable) {
+    PHG_API_BEGIN
     if (!o) return fail(PHG_ERR_ARG, "NULL handle");
     if (enable && o->ev.empty()) {
         o->ev.resize(8192);
@@ -950,9 +1016,11 @@ extern "C" int phg_ops_profile(phg_ops o, int enable) {
     o->prof = enable != 0;
     if (enable) o->nev = 0;
     return PHG_OK;
+    PHG_API_END
 }
 
 extern "C" int phg_ops_profile_read_family(phg_ops o, int family, int *launches, double *ms, double *bytes) {
+    PHG_API_BEGIN
     if (!o) return fail(PHG_ERR_ARG, "NULL handle");
     const int n = o->nev / 2;
     double t = 0.0, b = 0.0;
@@ -974,13 +1042,17 @@ extern "C" int phg_ops_profile_read_family(phg_ops o, int family, int *launches,
     if (ms) *ms = t;
     if (bytes) *bytes = b;
     return PHG_OK;
+    PHG_API_END
 }
 
 extern "C" int phg_ops_profile_read(phg_ops o, int *launches, double *ms, double *bytes) {
+    PHG_API_BEGIN
     return phg_ops_profile_read_family(o, -1, launches, ms, bytes);
+    PHG_API_END
 }
 
 extern "C" int phg_laplace_calc2(phg_ops o, double *ans, const double *F, void *stream) {
+    PHG_API_BEGIN
     if (!o || !ans || !F) return fail(PHG_ERR_ARG, "NULL argument");
     cudaStream_t s = o->str(stream);
     Stage st(o, s);
@@ -990,9 +1062,11 @@ extern "C" int phg_laplace_calc2(phg_ops o, double *ans, const double *F, void *
     if (r) return r;
     CK(st.finish());
     return st.host ? check_stats(o, 1, s) : PHG_OK;
+    PHG_API_END
 }
 
 extern "C" int phg_laplace_calc1(phg_ops o, double *ans, const double *F, const double *bnd, void *stream) {
+    PHG_API_BEGIN
     if (!o || !ans || !F) return fail(PHG_ERR_ARG, "NULL argument");
     cudaStream_t s = o->str(stream);
     Stage st(o, s);
@@ -1004,9 +1078,11 @@ extern "C" int phg_laplace_calc1(phg_ops o, double *ans, const double *F, const 
     CK(p2u(dA, o->V, o->s_c.as<double>(), o->rs, dB, o->os, o->p2io.as<int>(), o->isb.as<int>(), o->V, 1, s));
     CK(st.finish());
     return st.host ? check_stats(o, 1, s) : PHG_OK;
+    PHG_API_END
 }
 
 extern "C" int phg_laplace_solve(phg_ops o, double *ans, const double *F, const double *bnd, void *stream) {
+    PHG_API_BEGIN
     if (!o || !ans || !F) return fail(PHG_ERR_ARG, "NULL argument");
     cudaStream_t s = o->str(stream);
     Stage st(o, s);
@@ -1022,10 +1098,12 @@ extern "C" int phg_laplace_solve(phg_ops o, double *ans, const double *F, const 
     CK(p2u(dA, o->V, x, o->rs, dB, o->os, o->p2io.as<int>(), o->isb.as<int>(), o->V, 1, s));
     CK(st.finish());
     return st.host ? check_stats(o, 1, s) : PHG_OK;
+    PHG_API_END
 }
 
 extern "C" int phg_laplace_solve_batch(phg_ops o, int nv, double *ans, const double *F, const double *bnd,
                                        void *stream) {
+    PHG_API_BEGIN
     if (!o || !ans || !F || nv < 1) return fail(PHG_ERR_ARG, "NULL argument");
     cudaStream_t s = o->str(stream);
     Stage st(o, s);
@@ -1042,6 +1120,7 @@ extern "C" int phg_laplace_solve_batch(phg_ops o, int nv, double *ans, const dou
     CK(p2u(dA, V, x, rs, dB, os, o->p2io.as<int>(), o->isb.as<int>(), V, nv, s));
     CK(st.finish());
     return st.host ? check_stats(o, 1, s) : PHG_OK;
+    PHG_API_END
 }
 
 // the handle's copy of a named inner x inner operator (FP64 values, and the
@@ -1064,6 +1143,7 @@ static int named_op(phg_ops o, const char *name, const double **v64, const float
 }
 
 extern "C" int phg_ops_mult(phg_ops o, const char *name, double *y, const double *x, int nv, void *stream) {
+    PHG_API_BEGIN
     if (!o || !y || !x || nv < 1) return fail(PHG_ERR_ARG, "NULL argument");
     const double *v64; const float *v32;
     int r = named_op(o, name, &v64, &v32);
@@ -1075,9 +1155,11 @@ extern "C" int phg_ops_mult(phg_ops o, const char *name, double *y, const double
     CK(spmm<double>(o->pcol.as<int>(), v64, o->rs, o->W, dx, o->rs, dy, o->rs, nv, s));
     CK(st.finish());
     return PHG_OK;
+    PHG_API_END
 }
 
 extern "C" int phg_ops_mult32(phg_ops o, const char *name, float *y, const float *x, int nv, void *stream) {
+    PHG_API_BEGIN
     if (!o || !y || !x || nv < 1) return fail(PHG_ERR_ARG, "NULL argument");
     if (!is_device_ptr(x) || !is_device_ptr(y)) return fail(PHG_ERR_ARG, "device pointers only");
     if (nv < 4 || nv > 256 || nv % 4 || ((nv / 4) & (nv / 4 - 1)) || ((uintptr_t)x & 15) || ((uintptr_t)y & 15))
@@ -1091,10 +1173,12 @@ extern "C" int phg_ops_mult32(phg_ops o, const char *name, float *y, const float
     if (pk) CK(spmm_pk32(pk, o->rs, x, y, nv, o->str(stream)));
     else CK(spmm_il32(o->pcol.as<int>(), v32, o->rs, o->W, x, y, nv, o->str(stream)));
     return PHG_OK;
+    PHG_API_END
 }
 
 // --------------------------------------------------------- validation ---
 extern "C" int phg_ops_validate(phg_ops o, long long *bad_entries, void *stream) {
+    PHG_API_BEGIN
     if (!o || !bad_entries) return fail(PHG_ERR_ARG, "NULL argument");
     cudaStream_t s = o->str(stream);
     DBuf cnt;
@@ -1135,6 +1219,7 @@ extern "C" int phg_ops_validate(phg_ops o, long long *bad_entries, void *stream)
     CK(cudaStreamSynchronize(s));
     *bad_entries = (long long)h;
     return PHG_OK;
+    PHG_API_END
 }
 
 // ------------------------------------------------------------- autotuner ---
@@ -1298,6 +1383,7 @@ void copy_out(const std::string &t, char *buf, int len) {
 }  // namespace
 
 extern "C" int phg_ops_autotune(phg_ops o, int nmembers, char *report, int report_len, void *stream) {
+    PHG_API_BEGIN
     if (!o || nmembers < 1) return fail(PHG_ERR_ARG, "bad argument");
     cudaStream_t s = o->str(stream);
     Report rep;
@@ -1313,34 +1399,44 @@ extern "C" int phg_ops_autotune(phg_ops o, int nmembers, char *report, int repor
     g_alloc_epoch++;   // captured steps pick up the new shapes
     copy_out(rep.text, report, report_len);
     return PHG_OK;
+    PHG_API_END
 }
 
 extern "C" int phg_tune_describe(char *buf, int len) {
+    PHG_API_BEGIN
     if (!buf || len <= 0) return fail(PHG_ERR_ARG, "bad argument");
     copy_out(tune_describe(), buf, len);
     return PHG_OK;
+    PHG_API_END
 }
 
 extern "C" int phg_tune_save(const char *path) {
+    PHG_API_BEGIN
     if (!path) return fail(PHG_ERR_ARG, "NULL path");
     return tune_save(path) ? fail(PHG_ERR_IO, "cannot write %s", path) : PHG_OK;
+    PHG_API_END
 }
 
 extern "C" int phg_tune_load(const char *path, int *entries) {
+    PHG_API_BEGIN
     if (!path) return fail(PHG_ERR_ARG, "NULL path");
     const int k = tune_load(path);
     g_alloc_epoch++;   // captured steps pick up the new shapes
     if (k < 0) return fail(PHG_ERR_IO, "cannot read %s (missing or malformed)", path);
     if (entries) *entries = k;
     return PHG_OK;
+    PHG_API_END
 }
 
 extern "C" void phg_tune_clear(void) {
+    PHG_API_BEGIN
     tune_clear();
     g_alloc_epoch++;
+    PHG_API_END_VOID
 }
 
 extern "C" int phg_ops_check(phg_ops o, void *stream) {
+    PHG_API_BEGIN
     if (!o) return fail(PHG_ERR_ARG, "NULL handle");
     cudaStream_t s = o->str(stream);
     if (o->pending_slots == 0) {
@@ -1348,12 +1444,15 @@ extern "C" int phg_ops_check(phg_ops o, void *stream) {
         return PHG_OK;
     }
     return check_stats(o, o->pending_slots, s);
+    PHG_API_END
 }
 
 extern "C" int phg_device_bytes(long long *total, long long *this_thread) {
+    PHG_API_BEGIN
     if (total) *total = g_dev_bytes.load();
     if (this_thread) *this_thread = t_dev_bytes;
     return PHG_OK;
+    PHG_API_END
 }
 
 static int jacobian_common(phg_ops o, double *ans, const double *u, const double *v, const double *bnd,
@@ -1377,13 +1476,19 @@ static int jacobian_common(phg_ops o, double *ans, const double *u, const double
 }
 
 extern "C" int phg_jacobian_calc1(phg_ops o, double *ans, const double *u, const double *v, const double *bnd, void *s) {
+    PHG_API_BEGIN
     return jacobian_common(o, ans, u, v, bnd, true, false, s);
+    PHG_API_END
 }
 extern "C" int phg_jacobian_calc2(phg_ops o, double *ans, const double *u, const double *v, void *s) {
+    PHG_API_BEGIN
     return jacobian_common(o, ans, u, v, nullptr, false, false, s);
+    PHG_API_END
 }
 extern "C" int phg_jacobian_calc2t(phg_ops o, double *ans, const double *u, const double *v, void *s) {
+    PHG_API_BEGIN
     return jacobian_common(o, ans, u, v, nullptr, false, true, s);
+    PHG_API_END
 }
 
 static int norm_common(phg_ops o, const double *u, const double *v, double *out, bool dist, bool sq, void *stream) {
@@ -1400,14 +1505,18 @@ static int norm_common(phg_ops o, const double *u, const double *v, double *out,
     return PHG_OK;
 }
 
-extern "C" int phg_norm(phg_ops o, const double *u, double *out, void *s) { return norm_common(o, u, nullptr, out, false, true, s); }
+extern "C" int phg_norm(phg_ops o, const double *u, double *out, void *s) { PHG_API_BEGIN return norm_common(o, u, nullptr, out, false, true, s); PHG_API_END }
 extern "C" int phg_dist(phg_ops o, const double *u, const double *v, double *out, void *s) {
+    PHG_API_BEGIN
     if (!v) return fail(PHG_ERR_ARG, "NULL argument");
     return norm_common(o, u, v, out, true, true, s);
+    PHG_API_END
 }
 extern "C" int phg_scalar(phg_ops o, const double *u, const double *v, double *out, void *s) {
+    PHG_API_BEGIN
     if (!v) return fail(PHG_ERR_ARG, "NULL argument");
     return norm_common(o, u, v, out, false, false, s);
+    PHG_API_END
 }
 
 // ------------------------------------------------------------ barvortex ---
@@ -1448,6 +1557,7 @@ struct phg_barvortex_s {
 };
 
 extern "C" int phg_barvortex_create(phg_ops o, const phg_bv_conf *c, const double *coriolis, phg_barvortex *out) {
+    PHG_API_BEGIN
     if (!o || !c || !out) return fail(PHG_ERR_ARG, "NULL argument");
     if (!(c->tau > 0) || c->picard_iters < 1) return fail(PHG_ERR_ARG, "bad configuration");
     auto b = std::make_unique<phg_barvortex_s>();
@@ -1470,14 +1580,17 @@ extern "C" int phg_barvortex_create(phg_ops o, const phg_bv_conf *c, const doubl
     o->refs++;
     *out = b.release();
     return PHG_OK;
+    PHG_API_END
 }
 
 extern "C" void phg_barvortex_destroy(phg_barvortex b) {
+    PHG_API_BEGIN
     if (!b) return;
     phg_ops_s *o = b->o;
     cudaStreamSynchronize(o->stream);
     delete b;
     ops_release(o);
+    PHG_API_END_VOID
 }
 
 namespace {
@@ -1579,13 +1692,17 @@ static int bv_calc(phg_barvortex b, int nv, double *u1, const double *u, const d
 
 extern "C" int phg_barvortex_calc(phg_barvortex b, double *u1, const double *u, const double *bnd_u,
                                   const double *bnd_w, const double *forcing, void *stream) {
+    PHG_API_BEGIN
     return bv_calc(b, 1, u1, u, bnd_u, bnd_w, forcing, stream);
+    PHG_API_END
 }
 
 extern "C" int phg_barvortex_calc_batch(phg_barvortex b, int nmembers, double *u1, const double *u,
                                         const double *bnd_u, const double *bnd_w, const double *forcing,
                                         void *stream) {
+    PHG_API_BEGIN
     return bv_calc(b, nmembers, u1, u, bnd_u, bnd_w, forcing, stream);
+    PHG_API_END
 }
 
 // check the solves folded into b->agg since the last check
@@ -1682,7 +1799,9 @@ static int bv_run(phg_barvortex b, int nv, int nsteps, double *u, const double *
 
 extern "C" int phg_barvortex_run(phg_barvortex b, int nmembers, int nsteps, double *u, const double *bnd_u,
                                  const double *bnd_w, const double *forcing, void *stream) {
+    PHG_API_BEGIN
     return bv_run(b, nmembers, nsteps, u, bnd_u, bnd_w, forcing, stream);
+    PHG_API_END
 }
 
 // ------------------------------------------- linearised / adjoint steps ---
@@ -1864,20 +1983,27 @@ static int bv_linear(phg_barvortex b, int kind, double *u1, const double *u, con
 
 extern "C" int phg_barvortex_calc_L(phg_barvortex b, double *u1, const double *u, const double *z,
                                     const double *bnd_u, const double *bnd_w, void *stream) {
+    PHG_API_BEGIN
     return bv_linear(b, 0, u1, u, z, bnd_u, bnd_w, stream);
+    PHG_API_END
 }
 
 extern "C" int phg_barvortex_calc_L_1(phg_barvortex b, double *u1, const double *u, const double *z,
                                       const double *bnd_u, const double *bnd_w, void *stream) {
+    PHG_API_BEGIN
     return bv_linear(b, 1, u1, u, z, bnd_u, bnd_w, stream);
+    PHG_API_END
 }
 
 extern "C" int phg_barvortex_calc_LT(phg_barvortex b, double *v1, const double *v, const double *z,
                                      const double *bnd_u, const double *bnd_w, void *stream) {
+    PHG_API_BEGIN
     return bv_linear(b, 2, v1, v, z, bnd_u, bnd_w, stream);
+    PHG_API_END
 }
 
 extern "C" int phg_barvortex_last_stats(phg_barvortex b, int *il, int *ia, int *imj, int *iml, double *worst) {
+    PHG_API_BEGIN
     if (!b) return fail(PHG_ERR_ARG, "NULL handle");
     phg_ops_s *o = b->o;
     cudaStream_t ls = b->last_stream ? b->last_stream : o->stream;
@@ -1903,6 +2029,7 @@ extern "C" int phg_barvortex_last_stats(phg_barvortex b, int *il, int *ia, int *
     if (iml) *iml = ml;
     if (worst) *worst = wr;
     return r;
+    PHG_API_END
 }
 
 // ------------------------------------------------------------- baroclin ---
@@ -2018,6 +2145,7 @@ int build_bc_system(phg_ops_s *o, const BaroclinParams &bp, double su, BcSystem 
 }  // namespace
 
 extern "C" int phg_baroclin_create(phg_ops o, const phg_bc_conf *c, const double *coriolis, phg_baroclin *out) {
+    PHG_API_BEGIN
     if (!o || !c || !out) return fail(PHG_ERR_ARG, "NULL argument");
     if (!(c->tau > 0) || c->picard_iters < 1 || c->picard_iters > 30) return fail(PHG_ERR_ARG, "bad configuration");
     auto b = std::make_unique<phg_baroclin_s>();
@@ -2045,14 +2173,17 @@ extern "C" int phg_baroclin_create(phg_ops o, const phg_bc_conf *c, const double
     o->refs++;
     *out = b.release();
     return PHG_OK;
+    PHG_API_END
 }
 
 extern "C" void phg_baroclin_destroy(phg_baroclin b) {
+    PHG_API_BEGIN
     if (!b) return;
     phg_ops_s *o = b->o;
     cudaStreamSynchronize(o->stream);
     delete b;
     ops_release(o);
+    PHG_API_END_VOID
 }
 
 namespace {
@@ -2236,16 +2367,21 @@ static int bc_linear(phg_baroclin b, int kind, double *u11, double *u21, const d
 
 extern "C" int phg_baroclin_calc_L(phg_baroclin b, double *u11, double *u21, const double *u1, const double *u2,
                                    const double *z1, const double *z2, const double *bnd, void *stream) {
+    PHG_API_BEGIN
     return bc_linear(b, 0, u11, u21, u1, u2, z1, z2, bnd, stream);
+    PHG_API_END
 }
 
 extern "C" int phg_baroclin_calc_L_1(phg_baroclin b, double *u11, double *u21, const double *u1, const double *u2,
                                      const double *z1, const double *z2, const double *bnd, void *stream) {
+    PHG_API_BEGIN
     return bc_linear(b, 1, u11, u21, u1, u2, z1, z2, bnd, stream);
+    PHG_API_END
 }
 
 extern "C" int phg_baroclin_calc(phg_baroclin b, double *u11, double *u21, const double *u1, const double *u2,
                                  const double *bnd, const double *f, const double *g, void *stream) {
+    PHG_API_BEGIN
     if (!b || !u11 || !u21 || !u1 || !u2) return fail(PHG_ERR_ARG, "NULL argument");
     phg_ops_s *o = b->o;
     cudaStream_t s = o->str(stream);
@@ -2260,6 +2396,7 @@ extern "C" int phg_baroclin_calc(phg_baroclin b, double *u11, double *u21, const
     CK(st.finish());
     if (!st.host) return PHG_OK;
     return check_stats(o, b->nslots, s, nullptr, b->each);
+    PHG_API_END
 }
 
 // ------------------------------------------------------- no allocation ---
@@ -2300,6 +2437,7 @@ int noalloc_scratch(int dev, unsigned char **out) {
 }  // namespace
 
 extern "C" int phg_laplace_calc2_noalloc(phg_ops o, double *ans, const double *F, void *stream) {
+    PHG_API_BEGIN
     if (!o || !ans || !F) return fail(PHG_ERR_ARG, "NULL argument");
     if (!is_device_ptr(ans) || !is_device_ptr(F))
         return fail(PHG_ERR_ARG, "phg_laplace_calc2_noalloc takes device pointers only");
@@ -2326,4 +2464,5 @@ extern "C" int phg_laplace_calc2_noalloc(phg_ops o, double *ans, const double *F
     CK(gmres_solve(o->ML.op, rhs, ans, 1, o->rs, o->restart, o->max_iter, mass_tol(o), prec_of(o), work, st, s,
                    /*no_alloc=*/true));
     return PHG_OK;
+    PHG_API_END
 }

@@ -34,6 +34,7 @@
 #include <vector>
 
 #include "../../include/phelm_gb300.h"
+#include "phg_api.hpp"
 
 namespace {
 
@@ -60,6 +61,7 @@ struct Lane {
     long long bytes = 0;   // reserved against the budget
     // shared state, under Server::mu
     std::deque<Pending *> queue;
+    std::vector<Pending *> act;   // members in flight, act[k] owns slot k (lane thread only)
     bool ready = false, failed = false, stop = false, closing = false, closed = false;
     int fail_status = PHG_OK;
     std::string fail_msg;
@@ -303,7 +305,7 @@ void lane_close(Lane *L) {
 void laplace_loop(Lane *L) {
     Server *S = L->srv;
     const int V = L->V, os = L->os;
-    std::vector<Pending *> batch;
+    std::vector<Pending *> &batch = L->act;
     for (;;) {
         batch.clear();
         {
@@ -339,6 +341,7 @@ void laplace_loop(Lane *L) {
             if (!st) memcpy(batch[k]->r.output, L->hOut + (size_t)k * V, 8 * (size_t)V);
         std::lock_guard<std::mutex> lk(S->mu);
         for (int k = 0; k < n; ++k) push_done(S, batch[k], st, n);
+        batch.clear();
         L->active = 0;
         L->last_busy = S->now();
     }
@@ -347,7 +350,7 @@ void laplace_loop(Lane *L) {
 void bv_loop(Lane *L) {
     Server *S = L->srv;
     const int V = L->V, os = L->os;
-    std::vector<Pending *> act;   // act[k] owns slot k
+    std::vector<Pending *> &act = L->act;
     std::vector<int> fin;
     for (;;) {
         int n0;
@@ -424,7 +427,23 @@ void bv_loop(Lane *L) {
     }
 }
 
-void lane_main(Lane *L) {
+// A C++ exception inside a lane (host memory exhausted) fails the lane and the
+// requests it holds instead of ending the process; queued ones fail at close.
+void lane_abort(Lane *L) {
+    Server *S = L->srv;
+    phg::api_exception();
+    std::lock_guard<std::mutex> lk(S->mu);
+    L->failed = true;
+    L->fail_status = PHG_ERR_HOST;
+    L->fail_msg = phg_last_error();
+    L->closing = true;
+    for (Pending *p : L->act) push_done(S, p, PHG_ERR_HOST, 0, L->fail_msg.c_str());
+    L->act.clear();
+    L->active = 0;
+    S->ready_cv.notify_all();
+}
+
+void lane_body(Lane *L) {
     Server *S = L->srv;
     cudaSetDevice(S->dev);
     int st = lane_open(L);
@@ -443,6 +462,14 @@ void lane_main(Lane *L) {
     if (!st) {
         if (L->kind == PHG_REQ_LAPLACE_SOLVE) laplace_loop(L);
         else bv_loop(L);
+    }
+}
+
+void lane_main(Lane *L) {
+    try {
+        lane_body(L);
+    } catch (...) {
+        lane_abort(L);
     }
     lane_close(L);
 }
@@ -468,6 +495,7 @@ Lane *lane_for(Server *S, int kind, int level) {
 struct phg_serve_s : Server {};
 
 extern "C" int phg_serve_create(const phg_serve_conf *conf, phg_serve *out) {
+    PHG_API_BEGIN
     if (!conf || !out) return PHG_ERR_ARG;
     if (!(conf->hbm_budget_bytes > 0) || (conf->precision != PHG_FP64 && conf->precision != PHG_MIXED) ||
         !(conf->solve_tol > 0) || !(conf->step_tol > 0) || conf->max_slots < 0)
@@ -482,20 +510,24 @@ extern "C" int phg_serve_create(const phg_serve_conf *conf, phg_serve *out) {
     s->t0 = Clock::now();
     *out = s.release();
     return PHG_OK;
+    PHG_API_END
 }
 
 extern "C" double phg_serve_clock(phg_serve s) { return s ? s->now() : 0.0; }
 
 extern "C" int phg_serve_preload(phg_serve s, int kind, int level) {
+    PHG_API_BEGIN
     if (!s || (kind != PHG_REQ_LAPLACE_SOLVE && kind != PHG_REQ_BARVORTEX) || level < 1 || level > 9)
         return PHG_ERR_ARG;
     std::unique_lock<std::mutex> lk(s->mu);
     Lane *L = lane_for(s, kind, level);
     s->ready_cv.wait(lk, [&] { return L->ready || L->failed || L->closed; });
     return L->failed ? L->fail_status : PHG_OK;
+    PHG_API_END
 }
 
 extern "C" int phg_serve_submit(phg_serve s, const phg_request *req) {
+    PHG_API_BEGIN
     if (!s || !req) return PHG_ERR_ARG;
     auto p = new Pending();
     p->r = *req;
@@ -515,9 +547,11 @@ extern "C" int phg_serve_submit(phg_serve s, const phg_request *req) {
     L->queue.push_back(p);
     L->cv.notify_all();
     return PHG_OK;
+    PHG_API_END
 }
 
 extern "C" int phg_serve_poll(phg_serve s, phg_completion *out, int max, double wait_s, int *n) {
+    PHG_API_BEGIN
     if (!s || !n || (max > 0 && !out)) return PHG_ERR_ARG;
     std::unique_lock<std::mutex> lk(s->mu);
     if (s->done.empty() && wait_s > 0)
@@ -529,9 +563,11 @@ extern "C" int phg_serve_poll(phg_serve s, phg_completion *out, int max, double 
     }
     *n = k;
     return PHG_OK;
+    PHG_API_END
 }
 
 extern "C" int phg_serve_stats(phg_serve s, double *bytes_in_use, int *lanes_open, long long *completed) {
+    PHG_API_BEGIN
     if (!s) return PHG_ERR_ARG;
     std::lock_guard<std::mutex> lk(s->mu);
     int open = 0;
@@ -540,9 +576,11 @@ extern "C" int phg_serve_stats(phg_serve s, double *bytes_in_use, int *lanes_ope
     if (lanes_open) *lanes_open = open;
     if (completed) *completed = s->ndone;
     return PHG_OK;
+    PHG_API_END
 }
 
 extern "C" void phg_serve_destroy(phg_serve s) {
+    PHG_API_BEGIN
     if (!s) return;
     {
         std::lock_guard<std::mutex> lk(s->mu);
@@ -557,4 +595,5 @@ extern "C" void phg_serve_destroy(phg_serve s) {
         if (L->th.joinable()) L->th.join();
     for (auto &kv : s->meshes) phg_mesh_destroy(kv.second);
     delete s;
+    PHG_API_END_VOID
 }

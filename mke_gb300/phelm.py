@@ -18,7 +18,7 @@ from . import build as _build
 
 PHG_FP64, PHG_MIXED = 0, 1
 _ERRORS = {1: "bad argument", 2: "CUDA error", 3: "solve did not converge", 4: "device wait timed out",
-           5: "mesh I/O error", 6: "over the HBM budget"}
+           5: "mesh I/O error", 6: "over the HBM budget", 7: "host failure"}
 PHG_REQ_LAPLACE_SOLVE, PHG_REQ_BARVORTEX = 0, 1
 
 _dp = C.POINTER(C.c_double)

@@ -110,6 +110,35 @@ def test_errors():
     assert e.value.code == 5
 
 
+HOST_OOM = r"""
+import ctypes as C, resource, sys
+sys.path.insert(0, sys.argv[1])
+from mke_gb300 import phelm
+L = phelm.lib()
+vm = next(int(x.split()[1]) * 1024 for x in open("/proc/self/status") if x.startswith("VmSize:"))
+resource.setrlimit(resource.RLIMIT_AS, (vm + 150 * 2**20, resource.RLIM_INFINITY))
+h = C.c_void_p()
+rc = L.phg_mesh_generate(9, C.byref(h))
+print(rc, L.phg_last_error().decode())
+print(L.phg_mesh_generate(2, C.byref(h)))
+"""
+
+
+def test_host_exception_becomes_status():
+    """A C++ exception inside an entry point (here std::bad_alloc: a level-9 mesh
+    under an address-space limit 150 MiB above the process's size) returns
+    PHG_ERR_HOST instead of unwinding into the C caller, and the library stays
+    usable.  One OpenMP thread, so that no thread creation meets the limit."""
+    import subprocess
+    import sys
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    p = subprocess.run([sys.executable, "-c", HOST_OOM, REPO], capture_output=True, text=True, env=env, timeout=300)
+    assert p.returncode == 0, p.stderr[-2000:]
+    first, second = p.stdout.strip().splitlines()[-2:]
+    assert first == "7 host memory exhausted", first
+    assert second == "0"
+
+
 def test_no_gpu_fails_loudly():
     import torch
     if torch.cuda.is_available():
