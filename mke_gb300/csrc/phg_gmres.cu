@@ -1361,15 +1361,18 @@ cudaError_t cheb_lockstep(const DevSolveOp &op, const double *B, double *X, int 
     return cudaGetLastError();
 }
 
-int g_sms = 0;
+// the device's SM count, read once (serving lanes call this from several threads)
+std::atomic<int> g_sms{0};
 
 int sm_count() {
-    if (!g_sms) {
+    int n = g_sms.load(std::memory_order_relaxed);
+    if (!n) {
         int dev = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        g_sms.store(n, std::memory_order_relaxed);
     }
-    return g_sms;
+    return n;
 }
 
 int env_int(const char *name, int dflt) {
@@ -2303,11 +2306,12 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
             const double frac = (double)Lv.n / (double)n * (op.block4 ? 2.0 : 1.0);
             p.mg_row_bytes += frac * ((op.mg.nu1 + op.mg.nu2 + 1) * (Lv.W * (4.0 + es) + 4.0 * es) + 4.0 * es);
         }
+    static std::once_flag timers_once;
     static long long *timers = nullptr;
     const bool timing = !no_alloc && getenv("PHG_PHASE_TIMING") != nullptr;
-    if (timing && !timers) cudaMalloc(&timers, sizeof(long long) * T_NPHASE);
+    if (timing) std::call_once(timers_once, [] { cudaMalloc(&timers, sizeof(long long) * T_NPHASE); });
     p.timers = timing ? timers : nullptr;
-    if (timing) cudaMemsetAsync(timers, 0, sizeof(long long) * T_NPHASE, s);
+    if (p.timers) cudaMemsetAsync(timers, 0, sizeof(long long) * T_NPHASE, s);
     if ((e = cudaMemsetAsync(w + L.bar, 0, L.total - L.bar, s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(stats_dev, 0, sizeof(GmresStats), s)) != cudaSuccess) return e;
     void *args[] = {&p};
@@ -2328,7 +2332,7 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     g_kernel_launches += 2;
     // a barrier timeout lands in stats->status (2)
     fold_err<<<1, 1, 0, s>>>(p.err, stats_dev);
-    if (timing) {   // debug: print block 0's phase cycles for this launch
+    if (p.timers) {   // debug: print block 0's phase cycles for this launch
         long long h[T_NPHASE];
         GmresStats st;
         cudaMemcpyAsync(h, timers, sizeof(h), cudaMemcpyDeviceToHost, s);
