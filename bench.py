@@ -370,8 +370,7 @@ def run_ours(args, ws, rank, local):
         "vs_baseline": None,
         "dtype": "f32+f64",
         "data": "synthetic (seeded Rossby-Haurwitz wave 4 + spherical-harmonic noise)",
-        "config": {"workload": "barvortex step, icosahedral level 6 (40962 points, 81920 triangles), "
-                               "tau=1e-3, theta=0.5, 3 Picard iterations, GMRES(30) to 1e-12",
+        "config": {"workload": workload(args.level), "solve_tol": args.tol,
                    "level": args.level, "members_per_gpu": 1, "parallelism": f"replicas x{ws}",
                    "l2": "flushed between steps (256 MB write, not timed)"},
         "fp64": {"value": ws * 1000.0 / ms64, "unit": "steps/s", "ms_per_step": ms64,
@@ -409,6 +408,13 @@ def run_ours(args, ws, rank, local):
     print(json.dumps(line))
     replicas.finish()
     return line
+
+
+def workload(level: int) -> str:
+    """The timed workload, named by its sizes (a level-L icosahedral sphere has
+    10 * 4^L + 2 points and 20 * 4^L triangles); both arms report the same one."""
+    return (f"barvortex step, icosahedral level {level} ({10 * 4 ** level + 2} points, {20 * 4 ** level} triangles), "
+            "tau=1e-3, theta=0.5, 3 Picard iterations")
 
 
 def host_threads() -> int:
@@ -474,8 +480,7 @@ def run_reference(args, ws, rank):
         "value": v, "unit": "steps/s", "n_gpus": ws, "steps": steps, "warmup": warm,
         "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded Rossby-Haurwitz wave 4 + spherical-harmonic noise)",
-        "config": {"workload": "barvortex step, icosahedral level 6 (40962 points, 81920 triangles), "
-                               "tau=1e-3, theta=0.5, 3 Picard iterations", "level": args.level},
+        "config": {"workload": workload(args.level), "level": args.level, "members_per_gpu": 1},
         "cpu_baseline": {"value": v, "unit": "steps/s", "cores": host_threads(), "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
