@@ -7,7 +7,11 @@
 // File: "PHGLVL01", int32 level, then the payload (every array as a uint64
 // count followed by its raw elements), then a uint64 FNV-1a hash of the
 // payload.  A file with another magic, level, a short payload or a hash
-// mismatch is rejected (the caller rebuilds the level and rewrites it).
+// mismatch is rejected (the caller rebuilds the level and rewrites it), and
+// so is a well-formed file whose contents are inconsistent (an index out of
+// range, operator or multigrid dimensions that do not fit the mesh): the
+// checksum only catches damage, and every index read here is later
+// dereferenced by the host assembly or the device kernels.
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -67,6 +71,49 @@ void put_mesh(Writer &w, const Mesh &m) {
     w.vec(m.orig); w.vec(m.par_a); w.vec(m.par_b); w.vec(m.raw_xyz);
 }
 
+// every index a consumer of a generated level dereferences lies in range
+bool mesh_indices_ok(const Mesh &m) {
+    const int V = m.V, T = m.T;
+    if (m.level < 1 || m.level > 9 || V != 10 * (1 << (2 * m.level)) + 2 || m.nz < 1 || m.nz > 4) return false;
+    for (int x : m.tri)
+        if (x < 0 || x >= V) return false;
+    for (int z : m.tz)
+        if (z < 0 || z >= m.nz) return false;
+    int nb = 0;
+    for (int b : m.bnd) {
+        if (b != 0 && b != 1) return false;
+        nb += b;
+    }
+    if (nb != m.os) return false;
+    // the inner/outer maps and the point -> triangle adjacency are exactly
+    // what finish_mesh derives from the triangles and the boundary flags
+    Mesh d;
+    d.V = V;
+    d.T = T;
+    d.tri = m.tri;
+    d.bnd = m.bnd;
+    finish_mesh(d);
+    if (d.rs != m.rs || d.inner != m.inner || d.outer != m.outer || d.p2io != m.p2io || d.adj_ptr != m.adj_ptr ||
+        d.adj != m.adj)
+        return false;
+    for (int p = 0; p < V; ++p)
+        if (m.adj_ptr[p + 1] == m.adj_ptr[p]) return false;   // every point lies on a triangle
+    // refinement history: orig is a permutation, the parents of a midpoint are
+    // points of the level below (which has (V - 2) / 4 + 2 points)
+    if (m.orig.size() != (size_t)V || m.par_a.size() != (size_t)V || m.par_b.size() != (size_t)V ||
+        m.raw_xyz.size() != 3 * (size_t)V)
+        return false;
+    std::vector<char> seen((size_t)V, 0);
+    for (int o : m.orig) {
+        if (o < 0 || o >= V || seen[o]) return false;
+        seen[o] = 1;
+    }
+    const int Vc = (V - 2) / 4 + 2;
+    for (int p = Vc; p < V; ++p)
+        if (m.par_a[p] < 0 || m.par_a[p] >= Vc || m.par_b[p] < 0 || m.par_b[p] >= Vc) return false;
+    return true;
+}
+
 bool get_mesh(Reader &r, Mesh &m, bool allow_empty = false) {
     int32_t lv, V, T, rs, os, nz;
     r.scalar(lv); r.scalar(V); r.scalar(T); r.scalar(rs); r.scalar(os); r.scalar(nz);
@@ -81,7 +128,7 @@ bool get_mesh(Reader &r, Mesh &m, bool allow_empty = false) {
            m.uv.size() == 8 * (size_t)V && m.tri.size() == 3 * (size_t)T && m.tz.size() == (size_t)T &&
            m.bnd.size() == (size_t)V && m.inner.size() == (size_t)rs && m.outer.size() == (size_t)os &&
            m.p2io.size() == (size_t)V && m.adj_ptr.size() == (size_t)V + 1 &&
-           m.adj.size() == (size_t)m.adj_ptr[V];
+           m.adj.size() == (size_t)m.adj_ptr[V] && mesh_indices_ok(m);
 }
 
 void put_csr(Writer &w, const Csr &a) {
@@ -103,6 +150,34 @@ bool get_csr(Reader &r, Csr &a) {
     for (int c : a.col)
         if (c < 0 || c >= m) return false;
     return true;
+}
+
+// the operators' shapes (inner x inner, inner x boundary, all x all)
+bool ops_dims_ok(const SphereOps &o, const Mesh &m) {
+    const Csr *sq[] = {&o.idt, &o.lapl, &o.jidt, &o.d1, &o.d2, &o.d1c, &o.d2c};
+    const Csr *bc[] = {&o.bnd2, &o.bnd3, &o.d1b, &o.d2b, &o.d1cb, &o.d2cb};
+    for (const Csr *a : sq)
+        if (a->n != m.rs || a->m != m.rs) return false;
+    for (const Csr *a : bc)
+        if (a->n != m.rs || a->m != m.os) return false;
+    return o.norm.n == m.V && o.norm.m == m.V;
+}
+
+// the hierarchy's levels one refinement apart, transfers and coarse
+// operators sized by the inner points of the levels they connect
+bool hierarchy_ok(const MgHierarchy &h, const Mesh &fine) {
+    const size_t nlev = h.mesh.size();
+    if (nlev < 2 || nlev > (size_t)fine.level || h.A.size() != nlev || h.P.size() != nlev - 1 ||
+        h.R.size() != nlev - 1 || h.mesh[0].V != 0 || h.A[0].n != 0)
+        return false;
+    auto rows = [&](size_t k) { return k == 0 ? fine.rs : h.mesh[k].rs; };
+    for (size_t k = 1; k < nlev; ++k)
+        if (h.mesh[k].level != fine.level - (int)k || h.A[k].n != rows(k) || h.A[k].m != rows(k)) return false;
+    for (size_t k = 0; k + 1 < nlev; ++k)
+        if (h.P[k].n != rows(k) || h.P[k].m != rows(k + 1) || h.R[k].n != rows(k + 1) || h.R[k].m != rows(k))
+            return false;
+    const size_t nc = (size_t)rows(nlev - 1);
+    return h.coarse_inv.size() == nc * nc;
 }
 
 }  // namespace
@@ -166,6 +241,7 @@ bool load_level_cache(const char *path, int level, Mesh &m, SphereOps &ops, MgHi
                       &oo.bnd2, &oo.bnd3, &oo.d1b, &oo.d2b, &oo.d1cb, &oo.d2cb, &oo.norm};
     for (Csr *a : all_ops)
         if (!get_csr(r, *a)) { err = "bad operator record"; return false; }
+    if (!ops_dims_ok(oo, mm)) { err = "operator shapes do not fit the mesh"; return false; }
     int32_t flag = 0;
     MgHierarchy hh;
     if (!r.scalar(flag)) { err = "truncated"; return false; }
@@ -184,6 +260,7 @@ bool load_level_cache(const char *path, int level, Mesh &m, SphereOps &ops, MgHi
                 if (!get_csr(r, a)) { err = "bad hierarchy operator"; return false; }
         }
         if (!r.vec(hh.coarse_inv)) { err = "bad coarse inverse"; return false; }
+        if (!hierarchy_ok(hh, mm)) { err = "hierarchy does not fit the mesh"; return false; }
     }
     if (r.p != r.end) { err = "trailing bytes"; return false; }
     m = std::move(mm);

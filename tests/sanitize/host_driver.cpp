@@ -1,9 +1,14 @@
 // Runs the library's host code (mesh generation, text round trip, operator
 // assembly, multigrid hierarchy, barotropic and baroclinic matrices, text
-// output) at levels 1-4 under AddressSanitizer and UndefinedBehaviorSanitizer.
-// Built and run by tests/test_sanitizers.py; exits non-zero on the first
-// inconsistency (the sanitizers abort on their own findings).
+// output) at levels 1-4 under AddressSanitizer and UndefinedBehaviorSanitizer,
+// then the level cache: a round trip, and the reader on damaged files --
+// truncated payloads and flipped bytes, each with its checksum recomputed so
+// that the parser itself sees them; what it accepts goes through the
+// assembly and the multigrid build.  Built and run by
+// tests/test_sanitizers.py (argument: a scratch directory); exits non-zero on
+// the first inconsistency (the sanitizers abort on their own findings).
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -26,7 +31,133 @@ static bool csr_ok(const Csr &a) {
     return true;
 }
 
-int main() {
+static uint64_t fnv1a(const unsigned char *p, size_t n) {
+    uint64_t h = 1469598103934665603ull;
+    for (size_t i = 0; i < n; ++i) { h ^= p[i]; h *= 1099511628211ull; }
+    return h;
+}
+
+static std::vector<unsigned char> read_all(const std::string &path) {
+    std::vector<unsigned char> b;
+    FILE *f = fopen(path.c_str(), "rb");
+    if (!f) return b;
+    unsigned char chunk[1 << 16];
+    size_t k;
+    while ((k = fread(chunk, 1, sizeof chunk, f)) > 0) b.insert(b.end(), chunk, chunk + k);
+    fclose(f);
+    return b;
+}
+
+// magic + level, then `payload` and its recomputed checksum
+static void write_with_hash(const std::string &path, const std::vector<unsigned char> &head,
+                            const std::vector<unsigned char> &payload) {
+    FILE *f = fopen(path.c_str(), "wb");
+    const uint64_t h = fnv1a(payload.data(), payload.size());
+    fwrite(head.data(), 1, head.size(), f);
+    if (!payload.empty()) fwrite(payload.data(), 1, payload.size(), f);
+    fwrite(&h, sizeof h, 1, f);
+    fclose(f);
+}
+
+// load a (possibly damaged) cache file; when accepted, run the consumers of
+// its indices.  Returns whether the reader accepted it.
+static bool load_and_use(const std::string &path, int level) {
+    Mesh m;
+    SphereOps ops;
+    MgHierarchy h;
+    bool has_mg = false;
+    std::string err;
+    if (!load_level_cache(path.c_str(), level, m, ops, h, has_mg, err)) return false;
+    SphereOps again;
+    assemble_sphere(m, again);
+    MgHierarchy h2;
+    build_mg(m, 1, h2, err);
+    return true;
+}
+
+static int cache_checks(const std::string &dir) {
+    int bad = 0;
+    std::string err;
+    // round trip at level 3
+    {
+        Mesh m;
+        generate_sphere(3, m, err);
+        SphereOps ops;
+        assemble_sphere(m, ops);
+        MgHierarchy h;
+        build_mg(m, 1, h, err);
+        const std::string path = dir + "/level3.cache";
+        bad += check(save_level_cache(path.c_str(), m, ops, &h), "save_level_cache", 3);
+        Mesh m2;
+        SphereOps o2;
+        MgHierarchy h2;
+        bool has_mg = false;
+        bad += check(load_level_cache(path.c_str(), 3, m2, o2, h2, has_mg, err) && has_mg, "load_level_cache", 3);
+        bad += check(m2.tri == m.tri && m2.xyz == m.xyz && o2.lapl.val == ops.lapl.val && o2.norm.col == ops.norm.col &&
+                     h2.P.size() == h.P.size() && h2.coarse_inv == h.coarse_inv, "cache round trip", 3);
+        bad += check(!load_level_cache(path.c_str(), 4, m2, o2, h2, has_mg, err), "wrong level accepted", 3);
+    }
+    // damaged files at level 2
+    Mesh m;
+    generate_sphere(2, m, err);
+    SphereOps ops;
+    assemble_sphere(m, ops);
+    MgHierarchy h;
+    build_mg(m, 1, h, err);
+    const std::string good = dir + "/level2.cache", path = dir + "/damaged.cache";
+    bad += check(save_level_cache(good.c_str(), m, ops, &h), "save_level_cache", 2);
+    const std::vector<unsigned char> file = read_all(good);
+    bad += check(file.size() > 20, "cache size", 2);
+    if (bad) return bad;
+    const std::vector<unsigned char> head(file.begin(), file.begin() + 12);
+    const std::vector<unsigned char> payload(file.begin() + 12, file.end() - 8);
+    const size_t n = payload.size();
+    bad += check(load_and_use(good, 2), "intact file rejected", 2);
+    // truncations: never accepted
+    int accepted = 0;
+    for (size_t k = 0; k < 200; ++k) {
+        const size_t cut = k < 32 ? k : k < 64 ? n - (64 - k) : (n * (k - 64)) / 136;
+        write_with_hash(path, head, std::vector<unsigned char>(payload.begin(), payload.begin() + cut));
+        accepted += load_and_use(path, 2);
+    }
+    bad += check(accepted == 0, "truncated payload accepted", 2);
+    // flipped bytes: every byte of the mesh scalars and the first counts, then
+    // positions spread over the payload; accepted files must be usable
+    uint64_t x = 88172645463325252ull;
+    int tried = 0;
+    const unsigned char flips[3] = {0xFF, 0x80, 0x01};
+    for (size_t k = 0; k < 64 + 300; ++k) {
+        size_t pos;
+        if (k < 64) {
+            pos = k;
+        } else {
+            x ^= x << 13; x ^= x >> 7; x ^= x << 17;
+            pos = (size_t)(x % n);
+        }
+        for (int f = 0; f < 3; ++f) {
+            if (k >= 64 && f != (int)(k % 3)) continue;   // one flip per spread position
+            std::vector<unsigned char> p = payload;
+            p[pos] ^= flips[f];
+            write_with_hash(path, head, p);
+            load_and_use(path, 2);
+            ++tried;
+        }
+    }
+    // garbage and empty files
+    {
+        FILE *f = fopen(path.c_str(), "wb");
+        fclose(f);
+        bad += check(!load_and_use(path, 2), "empty file accepted", 2);
+        f = fopen(path.c_str(), "wb");
+        for (int i = 0; i < 4096; ++i) fputc((i * 131 + 7) & 255, f);
+        fclose(f);
+        bad += check(!load_and_use(path, 2), "garbage accepted", 2);
+    }
+    printf("cache: %d damaged files read\n", tried + 200);
+    return bad;
+}
+
+int main(int argc, char **argv) {
     int bad = 0;
     for (int level = 1; level <= 4; ++level) {
         Mesh m;
@@ -70,6 +201,7 @@ int main() {
         print_function_text(g, m, u.data(), nullptr, nullptr, nullptr, true);
         fclose(g);
     }
+    bad += cache_checks(argc > 1 ? argv[1] : ".");
     if (!bad) printf("host code clean at levels 1-4\n");
     return bad ? 1 : 0;
 }

@@ -99,6 +99,55 @@ def test_damaged_file_is_rebuilt(cache, damage):
     assert same(fresh, snapshot(3))           # and the rewritten file reads back
 
 
+MESH_VECS = [("xyz", 8), ("uv", 8), ("tri", 4), ("tz", 4), ("bnd", 4), ("inner", 4), ("outer", 4), ("p2io", 4),
+             ("adj_ptr", 4), ("adj", 4), ("orig", 4), ("par_a", 4), ("par_b", 4), ("raw_xyz", 8)]
+
+
+def layout(raw):
+    """Byte offsets of the first mesh record's arrays and of the first
+    operator record (file: magic, int32 level, then the payload)."""
+    off = 12 + 24                      # level, V, T, rs, os, nz
+    where = {}
+    for name, size in MESH_VECS:
+        n = struct.unpack_from("<Q", raw, off)[0]
+        where[name] = (off + 8, n)
+        off += 8 + n * size
+    where["first_op"] = off            # int32 n, int32 m, then ptr / col / val
+    return where
+
+
+@pytest.mark.parametrize("edit", ["adjacency", "triangle", "orig", "operator_shape"])
+def test_inconsistent_file_is_rebuilt(cache, edit):
+    """A file with a valid checksum whose contents do not fit together (an
+    index the assembly or the kernels would follow out of range) is rejected
+    like a damaged one."""
+    phelm.cache_dir(None)
+    fresh = snapshot(3)
+    phelm.cache_dir(str(cache))
+    snapshot(3)
+    path = cache / "phelm_level3.cache"
+    original = path.read_bytes()
+    raw = bytearray(original)
+    w = layout(raw)
+    V = struct.unpack_from("<i", raw, 16)[0]
+    if edit == "adjacency":            # point 0's first triangle swapped for one not through it
+        off, n = w["adj"]
+        struct.pack_into("<i", raw, off, struct.unpack_from("<i", raw, off + 4 * (n - 1))[0])
+    elif edit == "triangle":
+        struct.pack_into("<i", raw, w["tri"][0], V)
+    elif edit == "orig":               # no longer a permutation
+        off, _ = w["orig"]
+        struct.pack_into("<i", raw, off, struct.unpack_from("<i", raw, off + 4)[0])
+    else:                              # idt: one column more than the inner points
+        off = w["first_op"] + 4
+        struct.pack_into("<i", raw, off, struct.unpack_from("<i", raw, off)[0] + 1)
+    struct.pack_into("<Q", raw, len(raw) - 8, fnv1a(bytes(raw[12:-8])))
+    path.write_bytes(bytes(raw))
+    assert same(fresh, snapshot(3))           # rebuilt from scratch
+    assert path.read_bytes() == original      # the rejected file was rewritten
+    assert same(fresh, snapshot(3))
+
+
 def test_unwritable_directory_is_not_an_error(tmp_path):
     missing = tmp_path / "does" / "not" / "exist"
     phelm.cache_dir(str(missing))

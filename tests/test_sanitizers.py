@@ -1,6 +1,7 @@
 """The host code and the CPU oracle under AddressSanitizer and
 UndefinedBehaviorSanitizer (no GPU): tests/sanitize/host_driver.cpp runs the
-library's mesh generation, text I/O and assembly at levels 1-4,
+library's mesh generation, text I/O and assembly at levels 1-4 and the level
+cache reader on damaged files,
 tests/sanitize/oracle_driver.c the oracle's solves and steps at levels 2-3.
 Each is compiled here with -fsanitize=address,undefined and must exit 0 with
 no sanitizer report."""
@@ -26,10 +27,10 @@ def sanitizers_available(tmp_path):
     return r.returncode == 0
 
 
-def run_checked(cmd, exe):
+def run_checked(cmd, exe, *args):
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
-    p = subprocess.run([exe], capture_output=True, text=True, env=ENV, timeout=900)
+    p = subprocess.run([exe, *args], capture_output=True, text=True, env=ENV, timeout=900)
     report = p.stdout + p.stderr
     assert p.returncode == 0, report[-4000:]
     assert "runtime error" not in report and "AddressSanitizer" not in report, report[-4000:]
@@ -43,8 +44,9 @@ def test_host_code(tmp_path):
     exe = str(tmp_path / "host_driver")
     cmd = ["g++", "-std=c++17", "-fopenmp", "-ffp-contract=off", *SAN, "-I", csrc,
            os.path.join(HERE, "sanitize", "host_driver.cpp"), os.path.join(csrc, "phg_mesh.cpp"),
-           os.path.join(csrc, "phg_assemble.cpp"), "-o", exe]
-    assert "host code clean" in run_checked(cmd, exe)
+           os.path.join(csrc, "phg_assemble.cpp"), os.path.join(csrc, "phg_cache.cpp"), "-o", exe]
+    report = run_checked(cmd, exe, str(tmp_path))
+    assert "host code clean" in report and "damaged files read" in report
 
 
 def test_oracle(tmp_path):
