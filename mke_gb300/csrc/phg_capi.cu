@@ -777,6 +777,7 @@ extern "C" int phg_ops_create(phg_mesh h, int precision, phg_ops *out) {
     o->prec = precision;
     CK(cudaGetDevice(&o->dev));
     CK(cudaStreamCreateWithFlags(&o->stream, cudaStreamNonBlocking));
+    lockstep_prepare();
     o->V = m.V; o->rs = m.rs; o->os = m.os;
     int W = 0;
     for (int i = 0; i < m.rs; ++i) W = std::max(W, so.idt.ptr[i + 1] - so.idt.ptr[i]);

@@ -137,6 +137,9 @@ int tune_load(const char *path);
 enum class SolvePath { Persistent, ChebLockstep, MgLockstep };
 SolvePath choose_path(const DevSolveOp &op, int nv, int m, Precision prec, bool no_alloc, const SolveShape *shape,
                       SolveShape *sh_out);
+// query the lockstep kernels' launch grids once; call outside any stream
+// capture (operator creation does) so that a captured solve only reads them
+void lockstep_prepare();
 // workspace bytes of the path a solve with this shape (null = tuned/default) takes
 size_t gmres_work_bytes(const DevSolveOp &op, int nv, int m, Precision p, const SolveShape *shape = nullptr);
 // no_alloc: never allocate (the optional debug phase timers stay off)

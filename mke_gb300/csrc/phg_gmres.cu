@@ -87,7 +87,6 @@ struct Params {
 enum { T_RESID, T_VCYCLE, T_SPMV_DOT, T_DOT_SUM, T_UPDATE, T_NORM_SUM, T_GIVENS, T_CORR, T_BARRIER,
        T_BARRIERS, T_TOTAL, T_NPHASE };
 
-__device__ __forceinline__ unsigned ld_volatile(const unsigned *p) { return *(const volatile unsigned *)p; }
 __device__ __forceinline__ int ld_volatile(const int *p) { return *(const volatile int *)p; }
 
 // Barrier over the G blocks of one group; false if the grid is aborting.
@@ -1048,45 +1047,51 @@ Layout layout(const DevSolveOp &op, int nv, int m, Precision prec) {
 constexpr int LS_MAXC = 6;     // refinement cycles at most
 constexpr int LS_MG = 16;      // members per thread in the FP64 residual
 
-// R = B - A X for LS_MG members per block row (FP64, ascending slot order),
-// and each member's sum of R^2 over the block's rows into part[v][block]
-// (fixed order: the norms are reproducible)
+// R = B - A X for LS_MG members per 256-row block (FP64, ascending slot
+// order), and each member's sum of R^2 over the block's rows into
+// part[v][row block] (fixed order: the norms are reproducible).  Grid-stride
+// over (row block, member group) tiles, at most one resident wave of blocks:
+// a launch after convergence then costs one short wave.
 template <int W>
 __global__ void __launch_bounds__(256) k_ls_resid(const int *__restrict__ col, const double *__restrict__ val, int n,
                                                   const double *__restrict__ B, const double *__restrict__ X, int ld,
-                                                  double *__restrict__ R, int nv, double *__restrict__ part,
+                                                  double *__restrict__ R, int nv, double *__restrict__ part, int nbx,
                                                   const int *done) {
     if (*(volatile const int *)done) return;
     __shared__ double sq[LS_MG][256];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool row = i < n;
-    const int v0 = blockIdx.y * LS_MG, v1 = min(nv, v0 + LS_MG);
-    int c[W];
-    double a[W];
+    const int ntile = nbx * ((nv + LS_MG - 1) / LS_MG);
+    for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+        const int rb = tile % nbx, i = rb * 256 + threadIdx.x;
+        const bool row = i < n;
+        const int v0 = (tile / nbx) * LS_MG, v1 = min(nv, v0 + LS_MG);
+        int c[W];
+        double a[W];
 #pragma unroll
-    for (int k = 0; k < W; ++k) {
-        c[k] = row ? __ldg(&col[(size_t)k * n + i]) : 0;
-        a[k] = row ? __ldg(&val[(size_t)k * n + i]) : 0.0;
-    }
-    for (int v = v0; v < v1; ++v) {
-        double r = 0.0;
-        if (row) {
-            const double *x = X + (size_t)v * ld;
-            double sum = 0.0;
-#pragma unroll
-            for (int k = 0; k < W; ++k) sum += a[k] * x[c[k]];
-            r = B[(size_t)v * ld + i] - sum;
-            R[(size_t)v * n + i] = r;
+        for (int k = 0; k < W; ++k) {
+            c[k] = row ? __ldg(&col[(size_t)k * n + i]) : 0;
+            a[k] = row ? __ldg(&val[(size_t)k * n + i]) : 0.0;
         }
-        sq[v - v0][threadIdx.x] = r * r;
-    }
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int j = warp; j < v1 - v0; j += NWARP) {
-        double t = 0.0;
-        for (int q = lane; q < 256; q += 32) t += sq[j][q];
-        t = warp_sum(t);
-        if (lane == 0) part[(size_t)(v0 + j) * gridDim.x + blockIdx.x] = t;
+        for (int v = v0; v < v1; ++v) {
+            double r = 0.0;
+            if (row) {
+                const double *x = X + (size_t)v * ld;
+                double sum = 0.0;
+#pragma unroll
+                for (int k = 0; k < W; ++k) sum += a[k] * x[c[k]];
+                r = B[(size_t)v * ld + i] - sum;
+                R[(size_t)v * n + i] = r;
+            }
+            sq[v - v0][threadIdx.x] = r * r;
+        }
+        __syncthreads();
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        for (int j = warp; j < v1 - v0; j += NWARP) {
+            double t = 0.0;
+            for (int q = lane; q < 256; q += 32) t += sq[j][q];
+            t = warp_sum(t);
+            if (lane == 0) part[(size_t)(v0 + j) * nbx + rb] = t;
+        }
+        __syncthreads();   // sq is refilled by the next tile
     }
 }
 
@@ -1167,26 +1172,31 @@ __global__ void __launch_bounds__(256) k_ls_scale(const double *nrm, int nv, int
     }
 }
 
-// rv = (float)(r * scale), e_1 = c0 D^-1 rv, e_0 = 0: member-major FP64 -> interleaved FP32 (tiled transpose)
+// rv = (float)(r * scale), e_1 = c0 D^-1 rv, e_0 = 0: member-major FP64 -> interleaved FP32 (tiled transpose,
+// grid-stride over the 32 x 32 tiles, row tiles fastest)
 __global__ void __launch_bounds__(256) k_ls_init(const double *__restrict__ R, int n, int nv, int nvp,
                                                  const double *__restrict__ sc, const float *__restrict__ dinv, float c0,
                                                  float *rv, float *e0, float *e1, const int *done) {
     if (*(volatile const int *)done) return;
     __shared__ float t[32][33];
-    const int i0 = blockIdx.x * 32, v0 = blockIdx.y * 32, tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    for (int j = ty; j < 32; j += 8) {
-        const int v = v0 + j, i = i0 + tx;
-        t[j][tx] = (v < nv && i < n) ? (float)(R[(size_t)v * n + i] * sc[v]) : 0.f;
-    }
-    __syncthreads();
-    for (int j = ty; j < 32; j += 8) {
-        const int i = i0 + j, v = v0 + tx;
-        if (i >= n) continue;
-        const float r = t[tx][j];
-        const size_t q = (size_t)i * nvp + v;
-        rv[q] = r;
-        e0[q] = 0.f;
-        e1[q] = c0 * dinv[i] * r;
+    const int ntx = (n + 31) / 32, ntile = ntx * (nvp / 32), tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+        const int i0 = (tile % ntx) * 32, v0 = (tile / ntx) * 32;
+        for (int j = ty; j < 32; j += 8) {
+            const int v = v0 + j, i = i0 + tx;
+            t[j][tx] = (v < nv && i < n) ? (float)(R[(size_t)v * n + i] * sc[v]) : 0.f;
+        }
+        __syncthreads();
+        for (int j = ty; j < 32; j += 8) {
+            const int i = i0 + j, v = v0 + tx;
+            if (i >= n) continue;
+            const float r = t[tx][j];
+            const size_t q = (size_t)i * nvp + v;
+            rv[q] = r;
+            e0[q] = 0.f;
+            e1[q] = c0 * dinv[i] * r;
+        }
+        __syncthreads();   // t is refilled by the next tile
     }
 }
 
@@ -1201,29 +1211,30 @@ __global__ void __launch_bounds__(256) k_ls_step(const int *__restrict__ col, co
                                                  const float4 *__restrict__ ec, const float4 *__restrict__ rv,
                                                  float4 *ep, float ca, float cb, const int *done) {
     if (*(volatile const int *)done) return;
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = (int)(t / (unsigned)q4), q = (int)(t - (unsigned)i * (unsigned)q4);
-    if (i >= n) return;
-    int c[W];
-    float a[W];
+    const unsigned total = (unsigned)n * (unsigned)q4;   // < 2^31 (checked by the caller)
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        const int i = (int)(t / (unsigned)q4), q = (int)(t - (unsigned)i * (unsigned)q4);
+        int c[W];
+        float a[W];
 #pragma unroll
-    for (int k = 0; k < W; ++k) { c[k] = __ldg(&col[(size_t)k * n + i]); a[k] = __ldg(&a32[(size_t)k * n + i]); }
-    float4 g[W];
+        for (int k = 0; k < W; ++k) { c[k] = __ldg(&col[(size_t)k * n + i]); a[k] = __ldg(&a32[(size_t)k * n + i]); }
+        float4 g[W];
 #pragma unroll
-    for (int k = 0; k < W; ++k) g[k] = ec[(size_t)c[k] * q4 + q];
-    float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int k = 0; k < W; ++k) g[k] = ec[(size_t)c[k] * q4 + q];
+        float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-    for (int k = 0; k < W; ++k) {
-        sum.x = fmaf(a[k], g[k].x, sum.x); sum.y = fmaf(a[k], g[k].y, sum.y);
-        sum.z = fmaf(a[k], g[k].z, sum.z); sum.w = fmaf(a[k], g[k].w, sum.w);
+        for (int k = 0; k < W; ++k) {
+            sum.x = fmaf(a[k], g[k].x, sum.x); sum.y = fmaf(a[k], g[k].y, sum.y);
+            sum.z = fmaf(a[k], g[k].z, sum.z); sum.w = fmaf(a[k], g[k].w, sum.w);
+        }
+        const size_t idx = (size_t)i * q4 + q;
+        const float di = cb * __ldg(&dinv[i]);
+        const float4 r = rv[idx], e = ec[idx], eo = ep[idx];
+        float4 dn;
+        dn.x = ca * (e.x - eo.x) + di * (r.x - sum.x); dn.y = ca * (e.y - eo.y) + di * (r.y - sum.y);
+        dn.z = ca * (e.z - eo.z) + di * (r.z - sum.z); dn.w = ca * (e.w - eo.w) + di * (r.w - sum.w);
+        ep[idx] = make_float4(e.x + dn.x, e.y + dn.y, e.z + dn.z, e.w + dn.w);
     }
-    const size_t idx = (size_t)i * q4 + q;
-    const float di = cb * __ldg(&dinv[i]);
-    const float4 r = rv[idx], e = ec[idx], eo = ep[idx];
-    float4 dn;
-    dn.x = ca * (e.x - eo.x) + di * (r.x - sum.x); dn.y = ca * (e.y - eo.y) + di * (r.y - sum.y);
-    dn.z = ca * (e.z - eo.z) + di * (r.z - sum.z); dn.w = ca * (e.w - eo.w) + di * (r.w - sum.w);
-    ep[idx] = make_float4(e.x + dn.x, e.y + dn.y, e.z + dn.z, e.w + dn.w);
 }
 
 // k_ls_step reading A from the 64-byte row records (one matrix stream)
@@ -1232,59 +1243,107 @@ __global__ void __launch_bounds__(256) k_ls_step_pk(const uint4 *__restrict__ pk
                                                     const float4 *__restrict__ rv, float4 *ep, float ca, float cb,
                                                     const int *done) {
     if (*(volatile const int *)done) return;
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = (int)(t / (unsigned)q4), q = (int)(t - (unsigned)i * (unsigned)q4);
-    if (i >= n) return;
-    int c[8];
-    float a[8];
+    const unsigned total = (unsigned)n * (unsigned)q4;   // < 2^31 (checked by the caller)
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        const int i = (int)(t / (unsigned)q4), q = (int)(t - (unsigned)i * (unsigned)q4);
+        int c[8];
+        float a[8];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const uint4 e = __ldg(&pk[(size_t)i * 4 + k]);
-        c[2 * k] = (int)e.x; a[2 * k] = __uint_as_float(e.y);
-        c[2 * k + 1] = (int)e.z; a[2 * k + 1] = __uint_as_float(e.w);
+        for (int k = 0; k < 4; ++k) {
+            const uint4 e = __ldg(&pk[(size_t)i * 4 + k]);
+            c[2 * k] = (int)e.x; a[2 * k] = __uint_as_float(e.y);
+            c[2 * k + 1] = (int)e.z; a[2 * k + 1] = __uint_as_float(e.w);
+        }
+        float4 g[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) g[k] = ec[(size_t)c[k] * q4 + q];
+        float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            sum.x = fmaf(a[k], g[k].x, sum.x); sum.y = fmaf(a[k], g[k].y, sum.y);
+            sum.z = fmaf(a[k], g[k].z, sum.z); sum.w = fmaf(a[k], g[k].w, sum.w);
+        }
+        const size_t idx = (size_t)i * q4 + q;
+        const float di = cb * __ldg(&dinv[i]);
+        const float4 r = rv[idx], e = ec[idx], eo = ep[idx];
+        float4 dn;
+        dn.x = ca * (e.x - eo.x) + di * (r.x - sum.x); dn.y = ca * (e.y - eo.y) + di * (r.y - sum.y);
+        dn.z = ca * (e.z - eo.z) + di * (r.z - sum.z); dn.w = ca * (e.w - eo.w) + di * (r.w - sum.w);
+        ep[idx] = make_float4(e.x + dn.x, e.y + dn.y, e.z + dn.z, e.w + dn.w);
     }
-    float4 g[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) g[k] = ec[(size_t)c[k] * q4 + q];
-    float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        sum.x = fmaf(a[k], g[k].x, sum.x); sum.y = fmaf(a[k], g[k].y, sum.y);
-        sum.z = fmaf(a[k], g[k].z, sum.z); sum.w = fmaf(a[k], g[k].w, sum.w);
-    }
-    const size_t idx = (size_t)i * q4 + q;
-    const float di = cb * __ldg(&dinv[i]);
-    const float4 r = rv[idx], e = ec[idx], eo = ep[idx];
-    float4 dn;
-    dn.x = ca * (e.x - eo.x) + di * (r.x - sum.x); dn.y = ca * (e.y - eo.y) + di * (r.y - sum.y);
-    dn.z = ca * (e.z - eo.z) + di * (r.z - sum.z); dn.w = ca * (e.w - eo.w) + di * (r.w - sum.w);
-    ep[idx] = make_float4(e.x + dn.x, e.y + dn.y, e.z + dn.z, e.w + dn.w);
 }
 
-// x += beta * e: interleaved FP32 -> member-major FP64 (tiled transpose)
+// x += beta * e: interleaved FP32 -> member-major FP64 (tiled transpose, grid-stride as k_ls_init)
 __global__ void __launch_bounds__(256) k_ls_update(double *X, int ld, int n, int nv, int nvp,
                                                    const double *__restrict__ beta, const float *__restrict__ e,
                                                    const int *done) {
     if (*(volatile const int *)done) return;
     __shared__ float t[32][33];
-    const int i0 = blockIdx.x * 32, v0 = blockIdx.y * 32, tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    for (int j = ty; j < 32; j += 8) {
-        const int i = i0 + j, v = v0 + tx;
-        t[j][tx] = i < n ? e[(size_t)i * nvp + v] : 0.f;
-    }
-    __syncthreads();
-    for (int j = ty; j < 32; j += 8) {
-        const int v = v0 + j, i = i0 + tx;
-        if (v < nv && i < n) X[(size_t)v * ld + i] += beta[v] * (double)t[tx][j];
+    const int ntx = (n + 31) / 32, ntile = ntx * (nvp / 32), tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+        const int i0 = (tile % ntx) * 32, v0 = (tile / ntx) * 32;
+        for (int j = ty; j < 32; j += 8) {
+            const int i = i0 + j, v = v0 + tx;
+            t[j][tx] = i < n ? e[(size_t)i * nvp + v] : 0.f;
+        }
+        __syncthreads();
+        for (int j = ty; j < 32; j += 8) {
+            const int v = v0 + j, i = i0 + tx;
+            if (v < nv && i < n) X[(size_t)v * ld + i] += beta[v] * (double)t[tx][j];
+        }
+        __syncthreads();   // t is refilled by the next tile
     }
 }
+
+int sm_count();
+
+// Blocks of 256 threads resident at once for `kernel`: the grid of a
+// grid-stride lockstep launch.  The launches of cycles after convergence only
+// read the stop flag, and a full-size grid (one block per 256 work items)
+// took about as long to retire as a short real step.
+template <typename Kern>
+unsigned resident_grid(Kern kernel, size_t smem) {
+    int per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 256, smem) != cudaSuccess || per < 1) {
+        cudaGetLastError();
+        per = 1;
+    }
+    return (unsigned)(per * sm_count());
+}
+
+unsigned capped(long long want, unsigned cap) { return (unsigned)std::max(1LL, std::min<long long>(want, cap)); }
+
+// the resident grids, queried once (lockstep_prepare runs this at operator
+// creation, outside any stream capture); index W - 6 for the templates
+struct LsGrids {
+    unsigned step_pk, step[3], resid[3], init, update;
+};
+const LsGrids &ls_grids() {
+    static std::once_flag once;
+    static LsGrids g;
+    std::call_once(once, [] {
+        g.step_pk = resident_grid(k_ls_step_pk, 0);
+        g.step[0] = resident_grid(k_ls_step<6>, 0);
+        g.step[1] = resident_grid(k_ls_step<7>, 0);
+        g.step[2] = resident_grid(k_ls_step<8>, 0);
+        g.resid[0] = resident_grid(k_ls_resid<6>, 0);
+        g.resid[1] = resident_grid(k_ls_resid<7>, 0);
+        g.resid[2] = resident_grid(k_ls_resid<8>, 0);
+        g.init = resident_grid(k_ls_init, 0);
+        g.update = resident_grid(k_ls_update, 0);
+    });
+    return g;
+}
+
+// grid of a k_ls_resid<W> launch over `tiles` (row block, member group) tiles
+unsigned resid_grid(int W, long long tiles) { return capped(tiles, ls_grids().resid[W - 6]); }
 
 template <int W>
 cudaError_t ls_steps(const DevSolveOp &op, int n, int q4, float *&ec, float *&ep, const float *rv,
                      const double *ca, const double *cb, int K, const int *done, cudaStream_t s) {
     const long long work = (long long)n * q4;
-    const unsigned blocks = (unsigned)((work + 255) / 256);
     const bool pk = op.pk32 != nullptr;   // row records: one matrix stream (ensemble steps -0.6 %)
+    const unsigned blocks = capped((work + 255) / 256, pk ? ls_grids().step_pk : ls_grids().step[W - 6]);
     for (int k = 1; k < K; ++k) {
         if (pk)
             k_ls_step_pk<<<blocks, 256, 0, s>>>(op.pk32, op.dinv32, n, q4, (const float4 *)ec, (const float4 *)rv,
@@ -1337,17 +1396,20 @@ cudaError_t cheb_lockstep(const DevSolveOp &op, const double *B, double *X, int 
     if ((e = cudaMemsetAsync(done, 0, sizeof(int), s)) != cudaSuccess) return e;
     const dim3 rgrid((unsigned)nbx, (unsigned)((nv + LS_MG - 1) / LS_MG));
     k_ls_sq<<<rgrid, 256, 0, s>>>(B, n, ld, nv, bpart);
-    const dim3 tgrid((unsigned)((n + 31) / 32), (unsigned)(nvp / 32));
+    const unsigned cap_init = ls_grids().init, cap_upd = ls_grids().update;
+    const long long ntile = (long long)((n + 31) / 32) * (nvp / 32);
+    const unsigned rblocks = resid_grid(W, (long long)rgrid.x * rgrid.y);
     for (int c = 0; c <= LS_MAXC; ++c) {
         switch (W) {
-        case 6: k_ls_resid<6><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, R, nv, rpart, done); break;
-        case 7: k_ls_resid<7><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, R, nv, rpart, done); break;
-        default: k_ls_resid<8><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, R, nv, rpart, done); break;
+        case 6: k_ls_resid<6><<<rblocks, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, R, nv, rpart, nbx, done); break;
+        case 7: k_ls_resid<7><<<rblocks, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, R, nv, rpart, nbx, done); break;
+        default: k_ls_resid<8><<<rblocks, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, R, nv, rpart, nbx, done); break;
         }
         k_ls_nrm<<<(nv + NWARP - 1) / NWARP, 256, 0, s>>>(rpart, bpart, nbx, nrm, nv, done);
         k_ls_scale<<<1, 256, 0, s>>>(nrm, nv, nvp, tol, beta, sc, done, st, c, K, c ? cyc : 0.0);
         if (c == LS_MAXC) break;
-        k_ls_init<<<tgrid, 256, 0, s>>>(R, n, nv, nvp, sc, op.dinv32, (float)(1.0 / theta), rv, e0, e1, done);
+        k_ls_init<<<capped(ntile, cap_init), 256, 0, s>>>(R, n, nv, nvp, sc, op.dinv32, (float)(1.0 / theta), rv, e0,
+                                                          e1, done);
         float *ec = e1, *ep = e0;
         switch (W) {
         case 6: e = ls_steps<6>(op, n, q4, ec, ep, rv, ca, cb, K, done, s); break;
@@ -1355,7 +1417,7 @@ cudaError_t cheb_lockstep(const DevSolveOp &op, const double *B, double *X, int 
         default: e = ls_steps<8>(op, n, q4, ec, ep, rv, ca, cb, K, done, s); break;
         }
         if (e != cudaSuccess) return e;
-        k_ls_update<<<tgrid, 256, 0, s>>>(X, ld, n, nv, nvp, beta, ec, done);
+        k_ls_update<<<capped(ntile, cap_upd), 256, 0, s>>>(X, ld, n, nv, nvp, beta, ec, done);
     }
     g_kernel_launches += 1 + (LS_MAXC + 1) * 3 + LS_MAXC * (K + 1);
     return cudaGetLastError();
@@ -2100,6 +2162,7 @@ cudaError_t lsg_solve(const DevSolveOp &op, const double *B, double *X, int nv, 
     if (small_smem > LSG_SMALL_SMEM) return cudaErrorInvalidValue;
     long long launches = 0;
     const dim3 rgrid((unsigned)Lo.nbx, (unsigned)((nv + LS_MG - 1) / LS_MG));
+    const unsigned rblocks = resid_grid(W, (long long)rgrid.x * rgrid.y);
     k_lsg_levels<<<1, 32, 0, s>>>(P);
     k_ls_sq<<<rgrid, 256, 0, s>>>(B, n, ld, nv, P.bpart);
     launches += 2;
@@ -2110,9 +2173,9 @@ cudaError_t lsg_solve(const DevSolveOp &op, const double *B, double *X, int nv, 
     P.maxc = lsg_maxc;
     for (int c = 0; c <= lsg_maxc; ++c) {
         switch (W) {
-        case 6: k_ls_resid<6><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, P.R, nv, P.rpart, P.done); break;
-        case 7: k_ls_resid<7><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, P.R, nv, P.rpart, P.done); break;
-        default: k_ls_resid<8><<<rgrid, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, P.R, nv, P.rpart, P.done); break;
+        case 6: k_ls_resid<6><<<rblocks, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, P.R, nv, P.rpart, Lo.nbx, P.done); break;
+        case 7: k_ls_resid<7><<<rblocks, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, P.R, nv, P.rpart, Lo.nbx, P.done); break;
+        default: k_ls_resid<8><<<rblocks, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, P.R, nv, P.rpart, Lo.nbx, P.done); break;
         }
         k_ls_nrm<<<(nv + NWARP - 1) / NWARP, 256, 0, s>>>(P.rpart, P.bpart, Lo.nbx, P.nrm, nv, P.done);
         k_lsg_begin<<<1, 256, 0, s>>>(P, c);
@@ -2347,5 +2410,7 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     }
     return cudaGetLastError();
 }
+
+void lockstep_prepare() { (void)ls_grids(); }
 
 }  // namespace phg
