@@ -281,7 +281,7 @@ def run_ours(args, ws, rank, local):
                     bbv.calc_batch(U, zB, zB, out=U, stream=stream)
                     stream.synchronize()
                     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                    nb = 3
+                    nb = 10   # steps per timing (the inputs exceed L2 at these sizes)
                     flush.zero_()
                     e0.record(stream)
                     for _ in range(nb):
