@@ -211,7 +211,12 @@ bool load_mesh_text(FILE *f, Mesh &m, std::string &err) {
         double uv[8];
         for (double &d : uv) d = NAN;
         int nuv = 0; bool have_xyz = false;
-        for (char *tok = std::strtok(s, ";"); tok; tok = std::strtok(nullptr, ";")) {
+        // the ';'-separated fields, empty ones skipped (strtok's splitting,
+        // without its hidden state: several threads may load meshes at once)
+        for (char *tok = s, *semi; tok; tok = semi ? semi + 1 : nullptr) {
+            semi = std::strchr(tok, ';');
+            if (semi) *semi = '\0';
+            if (!*tok) continue;
             double a = 0, b = 0, c = 0;
             int k = std::sscanf(tok, "%lf%lf%lf", &a, &b, &c);
             if (k == 3) { xyz[0] = a; xyz[1] = b; xyz[2] = c; have_xyz = true; }

@@ -101,6 +101,33 @@ def test_load_text_roundtrip(tmp_path):
     assert np.array_equal(m.csr("lapl")[2], m2.csr("lapl")[2])
 
 
+def test_concurrent_text_loads(tmp_path):
+    """Mesh files parse correctly when several threads load at once (ctypes
+    releases the GIL during the call; the parser keeps no shared state)."""
+    import threading
+    m = phelm.Mesh.sphere(4)
+    path = str(tmp_path / "ss4.txt")
+    write_reference_text(path, m)
+    want = m.arrays()
+    bad = []
+
+    def work():
+        for _ in range(3):
+            try:
+                got = phelm.Mesh.load(path).arrays()
+                if not all(np.array_equal(want[k], got[k], equal_nan=True) for k in want):
+                    bad.append("arrays differ")
+            except phelm.PhgError as e:
+                bad.append(str(e))
+
+    threads = [threading.Thread(target=work) for _ in range(8)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(300)
+    assert not bad, bad[:3]
+
+
 def test_errors():
     with pytest.raises(phelm.PhgError) as e:
         phelm.Mesh.sphere(0)
