@@ -4,7 +4,8 @@
 // then the level cache: a round trip, and the reader on damaged files --
 // truncated payloads and flipped bytes, each with its checksum recomputed so
 // that the parser itself sees them; what it accepts goes through the
-// assembly and the multigrid build.  Built and run by
+// assembly and the multigrid build -- and the mesh text parser on truncated
+// and edited files, an accepted mesh going through the assembly.  Built and run by
 // tests/test_sanitizers.py (argument: a scratch directory); exits non-zero on
 // the first inconsistency (the sanitizers abort on their own findings).
 #include <cmath>
@@ -157,6 +158,54 @@ static int cache_checks(const std::string &dir) {
     return bad;
 }
 
+// the mesh text parser on damaged files: truncations and single-character
+// edits of a level-2 mesh; an accepted mesh goes through the assembly
+static int text_checks(const std::string &dir) {
+    int bad = 0;
+    std::string err;
+    Mesh m;
+    generate_sphere(2, m, err);
+    const std::string good = dir + "/level2.txt", path = dir + "/damaged.txt";
+    FILE *f = fopen(good.c_str(), "wb");
+    bad += check(f && save_mesh_text(f, m), "save_mesh_text", 2);
+    if (f) fclose(f);
+    const std::vector<unsigned char> text = read_all(good);
+    bad += check(text.size() > 1000, "mesh text size", 2);
+    if (bad) return bad;
+    auto try_load = [&](const std::vector<unsigned char> &t) {
+        FILE *g = fopen(path.c_str(), "wb");
+        if (!t.empty()) fwrite(t.data(), 1, t.size(), g);
+        fclose(g);
+        g = fopen(path.c_str(), "rb");
+        Mesh back;
+        const bool ok = load_mesh_text(g, back, err);
+        fclose(g);
+        if (ok) {
+            SphereOps ops;
+            assemble_sphere(back, ops);
+        }
+        return ok;
+    };
+    bad += check(try_load(text), "intact mesh text rejected", 2);
+    const size_t n = text.size();
+    int tried = 0;
+    for (size_t k = 0; k < 100; ++k) {   // truncations
+        try_load(std::vector<unsigned char>(text.begin(), text.begin() + (n * k) / 100));
+        ++tried;
+    }
+    const char edits[] = "0123456789;; -\nex";
+    uint64_t x = 2463534242ull;
+    for (int k = 0; k < 400; ++k) {      // one character replaced
+        x ^= x << 13; x ^= x >> 7; x ^= x << 17;
+        std::vector<unsigned char> t = text;
+        t[(size_t)(x % n)] = (unsigned char)edits[(x >> 32) % (sizeof edits - 1)];
+        try_load(t);
+        ++tried;
+    }
+    printf("text: %d damaged mesh files read\n", tried);
+    return bad;
+}
+
 int main(int argc, char **argv) {
     int bad = 0;
     for (int level = 1; level <= 4; ++level) {
@@ -202,6 +251,7 @@ int main(int argc, char **argv) {
         fclose(g);
     }
     bad += cache_checks(argc > 1 ? argv[1] : ".");
+    bad += text_checks(argc > 1 ? argv[1] : ".");
     if (!bad) printf("host code clean at levels 1-4\n");
     return bad ? 1 : 0;
 }

@@ -1,7 +1,7 @@
 """The host code and the CPU oracle under AddressSanitizer and
 UndefinedBehaviorSanitizer (no GPU): tests/sanitize/host_driver.cpp runs the
-library's mesh generation, text I/O and assembly at levels 1-4 and the level
-cache reader on damaged files,
+library's mesh generation, text I/O and assembly at levels 1-4, and the level
+cache reader and the mesh text parser on damaged files,
 tests/sanitize/oracle_driver.c the oracle's solves and steps at levels 2-3.
 Each is compiled here with -fsanitize=address,undefined and must exit 0 with
 no sanitizer report."""
@@ -46,7 +46,7 @@ def test_host_code(tmp_path):
            os.path.join(HERE, "sanitize", "host_driver.cpp"), os.path.join(csrc, "phg_mesh.cpp"),
            os.path.join(csrc, "phg_assemble.cpp"), os.path.join(csrc, "phg_cache.cpp"), "-o", exe]
     report = run_checked(cmd, exe, str(tmp_path))
-    assert "host code clean" in report and "damaged files read" in report
+    assert "host code clean" in report and "damaged files read" in report and "damaged mesh files read" in report
 
 
 def test_oracle(tmp_path):
