@@ -12,11 +12,14 @@
 // range, operator or multigrid dimensions that do not fit the mesh): the
 // checksum only catches damage, and every index read here is later
 // dereferenced by the host assembly or the device kernels.
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
+
+#include <unistd.h>
 
 #include "phg_host.hpp"
 
@@ -199,8 +202,13 @@ bool save_level_cache(const char *path, const Mesh &m, const SphereOps &ops, con
         }
         w.vec(mg->coarse_inv);
     }
-    // write to a temporary name and rename: readers never see a partial file
-    const std::string tmp = std::string(path) + ".tmp";
+    // write to a temporary name of this writer (process and call) and rename:
+    // readers never see a partial file, and processes that build the same
+    // level at once each write their own copy (the last rename wins; the
+    // copies are identical)
+    static std::atomic<unsigned> seq{0};
+    const std::string tmp = std::string(path) + "." + std::to_string((long)getpid()) + "." +
+                            std::to_string(seq.fetch_add(1)) + ".tmp";
     FILE *f = std::fopen(tmp.c_str(), "wb");
     if (!f) return false;
     const int32_t level = m.level;

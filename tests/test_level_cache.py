@@ -148,6 +148,42 @@ def test_inconsistent_file_is_rebuilt(cache, edit):
     assert same(fresh, snapshot(3))
 
 
+WRITER = r"""
+import sys
+sys.path.insert(0, sys.argv[1])
+from mke_gb300 import phelm
+phelm.cache_dir(sys.argv[2])
+m = phelm.Mesh.sphere(4)
+print(m.size)
+"""
+
+
+def test_processes_building_one_level_at_once(tmp_path):
+    """Processes that build the same level into one cache directory at the
+    same time each write a temporary file of their own and rename it: one
+    valid file remains, no temporary is left behind."""
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    procs = [subprocess.Popen([sys.executable, "-c", WRITER, root, str(tmp_path)], stdout=subprocess.PIPE,
+                              stderr=subprocess.PIPE, text=True) for _ in range(4)]
+    for p in procs:
+        out, err = p.communicate(timeout=300)
+        assert p.returncode == 0, err[-2000:]
+        assert out.strip() == "2562"
+    assert sorted(f.name for f in tmp_path.iterdir()) == ["phelm_level4.cache"]
+    phelm.cache_dir(None)
+    fresh = snapshot(4)
+    phelm.cache_dir(str(tmp_path))
+    try:
+        inode = (tmp_path / "phelm_level4.cache").stat().st_ino
+        assert same(fresh, snapshot(4))                            # read from the file
+        assert (tmp_path / "phelm_level4.cache").stat().st_ino == inode   # accepted: a rewrite renames a new file
+    finally:
+        phelm.cache_dir(None)
+        gc.collect()
+
+
 def test_unwritable_directory_is_not_an_error(tmp_path):
     missing = tmp_path / "does" / "not" / "exist"
     phelm.cache_dir(str(missing))
