@@ -126,6 +126,34 @@ void orc_jacobian_calc1(orc_ops *o, double *ans, const double *u, const double *
 	free(p1);
 }
 
+/* SphereJacobian::calc1t (src/sjacobian.cpp:463-468 with calc2t :404-408):
+ * -J(u, v) on the inner points, boundary values bnd */
+void orc_jacobian_calc1t(orc_ops *o, double *ans, const double *u, const double *v, const double *bnd)
+{
+	int rs = o->m->rs;
+	double *p1 = VEC(rs);
+	orc_jacobian_calc2(o, p1, u, v);
+	for (int i = 0; i < rs; ++i) p1[i] = p1[i] * -1.0;
+	orc_p2u(o->m, ans, p1, bnd);
+	free(p1);
+}
+
+/* SphereJacobian::calc2_diff_x / calc2_diff_cos_y (src/sjacobian.cpp:364-402):
+ * M_J^{-1} (D1 v_in + D1_bnd v_bnd) and M_J^{-1} (D2cos v_in + D2cos_bnd v_bnd) */
+static void jac_diff(orc_ops *o, orc_csr *D, orc_csr *Db, double *ans, const double *v)
+{
+	const orc_mesh *m = o->m;
+	double *vi = VEC(m->rs), *vb = VEC(m->os);
+	orc_u2p(m, vi, v);
+	orc_proj_bnd(m, vb, v);
+	jderiv(o, D, Db, ans, vi, vb);
+	free(vi); free(vb);
+}
+
+void orc_jacobian_diff_x(orc_ops *o, double *ans, const double *v) { jac_diff(o, &o->d1, &o->d1b, ans, v); }
+
+void orc_jacobian_diff_cos_y(orc_ops *o, double *ans, const double *v) { jac_diff(o, &o->d2c, &o->d2cb, ans, v); }
+
 double orc_scalar(orc_ops *o, const double *u, const double *v)
 {
 	int sz = o->m->V;

@@ -115,6 +115,10 @@ void orc_laplace_solve(orc_ops *o, double *ans, const double *F, const double *b
 void orc_jacobian_calc2(orc_ops *o, double *ans, const double *u, const double *v);
 void orc_jacobian_calc1(orc_ops *o, double *ans, const double *u, const double *v,
                         const double *bnd);
+void orc_jacobian_calc1t(orc_ops *o, double *ans, const double *u, const double *v,
+                         const double *bnd);
+void orc_jacobian_diff_x(orc_ops *o, double *ans, const double *v);
+void orc_jacobian_diff_cos_y(orc_ops *o, double *ans, const double *v);
 double orc_norm(orc_ops *o, const double *u);
 double orc_dist(orc_ops *o, const double *u, const double *v);
 double orc_scalar(orc_ops *o, const double *u, const double *v);

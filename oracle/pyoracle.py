@@ -86,6 +86,9 @@ def lib():
         L.orc_laplace_solve.argtypes = [C.POINTER(Ops), _dp, _dp, _dp]
         L.orc_jacobian_calc2.argtypes = [C.POINTER(Ops), _dp, _dp, _dp]
         L.orc_jacobian_calc1.argtypes = [C.POINTER(Ops), _dp, _dp, _dp, _dp]
+        L.orc_jacobian_calc1t.argtypes = [C.POINTER(Ops), _dp, _dp, _dp, _dp]
+        L.orc_jacobian_diff_x.argtypes = [C.POINTER(Ops), _dp, _dp]
+        L.orc_jacobian_diff_cos_y.argtypes = [C.POINTER(Ops), _dp, _dp]
         for f in ("orc_norm",):
             getattr(L, f).argtypes = [C.POINTER(Ops), _dp]
             getattr(L, f).restype = C.c_double
@@ -178,6 +181,22 @@ class Oracle:
         out = np.zeros(self.V)
         lib().orc_jacobian_calc1(C.byref(self.ops), _p(out), _p(_f8(u)), _p(_f8(v)),
                                  _p(None if bnd is None else _f8(bnd)))
+        return out
+
+    def jacobian_calc1t(self, u, v, bnd=None):
+        out = np.zeros(self.V)
+        lib().orc_jacobian_calc1t(C.byref(self.ops), _p(out), _p(_f8(u)), _p(_f8(v)),
+                                  _p(None if bnd is None else _f8(bnd)))
+        return out
+
+    def jacobian_diff_x(self, v):
+        out = np.zeros(self.rs)
+        lib().orc_jacobian_diff_x(C.byref(self.ops), _p(out), _p(_f8(v)))
+        return out
+
+    def jacobian_diff_cos_y(self, v):
+        out = np.zeros(self.rs)
+        lib().orc_jacobian_diff_cos_y(C.byref(self.ops), _p(out), _p(_f8(v)))
         return out
 
     def norm(self, u):

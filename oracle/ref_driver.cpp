@@ -117,6 +117,103 @@ static void dump_csr(const std::string &dir, const std::string &name, const M &A
 
 static double cor_zero(double, double) { return 0.0; }
 static double cor_sin(double phi, double) { return sin(phi); }
+/* a smooth, time-dependent forcing for the boundary + forcing run (any
+ * function of the reference's rp_t shape would do) */
+static double rp_test(double phi, double lambda, double t, double mu, double sigma)
+{
+	(void)mu; (void)sigma;
+	return 0.05 * cos(phi) * sin(2.0 * lambda + 40.0 * t) + 0.02 * sin(phi);
+}
+
+/* The analytic fields of tests/manufactured.py (same formulas, see there for
+ * their derivation), for the reference's own accuracy checks run on the
+ * same inputs as the GPU tests. */
+static double mf_lap_u(double phi, double lam)
+{
+	double x = cos(phi) * cos(lam), z = sin(phi);
+	return 0.5 * (x - 1.0) * (x - 1.0) + (x - z) * (x - z) + 2.0 * (z - 3.0) * (z - 3.0);
+}
+static double mf_lap_f(double phi, double lam)
+{
+	double x = cos(phi) * cos(lam), z = sin(phi);
+	return 9.0 - 9.0 * x * x + 12.0 * x * z - 18.0 * z * z + 2.0 * x + 24.0 * z;
+}
+static double mf_jac_f1(double phi, double lam) { return sin(phi) * sin(lam); }
+static double mf_jac_f2(double phi, double lam) { return cos(phi) * cos(lam); }
+static double mf_jac_an(double phi, double lam)
+{
+	double c = cos(phi), s = sin(phi);
+	return (-s * s * cos(lam) * cos(lam) + c * c * sin(lam) * sin(lam)) / c;
+}
+static double mf_bv_psi(double phi, double lam, double t)
+{
+	double c = cos(phi);
+	return phi * c * c * c * c * sin(lam + t);
+}
+static double mf_bv_forcing(double phi, double lam, double t, double mu, double sigma)
+{
+	double c = cos(phi), s = sin(phi), S = sin(lam + t), C = cos(lam + t);
+	double g = phi * c * c * c * c, g1 = c * c * c * c - 4.0 * phi * c * c * c * s;
+	double w = -9.0 * c * c * c * s + 15.0 * phi * c * c - 20.0 * phi * c * c * c * c;
+	double w1 = 27.0 * c * c * s * s - 29.0 * c * c * c * c + 15.0 * c * c - 30.0 * phi * c * s
+	            + 80.0 * phi * c * c * c * s;
+	double w2 = -54.0 * c * s * s * s + 250.0 * c * c * c * s - 60.0 * c * s - 30.0 * phi * c * c
+	            + 30.0 * phi * s * s - 240.0 * phi * c * c * s * s + 80.0 * phi * c * c * c * c;
+	double jac = C * S * (g * w1 - g1 * w) / c;
+	double lap_w = w2 - tan(phi) * w1 - w / (c * c);
+	return w * C + jac + sigma * w * S - mu * lap_w * S;
+}
+
+/* examples/test_slaplace.cpp:100-199, examples/test_barvortex.cpp:57-105 and
+ * 488-559 on the fields above; writes out_pin_* */
+static void run_pins(const Mesh &m, const std::string &dir, bool with_bv)
+{
+	int sz = (int)m.ps.size(), os = (int)m.outer.size();
+	std::vector<double> U(sz), LU(sz), LU1(sz), Ans(sz), B1(std::max(os, 1)), B2(std::max(os, 1));
+	proj(&U[0], m, mf_lap_u);
+	proj(&LU[0], m, mf_lap_f);
+	proj_bnd(&B1[0], m, mf_lap_f);
+	proj_bnd(&B2[0], m, mf_lap_u);
+	SphereLaplace<double> l(m);
+	SphereNorm<double> nr(m);
+	std::vector<double> e;
+	l.solve(&Ans[0], &LU[0], &B2[0]);
+	e.push_back(nr.dist(&Ans[0], &U[0]));            // L1: invert
+	l.calc1(&LU1[0], &U[0], &B1[0]);
+	e.push_back(nr.dist(&LU[0], &LU1[0]));           // L2: laplace
+	l.solve(&LU[0], &LU1[0], &B2[0]);
+	e.push_back(nr.dist(&U[0], &LU[0]));             // L3: round trip
+	wf8(dir, "out_pin_slaplace", e);
+
+	SphereJacobian j(m);
+	std::vector<double> F1(sz), F2(sz), a1(sz), r1(sz), bj(std::max(os, 1));
+	proj(&F1[0], m, mf_jac_f1);
+	proj(&F2[0], m, mf_jac_f2);
+	proj(&r1[0], m, mf_jac_an);
+	proj_bnd(&bj[0], m, mf_jac_an);
+	j.calc1(&a1[0], &F1[0], &F2[0], &bj[0]);
+	std::vector<double> ej(1, phelm::dist(&a1[0], &r1[0], m, sphere_scalar_cb, (void *)0));
+	wf8(dir, "out_pin_jacobian", ej);
+
+	if (!with_bv) return;
+	BarVortexConf conf;
+	memset(&conf, 0, sizeof(conf));
+	conf.tau = 0.001; conf.sigma = 1.6e-2; conf.mu = 8e-5; conf.k1 = 1.0; conf.k2 = 1.0; conf.theta = 0.5;
+	conf.rp = mf_bv_forcing;
+	conf.coriolis = cor_zero;
+	orc_ref_bv_max_iter = 1000;
+	SBarVortex bv(m, conf);
+	std::vector<double> u(sz), bu(std::max(os, 1), 0.0), bw(std::max(os, 1), 0.0), an(sz);
+	for (int i = 0; i < sz; ++i) u[i] = mf_bv_psi(m.ps[i].x(), m.ps[i].y(), 0.0);
+	double t = 0.0, T = 0.01;
+	while (t < T) {
+		bv.calc(&u[0], &u[0], &bu[0], &bw[0], t);
+		t += conf.tau;
+	}
+	for (int i = 0; i < sz; ++i) an[i] = mf_bv_psi(m.ps[i].x(), m.ps[i].y(), t);
+	std::vector<double> eb(1, bv.dist(&u[0], &an[0]));
+	wf8(dir, "out_pin_barvortex", eb);
+}
 
 int main(int argc, char **argv)
 {
@@ -194,6 +291,9 @@ int main(int argc, char **argv)
 			ns.push_back(nrm.scalar(&u[0], &v[0]));
 			j.calc2(&b[0], &u[0], &v[0]); wf8(dir, "out_jac_calc2", b);
 			j.calc1(&a[0], &u[0], &v[0], &bnd[0]); wf8(dir, "out_jac_calc1", a);
+			j.calc1t(&a[0], &u[0], &v[0], &bnd[0]); wf8(dir, "out_jac_calc1t", a);
+			j.calc2_diff_x(&b[0], &u[0]); wf8(dir, "out_jac_diff_x", b);
+			j.calc2_diff_cos_y(&b[0], &u[0]); wf8(dir, "out_jac_diff_cos_y", b);
 		}
 		wf8(dir, "out_norms", ns);
 		// the text output routines (src/phelm.cpp:160-321), default coordinates
@@ -225,6 +325,28 @@ int main(int argc, char **argv)
 			if (s == 0) wf8(dir, "out_bv_step1", st);
 		}
 		wf8(dir, "out_bv_final", st);
+		if (get("bv_bf", 0)) {
+			// two steps with non-zero pole values (bnd_u = in_bnd, bnd_w = -2 in_bnd)
+			// and the time-dependent forcing rp_test at t = 0 and t = tau; the
+			// forcing values at the points are written for the callers
+			BarVortexConf cf = conf;
+			cf.rp = rp_test;
+			SBarVortex bvf(m, cf);
+			std::vector<double> sf(u), fu(std::max(os, 1)), fw(std::max(os, 1)), f0(sz), f1(sz);
+			for (int k = 0; k < os; ++k) { fu[k] = bnd[k]; fw[k] = -2.0 * bnd[k]; }
+			for (int i = 0; i < sz; ++i) {
+				f0[i] = rp_test(m.ps[i].x(), m.ps[i].y(), 0.0, cf.mu, cf.sigma);
+				f1[i] = rp_test(m.ps[i].x(), m.ps[i].y(), cf.tau, cf.mu, cf.sigma);
+			}
+			wf8(dir, "out_bv_bf_forcing0", f0);
+			wf8(dir, "out_bv_bf_forcing1", f1);
+			wf8(dir, "out_bv_bf_bnd_u", fu);
+			wf8(dir, "out_bv_bf_bnd_w", fw);
+			bvf.calc(&sf[0], &sf[0], &fu[0], &fw[0], 0.0);
+			wf8(dir, "out_bv_bf_step1", sf);
+			bvf.calc(&sf[0], &sf[0], &fu[0], &fw[0], cf.tau);
+			wf8(dir, "out_bv_bf_step2", sf);
+		}
 		if (have_v && get("bv_lin", 0)) {
 			// linearised step around z = u, its inverse and its adjoint, applied to v
 			std::vector<double> r(sz, 0.0);
@@ -235,6 +357,8 @@ int main(int argc, char **argv)
 			bv.calc_LT(&r[0], &v[0], &u[0], &bu[0], &bw[0], 0.0); wf8(dir, "out_bv_LT", r);
 		}
 	}
+
+	if (get("pins", 0)) run_pins(m, dir, get("pins", 0) > 1);
 
 	int bc_steps = (int)get("bc_steps", 0);
 	if (bc_steps > 0 && have_u && have_v) {

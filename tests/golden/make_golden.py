@@ -66,7 +66,8 @@ def run_level(ref_bin, level, work, bv_steps=0, bc_steps=0, seed=1234, extra=())
     np.save(os.path.join(out, "in_v.npy"), v)
     np.save(os.path.join(out, "in_bnd.npy"), u[bnd == 1].copy())
     args = [os.path.join(ref_bin, "ref_driver"), mesh_txt, out,
-            f"bv_steps={bv_steps}", f"bc_steps={bc_steps}", "bv_iters=3", "bc_iters=3", "bv_lin=1", "bc_lin=1", *extra]
+            f"bv_steps={bv_steps}", f"bc_steps={bc_steps}", "bv_iters=3", "bc_iters=3", "bv_lin=1", "bc_lin=1",
+            "bv_bf=1", *extra]
     subprocess.run(args, check=True, stderr=subprocess.DEVNULL)
     return out
 
@@ -109,6 +110,20 @@ def main():
                 keep["pattern_" + op] = np.array(digest(d[op + "_ptr"], d[op + "_col"]))
             np.savez_compressed(os.path.join(HERE, f"ref_L{level}.npz"), **keep)
             print("level", level, "arrays", len(keep))
+        # the reference's accuracy checks on the analytic fields of tests/manufactured.py
+        pins = {}
+        for level in (3, 4, 5):
+            mesh_txt = os.path.join(work, f"ss{level}.txt")
+            out = os.path.join(work, f"pins{level}")
+            os.makedirs(out, exist_ok=True)
+            subprocess.run([os.path.join(ref_bin, "ref_driver"), mesh_txt, out, f"pins={1 if level == 3 else 2}"],
+                           check=True, stderr=subprocess.DEVNULL)
+            for k in ("slaplace", "jacobian", "barvortex"):
+                f = os.path.join(out, f"out_pin_{k}.npy")
+                if os.path.exists(f):
+                    pins[f"{k}_L{level}"] = np.load(f)
+        np.savez_compressed(os.path.join(HERE, "ref_pins.npz"), **pins)
+        print("accuracy pins", {k: v.tolist() for k, v in pins.items()})
         if a.traj:
             level = 6
             mesh_txt = os.path.join(work, "ss6.txt")

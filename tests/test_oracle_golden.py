@@ -160,3 +160,34 @@ def test_baroclin_linear_steps(golden, level):
         a, b = o.bc_linear(bc, which, g["in_v"], g["in_u"], g["in_u"], g["in_v"], z)
         assert np.array_equal(bits(a), bits(g[f"out_bc_{which}_u1"])), which
         assert np.array_equal(bits(b), bits(g[f"out_bc_{which}_u2"])), which
+
+
+@pytest.mark.parametrize("level", [1, 2, 3, 4, 5])
+def test_jacobian_adjoint_and_derivatives(golden, level):
+    """SphereJacobian::calc1t, calc2_diff_x and calc2_diff_cos_y
+    (src/sjacobian.cpp:364-402, 463-468): the restatement returns the
+    reference's bits."""
+    g = golden(f"ref_L{level}.npz")
+    o = po.Oracle(level)
+    u, v, bnd = g["in_u"], g["in_v"], g["in_bnd"]
+    assert np.array_equal(bits(o.jacobian_calc1t(u, v, bnd)), bits(g["out_jac_calc1t"]))
+    assert np.array_equal(bits(o.jacobian_diff_x(u)), bits(g["out_jac_diff_x"]))
+    assert np.array_equal(bits(o.jacobian_diff_cos_y(u)), bits(g["out_jac_diff_cos_y"]))
+
+
+@pytest.mark.parametrize("level", [1, 2, 3, 4])
+def test_barvortex_boundary_and_forcing(golden, level):
+    """Two BarVortex::calc steps with non-zero pole values (bnd_u, bnd_w) and a
+    time-dependent forcing evaluated by the reference at t = 0 and t = tau
+    (examples/barvortex_impl.h:171-310): the restatement returns the
+    reference's bits."""
+    g = golden(f"ref_L{level}.npz")
+    o = po.Oracle(level)
+    lat = o.mesh_arrays()["uv"].reshape(-1, 4, 2)[:, 0, 0]
+    bv = o.barvortex(max_iter=3, coriolis=np.sin(lat))
+    bu, bw = g["out_bv_bf_bnd_u"], g["out_bv_bf_bnd_w"]
+    assert np.all(bu != 0) and np.all(bw != 0)
+    s1 = o.bv_step(bv, g["in_u"], bu, bw, g["out_bv_bf_forcing0"])
+    assert np.array_equal(bits(s1), bits(g["out_bv_bf_step1"]))
+    s2 = o.bv_step(bv, s1, bu, bw, g["out_bv_bf_forcing1"])
+    assert np.array_equal(bits(s2), bits(g["out_bv_bf_step2"]))
