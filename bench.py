@@ -297,13 +297,18 @@ def run_ours(args, ws, rank, local):
                     bbv.run(U, nb, zB, zB, stream=stream)
                     e1.record(stream)
                 stream.synchronize()
-                bbv.last_stats()
+                bst = bbv.last_stats()
                 graph_ms = e0.elapsed_time(e1) / nb
                 bms = min(eager_ms, graph_ms)
                 row[name] = {"member_steps_per_s": B * 1000.0 / bms, "ms_per_step": bms, "eager_ms": eager_ms,
-                             "graph_ms": graph_ms}
+                             "graph_ms": graph_ms, "worst_relres": bst["worst_relres"],
+                             "state": U.cpu().numpy()}
                 del bbv, bops
             row["mixed_over_fp64"] = row["mixed"]["member_steps_per_s"] / row["fp64"]["member_steps_per_s"]
+            # the same members, the same 1 + 2 + 2 nb steps in both precisions
+            a, b = row["mixed"].pop("state"), row["fp64"].pop("state")
+            row["steps_compared"] = 3 + 2 * nb
+            row["rel_err_vs_fp64"] = float(max(np.linalg.norm(a[k] - b[k]) / np.linalg.norm(b[k]) for k in range(B)))
             batched[f"L{lvl}x{B}"] = row
 
     # two-layer baroclinic steps, level 6 (the reference's baroclin configuration)
@@ -312,12 +317,18 @@ def run_ours(args, ws, rank, local):
     # operator apply at a streaming size (level 8, 64 FP32 vectors; one FP64 vector)
     spmv = None if args.no_spmv else run_spmv(8, 64)
 
+    # BASELINE config 1: the level-3 Laplace solve to 1e-12 against the exact solution
+    lap3 = None if args.no_laplace3 else run_laplace_l3()
+
     # serving trace (the first --bench-serve-requests requests of the 10,000-request trace)
     served = None
     if not args.no_serve and args.bench_serve_requests > 0:
-        served = {"trace": f"first {args.bench_serve_requests} of 10,000 requests, Poisson arrivals at "
-                           f"{args.serve_rate:g}/s, levels 3..7, 60% Laplace solves to 1e-10, 40% 10-step "
-                           "barvortex integrations, HBM budget 150 GB, lanes opened before the trace"}
+        nreq = args.bench_serve_requests
+        served = {"trace": f"{'all' if nreq >= 10000 else 'the first %d of' % nreq} 10,000 requests, Poisson "
+                           f"arrivals at {args.serve_rate:g}/s, levels 3..7, 60% Laplace solves to 1e-10, 40% 10-step "
+                           "barvortex integrations, HBM budget 150 GB, lanes opened before the trace",
+                  "trace_short": f"{'full' if nreq >= 10000 else 'first %d of' % nreq} 10,000-request trace, "
+                                 f"{args.serve_rate:g}/s Poisson, levels 3..7, 60/40 solve/10-step"}
         for name in ("mixed", "fp64"):
             served[name] = run_serve(name, args.bench_serve_requests, args.serve_rate)
 
@@ -357,6 +368,23 @@ def run_ours(args, ws, rank, local):
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args.level, steps=1)
+        if lap3 is not None:   # config 1's error against the CPU reference algorithm's own solve
+            ref = cpu.pop("laplace_l3_solution")
+            lap3["rel_err_vs_cpu_reference_solve"] = float(np.linalg.norm(lap3.pop("solution") - ref)
+                                                           / np.linalg.norm(ref))
+        else:
+            cpu.pop("laplace_l3_solution", None)
+    if lap3 is not None:
+        lap3.pop("solution", None)
+    def r3(x):
+        return None if x is None else float(f"{x:.4g}")
+
+    roof = {"kernel": "gmres_kernel<float>", "bound": "hbm", "achieved": r3(achieved), "peak": peak, "unit": "GB/s",
+            "frac": r3(achieved / peak), "traffic": traffic,
+            "bytes_per_launch": r3(prof["bytes"] / max(prof["launches"], 1)),
+            "ms_per_launch": r3(prof["ms"] / max(prof["launches"], 1)),
+            "share_of_step": r3(prof["ms"] / (mixed["eager_ms"] * args.steps)),
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s"}
     line = {
         "metric": METRIC,
         "value": ws * 1000.0 / ms,
@@ -370,41 +398,52 @@ def run_ours(args, ws, rank, local):
         "vs_baseline": None,
         "dtype": "f32+f64",
         "data": "synthetic (seeded Rossby-Haurwitz wave 4 + spherical-harmonic noise)",
-        "config": {"workload": workload(args.level), "solve_tol": args.tol,
-                   "level": args.level, "members_per_gpu": 1, "parallelism": f"replicas x{ws}",
-                   "l2": "flushed between steps (256 MB write, not timed)"},
-        "fp64": {"value": ws * 1000.0 / ms64, "unit": "steps/s", "ms_per_step": ms64,
-                 "mixed_over_fp64": ms64 / ms, "path": fp64["path"], "eager_ms": fp64["eager_ms"],
-                 "graph_ms": fp64["graph_ms"]},
-        "step_path": {"mixed": mixed["path"], "eager_ms": mixed["eager_ms"], "graph_ms": mixed["graph_ms"],
-                      "e2e_eager_s": mixed["e2e_eager_s"], "e2e_graph_s": mixed["e2e_graph_s"]},
-        "state_rel_diff_mixed_vs_fp64": rel,
-        "batched": batched,
-        "serve": served,
-        "spmv": spmv,
-        "baroclin": baroclin,
-        "solver": {"mixed": mixed["stats"], "fp64": fp64["stats"]},
-        "autotuned": tuned or None,
-        "roofline": {"kernel": "gmres_kernel<float> (persistent multigrid-preconditioned FGMRES, the three "
-                               "Laplacian solves of a step)", "bound": "hbm", "achieved": achieved,
-                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "launches_timed": prof["launches"],
-                     "bytes_per_launch": prof["bytes"] / max(prof["launches"], 1),
-                     "ms_per_launch": prof["ms"] / max(prof["launches"], 1),
-                     "share_of_step": prof["ms"] / (mixed["eager_ms"] * args.steps),
-                     "all_solver_launches": {"launches": mixed["prof_all"]["launches"],
-                                             "share_of_step": mixed["prof_all"]["ms"] / (mixed["eager_ms"] * args.steps),
-                                             "gbs": mixed["prof_all"]["bytes"] / (mixed["prof_all"]["ms"] * 1e-3) / 1e9
-                                             if mixed["prof_all"]["ms"] > 0 else None},
-                     "note": "L2-resident working set (level-6 operators ~30 MB < 129 MB L2): the solve is bound by "
-                             "group-barrier and gather latency, not HBM; traffic = DRAM bytes per launch from ncu",
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s"},
+        "config": {"workload": workload(args.level)},
+        "solve_tol": args.tol, "parallelism": f"replicas x{ws}", "l2": "flushed between steps (256 MB write, not timed)",
+        "fp64": {"value": r3(ws * 1000.0 / ms64), "mixed_over_fp64": r3(ms64 / ms)},
+        "state_rel_diff_mixed_vs_fp64": r3(rel),
+        "batched": {k: {"mixed": r3(v["mixed"]["member_steps_per_s"]), "fp64": r3(v["fp64"]["member_steps_per_s"]),
+                        "mixed_over_fp64": r3(v["mixed_over_fp64"]), "rel_err_vs_fp64": r3(v["rel_err_vs_fp64"]),
+                        "unit": "member-steps/s"} for k, v in batched.items()} or None,
+        "serve": None if served is None else {
+            "requests": served["mixed"]["requests"], "trace": served["trace_short"],
+            **{p: {"p50_ms": r3(served[p]["p50_ms"]), "p99_ms": r3(served[p]["p99_ms"]),
+                   "req_per_s": r3(served[p]["requests_per_s"]), "errors": served[p]["errors"]}
+               for p in ("mixed", "fp64")}},
+        "spmv": None if spmv is None else {
+            "level": spmv["level"], "fp32_x64_frac_of_hbm": r3(spmv["fp32_multivector"]["frac_of_peak"]),
+            "fp32_x64_gbs": r3(spmv["fp32_multivector"]["gbs"]), "fp64_frac_of_hbm": r3(spmv["fp64_single"]["frac_of_peak"])},
+        "baroclin": None if baroclin is None else {
+            "mixed": r3(baroclin["mixed"]["steps_per_s"]), "fp64": r3(baroclin["fp64"]["steps_per_s"]),
+            "mixed_over_fp64": r3(baroclin["mixed_over_fp64"]),
+            "rel_diff": r3(baroclin[f"state_rel_diff_mixed_vs_fp64_after_{baroclin['steps']}"])},
+        "laplace_l3": None if lap3 is None else {k: (r3(v) if isinstance(v, float) else v) for k, v in lap3.items()},
+        "worst_solve_relres": r3(max(mixed["stats"]["worst_relres"], fp64["stats"]["worst_relres"])),
+        "roofline": roof,
         "e2e": {"value": replicas.whole_job_rate(args.steps, e2e, ws), "unit": "steps/s",
                 "h2d_bytes_per_step": 8 * (V + 2 * max(os_, 1)), "d2h_bytes_per_step": 8 * V},
         "gpu_launches": mixed["launches"],
         "clocks": mixed["clocks"],
         "cpu_baseline": cpu,
     }
+    # everything else (per-path timings, per-level serving, tuned shapes) goes to a side file
+    detail = {"fp64": {"ms_per_step": ms64, "path": fp64["path"], "eager_ms": fp64["eager_ms"],
+                       "graph_ms": fp64["graph_ms"]},
+              "step_path": {"mixed": mixed["path"], "eager_ms": mixed["eager_ms"], "graph_ms": mixed["graph_ms"],
+                            "e2e_eager_s": mixed["e2e_eager_s"], "e2e_graph_s": mixed["e2e_graph_s"]},
+              "batched": batched, "serve": served, "spmv": spmv, "baroclin": baroclin,
+              "solver": {"mixed": mixed["stats"], "fp64": fp64["stats"]}, "autotuned": tuned or None,
+              "roofline_all_solver_launches": {
+                  "launches": mixed["prof_all"]["launches"],
+                  "share_of_step": mixed["prof_all"]["ms"] / (mixed["eager_ms"] * args.steps),
+                  "gbs": mixed["prof_all"]["bytes"] / (mixed["prof_all"]["ms"] * 1e-3) / 1e9
+                  if mixed["prof_all"]["ms"] > 0 else None}}
+    try:
+        os.makedirs(os.path.join(HERE, "gpurun_out"), exist_ok=True)
+        with open(os.path.join(HERE, "gpurun_out", "bench_detail.json"), "w") as f:
+            json.dump(detail, f, indent=1, default=float)
+    except OSError:
+        pass
     print(json.dumps(line))
     replicas.finish()
     return line
@@ -430,10 +469,16 @@ THREAD_NOTE = ("OpenMP over the host cores in the port's parallel loops (assembl
 
 
 def cpu_baseline(level, steps=1):
-    """The oracle (C restatement of the reference algorithm) on the host."""
+    """The oracle (C restatement of the reference algorithm) on the host:
+    timed steps of the bench workload, and (untimed) the level-3 Laplace
+    solve of the accuracy leg, the CPU reference answer it is compared with."""
     sys.path.insert(0, os.path.join(HERE, "oracle"))
     import pyoracle as po
     from mke_gb300 import fields
+    o3 = po.Oracle(3)
+    uv3 = o3.mesh_arrays()["uv"].reshape(-1, 4, 2)
+    ustar, f = fields.laplace_problem(uv3[:, 0, 0], uv3[:, 0, 1], seed=SEED)
+    ref3 = o3.laplace_solve(f, ustar[o3.mesh_arrays()["bnd"] == 1])
     o = po.Oracle(level)
     uv = o.mesh_arrays()["uv"].reshape(-1, 4, 2)
     lat, lon = uv[:, 0, 0], uv[:, 0, 1]
@@ -446,14 +491,15 @@ def cpu_baseline(level, steps=1):
         s = o.bv_step(bv, s, z, z)
     dt = time.perf_counter() - t0
     return {"value": steps / dt, "unit": "steps/s", "cores": host_threads(), "kind": "port",
-            "sample": f"{steps} step(s) of the level-{level} workload after setup (solves by GMRES+ILU(0) to 1e-13); "
-                      + THREAD_NOTE}
+            "sample": f"{steps} step(s) of the level-{level} workload after setup; OpenMP loops, sequential "
+                      "GMRES+ILU(0) solves to 1e-13",
+            "laplace_l3_solution": ref3}
 
 
 def run_reference(args, ws, rank):
     if rank != 0:
         return
-    steps = max(1, min(args.steps, 3))
+    steps = max(1, args.steps)   # about 7 s a step at level 6 on 16 Arm cores: 20 steps ~2.5 min
     warm = min(args.warmup, 1)
     sys.path.insert(0, os.path.join(HERE, "oracle"))
     import pyoracle as po
@@ -480,10 +526,45 @@ def run_reference(args, ws, rank):
         "value": v, "unit": "steps/s", "n_gpus": ws, "steps": steps, "warmup": warm,
         "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded Rossby-Haurwitz wave 4 + spherical-harmonic noise)",
-        "config": {"workload": workload(args.level), "level": args.level, "members_per_gpu": 1},
+        "config": {"workload": workload(args.level)},
         "cpu_baseline": {"value": v, "unit": "steps/s", "cores": host_threads(), "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
+
+
+def run_laplace_l3(reps: int = 20):
+    """BASELINE config 1: the Laplace solve on the level-3 sphere (642 points).
+    u* = sum of c_lm Y_lm (l = 1..6, c ~ N(0, 1), seeded; l = 0 dropped, so the
+    mean is removed), f = Laplacian of u* (exact: -l(l+1) per degree), the
+    boundary (south pole) value u*(pole).  FP64 handle, FGMRES(30) to a 1e-12
+    relative residual.  Reports iterations, the final residual, the error
+    against u* (the discretisation error, O(h^2)) and the solve time."""
+    import torch
+    from mke_gb300 import fields, phelm
+    m = phelm.Mesh.sphere(3)
+    lat, lon = m.latlon()
+    ustar, f = fields.laplace_problem(lat, lon, seed=SEED)
+    bnd = ustar[m.arrays()["bnd"] == 1].copy()
+    ops = phelm.Operators(m, phelm.PHG_FP64, restart=30, tol=1e-12)
+    L = phelm.SphereLaplace(ops)
+    x = L.solve(f, bnd)
+    st = ops.last_solve()
+    dev = torch.device("cuda")
+    df, db = torch.tensor(f, device=dev), torch.tensor(bnd, device=dev)
+    out = torch.empty_like(df)
+    s = torch.cuda.Stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(s):
+        L.solve(df, db, out=out, stream=s)
+        e0.record(s)
+        for _ in range(reps):
+            L.solve(df, db, out=out, stream=s)
+        e1.record(s)
+    s.synchronize()
+    ops.check(s)
+    return {"level": 3, "points": m.size, "iters": st["iters"], "relres": st["relres"],
+            "rel_err_vs_exact": float(np.linalg.norm(x - ustar) / np.linalg.norm(ustar)),
+            "ms_per_solve": e0.elapsed_time(e1) / reps, "solution": x}
 
 
 def run_serve(precision: str, n: int, rate: float, levels=(3, 4, 5, 6, 7)):
@@ -733,6 +814,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving trace")
     ap.add_argument("--no-spmv", action="store_true", help="skip the streaming operator-apply measurement")
     ap.add_argument("--no-baroclin", action="store_true", help="skip the two-layer baroclinic steps")
+    ap.add_argument("--no-laplace3", action="store_true", help="skip the level-3 Laplace solve accuracy leg")
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--members", type=int, default=16, help="ensemble members for --case batch")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])

@@ -132,6 +132,12 @@ int phg_ops_set_solver(phg_ops o, int restart, double tol, int max_iter);
  * at the same time on different streams then share the GPU instead of
  * queueing behind each other.  No reference counterpart. */
 int phg_ops_set_sms(phg_ops o, int max_sms);
+/* Bounded waits (no reference counterpart): a group-barrier wait inside the
+ * persistent solver kernels of this handle gives up after `cycles` GPU clock
+ * cycles (0 = the default, about one second); the launch then ends early and
+ * the call (or the next phg_ops_check) returns PHG_ERR_TIMEOUT.  The handle
+ * stays usable. */
+int phg_ops_set_wait_limit(phg_ops o, long long cycles);
 /* Statistics of the last solve on this handle (host memory). */
 int phg_ops_last_solve(phg_ops o, int *iters, int *cycles, double *relres);
 /* phelm::Solver::mult_vector (src/impl/slaplace_impl.h:109-113,
@@ -214,19 +220,41 @@ int phg_laplace_solve_batch(phg_ops o, int nv, double *ans, const double *F, con
  * let a library allocate device memory (memory owned by their own pool or
  * allocator, or loops where the device synchronisation of a cudaMalloc would
  * stall their other streams).  It calls no cudaMalloc/cudaFree: its
- * right-hand side and GMRES workspace live in one fixed 16 MiB device array
+ * right-hand side and solver workspace live in one fixed 16 MiB device array
  * inside the library (held by every GPU that loads the library until the
- * process exits), enough for up to level-6 meshes (40,961 inner points) at
- * restart 30 in FP64; larger needs are rejected with PHG_ERR_ARG.
+ * process exits).  That holds the default Chebyshev mass solve up to level 7
+ * in FP64 (163,841 inner points), or a GMRES(30) mass solve up to level 6;
+ * larger needs are rejected with PHG_ERR_ARG.
  * ans[rs] and F[V] must be device pointers; the call only enqueues work on
- * `stream`.  The first call on each device looks up the array's device
- * address (make it before any stream capture).  All calls share the array:
- * calls that overlap on the GPU (e.g. on two streams) race. */
+ * `stream`, so it reports no solver failure itself: call phg_ops_check to
+ * learn whether the mass solve converged (PHG_ERR_NOT_CONVERGED for a
+ * non-finite F or a missed tolerance).  The first call on each device looks
+ * up the array's device address (make it before any stream capture).  All
+ * calls share the array: calls that overlap on the GPU (e.g. on two streams)
+ * race. */
 int phg_laplace_calc2_noalloc(phg_ops o, double *ans, const double *F, void *stream);
 /* SphereJacobian::calc1 / calc2 / calc2t (src/sjacobian.cpp:348-408, 456-461). */
 int phg_jacobian_calc1(phg_ops o, double *ans, const double *u, const double *v, const double *bnd, void *stream);
 int phg_jacobian_calc2(phg_ops o, double *ans, const double *u, const double *v, void *stream);
 int phg_jacobian_calc2t(phg_ops o, double *ans, const double *u, const double *v, void *stream);
+/* The 8 derivative products inside SphereJacobian::calc2 before its mass
+ * solves (src/sjacobian.cpp:136-362: D2cos u, D1 v, D1cos u, D2 v, D2 u,
+ * D1cos v, D1 u, D2cos v, each with its boundary columns) for nv members:
+ * u, v full vectors (nv x V, member-major), out nv x 8 x rs.  quad = 0: the
+ * assembled FP64 operators (the same bits as the CPU CSR products); quad = 1:
+ * the FP32 element-loop quadrature the mixed-precision time steps use (the
+ * integrals formed from the mesh geometry on the fly).  Device pointers only;
+ * the call only enqueues work. */
+int phg_jacobian_derivs(phg_ops o, int quad, double *out, const double *u, const double *v, int nv, void *stream);
+/* SphereJacobian::calc1t (src/sjacobian.h:116, src/sjacobian.cpp:463-468):
+ * the adjoint -J(u, v) on the inner points, ans[V] with bnd[os] on the boundary. */
+int phg_jacobian_calc1t(phg_ops o, double *ans, const double *u, const double *v, const double *bnd, void *stream);
+/* SphereJacobian::calc2_diff_x / calc2_diff_cos_y (src/sjacobian.h:143-148,
+ * src/sjacobian.cpp:364-402): ans[rs] = du/dx, resp. (1/cos y) du/dy, of the
+ * full vector v[V] on the inner points (derivative operator with its boundary
+ * columns, then the Jacobian mass solve). */
+int phg_jacobian_calc2_diff_x(phg_ops o, double *ans, const double *v, void *stream);
+int phg_jacobian_calc2_diff_cos_y(phg_ops o, double *ans, const double *v, void *stream);
 /* SphereNorm::norm / dist / scalar (src/norm.h:81-94); result to *out (host). */
 int phg_norm(phg_ops o, const double *u, double *out, void *stream);
 int phg_dist(phg_ops o, const double *u, const double *v, double *out, void *stream);

@@ -29,6 +29,7 @@ UNITS = [
     ("phg_capi.cu", "cuda", []),
     ("phg_serve.cu", "cuda", []),
     ("phg_tune.cu", "cuda", []),
+    ("phg_jacquad.cu", "cuda", []),
 ]
 
 

@@ -18,6 +18,7 @@
 #include "phg_host.hpp"
 #include <nvtx3/nvToolsExt.h>
 #include "phg_kernels.cuh"
+#include "phg_jacquad.cuh"
 
 using namespace phg;
 
@@ -503,11 +504,16 @@ struct phg_ops_s {
     DBuf vd1, vd2, vd1c, vd2c;
     ColsBufs bnd2, bnd3, d1b, d2b, d1cb, d2cb;
     JacOps J;
+    // element-loop geometry of the FP32 Jacobian right-hand sides (mixed time steps)
+    DBuf jq_idx, jq_geo, jq_cs;
+    JacQuadDev jq;
+    bool jq_on = false;              // mixed-precision steps use it (PHG_JAC_QUAD=0 turns it off)
     DBuf ncol, nval;                 // V x V norm matrix (its own pattern)
     DevEll norm;
     int restart = 30, max_iter = 20000;
     double tol = 1e-12;
     int max_sms = 0;                 // SMs the persistent solver may fill (0 = all)
+    long long wait_limit = 0;        // barrier wait limit of the persistent solvers (0 = default ~1 s)
     // scratch
     DBuf work, stats, s_a, s_b, s_c, s_d, s_e, s_part, s_out;
     GmresStats last{};
@@ -802,6 +808,18 @@ extern "C" int phg_ops_create(phg_mesh h, int precision, phg_ops *out) {
         return r;
     o->J.d1 = o->ell(o->vd1); o->J.d2 = o->ell(o->vd2); o->J.d1c = o->ell(o->vd1c); o->J.d2c = o->ell(o->vd2c);
     o->J.d1b = o->d1b.c; o->J.d2b = o->d2b.c; o->J.d1cb = o->d1cb.c; o->J.d2cb = o->d2cb.c;
+    {
+        JacQuadHost jh;
+        build_jac_quad(m, jh);
+        if (jh.max_tri <= 6) {   // the kernel's 8-lane rows take at most 6 triangles per point
+            CK(upload(o->jq_idx, jh.idx)); CK(upload(o->jq_geo, jh.geo)); CK(upload(o->jq_cs, jh.cs0));
+            o->jq.n = m.rs;
+            o->jq.idx = (const int2 *)o->jq_idx.p;
+            o->jq.geo = (const float4 *)o->jq_geo.p;
+            o->jq.cs0 = (const float2 *)o->jq_cs.p;
+            o->jq_on = precision == PHG_MIXED && env_int("PHG_JAC_QUAD", 1) != 0;
+        }
+    }
     // norm matrix: V x V on its own pattern
     int Wn = 0;
     for (int i = 0; i < m.V; ++i) Wn = std::max(Wn, so.norm.ptr[i + 1] - so.norm.ptr[i]);
@@ -866,7 +884,7 @@ int solve(phg_ops_s *o, const DevSolveOp &op, const double *B, double *X, int nv
     const bool rec = o->prof && o->nev + 2 <= (int)o->ev.size();
     if (rec) CK(cudaEventRecord(o->ev[o->nev], s));
     CK(gmres_solve(op, B, X, nv, ld, o->restart, o->max_iter, tol, prec_of(o), o->work.p,
-                   o->stats.as<GmresStats>() + slot, s, false, o->max_sms));
+                   o->stats.as<GmresStats>() + slot, s, false, o->max_sms, nullptr, o->wait_limit));
     if (rec) {
         o->ev_family[o->nev / 2] = solve_family(op);
         CK(cudaEventRecord(o->ev[o->nev + 1], s));
@@ -955,12 +973,15 @@ int laplace_calc2_dev(phg_ops_s *o, double *ans, int lda, const double *F, int l
     return solve(o, o->ML.op, rhs, ans, nv, lda, tol, slot, s);
 }
 
-// the 8 derivative solves of a Jacobian for nv members; sol: nv x 8 x rs
+// the 8 derivative solves of a Jacobian for nv members; sol: nv x 8 x rs.
+// quad: right-hand sides by the FP32 element-loop quadrature (the mixed
+// precision time steps) instead of the assembled FP64 operators
 int jacobian_derivs_dev(phg_ops_s *o, const double *u, const double *v, int ld, double *sol, int nv, int slot,
-                        cudaStream_t s, double tol) {
+                        cudaStream_t s, double tol, bool quad = false) {
     CK(o->s_b.ensure(8 * (size_t)o->rs * 8 * nv));
     double *rhs = o->s_b.as<double>();
-    CK(jac_rhs(o->J, u, v, ld, o->imap(), o->bmap(), rhs, o->rs, nv, s));
+    if (quad && o->jq.n) CK(jac_quad(o->jq, o->J, u, v, ld, o->imap(), o->bmap(), rhs, o->rs, nv, s));
+    else CK(jac_rhs(o->J, u, v, ld, o->imap(), o->bmap(), rhs, o->rs, nv, s));
     CK(cudaMemsetAsync(sol, 0, 8 * (size_t)o->rs * 8 * nv, s));
     return solve(o, o->MJ.op, rhs, sol, 8 * nv, o->rs, tol, slot, s);
 }
@@ -990,6 +1011,14 @@ extern "C" int phg_ops_set_sms(phg_ops o, int max_sms) {
     PHG_API_BEGIN
     if (!o || max_sms < 0) return fail(PHG_ERR_ARG, "bad argument");
     o->max_sms = max_sms;
+    return PHG_OK;
+    PHG_API_END
+}
+
+extern "C" int phg_ops_set_wait_limit(phg_ops o, long long cycles) {
+    PHG_API_BEGIN
+    if (!o || cycles < 0) return fail(PHG_ERR_ARG, "bad argument");
+    o->wait_limit = cycles;
     return PHG_OK;
     PHG_API_END
 }
@@ -1492,6 +1521,58 @@ extern "C" int phg_jacobian_calc2t(phg_ops o, double *ans, const double *u, cons
     PHG_API_END
 }
 
+extern "C" int phg_jacobian_derivs(phg_ops o, int quad, double *out, const double *u, const double *v, int nv,
+                                   void *stream) {
+    PHG_API_BEGIN
+    if (!o || !out || !u || !v || nv < 1) return fail(PHG_ERR_ARG, "bad argument");
+    if (!is_device_ptr(out) || !is_device_ptr(u) || !is_device_ptr(v))
+        return fail(PHG_ERR_ARG, "phg_jacobian_derivs takes device pointers");
+    if (quad && !o->jq.n) return fail(PHG_ERR_ARG, "this mesh has points with more than 6 triangles");
+    cudaStream_t s = o->str(stream);
+    if (quad) CK(jac_quad(o->jq, o->J, u, v, o->V, o->imap(), o->bmap(), out, o->rs, nv, s));
+    else CK(jac_rhs(o->J, u, v, o->V, o->imap(), o->bmap(), out, o->rs, nv, s));
+    return PHG_OK;
+    PHG_API_END
+}
+
+extern "C" int phg_jacobian_calc1t(phg_ops o, double *ans, const double *u, const double *v, const double *bnd,
+                                   void *s) {
+    PHG_API_BEGIN
+    return jacobian_common(o, ans, u, v, bnd, true, true, s);
+    PHG_API_END
+}
+
+// M_J^-1 (D v_in + D_bnd v_bnd): one derivative of SphereJacobian
+static int jacobian_diff(phg_ops o, double *ans, const double *v, bool cos_y, void *stream) {
+    if (!o || !ans || !v) return fail(PHG_ERR_ARG, "NULL argument");
+    cudaStream_t s = o->str(stream);
+    Stage st(o, s);
+    const double *dv; double *dA;
+    CK(st.in(v, o->V, &dv));
+    CK(st.out(ans, o->rs, &dA));
+    CK(o->s_c.ensure(8 * (size_t)o->rs));
+    double *rhs = o->s_c.as<double>();
+    const DevEll &D = cos_y ? o->J.d2c : o->J.d1;
+    const DevCols &Db = cos_y ? o->J.d2cb : o->J.d1b;
+    CK(apply_op(D, Db, dv, o->V, o->imap(), dv, o->V, o->bmap(), rhs, o->rs, 1, s));
+    CK(cudaMemsetAsync(dA, 0, 8 * (size_t)o->rs, s));
+    int r = solve(o, o->MJ.op, rhs, dA, 1, o->rs, mass_tol(o), 0, s);
+    if (r) return r;
+    CK(st.finish());
+    return st.host ? check_stats(o, 1, s) : PHG_OK;
+}
+
+extern "C" int phg_jacobian_calc2_diff_x(phg_ops o, double *ans, const double *v, void *s) {
+    PHG_API_BEGIN
+    return jacobian_diff(o, ans, v, false, s);
+    PHG_API_END
+}
+extern "C" int phg_jacobian_calc2_diff_cos_y(phg_ops o, double *ans, const double *v, void *s) {
+    PHG_API_BEGIN
+    return jacobian_diff(o, ans, v, true, s);
+    PHG_API_END
+}
+
 static int norm_common(phg_ops o, const double *u, const double *v, double *out, bool dist, bool sq, void *stream) {
     if (!o || !u || !out) return fail(PHG_ERR_ARG, "NULL argument");
     cudaStream_t s = o->str(stream);
@@ -1636,8 +1717,7 @@ int bv_step_dev(phg_barvortex_s *b, int nv, double *u1, const double *u, const d
     if ((r = laplace_calc2_dev(o, x, rs, w, V, nv, slot++, s, o->tol))) return r;
     CK(p2u(dw, V, x, rs, nullptr, os, p2io, isb, V, nv, s));
     // FC = w/tau + mu(1-theta) dw - sigma(1-theta) w (+ f)
-    if (forcing && nv > 1) return fail(PHG_ERR_ARG, "batched forcing not supported");
-    CK(bv_fc(FC, w, dw, forcing, 1.0 / c.tau, c.mu * (1.0 - c.theta), -c.sigma * (1.0 - c.theta), NV, s));
+    CK(bv_fc(FC, w, dw, forcing, 1.0 / c.tau, c.mu * (1.0 - c.theta), -c.sigma * (1.0 - c.theta), V, NV, s));
     CK(cudaMemsetAsync(u_n, 0, 8 * NV, s));
     CK(cudaMemsetAsync(w_n, 0, 8 * NV, s));
     CK(cudaMemsetAsync(b->done.p, 0, 4 * (size_t)nv, s));
@@ -1645,7 +1725,7 @@ int bv_step_dev(phg_barvortex_s *b, int nv, double *u1, const double *u, const d
         CK(bv_mix(tmp1, tmp2, w_n, w, u_n, uu, b->lh.as<double>(), V, c.k1 * c.theta, c.k1 * (1.0 - c.theta), c.k2,
                   c.theta, 1.0 - c.theta, NV, s));
         // F = FC[inner] - J(tmp2, tmp1)
-        if ((r = jacobian_derivs_dev(o, tmp2, tmp1, V, jsol, nv, slot++, s, o->tol))) return r;
+        if ((r = jacobian_derivs_dev(o, tmp2, tmp1, V, jsol, nv, slot++, s, o->tol, o->jq_on))) return r;
         CK(jac_combine(jsol, rs, rs, F, rs, FC, V, o->imap(), nv, s));
         // rp = M_L F + bnd_ bnd_w ; w_n = p2u(A^-1 rp, bnd_w)
         CK(apply_op(o->ML.op.A, b->Ab.c, F, rs, nullptr, bnd_w, os, nullptr, rp, rs, nv, s));
@@ -2232,7 +2312,7 @@ int bc_step_dev(phg_baroclin_s *b, double *u11, double *u21, const double *u1, c
         CK(bc_jin(b->ju.as<double>(), b->jv.as<double>(), U, U + V, w, w + V, un, un + V, wn, wn + V,
                   b->lh.as<double>(), th, V, s));
         if ((r = jacobian_derivs_dev(o, b->ju.as<double>(), b->jv.as<double>(), V, b->jsol.as<double>(), 5, slot++, s,
-                                     o->tol)))
+                                     o->tol, o->jq_on)))
             return r;
         CK(jac_combine(b->jsol.as<double>(), rs, rs, b->jac.as<double>(), rs, nullptr, 0, nullptr, 5, s));
         CK(bc_fg(F, G, b->jac.as<double>(), FC, GC, o->imap(), k.alpha2, rs, s));
@@ -2444,26 +2524,29 @@ extern "C" int phg_laplace_calc2_noalloc(phg_ops o, double *ans, const double *F
         return fail(PHG_ERR_ARG, "phg_laplace_calc2_noalloc takes device pointers only");
     const size_t al = 256;
     const size_t rhs_bytes = (8 * (size_t)o->rs + al - 1) / al * al;
-    const size_t st_bytes = (sizeof(GmresStats) + al - 1) / al * al;
     const size_t work_bytes = gmres_work_bytes(o->ML.op, 1, o->restart, prec_of(o));
-    const size_t need = rhs_bytes + st_bytes + work_bytes;
+    const size_t need = rhs_bytes + work_bytes;
     if (need > NOALLOC_BYTES)
         return fail(PHG_ERR_ARG,
                     "phg_laplace_calc2_noalloc needs %zu bytes of scratch for %d inner points at restart %d; "
-                    "it holds %zu (16 MiB: a Chebyshev mass solve up to level 7 in FP64)",
+                    "it holds %zu (16 MiB: the Chebyshev mass solve up to level 7 in FP64, a GMRES(30) one up "
+                    "to level 6)",
                     need, o->rs, o->restart, NOALLOC_BYTES);
     unsigned char *base = nullptr;
     int r = noalloc_scratch(o->dev, &base);
     if (r) return r;
     cudaStream_t s = o->str(stream);
     double *rhs = (double *)base;
-    GmresStats *st = (GmresStats *)(base + rhs_bytes);
-    void *work = base + rhs_bytes + st_bytes;
-    // rhs = L F_in + B3 F_bnd ; ans = M_L^-1 rhs from a zero start
+    void *work = base + rhs_bytes;
+    // rhs = L F_in + B3 F_bnd ; ans = M_L^-1 rhs from a zero start.  The solve
+    // record goes to the handle's slot 0 (allocated with the handle), where
+    // phg_ops_check and phg_ops_last_solve read it, as for phg_laplace_calc2.
     CK(apply_op(o->L.op.A, o->bnd3.c, F, o->V, o->imap(), F, o->V, o->bmap(), rhs, o->rs, 1, s));
     CK(cudaMemsetAsync(ans, 0, 8 * (size_t)o->rs, s));
-    CK(gmres_solve(o->ML.op, rhs, ans, 1, o->rs, o->restart, o->max_iter, mass_tol(o), prec_of(o), work, st, s,
-                   /*no_alloc=*/true));
+    CK(gmres_solve(o->ML.op, rhs, ans, 1, o->rs, o->restart, o->max_iter, mass_tol(o), prec_of(o), work,
+                   o->stats.as<GmresStats>(), s, /*no_alloc=*/true, o->max_sms, nullptr, o->wait_limit));
+    o->stats_pending = true;
+    o->pending_slots = std::max(o->pending_slots, 1);
     return PHG_OK;
     PHG_API_END
 }

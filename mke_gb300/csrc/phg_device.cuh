@@ -148,10 +148,12 @@ size_t gmres_work_bytes(const DevSolveOp &op, int nv, int m, Precision p, const 
 // shape: the launch shape to use (null = the tuned one for this operator,
 // else the defaults); the environment variables PHG_ROWS_PER_BLOCK and
 // PHG_CHEB_LOCKSTEP override both
+// wait_limit: clock64 cycles a group-barrier wait of the persistent kernels
+// may spin before the launch gives up with status 2 (0 = the default, ~1 s)
 cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv, int ld,
                         int m, int max_iter, double tol, Precision p,
                         void *work, GmresStats *stats_dev, cudaStream_t s, bool no_alloc = false,
-                        int max_sms = 0, const SolveShape *shape = nullptr);
+                        int max_sms = 0, const SolveShape *shape = nullptr, long long wait_limit = 0);
 
 // y[v] = A x_in[v] + C x_bnd[v] with every row summed in ascending column
 // order from 0.0 and no fused multiply-add (same rounding as a CPU CSR

@@ -45,7 +45,7 @@ constexpr int MAXM = 48;         // largest restart length
 constexpr int BLOCK = 256;
 constexpr int NWARP = BLOCK / 32;
 constexpr double INNER_RTOL = 1e-5;  // FP32 cycle: reduce the residual 1e5x, then refine
-constexpr long long SPIN_LIMIT = 2000000000LL;  // clock64 cycles (~1 s)
+constexpr long long SPIN_LIMIT = 2000000000LL;  // default wait limit, clock64 cycles (~1 s)
 constexpr int CHEB_KMAX = 64;    // most Chebyshev steps per refinement cycle
 constexpr int LS_MIN_RHS = 32;   // right-hand sides from which the lockstep path runs
 constexpr int LS_MIN_TUNED = 8;  // the fewest for which the autotuner may choose it
@@ -81,6 +81,7 @@ struct Params {
     // coefficients d_k = ca[k] d_{k-1} + cb[k] D^-1 r_k, d_0 = c0 D^-1 r_0
     int cheb_k;
     double cheb_c0, cheb_ca[CHEB_KMAX], cheb_cb[CHEB_KMAX];
+    long long wait_limit;    // clock64 cycles a barrier wait may take before the launch gives up
 };
 
 // phase cycle counters kept by block 0 when PHG_PHASE_TIMING is set
@@ -96,13 +97,21 @@ __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long lon
     return v;
 }
 
+// The launch's barrier wait limit, held by thread 0 of every block (the only
+// thread that waits): set once at kernel entry from Params::wait_limit.
+__device__ __forceinline__ long long &wait_limit_slot() {
+    __shared__ long long lim;
+    return lim;
+}
+
 // Barrier of the G blocks of one group.  The group's 64-bit word at bar
 // counts arrivals and is never reset within a launch (nor wraps): a block
 // arriving as the k-th (0-based) waits until the count reaches the next
 // multiple of G, so the last arrival's one atomic releases everyone (no
 // reset, no second flag) and a block that runs ahead into the next barrier
-// only raises the count further.  The wait gives up after SPIN_LIMIT cycles
-// and raises the launch's error flag.
+// only raises the count further.  The wait gives up after the launch's wait
+// limit (wait_limit_slot, SPIN_LIMIT by default) and raises the launch's
+// error flag.
 __device__ bool group_sync(unsigned *bar, int G, int *err, long long *tm) {
     __shared__ int ok;
     long long tb = (tm && threadIdx.x == 0) ? clock64() : 0;
@@ -119,10 +128,10 @@ __device__ bool group_sync(unsigned *bar, int G, int *err, long long *tm) {
         asm volatile("fence.acq_rel.gpu;" ::: "memory");
         const unsigned long long old = atomicAdd(cnt, 1ull);
         const unsigned long long target = old - old % (unsigned long long)G + (unsigned long long)G;
-        const long long t0 = clock64();
+        const long long t0 = clock64(), lim = wait_limit_slot();
         while (ld_acquire(cnt) < target) {
             if (ld_volatile(err)) { ok = 0; break; }
-            if (clock64() - t0 > SPIN_LIMIT) { atomicExch(err, 1); ok = 0; break; }
+            if (clock64() - t0 > lim) { atomicExch(err, 1); ok = 0; break; }
         }
         // acquire: the load that saw the count completes before any later
         // access of the block (the __syncthreads below orders the others)
@@ -526,6 +535,7 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
     const double tol = p.tol;
     const int grp = blockIdx.x / G, bi = blockIdx.x % G;
     if (grp >= groups) return;
+    if (threadIdx.x == 0) wait_limit_slot() = p.wait_limit;   // read by this thread only
     unsigned *bar = p.bar + 2 * grp;
     int *err = p.err;
     double *part2 = p.part + (size_t)grp * 2 * G * (MAXM + 2);
@@ -854,6 +864,7 @@ __global__ void __launch_bounds__(BLOCK, 2) cheb_kernel(const Params p) {
     const int grp = blockIdx.x / G, bi = blockIdx.x % G;
     if (grp >= groups) return;
     if (threadIdx.x == 0) {   // constant indices: the parameter block stays in param space
+        wait_limit_slot() = p.wait_limit;
 #pragma unroll
         for (int k = 0; k < CHEB_KMAX; ++k) {
             cf[k] = (VT)p.cheb_ca[k];
@@ -2277,7 +2288,7 @@ size_t gmres_work_bytes(const DevSolveOp &op, int nv, int m, Precision p, const 
 cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv, int ld,
                         int m, int max_iter, double tol, Precision prec,
                         void *work, GmresStats *stats_dev, cudaStream_t s, bool no_alloc, int max_sms,
-                        const SolveShape *shape) {
+                        const SolveShape *shape, long long wait_limit) {
     if (m < 1 || m > MAXM || nv < 1) return cudaErrorInvalidValue;
     const int n = op.A.n;
     Params p;
@@ -2362,6 +2373,7 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     p.part = (double *)(w + L.part);
     p.bar = (unsigned *)(w + L.bar); p.err = (int *)(w + L.err); p.stats = stats_dev;
     p.groups = groups; p.G = G;
+    p.wait_limit = wait_limit > 0 ? wait_limit : SPIN_LIMIT;
     p.mg_row_bytes = 0.0;
     if (op.mgd)
         for (int l = 0; l < op.mg.nlev; ++l) {

@@ -148,12 +148,13 @@ __global__ void k_axpbz(double *y, const double *x, double a, const double *z, d
 
 // FC = (1/tau) w + mu(1-theta) dw ; FC = 1.0 FC + (-sigma(1-theta)) w ; FC += rp
 // (examples/barvortex_impl.h:238-256)
+// rp: one forcing field of V values shared by every member (null = none)
 __global__ void k_bv_fc(double *FC, const double *w, const double *dw, const double *rp,
-                        double c_w, double c_dw, double c_w2, long long n) {
+                        double c_w, double c_dw, double c_w2, int V, long long n) {
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         double f = c_w * w[t] + c_dw * dw[t];
         f = 1.0 * f + c_w2 * w[t];
-        if (rp) f += rp[t];
+        if (rp) f += rp[t % V];
         FC[t] = f;
     }
 }
@@ -379,8 +380,8 @@ cudaError_t axpbz(double *y, const double *x, double a, const double *z, double 
 }
 
 cudaError_t bv_fc(double *FC, const double *w, const double *dw, const double *rp, double c_w, double c_dw,
-                  double c_w2, long long n, cudaStream_t s) {
-    k_bv_fc<<<grid_for(n), TB, 0, s>>>(FC, w, dw, rp, c_w, c_dw, c_w2, n);
+                  double c_w2, int V, long long n, cudaStream_t s) {
+    k_bv_fc<<<grid_for(n), TB, 0, s>>>(FC, w, dw, rp, c_w, c_dw, c_w2, V, n);
     g_kernel_launches++;
     return cudaGetLastError();
 }

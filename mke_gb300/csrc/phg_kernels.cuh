@@ -27,8 +27,10 @@ cudaError_t jac_combine(const double *d, int ldd, int n, double *jac, int ldj, c
 cudaError_t p2u(double *u, int ldu, const double *p, int ldp, const double *bnd, int ldb,
                 const int *p2io, const int *isb, int V, int nv, cudaStream_t s);
 cudaError_t axpbz(double *y, const double *x, double a, const double *z, double b, long long n, cudaStream_t s);
+// FC = c_w w + c_dw dw, then FC + c_w2 w, then + rp (one field of V values
+// shared by the members, or null), over n = members x V entries
 cudaError_t bv_fc(double *FC, const double *w, const double *dw, const double *rp, double c_w, double c_dw,
-                  double c_w2, long long n, cudaStream_t s);
+                  double c_w2, int V, long long n, cudaStream_t s);
 cudaError_t bv_mix(double *tmp1, double *tmp2, const double *w_n, const double *w, const double *u_n,
                    const double *u, const double *lh, int V, double a1, double a2, double k2, double t1,
                    double t2, long long n, cudaStream_t s);

@@ -88,6 +88,7 @@ SIGNATURES = {
     "phg_laplace_solve_batch": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp]),
     "phg_ops_check": (C.c_int, [_vp, _vp]),
     "phg_ops_set_sms": (C.c_int, [_vp, C.c_int]),
+    "phg_ops_set_wait_limit": (C.c_int, [_vp, C.c_longlong]),
     "phg_ops_mult": (C.c_int, [_vp, C.c_char_p, _vp, _vp, C.c_int, _vp]),
     "phg_ops_mult32": (C.c_int, [_vp, C.c_char_p, _vp, _vp, C.c_int, _vp]),
     "phg_device_bytes": (C.c_int, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
@@ -95,6 +96,10 @@ SIGNATURES = {
     "phg_jacobian_calc1": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "phg_jacobian_calc2": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "phg_jacobian_calc2t": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "phg_jacobian_calc1t": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "phg_jacobian_derivs": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, C.c_int, _vp]),
+    "phg_jacobian_calc2_diff_x": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "phg_jacobian_calc2_diff_cos_y": (C.c_int, [_vp, _vp, _vp, _vp]),
     "phg_norm": (C.c_int, [_vp, _vp, _dp, _vp]),
     "phg_dist": (C.c_int, [_vp, _vp, _vp, _dp, _vp]),
     "phg_scalar": (C.c_int, [_vp, _vp, _vp, _dp, _vp]),
@@ -339,6 +344,15 @@ class Operators:
     def set_solver(self, restart=30, tol=1e-12, max_iter=20000):
         _check(lib().phg_ops_set_solver(self._h, restart, tol, max_iter))
 
+    def set_wait_limit(self, cycles: int = 0):
+        """Clock cycles a group-barrier wait of this handle's persistent solver
+        kernels may spin before the launch gives up (0 = the default, ~1 s)."""
+        _check(lib().phg_ops_set_wait_limit(self._h, int(cycles)))
+
+    def check(self, stream=None):
+        """phg_ops_check: synchronise and check the solves enqueued since the last check."""
+        _check(lib().phg_ops_check(self._h, _stream(stream)))
+
     def profile(self, enable=True):
         _check(lib().phg_ops_profile(self._h, 1 if enable else 0))
 
@@ -399,7 +413,8 @@ class SphereLaplace:
 
 
 class SphereJacobian:
-    """SphereJacobian (src/sjacobian.h:65-149): calc1, calc2, calc2t."""
+    """SphereJacobian (src/sjacobian.h:65-149): calc1, calc1t, calc2, calc2t,
+    calc2_diff_x, calc2_diff_cos_y."""
 
     def __init__(self, ops: Operators):
         self.ops = ops
@@ -421,6 +436,35 @@ class SphereJacobian:
         out = np.zeros(self.m.inner_size) if out is None else out
         u, v = _f8(u), _f8(v)
         _check(lib().phg_jacobian_calc2t(self.ops._h, _ptr(out), _ptr(u), _ptr(v), _stream(stream)))
+        return out
+
+    def derivs(self, u, v, out, quad=False, stream=None):
+        """The 8 derivative products of calc2 (CUDA float64 tensors: u, v
+        nv x V, out nv x 8 x rs); quad: the FP32 element-loop quadrature."""
+        nv = 1 if u.dim() == 1 else u.shape[0]
+        _check(lib().phg_jacobian_derivs(self.ops._h, 1 if quad else 0, _ptr(out), _ptr(u), _ptr(v), nv,
+                                         _stream(stream)))
+        return out
+
+    def calc1t(self, u, v, bnd=None, out=None, stream=None):
+        """SphereJacobian::calc1t: -J(u, v) on the inner points, bnd on the boundary."""
+        out = np.zeros(self.m.size) if out is None else out
+        u, v, bnd = _f8(u), _f8(v), _f8(bnd)
+        _check(lib().phg_jacobian_calc1t(self.ops._h, _ptr(out), _ptr(u), _ptr(v), _ptr(bnd), _stream(stream)))
+        return out
+
+    def calc2_diff_x(self, v, out=None, stream=None):
+        """SphereJacobian::calc2_diff_x: dv/dx on the inner points."""
+        out = np.zeros(self.m.inner_size) if out is None else out
+        v = _f8(v)
+        _check(lib().phg_jacobian_calc2_diff_x(self.ops._h, _ptr(out), _ptr(v), _stream(stream)))
+        return out
+
+    def calc2_diff_cos_y(self, v, out=None, stream=None):
+        """SphereJacobian::calc2_diff_cos_y: (1/cos y) dv/dy on the inner points."""
+        out = np.zeros(self.m.inner_size) if out is None else out
+        v = _f8(v)
+        _check(lib().phg_jacobian_calc2_diff_cos_y(self.ops._h, _ptr(out), _ptr(v), _stream(stream)))
         return out
 
 

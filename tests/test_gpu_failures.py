@@ -88,3 +88,28 @@ def test_device_index_arrays_in_range(level, precision):
     maps, boundary lists, multigrid transfers) and finds none out of range."""
     ops = phelm.Operators(phelm.Mesh.sphere(level), precision)
     assert ops.validate() == 0
+
+
+TIMEOUT = 4
+
+
+@pytest.mark.parametrize("precision", [phelm.PHG_FP64, phelm.PHG_MIXED])
+def test_barrier_wait_runs_out(precision):
+    """A device-side wait made to run out: with a wait limit of one clock
+    cycle every group-barrier wait of the persistent multigrid solver (161
+    blocks share one level-6 Laplace solve) gives up at once, sets the
+    launch's error flag and returns; the call reports PHG_ERR_TIMEOUT.  Back
+    at the default limit the same handle solves the same input again."""
+    m = phelm.Mesh.sphere(6)
+    lat, lon = m.latlon()
+    ops = phelm.Operators(m, precision, tol=1e-12)
+    L = phelm.SphereLaplace(ops)
+    F = serve.solve_inputs(lat, lon, 1, seed=5)[0]
+    good = L.solve(F)
+    ops.set_wait_limit(1)
+    with pytest.raises(phelm.PhgError) as e:
+        L.solve(F)
+    assert e.value.code == TIMEOUT
+    ops.set_wait_limit(0)
+    assert rel(L.solve(F), good) <= 1e-9
+    assert ops.last_solve()["relres"] <= 1e-12

@@ -150,3 +150,46 @@ def test_operator_apply_fp32():
     ops.mult32("lapl", x, y)
     torch.cuda.synchronize()
     assert rel(y.cpu().numpy().T, ref) <= 1e-5
+
+
+@pytest.mark.parametrize("level", [2, 3, 4, 5])
+def test_jacobian_adjoint_and_derivatives(level, golden):
+    """SphereJacobian::calc1t, calc2_diff_x, calc2_diff_cos_y vs the oracle,
+    and at levels 2-5 vs the reference's own results (tests/golden).  Each is
+    a derivative product and one mass solve: 1e-13."""
+    m, ops, o, u, v, bnd, *_ = setup(level)
+    J = phelm.SphereJacobian(ops)
+    assert rel(J.calc1t(u, v, bnd), o.jacobian_calc1t(u, v, bnd)) <= 1e-13
+    assert rel(J.calc1t(u, v, bnd)[m.arrays()["bnd"] == 0], -J.calc1(u, v, bnd)[m.arrays()["bnd"] == 0]) <= 1e-15
+    assert rel(J.calc2_diff_x(u), o.jacobian_diff_x(u)) <= 1e-13
+    assert rel(J.calc2_diff_cos_y(u), o.jacobian_diff_cos_y(u)) <= 1e-13
+    g = golden(f"ref_L{level}.npz")
+    gu, gv, gb = g["in_u"], g["in_v"], g["in_bnd"]
+    assert rel(J.calc1t(gu, gv, gb), g["out_jac_calc1t"]) <= 1e-13
+    assert rel(J.calc2_diff_x(gu), g["out_jac_diff_x"]) <= 1e-13
+    assert rel(J.calc2_diff_cos_y(gu), g["out_jac_diff_cos_y"]) <= 1e-13
+
+
+@pytest.mark.parametrize("precision", [phelm.PHG_FP64, phelm.PHG_MIXED])
+@pytest.mark.parametrize("level", [2, 3, 4])
+def test_barvortex_boundary_and_forcing(level, precision, golden):
+    """Two BarVortex::calc steps with non-zero pole values bnd_u, bnd_w and a
+    time-dependent forcing (the reference's own run, tests/golden: forcing
+    values as the reference evaluated them at t = 0 and t = tau), single call
+    and as a member of a batch; 1e-9 (solves to 1e-12)."""
+    m, ops, *_ = setup(level, precision)
+    g = golden(f"ref_L{level}.npz")
+    lat, _ = m.latlon()
+    bv = phelm.BarVortex(ops, picard_iters=3, coriolis=np.sin(lat))
+    bu, bw = g["out_bv_bf_bnd_u"], g["out_bv_bf_bnd_w"]
+    s1 = bv.calc(g["in_u"], bu, bw, forcing=g["out_bv_bf_forcing0"])
+    assert rel(s1, g["out_bv_bf_step1"]) <= 1e-9
+    s2 = bv.calc(s1, bu, bw, forcing=g["out_bv_bf_forcing1"])
+    assert rel(s2, g["out_bv_bf_step2"]) <= 1e-9
+    assert bv.last_stats()["worst_relres"] <= 1e-11
+    # the same member inside a batch of three (the others: zero boundary)
+    U = np.stack([g["in_u"], g["in_v"], g["in_u"]])
+    BU = np.stack([np.zeros_like(bu), np.zeros_like(bu), bu])
+    BW = np.stack([np.zeros_like(bw), np.zeros_like(bw), bw])
+    out = bv.calc_batch(U, BU, BW, forcing=g["out_bv_bf_forcing0"])
+    assert rel(out[2], g["out_bv_bf_step1"]) <= 1e-9

@@ -7,7 +7,8 @@ synchronisation would stall their other streams); this entry point serves
 them from a fixed device array inside the library.  Two calls in a row must
 each match the regular entry point within the apply tolerance of the parity
 tests (1e-13 relative L2); host pointers and workspaces beyond the array's
-16 MiB are refused.  This file is collected last on purpose.
+16 MiB are refused, and a mass solve that fails (a NaN input) is reported by
+phg_ops_check like any other.  This file is collected last on purpose.
 """
 import ctypes as C
 
@@ -63,3 +64,32 @@ def test_laplace_calc2_noalloc_rejects_oversize(monkeypatch):
     out = torch.zeros(m.inner_size, dtype=torch.float64, device="cuda")
     rc = L.phg_laplace_calc2_noalloc(ops._h, C.c_void_p(out.data_ptr()), C.c_void_p(dF.data_ptr()), None)
     assert rc == 1 and "16 MiB" in L.phg_last_error().decode()
+
+
+def test_laplace_calc2_noalloc_reports_failed_solve():
+    """The call only enqueues work; its mass solve's record goes to the
+    handle, so phg_ops_check reports a NaN input as PHG_ERR_NOT_CONVERGED and
+    a clean call after it as PHG_OK."""
+    import torch
+    L = phelm.lib()
+    m = phelm.Mesh.sphere(4)
+    ops = phelm.Operators(m, phelm.PHG_FP64, tol=1e-12)
+    lat, lon = m.latlon()
+    F = fields.sh_field(fields.random_coeffs(np.random.default_rng(12), 1, 8), lat, lon)
+    s = torch.cuda.Stream()
+    out = torch.zeros(m.inner_size, dtype=torch.float64, device="cuda")
+    bad = F.copy()
+    bad[40] = np.nan
+    dbad = torch.tensor(bad, dtype=torch.float64, device="cuda")
+    rc = L.phg_laplace_calc2_noalloc(ops._h, C.c_void_p(out.data_ptr()), C.c_void_p(dbad.data_ptr()),
+                                     C.c_void_p(s.cuda_stream))
+    assert rc == 0, L.phg_last_error().decode()
+    assert L.phg_ops_check(ops._h, C.c_void_p(s.cuda_stream)) == 3
+    dF = torch.tensor(F, dtype=torch.float64, device="cuda")
+    rc = L.phg_laplace_calc2_noalloc(ops._h, C.c_void_p(out.data_ptr()), C.c_void_p(dF.data_ptr()),
+                                     C.c_void_p(s.cuda_stream))
+    assert rc == 0, L.phg_last_error().decode()
+    assert L.phg_ops_check(ops._h, C.c_void_p(s.cuda_stream)) == 0
+    want = phelm.SphereLaplace(ops).calc2(F)
+    got = out.cpu().numpy()
+    assert np.linalg.norm(got - want) / np.linalg.norm(want) <= 1e-13
