@@ -507,7 +507,14 @@ struct phg_ops_s {
     // element-loop geometry of the FP32 Jacobian right-hand sides (mixed time steps)
     DBuf jq_idx, jq_geo, jq_cs;
     JacQuadDev jq;
-    bool jq_on = false;              // mixed-precision steps use it (PHG_JAC_QUAD=0 turns it off)
+    // which Picard iterations of a mixed-precision step use it: 2 (the default)
+    // every iteration of a barotropic step but the last, whose Jacobian is the
+    // assembled FP64 product, so the step's result carries no FP32 Jacobian
+    // error beyond what the Picard contraction leaves of the earlier ones
+    // (measured: <= 2e-9 relative on strongly nonlinear level-2..4 states, 1e-7
+    // with the quadrature in every iteration); 1 every iteration, barotropic and
+    // baroclinic; 0 never (PHG_JAC_QUAD at creation)
+    int jq_mode = 0;
     DBuf ncol, nval;                 // V x V norm matrix (its own pattern)
     DevEll norm;
     int restart = 30, max_iter = 20000;
@@ -817,7 +824,7 @@ extern "C" int phg_ops_create(phg_mesh h, int precision, phg_ops *out) {
             o->jq.idx = (const int2 *)o->jq_idx.p;
             o->jq.geo = (const float4 *)o->jq_geo.p;
             o->jq.cs0 = (const float2 *)o->jq_cs.p;
-            o->jq_on = precision == PHG_MIXED && env_int("PHG_JAC_QUAD", 1) != 0;
+            o->jq_mode = precision == PHG_MIXED ? env_int("PHG_JAC_QUAD", 2) : 0;
         }
     }
     // norm matrix: V x V on its own pattern
@@ -876,6 +883,8 @@ Precision prec_of(const phg_ops_s *o) { return o->prec == PHG_MIXED ? PREC_MIXED
 int solve(phg_ops_s *o, const DevSolveOp &op, const double *B, double *X, int nv, int ld, double tol,
           int slot, cudaStream_t s) {
     NvtxRange nvtx("phg:solve");
+    if (slot < 0 || (size_t)(slot + 1) * sizeof(GmresStats) > o->stats.n)
+        return fail(PHG_ERR_ARG, "solve record slot %d beyond the handle's %zu", slot, o->stats.n / sizeof(GmresStats));
     size_t need = gmres_work_bytes(op, nv, o->restart, prec_of(o));
     if (need > o->work.n) {
         CK(cudaStreamSynchronize(s));
@@ -902,6 +911,7 @@ double max_keep_nan(double a, double b) { return a != a ? a : (b != b ? b : std:
 
 // read back and check the stats of slots [0, nslots)
 int check_stats(phg_ops_s *o, int nslots, cudaStream_t s, GmresStats *agg = nullptr, GmresStats *each = nullptr) {
+    nslots = std::min<int>(nslots, (int)(o->stats.n / sizeof(GmresStats)));
     std::vector<GmresStats> st(nslots);
     CK(cudaMemcpyAsync(st.data(), o->stats.p, sizeof(GmresStats) * nslots, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -1610,7 +1620,7 @@ struct phg_barvortex_s {
     DBuf lh;
     int cap = 0;   // members the buffers hold
     DBuf w, dw, FC, u_n, w_n, u_n1, tmp1, tmp2, uin, F, rp, x, jsol, nr0, nr, done, ubnd, wbnd, frc;
-    GmresStats each[64];
+    std::vector<GmresStats> each;   // the last step's solve records, one per slot
     int nslots = 0;
     cudaStream_t last_stream = nullptr;   // stream of the last step (its stats live there)
     // linearised / adjoint steps: the backward matrix Ab_ and its boundary
@@ -1641,10 +1651,20 @@ struct phg_barvortex_s {
 extern "C" int phg_barvortex_create(phg_ops o, const phg_bv_conf *c, const double *coriolis, phg_barvortex *out) {
     PHG_API_BEGIN
     if (!o || !c || !out) return fail(PHG_ERR_ARG, "NULL argument");
-    if (!(c->tau > 0) || c->picard_iters < 1) return fail(PHG_ERR_ARG, "bad configuration");
+    if (!(c->tau > 0) || c->picard_iters < 1 || c->picard_iters > 1000)
+        return fail(PHG_ERR_ARG, "bad configuration (tau > 0, 1 <= picard_iters <= 1000)");
     auto b = std::make_unique<phg_barvortex_s>();
     b->o = o;
     b->c = *c;
+    // solve records of one step: two Laplace applies, then a Jacobian, an A
+    // and a Laplace solve per Picard iteration (the linearised steps use fewer)
+    const int slots = std::max(64, 2 + 3 * c->picard_iters);
+    if (o->stats.n < sizeof(GmresStats) * (size_t)slots) {
+        CK(cudaStreamSynchronize(o->stream));
+        CK(o->stats.ensure(sizeof(GmresStats) * (size_t)slots));
+        CK(cudaMemset(o->stats.p, 0, sizeof(GmresStats) * (size_t)slots));
+    }
+    b->each.assign(slots, GmresStats{});
     Csr A, Ab;
     const double c1 = 1.0 / c->tau + c->sigma * c->theta;
     const double c2 = -c->theta * c->mu;
@@ -1725,7 +1745,8 @@ int bv_step_dev(phg_barvortex_s *b, int nv, double *u1, const double *u, const d
         CK(bv_mix(tmp1, tmp2, w_n, w, u_n, uu, b->lh.as<double>(), V, c.k1 * c.theta, c.k1 * (1.0 - c.theta), c.k2,
                   c.theta, 1.0 - c.theta, NV, s));
         // F = FC[inner] - J(tmp2, tmp1)
-        if ((r = jacobian_derivs_dev(o, tmp2, tmp1, V, jsol, nv, slot++, s, o->tol, o->jq_on))) return r;
+        const bool quad = o->jq_mode == 1 || (o->jq_mode == 2 && it + 1 < c.picard_iters);
+        if ((r = jacobian_derivs_dev(o, tmp2, tmp1, V, jsol, nv, slot++, s, o->tol, quad))) return r;
         CK(jac_combine(jsol, rs, rs, F, rs, FC, V, o->imap(), nv, s));
         // rp = M_L F + bnd_ bnd_w ; w_n = p2u(A^-1 rp, bnd_w)
         CK(apply_op(o->ML.op.A, b->Ab.c, F, rs, nullptr, bnd_w, os, nullptr, rp, rs, nv, s));
@@ -1768,7 +1789,7 @@ static int bv_calc(phg_barvortex b, int nv, double *u1, const double *u, const d
     b->last_stream = s;
     CK(st.finish());
     if (!st.host) return PHG_OK;
-    return check_stats(o, b->nslots, s, nullptr, b->each);
+    return check_stats(o, b->nslots, s, nullptr, b->each.data());
 }
 
 extern "C" int phg_barvortex_calc(phg_barvortex b, double *u1, const double *u, const double *bnd_u,
@@ -1873,7 +1894,7 @@ static int bv_run(phg_barvortex b, int nv, int nsteps, double *u, const double *
     b->last_stream = s;
     CK(st.finish());
     if (!st.host) return PHG_OK;   // device arguments: checked by phg_barvortex_last_stats
-    r = check_stats(o, b->nslots, s, nullptr, b->each);   // the last step, for phg_barvortex_last_stats
+    r = check_stats(o, b->nslots, s, nullptr, b->each.data());   // the last step, for phg_barvortex_last_stats
     int r2 = bv_check_agg(b, s);
     return r2 ? r2 : r;
 }
@@ -2059,7 +2080,7 @@ static int bv_linear(phg_barvortex b, int kind, double *u1, const double *u, con
     if (r) return r;
     CK(st.finish());
     if (!st.host) return PHG_OK;
-    return check_stats(o, b->nslots, s, nullptr, b->each);
+    return check_stats(o, b->nslots, s, nullptr, b->each.data());
 }
 
 extern "C" int phg_barvortex_calc_L(phg_barvortex b, double *u1, const double *u, const double *z,
@@ -2088,7 +2109,7 @@ extern "C" int phg_barvortex_last_stats(phg_barvortex b, int *il, int *ia, int *
     if (!b) return fail(PHG_ERR_ARG, "NULL handle");
     phg_ops_s *o = b->o;
     cudaStream_t ls = b->last_stream ? b->last_stream : o->stream;
-    int r = check_stats(o, b->nslots, ls, nullptr, b->each);
+    int r = check_stats(o, b->nslots, ls, nullptr, b->each.data());
     if (b->agg_pending) {   // every step of the runs since the last check
         int r2 = bv_check_agg(b, ls);
         if (r2) r = r2;
@@ -2144,7 +2165,7 @@ struct phg_baroclin_s {
     // linearised steps: background fields, their Laplacians, 10 Jacobian pairs
     DBuf Z, dZ, lju, ljv, ljsol, ljac;
     DBuf U, w, dw, FC, un, wn, un1, ju, jv, jsol, jac, FG, MFG, rp, x, xi, nr, done;
-    GmresStats each[64];
+    std::vector<GmresStats> each;   // the last step's solve records, one per slot
     int nslots = 0;
     int *hdone = nullptr;   // pinned copy of the Picard stop flag
     ~phg_baroclin_s() { if (hdone) cudaFreeHost(hdone); }
@@ -2232,6 +2253,7 @@ extern "C" int phg_baroclin_create(phg_ops o, const phg_bc_conf *c, const double
     auto b = std::make_unique<phg_baroclin_s>();
     b->o = o;
     b->c = *c;
+    b->each.assign(64, GmresStats{});   // 2 + 2 x picard_iters <= 62 solve records a step
     const int rs = o->rs, n = 4 * rs;
     b->su = std::ldexp(1.0, (int)std::lround(std::log2(1.0 / c->tau)));
     int r;
@@ -2312,7 +2334,7 @@ int bc_step_dev(phg_baroclin_s *b, double *u11, double *u21, const double *u1, c
         CK(bc_jin(b->ju.as<double>(), b->jv.as<double>(), U, U + V, w, w + V, un, un + V, wn, wn + V,
                   b->lh.as<double>(), th, V, s));
         if ((r = jacobian_derivs_dev(o, b->ju.as<double>(), b->jv.as<double>(), V, b->jsol.as<double>(), 5, slot++, s,
-                                     o->tol, o->jq_on)))
+                                     o->tol, o->jq_mode == 1)))
             return r;
         CK(jac_combine(b->jsol.as<double>(), rs, rs, b->jac.as<double>(), rs, nullptr, 0, nullptr, 5, s));
         CK(bc_fg(F, G, b->jac.as<double>(), FC, GC, o->imap(), k.alpha2, rs, s));
@@ -2443,7 +2465,7 @@ static int bc_linear(phg_baroclin b, int kind, double *u11, double *u21, const d
     if (r) return r;
     CK(st.finish());
     if (!st.host) return PHG_OK;
-    return check_stats(o, b->nslots, s, nullptr, b->each);
+    return check_stats(o, b->nslots, s, nullptr, b->each.data());
 }
 
 extern "C" int phg_baroclin_calc_L(phg_baroclin b, double *u11, double *u21, const double *u1, const double *u2,
@@ -2476,7 +2498,7 @@ extern "C" int phg_baroclin_calc(phg_baroclin b, double *u11, double *u21, const
     if (r) return r;
     CK(st.finish());
     if (!st.host) return PHG_OK;
-    return check_stats(o, b->nslots, s, nullptr, b->each);
+    return check_stats(o, b->nslots, s, nullptr, b->each.data());
     PHG_API_END
 }
 

