@@ -761,6 +761,50 @@ int build_mg_dev(phg_ops_s *o, phg_mesh_s *mh, SolveOpBufs &Lb, MgBufs &mb, int 
     mg.red_elems = e;
     mg.group_elems = 0;
     for (int l = 0; l < nred; ++l) mg.group_elems += 4 * (size_t)mg.lev[l].n;
+    // cluster tail: the parallel levels of at most cl_rows rows (never the
+    // finest) run in one cluster of cl CTAs, as long as a CTA's share of their
+    // four vectors keeps two blocks per SM within the shared memory.  Off by
+    // default (PHG_MG_CLUSTER=8 turns it on): measured on the level-6 step, the
+    // tail is bit-identical but slower -- 5.23 -> 5.34 ms mixed with levels
+    // <= 2561 rows in the cluster, 6.01 ms with levels <= 10241 rows (8 CTAs
+    // then stream a level's matrix and restriction through L2 alone), 5.38 ms
+    // with the 641-row level only: the cluster barrier (~400 cycles) and
+    // distributed shared memory loads (~250 cycles) save less than the entry
+    // handshake and the serialised restriction into the tail cost.
+    mg.ncl = nred;
+    mg.cl_size = 0;
+    mg.cl_elems = 0;
+    {
+        const int cl = env_int("PHG_MG_CLUSTER", 0);
+        const int cl_rows = env_int("PHG_MG_CLUSTER_ROWS", 12000);
+        if (cl >= 2 && cl <= 16) {
+            int ncl = nred;
+            size_t elems = 0;
+            for (int l = nred - 1; l >= 1; --l) {
+                const int n = mg.lev[l].n;
+                const size_t ch = ((size_t)n + cl - 1) / cl;
+                if (n > cl_rows || 21 * 1024 + es * (e + elems + 4 * ch) > 100 * 1024) break;
+                elems += 4 * ch;
+                ncl = l;
+            }
+            bool exact = true;
+            for (int l = ncl; l < nred && exact; ++l) {
+                const int n = mg.lev[l].n, ch = (n + cl - 1) / cl;
+                const unsigned magic = (unsigned)((0x100000000ULL + ch - 1) / ch);
+                for (int i = 0; i < n && exact; ++i)
+                    exact = (int)(((unsigned long long)(unsigned)i * magic) >> 32) == i / ch;
+                mg.cl_chunk[l] = ch;
+                mg.cl_magic[l] = magic;
+            }
+            if (exact && ncl < nred) {
+                size_t off = 0;
+                for (int l = ncl; l < nred; ++l) { mg.cl_off[l] = (int)off; off += 4 * (size_t)mg.cl_chunk[l]; }
+                mg.ncl = ncl;
+                mg.cl_size = cl;
+                mg.cl_elems = off;
+            }
+        }
+    }
     CK(mb.desc.ensure(sizeof(MgDev)));
     CK(cudaMemcpy(mb.desc.p, &mg, sizeof(MgDev), cudaMemcpyHostToDevice));
     Lb.op.mgd = mb.desc.as<MgDev>();

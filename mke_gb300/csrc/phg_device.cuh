@@ -51,6 +51,19 @@ struct MgDev {
     int red_off[MG_MAXLEV] = {0};  // shared-memory element offsets of levels [nred, nlev)
     size_t red_elems = 0;          // shared-memory elements of those levels (x, xt, b, r each)
     size_t group_elems = 0;        // global elements per group for levels [0, nred)
+    // Cluster tail: levels [ncl, nred) of a group's V-cycle run inside the
+    // group's first thread-block cluster (cl_size CTAs) from distributed shared
+    // memory with hardware cluster barriers, instead of over the whole group
+    // with global-memory group barriers (ncl == nred: no tail).  Level l's rows
+    // are split in chunks of cl_chunk[l] over the cluster's CTAs; each CTA keeps
+    // its rows' x, xt, b, r at cl_off[l] (elements) of its cluster region of
+    // cl_elems elements.  cl_magic[l]: q = umulhi(i, cl_magic[l]) is the owner
+    // CTA of row i (exact for every row, checked when built).
+    int ncl = 0, cl_size = 0;
+    int cl_chunk[MG_MAXLEV] = {0};
+    int cl_off[MG_MAXLEV] = {0};
+    unsigned cl_magic[MG_MAXLEV] = {0};
+    size_t cl_elems = 0;
 };
 
 // Operator of the Krylov solver: the exact A (FP64 residuals), Jacobi-scaled

@@ -35,9 +35,13 @@
 #include <cstdio>
 #include <mutex>
 
+#include <cooperative_groups.h>
+
 #include "phg_kernels.cuh"
 
 namespace phg {
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -82,6 +86,8 @@ struct Params {
     int cheb_k;
     double cheb_c0, cheb_ca[CHEB_KMAX], cheb_cb[CHEB_KMAX];
     long long wait_limit;    // clock64 cycles a barrier wait may take before the launch gives up
+    int cluster;             // > 0: clustered launch, V-cycle levels [ncl, nred) as a cluster tail
+    unsigned long long *ccnt;  // groups: cluster-tail entry counters
 };
 
 // phase cycle counters kept by block 0 when PHG_PHASE_TIMING is set
@@ -373,62 +379,13 @@ __device__ __forceinline__ void residual_first_rows(const MgLevelDev &L, const V
     }
 }
 
-// Damped-Jacobi V-cycle: x0 = M^-1 b0 for the group's right-hand side.
-// Returns false if the grid is aborting.
-// b0_visible: b0 is complete on every block at entry (a barrier since it was
-// written), so the finest level's residual is formed without a barrier.
+// The redundant levels [nred, nlev) of a V-cycle, entirely in this block's
+// shared memory (x, xt, b, r per level at red_off): level nred's right-hand
+// side is in place; on return level nred's x holds the coarse correction.
 template <typename VT>
-__device__ __noinline__ bool vcycle(const MgDev *__restrict__ mgp, const VT *b0, VT *x0, VT *gbuf, VT *sm,
-                                    unsigned *bar, int G, int bi, int *err, long long *tm, bool b0_visible) {
+__device__ __forceinline__ void smem_levels(const MgDev *__restrict__ mgp, VT *sm) {
     const int nred = mgp->nred, nlev = mgp->nlev, nu1 = mgp->nu1, nu2 = mgp->nu2;
     const VT omega = (VT)mgp->omega;
-    VT *xcur[MG_MAXLEV];
-    const VT *bl[MG_MAXLEV];
-    size_t offs[MG_MAXLEV];
-    // ---- parallel levels, down
-    size_t off = 0;
-    for (int l = 0; l < nred; ++l) {
-        const MgLevelDev &L = mgp->lev[l];
-        const int n = L.n;
-        offs[l] = off;
-        VT *xa = gbuf + off, *xb = xa + n, *r = xb + n;
-        VT *bn = r + n;  // rhs of level l+1 when that level is parallel too
-        off += 4 * (size_t)n;
-        const VT *b = l == 0 ? b0 : bl[l];
-        bl[l] = b;
-        int r0, r1;
-        own_rows(n, G, bi, r0, r1);
-        VT *x = xa, *xo = xb;
-        jacobi_rows<VT, true>(L, b, nullptr, x, omega, r0, r1, true);
-        // FP32 only: in FP64 the two extra multiplies per gathered entry cost
-        // more than the barrier (measured at level 6)
-        if (sizeof(VT) == 4 && l == 0 && b0_visible && nu1 == 1) {
-            residual_first_rows<VT>(L, b, omega, r, r0, r1);
-        } else {
-            for (int s = 1; s < nu1; ++s) {
-                if (!group_sync(bar, G, err, tm)) return false;
-                jacobi_rows<VT, true>(L, b, x, xo, omega, r0, r1, false);
-                VT *t = x; x = xo; xo = t;
-            }
-            if (!group_sync(bar, G, err, tm)) return false;
-            residual_rows<VT, true>(L, b, x, r, r0, r1);
-        }
-        xcur[l] = x;
-        if (!group_sync(bar, G, err, tm)) return false;
-        const MgLevelDev &C = mgp->lev[l + 1];
-        const VT *rw = Prec<VT>::lr(L);
-        if (l + 1 < nred) {
-            int c0, c1;
-            own_rows(C.n, G, bi, c0, c1);
-            for (int c = c0 + threadIdx.x; c < c1; c += BLOCK) bn[c] = restrict_row<VT, true>(L.rf, rw, L.Wr, C.n, r, c);
-            bl[l + 1] = bn;
-        } else {
-            VT *sb = sm + mgp->red_off[l + 1] + 2 * C.n;
-            for (int c = threadIdx.x; c < C.n; c += BLOCK) sb[c] = restrict_row<VT, true>(L.rf, rw, L.Wr, C.n, r, c);
-        }
-    }
-    __syncthreads();
-    // ---- redundant levels in shared memory (x, xt, b, r per level)
     const int last = nlev - 1;
     for (int l = nred; l < last; ++l) {
         const MgLevelDev &L = mgp->lev[l];
@@ -481,15 +438,269 @@ __device__ __noinline__ bool vcycle(const MgDev *__restrict__ mgp, const VT *b0,
             __syncthreads();
         }
     }
+}
+
+// ------------------------------------------------------------ cluster tail --
+// Levels [ncl, nred) of the V-cycle in the group's first cluster of cl_size
+// CTAs: each level's rows are split in chunks over the CTAs, each CTA keeps its
+// rows' x, xt, b, r in its own shared memory, reads neighbours' values through
+// distributed shared memory (one remote load, ~250 cycles, instead of an L2
+// round trip) and the CTAs synchronise with the hardware cluster barrier
+// (~400 cycles) instead of the group's global-memory barrier.  The arithmetic
+// and its order are those of the group-wide levels, so the correction is the
+// same bit for bit.
+//
+// Entry is agreed through a per-group counter in global memory before any
+// distributed shared memory is touched: every CTA of the cluster adds one and
+// waits (bounded) for all cl_size arrivals.  A CTA that gives up marks the
+// counter poisoned -- only while it is still incomplete -- so either every CTA
+// of the cluster sees the count complete and runs the whole tail (whose
+// control flow depends only on the level sizes: the cluster barriers always
+// match and no CTA leaves while a peer may read its memory), or every CTA sees
+// the poison and none enters.  A cluster barrier at the end keeps each CTA's
+// memory alive until its peers are done with it.
+constexpr unsigned long long CCNT_POISON = 1ull << 62;
+constexpr unsigned long long CCNT_MASK = (1ull << 40) - 1;
+
+__device__ __forceinline__ bool tail_enter(unsigned long long *ccnt, int CS, int *err) {
+    __shared__ int go;
+    if (threadIdx.x == 0) {
+        const unsigned long long old = atomicAdd(ccnt, 1ull);
+        int g = 0;
+        if (!(old & CCNT_POISON)) {
+            const unsigned long long target = ((old & CCNT_MASK) / CS + 1) * CS;
+            const long long t0 = clock64(), lim = wait_limit_slot();
+            for (;;) {
+                unsigned long long v = ld_acquire(ccnt);
+                if (v & CCNT_POISON) break;
+                if ((v & CCNT_MASK) >= target) { g = 1; break; }
+                if (clock64() - t0 > lim) {
+                    // give up only while the count is incomplete
+                    while (!(v & CCNT_POISON) && (v & CCNT_MASK) < target) {
+                        const unsigned long long prev = atomicCAS(ccnt, v, v | CCNT_POISON);
+                        if (prev == v) { v |= CCNT_POISON; break; }
+                        v = prev;
+                    }
+                    g = (v & CCNT_POISON) ? 0 : 1;
+                    if (!g) atomicExch(err, 1);
+                    break;
+                }
+            }
+        }
+        go = g;
+    }
+    __syncthreads();
+    return go != 0;
+}
+
+template <typename VT>
+__device__ __noinline__ bool cluster_tail(const MgDev *__restrict__ mgp, const VT *rprev, VT *xout, VT *sm, VT *csm,
+                                          unsigned long long *ccnt, int *err) {
+    cg::cluster_group cl = cg::this_cluster();
+    const int CS = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+    if (!tail_enter(ccnt, CS, err)) return false;
+    const int ncl = mgp->ncl, nred = mgp->nred, nu1 = mgp->nu1, nu2 = mgp->nu2;
+    const VT omega = (VT)mgp->omega;
+    int cur[MG_MAXLEV];   // which of x (0) / xt (1) holds the level's iterate
+    int chunk[MG_MAXLEV];
+    unsigned magic[MG_MAXLEV];
+    VT *lbase[MG_MAXLEV];
+    for (int l = ncl; l < nred; ++l) {
+        chunk[l] = mgp->cl_chunk[l];
+        magic[l] = mgp->cl_magic[l];
+        lbase[l] = csm + mgp->cl_off[l];
+    }
+    // element c of the cluster level vector whose slice in this CTA starts at
+    // v (x, xt, b or r of a level with chunk ch and owner magic mg)
+    auto rdv = [&](const VT *v, int ch, unsigned mg, int c) -> VT {
+        const int q = (int)__umulhi((unsigned)c, mg);
+        return cl.map_shared_rank(v, q)[c - q * ch];
+    };
+    auto rd = [&](int l, int v, int c) -> VT { return rdv(lbase[l] + (size_t)v * chunk[l], chunk[l], magic[l], c); };
+    // ---- down
+    for (int l = ncl; l < nred; ++l) {
+        const MgLevelDev &L = mgp->lev[l];
+        const int n = L.n, ch = mgp->cl_chunk[l];
+        const int i0 = min(n, rank * ch), i1 = min(n, i0 + ch);
+        VT *xl = csm + mgp->cl_off[l], *bl = xl + 2 * ch, *rl = xl + 3 * ch;
+        const VT *A = Prec<VT>::la(L), *D = Prec<VT>::ld(L);
+        if (l == ncl) {   // right-hand side: restriction of the group's residual (global)
+            const MgLevelDev &F = mgp->lev[l - 1];
+            const VT *rw = Prec<VT>::lr(F);
+            for (int i = i0 + threadIdx.x; i < i1; i += BLOCK)
+                bl[i - i0] = restrict_row<VT, true>(F.rf, rw, F.Wr, n, rprev, i);
+        }
+        cl.sync();   // b complete
+        if (nu1 == 1) {
+            // x1 = w D^-1 b and r = b - A x1 from b alone (no barrier between)
+            for (int i = i0 + threadIdx.x; i < i1; i += BLOCK) {
+                const VT bi_ = bl[i - i0];
+                xl[i - i0] = omega * __ldg(&D[i]) * bi_;
+                const VT s = spmv_row_fx<VT>(L.col, A, n, L.W, i,
+                                             [&](int c) { return omega * __ldg(&D[c]) * rd(l, 2, c); });
+                rl[i - i0] = bi_ - s;
+            }
+            cur[l] = 0;
+        } else {
+            for (int i = i0 + threadIdx.x; i < i1; i += BLOCK) xl[i - i0] = omega * __ldg(&D[i]) * bl[i - i0];
+            int c = 0;
+            for (int s = 1; s < nu1; ++s) {
+                cl.sync();
+                VT *xo = xl + (size_t)(1 - c) * ch;
+                for (int i = i0 + threadIdx.x; i < i1; i += BLOCK)
+                    xo[i - i0] = rd(l, c, i) + omega * __ldg(&D[i]) *
+                                 (bl[i - i0] - spmv_row_fx<VT>(L.col, A, n, L.W, i, [&](int q) { return rd(l, c, q); }));
+                c = 1 - c;
+            }
+            cl.sync();
+            for (int i = i0 + threadIdx.x; i < i1; i += BLOCK)
+                rl[i - i0] = bl[i - i0] - spmv_row_fx<VT>(L.col, A, n, L.W, i, [&](int q) { return rd(l, c, q); });
+            cur[l] = c;
+        }
+        cl.sync();   // r complete
+        const MgLevelDev &C = mgp->lev[l + 1];
+        const VT *rw = Prec<VT>::lr(L);
+        auto rsum = [&](int cc) {   // restrict_row with r read wherever it lives
+            VT acc = 0;
+            for (int q = 0; q < L.Wr; ++q) {
+                const int f = __ldg(&L.rf[(size_t)q * C.n + cc]);
+                if (f >= 0) acc += __ldg(&rw[(size_t)q * C.n + cc]) * rd(l, 3, f);
+            }
+            return acc;
+        };
+        if (l + 1 < nred) {
+            const int chc = mgp->cl_chunk[l + 1];
+            const int c0 = min(C.n, rank * chc), c1 = min(C.n, c0 + chc);
+            VT *bc = csm + mgp->cl_off[l + 1] + 2 * chc;
+            for (int cc = c0 + threadIdx.x; cc < c1; cc += BLOCK) bc[cc - c0] = rsum(cc);
+        } else {
+            VT *sb = sm + mgp->red_off[l + 1] + 2 * C.n;
+            for (int cc = threadIdx.x; cc < C.n; cc += BLOCK) sb[cc] = rsum(cc);
+        }
+    }
+    __syncthreads();
+    smem_levels<VT>(mgp, sm);
+    // ---- up
+    for (int l = nred - 1; l >= ncl; --l) {
+        const MgLevelDev &L = mgp->lev[l];
+        const int n = L.n, ch = mgp->cl_chunk[l];
+        const int i0 = min(n, rank * ch), i1 = min(n, i0 + ch);
+        VT *xl = csm + mgp->cl_off[l], *bl = xl + 2 * ch;
+        const VT *A = Prec<VT>::la(L), *D = Prec<VT>::ld(L), *pw = Prec<VT>::lp(L);
+        int c = cur[l];
+        VT *x = xl + (size_t)c * ch;
+        if (l + 1 == nred) {
+            const VT *xc = sm + mgp->red_off[l + 1];
+            for (int i = i0 + threadIdx.x; i < i1; i += BLOCK) x[i - i0] += prolong_row<VT, false>(L.pc, pw, xc, i);
+        } else {
+            cl.sync();   // level l + 1 smoothed on every CTA
+            const int cc = cur[l + 1];
+            for (int i = i0 + threadIdx.x; i < i1; i += BLOCK) {
+                const int q0 = __ldg(&L.pc[2 * i]), q1 = __ldg(&L.pc[2 * i + 1]);
+                const VT w0 = __ldg(&pw[2 * i]), w1 = __ldg(&pw[2 * i + 1]);
+                VT s = 0;
+                if (q0 >= 0) s += w0 * rd(l + 1, cc, q0);
+                if (q1 >= 0) s += w1 * rd(l + 1, cc, q1);
+                x[i - i0] += s;
+            }
+        }
+        for (int s = 0; s < nu2; ++s) {
+            cl.sync();
+            VT *xo = xl + (size_t)(1 - c) * ch;
+            for (int i = i0 + threadIdx.x; i < i1; i += BLOCK)
+                xo[i - i0] = rd(l, c, i) + omega * __ldg(&D[i]) *
+                             (bl[i - i0] - spmv_row_fx<VT>(L.col, A, n, L.W, i, [&](int q) { return rd(l, c, q); }));
+            c = 1 - c;
+        }
+        cur[l] = c;
+        if (l == ncl) {
+            const VT *xf = xl + (size_t)c * ch;
+            for (int i = i0 + threadIdx.x; i < i1; i += BLOCK) xout[i] = xf[i - i0];
+        }
+    }
+    cl.sync();   // no CTA reuses or leaves its memory while a peer may still read it
+    return true;
+}
+
+// Damped-Jacobi V-cycle: x0 = M^-1 b0 for the group's right-hand side.
+// Returns false if the grid is aborting.
+// b0_visible: b0 is complete on every block at entry (a barrier since it was
+// written), so the finest level's residual is formed without a barrier.
+// csm / ccnt: this block's cluster region and the group's tail counter when
+// the launch runs levels [ncl, nred) as a cluster tail (null: no tail).
+template <typename VT>
+__device__ __noinline__ bool vcycle(const MgDev *__restrict__ mgp, const VT *b0, VT *x0, VT *gbuf, VT *sm,
+                                    unsigned *bar, int G, int bi, int *err, long long *tm, bool b0_visible,
+                                    VT *csm, unsigned long long *ccnt) {
+    const int nred = mgp->nred, nu1 = mgp->nu1, nu2 = mgp->nu2;
+    const bool tail = ccnt != nullptr;
+    const int npar = tail ? mgp->ncl : nred;   // levels run over the whole group
+    const VT omega = (VT)mgp->omega;
+    VT *xcur[MG_MAXLEV];
+    const VT *bl[MG_MAXLEV];
+    size_t offs[MG_MAXLEV];
+    // ---- parallel levels, down
+    size_t off = 0;
+    for (int l = 0; l < npar; ++l) {
+        const MgLevelDev &L = mgp->lev[l];
+        const int n = L.n;
+        offs[l] = off;
+        VT *xa = gbuf + off, *xb = xa + n, *r = xb + n;
+        VT *bn = r + n;  // rhs of level l+1 when that level is parallel too
+        off += 4 * (size_t)n;
+        const VT *b = l == 0 ? b0 : bl[l];
+        bl[l] = b;
+        int r0, r1;
+        own_rows(n, G, bi, r0, r1);
+        VT *x = xa, *xo = xb;
+        jacobi_rows<VT, true>(L, b, nullptr, x, omega, r0, r1, true);
+        // FP32 only: in FP64 the two extra multiplies per gathered entry cost
+        // more than the barrier (measured at level 6)
+        if (sizeof(VT) == 4 && l == 0 && b0_visible && nu1 == 1) {
+            residual_first_rows<VT>(L, b, omega, r, r0, r1);
+        } else {
+            for (int s = 1; s < nu1; ++s) {
+                if (!group_sync(bar, G, err, tm)) return false;
+                jacobi_rows<VT, true>(L, b, x, xo, omega, r0, r1, false);
+                VT *t = x; x = xo; xo = t;
+            }
+            if (!group_sync(bar, G, err, tm)) return false;
+            residual_rows<VT, true>(L, b, x, r, r0, r1);
+        }
+        xcur[l] = x;
+        if (!group_sync(bar, G, err, tm)) return false;
+        const MgLevelDev &C = mgp->lev[l + 1];
+        const VT *rw = Prec<VT>::lr(L);
+        if (l + 1 < npar) {
+            int c0, c1;
+            own_rows(C.n, G, bi, c0, c1);
+            for (int c = c0 + threadIdx.x; c < c1; c += BLOCK) bn[c] = restrict_row<VT, true>(L.rf, rw, L.Wr, C.n, r, c);
+            bl[l + 1] = bn;
+        } else if (!tail) {
+            VT *sb = sm + mgp->red_off[l + 1] + 2 * C.n;
+            for (int c = threadIdx.x; c < C.n; c += BLOCK) sb[c] = restrict_row<VT, true>(L.rf, rw, L.Wr, C.n, r, c);
+        } else if (bi < mgp->cl_size) {
+            // the group's first cluster runs the remaining levels and leaves
+            // the coarse correction of level npar in the group buffer
+            xcur[npar] = gbuf + off;
+            if (!cluster_tail<VT>(mgp, r, gbuf + off, sm, csm, ccnt, err)) return false;
+        } else {
+            xcur[npar] = gbuf + off;
+        }
+    }
+    if (!tail) {
+        __syncthreads();
+        smem_levels<VT>(mgp, sm);
+    }
     // ---- parallel levels, up
-    for (int l = nred - 1; l >= 0; --l) {
+    for (int l = npar - 1; l >= 0; --l) {
         const MgLevelDev &L = mgp->lev[l];
         const int n = L.n;
         VT *xa = gbuf + offs[l], *xb = xa + n;
         VT *x = xcur[l], *xo = (x == xa) ? xb : xa;
         const VT *b = bl[l];
         const VT *pw = Prec<VT>::lp(L);
-        const bool coarse_in_smem = (l + 1 == nred);
+        const bool coarse_in_smem = !tail && (l + 1 == nred);
         const VT *xc = coarse_in_smem ? sm + mgp->red_off[l + 1] : xcur[l + 1];
         if (!coarse_in_smem && !group_sync(bar, G, err, tm)) return false;
         int r0, r1;
@@ -557,6 +768,9 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
     // block preconditioner: the second V-cycle gets its own level scratch so
     // that it can start while other blocks still read the first one's
     VT *gbuf2 = (gbuf && block4) ? gbuf + p.op.mg.group_elems : nullptr;
+    // cluster tail: this block's region after the redundant levels, and the group's entry counter
+    VT *csm = p.cluster ? msm + p.op.mg.red_elems : nullptr;
+    unsigned long long *tcnt = p.cluster ? p.ccnt + grp : nullptr;
     VT *bt3 = gbuf2 ? gbuf2 + p.op.mg.group_elems : nullptr;
     VT *bt4 = bt3 ? bt3 + rsb : nullptr, *bu3 = bt4 ? bt4 + rsb : nullptr, *bu4 = bu3 ? bu3 + rsb : nullptr;
     const int *cpl_col = p.op.cpl.col;
@@ -679,8 +893,8 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
                         bt3[k] = ldcg(&vj[4 * k + 2]) - s3;
                         bt4[k] = ldcg(&vj[4 * k + 3]) - s4;
                     }
-                    if (!vcycle<VT>(mgp, bt3, bu3, gbuf, msm, bar, G, bi, err, tm, false)) return;
-                    if (!vcycle<VT>(mgp, bt4, bu4, gbuf2, msm, bar, G, bi, err, tm, false)) return;
+                    if (!vcycle<VT>(mgp, bt3, bu3, gbuf, msm, bar, G, bi, err, tm, false, csm, tcnt)) return;
+                    if (!vcycle<VT>(mgp, bt4, bu4, gbuf2, msm, bar, G, bi, err, tm, false, csm, tcnt)) return;
                     if (!group_sync(bar, G, err, tm)) return;
                     for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
                         const int q = i & 3;
@@ -692,7 +906,7 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
                     my_bytes += nrows * mg_row_bytes;
                 } else if (use_mg) {
                     VT *zz = Z + (size_t)j * n;
-                    if (!vcycle<VT>(mgp, vj, zz, gbuf, msm, bar, G, bi, err, tm, true)) return;
+                    if (!vcycle<VT>(mgp, vj, zz, gbuf, msm, bar, G, bi, err, tm, true, csm, tcnt)) return;
                     if (!group_sync(bar, G, err, tm)) return;   // z_j complete
                     PHG_TICK(T_VCYCLE);
                     zj = zz;
@@ -999,7 +1213,7 @@ size_t smem_gmres_bytes() { return sizeof(double) * ((MAXM + 1) * MAXM + 2 * MAX
 
 constexpr int GROUPS_CAP = 4096;
 
-struct Layout { size_t v, z, w, r, mg, part, bar, err, total; };
+struct Layout { size_t v, z, w, r, mg, part, bar, err, ccnt, total; };
 
 // per-group multigrid scratch: one V-cycle's levels, or two V-cycles' levels
 // and the 4 vertex vectors of the block preconditioner
@@ -1042,7 +1256,8 @@ Layout layout(const DevSolveOp &op, int nv, int m, Precision prec) {
     // groups * G <= co-resident blocks (< 4096)
     L.bar = L.part + al(8 * (size_t)4096 * 2 * (MAXM + 2));
     L.err = L.bar + al(8 * (size_t)GROUPS_CAP);
-    L.total = L.err + 256;
+    L.ccnt = L.err + 256;
+    L.total = L.ccnt + al(8 * (size_t)GROUPS_CAP);
     return L;
 }
 
@@ -2317,8 +2532,12 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
                            layout(op, nv, m, prec), stats_dev, s);
         if (e0 != cudaErrorNotSupported) return e0;
     }
+    // cluster tail of the V-cycle: the levels [ncl, nred) in the group's first
+    // cluster (needs a group of at least one whole cluster, see below)
+    const bool want_tail = !cheb && op.mgd && op.mg.cl_size > 1 && op.mg.ncl < op.mg.nred;
     const size_t smem = cheb ? sizeof(double) * (4 + 2 * CHEB_KMAX)
-                             : smem_gmres_bytes() + (op.mgd ? es * op.mg.red_elems : 0) + 16;
+                             : smem_gmres_bytes() +
+                                   (op.mgd ? es * (op.mg.red_elems + (want_tail ? op.mg.cl_elems : 0)) : 0) + 16;
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
     void *fn = cheb ? (prec == PREC_MIXED ? (void *)cheb_kernel<float> : (void *)cheb_kernel<double>)
                     : (prec == PREC_MIXED ? (void *)gmres_kernel<float> : (void *)gmres_kernel<double>);
@@ -2339,6 +2558,27 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     const int Gmax = (n + rpb - 1) / (rpb > 32 ? rpb : 32);
     if (G > Gmax) G = Gmax;
     if (G < 1) G = 1;
+    // groups of whole clusters (the first one runs the tail) when the grid
+    // of clusters is co-resident; otherwise the plain launch
+    int CS = 0;
+    if (want_tail && G >= op.mg.cl_size) {
+        CS = op.mg.cl_size;
+        G = G / CS * CS;
+        cudaLaunchConfig_t qc = {};
+        cudaLaunchAttribute qa[1];
+        qa[0].id = cudaLaunchAttributeClusterDimension;
+        qa[0].val.clusterDim.x = CS; qa[0].val.clusterDim.y = 1; qa[0].val.clusterDim.z = 1;
+        qc.gridDim = dim3(groups * G);
+        qc.blockDim = dim3(BLOCK);
+        qc.dynamicSmemBytes = smem;
+        qc.attrs = qa;
+        qc.numAttrs = 1;
+        int nclu = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclu, fn, &qc) != cudaSuccess || (long long)nclu * CS < (long long)groups * G) {
+            cudaGetLastError();
+            CS = 0;
+        }
+    }
     Layout L = layout(op, nv, m, prec);
     char *w = (char *)work;
     p.op = op; p.B = B; p.X = X; p.n = n; p.nv = nv; p.ld = ld; p.m = m; p.max_iter = max_iter; p.tol = tol;
@@ -2374,6 +2614,8 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     p.bar = (unsigned *)(w + L.bar); p.err = (int *)(w + L.err); p.stats = stats_dev;
     p.groups = groups; p.G = G;
     p.wait_limit = wait_limit > 0 ? wait_limit : SPIN_LIMIT;
+    p.cluster = CS;
+    p.ccnt = (unsigned long long *)(w + L.ccnt);
     p.mg_row_bytes = 0.0;
     if (op.mgd)
         for (int l = 0; l < op.mg.nlev; ++l) {
@@ -2393,15 +2635,17 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     // cooperative (all blocks co-resident) through the attribute form, which
     // stream capture records as a cooperative kernel node
     cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute coop[1];
+    cudaLaunchAttribute coop[2];
     coop[0].id = cudaLaunchAttributeCooperative;
     coop[0].val.cooperative = 1;
+    coop[1].id = cudaLaunchAttributeClusterDimension;
+    coop[1].val.clusterDim.x = CS; coop[1].val.clusterDim.y = 1; coop[1].val.clusterDim.z = 1;
     cfg.gridDim = dim3(groups * G);
     cfg.blockDim = dim3(BLOCK);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cfg.attrs = coop;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = CS > 0 ? 2 : 1;
     e = cudaLaunchKernelExC(&cfg, fn, args);
     if (e != cudaSuccess) return e;
     g_kernel_launches += 2;
