@@ -216,6 +216,19 @@ int phg_laplace_solve(phg_ops o, double *ans, const double *F, const double *bnd
  * (member-major: ans, F: nv x V; bnd: nv x os or NULL).  The reference calls
  * solve once per right-hand side. */
 int phg_laplace_solve_batch(phg_ops o, int nv, double *ans, const double *F, const double *bnd, void *stream);
+/* SphereLaplace::solve (src/impl/slaplace_impl.h:84-131) for right-hand sides
+ * on meshes of DIFFERENT levels in one persistent launch (no reference
+ * counterpart: the reference solves one mesh at a time).  Handle k (count <=
+ * 6 handles of one precision on one device, each with its multigrid
+ * hierarchy) takes nv[k] right-hand sides F[k] (nv[k] x V_k, member-major)
+ * with boundary values bnd[k] (nv[k] x os_k, or bnd / bnd[k] NULL) into
+ * ans[k].  Every solve runs to the first handle's restart, tolerance and
+ * iteration cap; the solve record goes to the first handle (phg_ops_check /
+ * phg_ops_last_solve on ops[0]).  Groups of blocks of the one launch take
+ * right-hand sides of any mesh, each with its own operator and hierarchy, so
+ * small meshes share the GPU instead of each holding a launch. */
+int phg_laplace_solve_levels(int count, const phg_ops *ops, const int *nv, double *const *ans, const double *const *F,
+                             const double *const *bnd, void *stream);
 /* No counterpart in the reference.  phg_laplace_calc2 for callers that cannot
  * let a library allocate device memory (memory owned by their own pool or
  * allocator, or loops where the device synchronisation of a cudaMalloc would

@@ -1207,6 +1207,63 @@ extern "C" int phg_laplace_solve_batch(phg_ops o, int nv, double *ans, const dou
     PHG_API_END
 }
 
+extern "C" int phg_laplace_solve_levels(int count, const phg_ops *ops, const int *nv, double *const *ans,
+                                        const double *const *F, const double *const *bnd, void *stream) {
+    PHG_API_BEGIN
+    if (count < 1 || count > 6 || !ops || !nv || !ans || !F) return fail(PHG_ERR_ARG, "bad argument (1 <= count <= 6)");
+    phg_ops o0 = ops[0];
+    for (int k = 0; k < count; ++k) {
+        phg_ops o = ops[k];
+        if (!o || nv[k] < 1 || !ans[k] || !F[k]) return fail(PHG_ERR_ARG, "bad argument for mesh %d", k);
+        if (o->prec != o0->prec || o->dev != o0->dev) return fail(PHG_ERR_ARG, "handles of one precision and device only");
+        if (!o->L.op.mgd) return fail(PHG_ERR_ARG, "mesh %d has no multigrid hierarchy", k);
+    }
+    cudaStream_t s = o0->str(stream);
+    std::vector<Stage> st;
+    st.reserve(count);
+    std::vector<const DevSolveOp *> opk(count);
+    std::vector<const double *> Bk(count), dB(count);
+    std::vector<double *> Xk(count), dA(count);
+    std::vector<int> ldk(count);
+    for (int k = 0; k < count; ++k) {
+        phg_ops o = ops[k];
+        st.emplace_back(o, s);
+        const int V = o->V, rs = o->rs, os = o->os, n = nv[k];
+        const double *dF;
+        CK(st[k].in(F[k], (size_t)V * n, &dF));
+        CK(st[k].in(bnd ? bnd[k] : nullptr, (size_t)os * n, &dB[k]));
+        CK(st[k].out(ans[k], (size_t)V * n, &dA[k]));
+        if (os == 0) dB[k] = nullptr;
+        CK(o->s_a.ensure(8 * (size_t)rs * n)); CK(o->s_c.ensure(8 * (size_t)rs * n));
+        double *b = o->s_a.as<double>(), *x = o->s_c.as<double>();
+        // b = M_L F_in + B2 bnd, x = 0 (src/impl/slaplace_impl.h:84-131)
+        CK(apply_op(o->ML.op.A, o->bnd2.c, dF, V, o->imap(), dB[k], os, nullptr, b, rs, n, s));
+        CK(cudaMemsetAsync(x, 0, 8 * (size_t)rs * n, s));
+        opk[k] = &o->L.op; Bk[k] = b; Xk[k] = x; ldk[k] = rs;
+    }
+    const size_t need = gmres_multi_work_bytes(opk.data(), nv, count, o0->restart, prec_of(o0));
+    if (need > o0->work.n) {
+        CK(cudaStreamSynchronize(s));
+        CK(o0->work.ensure(need));
+    }
+    CK(gmres_solve_multi(opk.data(), nv, Bk.data(), Xk.data(), ldk.data(), count, o0->restart, o0->max_iter,
+                         o0->tol, prec_of(o0), o0->work.p, o0->stats.as<GmresStats>(), s, o0->max_sms,
+                         o0->wait_limit));
+    o0->stats_pending = true;
+    o0->pending_slots = std::max(o0->pending_slots, 1);
+    for (int k = 0; k < count; ++k) {
+        phg_ops o = ops[k];
+        CK(p2u(dA[k], o->V, Xk[k], o->rs, dB[k], o->os, o->p2io.as<int>(), o->isb.as<int>(), o->V, nv[k], s));
+    }
+    bool host = false;
+    for (int k = 0; k < count; ++k) {
+        CK(st[k].finish());
+        host = host || st[k].host;
+    }
+    return host ? check_stats(o0, 1, s) : PHG_OK;
+    PHG_API_END
+}
+
 // the handle's copy of a named inner x inner operator (FP64 values, and the
 // FP32 copy where the mixed path keeps one)
 static int named_op(phg_ops o, const char *name, const double **v64, const float **v32,

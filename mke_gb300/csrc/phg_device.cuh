@@ -168,6 +168,18 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
                         void *work, GmresStats *stats_dev, cudaStream_t s, bool no_alloc = false,
                         int max_sms = 0, const SolveShape *shape = nullptr, long long wait_limit = 0);
 
+// Several multigrid Laplacians (meshes of different levels) in ONE
+// persistent launch: segment k has nvk[k] right-hand sides B[k] + j ldk[k]
+// (solutions X[k] + j ldk[k], initial guesses on entry), all to the same
+// tolerance; groups of blocks take right-hand sides of any segment, each with
+// its own operator, multigrid hierarchy and vectors.  At most 6 segments;
+// work must hold gmres_multi_work_bytes bytes; one GmresStats (the worst
+// right-hand side) in stats_dev.
+size_t gmres_multi_work_bytes(const DevSolveOp *const *ops, const int *nvk, int nseg, int m, Precision p);
+cudaError_t gmres_solve_multi(const DevSolveOp *const *ops, const int *nvk, const double *const *B, double *const *X,
+                              const int *ldk, int nseg, int m, int max_iter, double tol, Precision p, void *work,
+                              GmresStats *stats_dev, cudaStream_t s, int max_sms = 0, long long wait_limit = 0);
+
 // y[v] = A x_in[v] + C x_bnd[v] with every row summed in ascending column
 // order from 0.0 and no fused multiply-add (same rounding as a CPU CSR
 // product); the two partial sums are added last.  x_bnd may be null.

@@ -60,6 +60,26 @@ constexpr int LS_MIN_TUNED = 8;  // the fewest for which the autotuner may choos
 constexpr int LSG_DEFAULT_RHS = 16;
 constexpr int LSG_DEFAULT_ROWS = 10000;
 
+// One operator's share of a multi-operator launch (meshes of several levels
+// in one persistent launch): right-hand sides [v0, next v0) use this
+// operator, read B + k ld and write X + k ld (k = v - v0), and own the Krylov,
+// multigrid-direction, work and residual vectors at the given element offsets
+// (+ k (m+1) n, k m n, k n, k n).
+constexpr int MAXSEG = 6;
+struct MultiSeg {
+    int v0, n, W, ld;
+    const int *col;
+    const double *aval;
+    const double *sval64;
+    const float *sval32;
+    const double *dinv;
+    const MgDev *mgd;
+    const double *B;
+    double *X;
+    size_t voff, zoff, woff, roff;
+    double mg_row_bytes;
+};
+
 struct Params {
     DevSolveOp op;
     const double *B;
@@ -88,6 +108,8 @@ struct Params {
     long long wait_limit;    // clock64 cycles a barrier wait may take before the launch gives up
     int cluster;             // > 0: clustered launch, V-cycle levels [ncl, nred) as a cluster tail
     unsigned long long *ccnt;  // groups: cluster-tail entry counters
+    int nseg;                // > 0: multi-operator launch, right-hand sides by segment (op: sizes only)
+    MultiSeg seg[MAXSEG];
 };
 
 // phase cycle counters kept by block 0 when PHG_PHASE_TIMING is set
@@ -723,8 +745,10 @@ __device__ __noinline__ bool vcycle(const MgDev *__restrict__ mgp, const VT *b0,
     return true;
 }
 
-template <typename VT>
-__global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
+// MULTI: the multi-operator variant (segments of right-hand sides with their
+// own operators); the single-operator launches use the plain instantiation
+template <typename VT, bool MULTI>
+__global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const __grid_constant__ Params p) {
     extern __shared__ double smem[];
     double *H = smem;                       // (m+1) x m
     double *cs = H + (MAXM + 1) * MAXM;     // m
@@ -741,8 +765,9 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
     __shared__ VT vscal[1];
 
     // everything the loops need, copied out of the parameter block
-    const int m = p.m, n = p.n, G = p.G, nv = p.nv, groups = p.groups, max_iter = p.max_iter;
-    const size_t ld = (size_t)p.ld;
+    const int m = p.m, G = p.G, nv = p.nv, groups = p.groups, max_iter = p.max_iter;
+    int n = p.n;              // per right-hand side in a multi-operator launch
+    size_t ld = (size_t)p.ld;
     const double tol = p.tol;
     const int grp = blockIdx.x / G, bi = blockIdx.x % G;
     if (grp >= groups) return;
@@ -753,11 +778,11 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
     int parity = 0;
     int r0, r1;
     own_rows(n, G, bi, r0, r1);
-    const int W = p.op.A.W;
+    int W = p.op.A.W;
     const int *__restrict__ col = p.op.A.col;
     const double *__restrict__ aval = p.op.A.val;
-    const MgDev *mgp = p.op.mgd;
-    const bool use_mg = mgp != nullptr;
+    const MgDev *mgp = MULTI ? p.seg[0].mgd : p.op.mgd;
+    const bool use_mg = mgp != nullptr;   // every segment of a multi-operator launch is multigrid
     const VT *__restrict__ sval;
     if (sizeof(VT) == 8) sval = (const VT *)(use_mg ? (const void *)p.op.A.val : (const void *)p.op.as64);
     else sval = (const VT *)(use_mg ? (const void *)p.op.a32 : (const void *)p.op.as32);
@@ -782,8 +807,9 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
     VT *Vp = (VT *)p.V, *Zp = (VT *)p.Z, *Wp = (VT *)p.Wv;
     double *Rp = p.R;
     const double inner_rtol = sizeof(VT) == 4 ? p.inner_rtol : 0.0;
-    const double es = (double)sizeof(VT), nrows = (double)(r1 - r0);
-    const double mg_row_bytes = p.mg_row_bytes;
+    const double es = (double)sizeof(VT);
+    double nrows = (double)(r1 - r0);
+    double mg_row_bytes = p.mg_row_bytes;
     long long t_start = clock64(), tph = 0;
 #define PHG_TICK(ph)                                                         \
     do {                                                                     \
@@ -808,6 +834,24 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const Params p) {
         VT *Z = use_mg ? Zp + (size_t)v * m * n : nullptr;
         VT *w = Wp + (size_t)v * n;
         double *R = Rp + (size_t)v * n;
+        if (MULTI) {   // the operator, rows and vectors of this right-hand side's segment
+            int k = 0;
+            while (k + 1 < p.nseg && v >= p.seg[k + 1].v0) ++k;
+            const MultiSeg &S = p.seg[k];
+            const int lv = v - S.v0;
+            n = S.n; W = S.W; ld = (size_t)S.ld;
+            col = S.col; aval = S.aval; dinv = S.dinv; mgp = S.mgd;
+            sval = (const VT *)(sizeof(VT) == 8 ? (const void *)S.sval64 : (const void *)S.sval32);
+            mg_row_bytes = S.mg_row_bytes;
+            own_rows(n, G, bi, r0, r1);
+            nrows = (double)(r1 - r0);
+            b = S.B + (size_t)lv * ld;
+            x = S.X + (size_t)lv * ld;
+            V = Vp + S.voff + (size_t)lv * (m + 1) * n;
+            Z = Zp + S.zoff + (size_t)lv * m * n;
+            w = Wp + S.woff + (size_t)lv * n;
+            R = Rp + S.roff + (size_t)lv * n;
+        }
 
         double acc[1];
         {
@@ -2453,12 +2497,13 @@ cudaError_t lsg_solve(const DevSolveOp &op, const double *B, double *X, int nv, 
 
 // The kernels may use all the opt-in shared memory; set once per kernel, so
 // that threads launching with different sizes never race on the attribute.
-static cudaError_t allow_smem(Precision prec) {
-    static std::once_flag once[2];
-    static cudaError_t err[2] = {cudaSuccess, cudaSuccess};
-    const int k = prec == PREC_MIXED ? 1 : 0;
+static cudaError_t allow_smem(Precision prec, bool multi = false) {
+    static std::once_flag once[4];
+    static cudaError_t err[4] = {cudaSuccess, cudaSuccess, cudaSuccess, cudaSuccess};
+    const int k = (prec == PREC_MIXED ? 1 : 0) + (multi ? 2 : 0);
     std::call_once(once[k], [k] {
-        void *fn = k ? (void *)gmres_kernel<float> : (void *)gmres_kernel<double>;
+        void *fn = k == 0 ? (void *)gmres_kernel<double, false> : k == 1 ? (void *)gmres_kernel<float, false>
+                 : k == 2 ? (void *)gmres_kernel<double, true> : (void *)gmres_kernel<float, true>;
         int dev = 0, optin = 0;
         cudaFuncAttributes fa;
         if ((err[k] = cudaGetDevice(&dev)) != cudaSuccess) return;
@@ -2540,7 +2585,7 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
                                    (op.mgd ? es * (op.mg.red_elems + (want_tail ? op.mg.cl_elems : 0)) : 0) + 16;
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
     void *fn = cheb ? (prec == PREC_MIXED ? (void *)cheb_kernel<float> : (void *)cheb_kernel<double>)
-                    : (prec == PREC_MIXED ? (void *)gmres_kernel<float> : (void *)gmres_kernel<double>);
+                    : (prec == PREC_MIXED ? (void *)gmres_kernel<float, false> : (void *)gmres_kernel<double, false>);
     cudaError_t e = cheb ? cudaSuccess : allow_smem(prec);
     if (e != cudaSuccess) return e;
     int per = 0;
@@ -2616,6 +2661,7 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
     p.wait_limit = wait_limit > 0 ? wait_limit : SPIN_LIMIT;
     p.cluster = CS;
     p.ccnt = (unsigned long long *)(w + L.ccnt);
+    p.nseg = 0;
     p.mg_row_bytes = 0.0;
     if (op.mgd)
         for (int l = 0; l < op.mg.nlev; ++l) {
@@ -2664,6 +2710,142 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
         for (int k = 0; k < T_NPHASE; ++k) fprintf(stderr, " %s=%lld", nm[k], k == T_BARRIERS ? h[k] : h[k] / 1000);
         fprintf(stderr, " (kcycles)\n");
     }
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------ several mesh levels ---
+// Workspace of a multi-operator launch: the per-RHS vectors of every segment
+// back to back, one group scratch sized for the largest hierarchy.
+struct MultiLayout {
+    size_t v, z, w, r, mg, part, bar, err, ccnt, total;
+    size_t voff[MAXSEG], zoff[MAXSEG], woff[MAXSEG], roff[MAXSEG];
+};
+
+static MultiLayout multi_layout(const DevSolveOp *const *ops, const int *nvk, int nseg, int m, Precision prec) {
+    MultiLayout L{};
+    const size_t es = prec == PREC_MIXED ? 4 : 8;
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    size_t ev = 0, ez = 0, ew = 0, er = 0, ge = 0;
+    int nv = 0;
+    for (int k = 0; k < nseg; ++k) {
+        const size_t n = (size_t)ops[k]->A.n;
+        L.voff[k] = ev; L.zoff[k] = ez; L.woff[k] = ew; L.roff[k] = er;
+        ev += (size_t)nvk[k] * (m + 1) * n;
+        ez += (size_t)nvk[k] * m * n;
+        ew += (size_t)nvk[k] * n;
+        er += (size_t)nvk[k] * n;
+        ge = std::max(ge, ops[k]->mg.group_elems);
+        nv += nvk[k];
+    }
+    const int groups = nv < GROUPS_CAP ? nv : GROUPS_CAP;
+    L.v = 0;
+    L.z = L.v + al(es * ev);
+    L.w = L.z + al(es * ez);
+    L.r = L.w + al(es * ew);
+    L.mg = L.r + al(8 * er);
+    L.part = L.mg + al(es * ge * (size_t)groups);
+    L.bar = L.part + al(8 * (size_t)4096 * 2 * (MAXM + 2));
+    L.err = L.bar + al(8 * (size_t)GROUPS_CAP);
+    L.ccnt = L.err + 256;
+    L.total = L.ccnt + al(8 * (size_t)GROUPS_CAP);
+    return L;
+}
+
+size_t gmres_multi_work_bytes(const DevSolveOp *const *ops, const int *nvk, int nseg, int m, Precision prec) {
+    if (nseg < 1 || nseg > MAXSEG) return 0;
+    return multi_layout(ops, nvk, nseg, m, prec).total;
+}
+
+cudaError_t gmres_solve_multi(const DevSolveOp *const *ops, const int *nvk, const double *const *B, double *const *X,
+                              const int *ldk, int nseg, int m, int max_iter, double tol, Precision prec, void *work,
+                              GmresStats *stats_dev, cudaStream_t s, int max_sms, long long wait_limit) {
+    if (nseg < 1 || nseg > MAXSEG || m < 1 || m > MAXM) return cudaErrorInvalidValue;
+    int nv = 0, nmax = 0;
+    size_t red = 0, ge = 0;
+    for (int k = 0; k < nseg; ++k) {
+        const DevSolveOp &op = *ops[k];
+        if (!op.mgd || op.block4 || nvk[k] < 1) return cudaErrorInvalidValue;   // multigrid Laplacians only
+        nv += nvk[k];
+        nmax = std::max(nmax, op.A.n);
+        red = std::max(red, op.mg.red_elems);
+        ge = std::max(ge, op.mg.group_elems);
+    }
+    const size_t es = prec == PREC_MIXED ? 4 : 8;
+    const size_t smem = smem_gmres_bytes() + es * red + 16;
+    if (smem > 227 * 1024) return cudaErrorInvalidValue;
+    void *fn = prec == PREC_MIXED ? (void *)gmres_kernel<float, true> : (void *)gmres_kernel<double, true>;
+    cudaError_t e = allow_smem(prec, true);
+    if (e != cudaSuccess) return e;
+    int per = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, BLOCK, smem)) != cudaSuccess) return e;
+    if (per < 1) return cudaErrorInvalidConfiguration;
+    const int sms = (max_sms > 0 && max_sms < sm_count()) ? max_sms : sm_count();
+    const int cap = sms * per;
+    // groups of G blocks, G from the largest mesh (no block below 256 rows there)
+    int groups = nv < cap ? nv : cap;
+    if (groups > GROUPS_CAP) groups = GROUPS_CAP;
+    int G = cap / groups;
+    const int Gmax = (nmax + 255) / 256;
+    if (G > Gmax) G = Gmax;
+    if (G < 1) G = 1;
+    const MultiLayout L = multi_layout(ops, nvk, nseg, m, prec);
+    char *w = (char *)work;
+    Params p;
+    p.op = *ops[0];   // launch bookkeeping only: every right-hand side reads its segment
+    p.B = B[0]; p.X = X[0]; p.n = ops[0]->A.n; p.nv = nv; p.ld = ldk[0]; p.m = m; p.max_iter = max_iter;
+    p.tol = tol;
+    p.V = w + L.v; p.Z = w + L.z; p.Wv = w + L.w; p.R = (double *)(w + L.r);
+    p.vstride = 0;
+    p.mgbuf = w + L.mg;
+    p.group_elems = ge;
+    {
+        const char *ev = getenv("PHG_INNER_RTOL");
+        p.inner_rtol = ev ? atof(ev) : INNER_RTOL;
+    }
+    p.cheb_k = 0;
+    p.part = (double *)(w + L.part);
+    p.bar = (unsigned *)(w + L.bar); p.err = (int *)(w + L.err); p.stats = stats_dev;
+    p.groups = groups; p.G = G;
+    p.wait_limit = wait_limit > 0 ? wait_limit : SPIN_LIMIT;
+    p.cluster = 0;
+    p.ccnt = (unsigned long long *)(w + L.ccnt);
+    p.mg_row_bytes = 0.0;
+    p.timers = nullptr;
+    p.nseg = nseg;
+    int v0 = 0;
+    for (int k = 0; k < MAXSEG; ++k) p.seg[k] = MultiSeg{};
+    for (int k = 0; k < nseg; ++k) {
+        const DevSolveOp &op = *ops[k];
+        MultiSeg &S = p.seg[k];
+        S.v0 = v0; S.n = op.A.n; S.W = op.A.W; S.ld = ldk[k];
+        S.col = op.A.col; S.aval = op.A.val; S.sval64 = op.A.val; S.sval32 = op.a32; S.dinv = op.dinv;
+        S.mgd = op.mgd;
+        S.B = B[k]; S.X = X[k];
+        S.voff = L.voff[k]; S.zoff = L.zoff[k]; S.woff = L.woff[k]; S.roff = L.roff[k];
+        S.mg_row_bytes = 0.0;
+        for (int l = 0; l < op.mg.nlev; ++l) {
+            const MgLevelDev &Lv = op.mg.lev[l];
+            S.mg_row_bytes += (double)Lv.n / (double)op.A.n *
+                              ((op.mg.nu1 + op.mg.nu2 + 1) * (Lv.W * (4.0 + es) + 4.0 * es) + 4.0 * es);
+        }
+        v0 += nvk[k];
+    }
+    if ((e = cudaMemsetAsync(w + L.bar, 0, L.total - L.bar, s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(stats_dev, 0, sizeof(GmresStats), s)) != cudaSuccess) return e;
+    void *args[] = {&p};
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute coop[1];
+    coop[0].id = cudaLaunchAttributeCooperative;
+    coop[0].val.cooperative = 1;
+    cfg.gridDim = dim3(groups * G);
+    cfg.blockDim = dim3(BLOCK);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = coop;
+    cfg.numAttrs = 1;
+    if ((e = cudaLaunchKernelExC(&cfg, fn, args)) != cudaSuccess) return e;
+    g_kernel_launches += 2;
+    fold_err<<<1, 1, 0, s>>>(p.err, stats_dev);
     return cudaGetLastError();
 }
 

@@ -86,6 +86,7 @@ SIGNATURES = {
     "phg_laplace_calc2": (C.c_int, [_vp, _vp, _vp, _vp]),
     "phg_laplace_solve": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "phg_laplace_solve_batch": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp]),
+    "phg_laplace_solve_levels": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "phg_ops_check": (C.c_int, [_vp, _vp]),
     "phg_ops_set_sms": (C.c_int, [_vp, C.c_int]),
     "phg_ops_set_wait_limit": (C.c_int, [_vp, C.c_longlong]),
@@ -602,6 +603,31 @@ class Baroclin:
     def calc_L_1(self, u1, u2, z1, z2, bnd=None, out1=None, out2=None, stream=None):
         """Baroclin::calc_L_1: the inverse linearised step around (z1, z2)."""
         return self._linear("phg_baroclin_calc_L_1", u1, u2, z1, z2, bnd, out1, out2, stream)
+
+
+def laplace_solve_levels(ops_list, F_list, bnd_list=None, stream=None):
+    """SphereLaplace::solve for right-hand sides on meshes of several levels in
+    one persistent launch (phg_laplace_solve_levels): ops_list[k] an Operators
+    handle, F_list[k] its nv_k x V_k right-hand sides (numpy arrays or CUDA
+    tensors); returns the solutions in the same layout."""
+    n = len(ops_list)
+    outs, Fs, Bs, keep = [], [], [], []
+    for k, (o, F) in enumerate(zip(ops_list, F_list)):
+        F2 = F if hasattr(F, "data_ptr") else _f8(np.atleast_2d(F))
+        keep.append(F2)
+        outs.append(np.zeros((F2.shape[0], o.mesh.size)) if not hasattr(F2, "data_ptr") else F2.new_zeros(F2.shape))
+        b = None if bnd_list is None else bnd_list[k]
+        if b is not None and not hasattr(b, "data_ptr"):
+            b = _f8(np.atleast_2d(b))
+        keep.append(b)
+        Fs.append(_ptr(F2)); Bs.append(_ptr(b))
+    h = (C.c_void_p * n)(*[o._h for o in ops_list])
+    nv = (C.c_int * n)(*[int(f.shape[0]) for f in keep[0::2]])
+    ans = (C.c_void_p * n)(*[_ptr(o) for o in outs])
+    fp = (C.c_void_p * n)(*Fs)
+    bp = (C.c_void_p * n)(*Bs)
+    _check(lib().phg_laplace_solve_levels(n, h, nv, ans, fp, bp if bnd_list is not None else None, _stream(stream)))
+    return outs
 
 
 def device_bytes():
