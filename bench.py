@@ -319,6 +319,8 @@ def run_ours(args, ws, rank, local):
 
     # BASELINE config 1: the level-3 Laplace solve to 1e-12 against the exact solution
     lap3 = None if args.no_laplace3 else run_laplace_l3()
+    # the element-loop Jacobian quadrature on an ensemble's fields
+    jq = None if args.no_spmv else run_jac_quad()
 
     # serving trace (the first --bench-serve-requests requests of the 10,000-request trace)
     served = None
@@ -418,6 +420,9 @@ def run_ours(args, ws, rank, local):
             "mixed_over_fp64": r3(baroclin["mixed_over_fp64"]),
             "rel_diff": r3(baroclin[f"state_rel_diff_mixed_vs_fp64_after_{baroclin['steps']}"])},
         "laplace_l3": None if lap3 is None else {k: (r3(v) if isinstance(v, float) else v) for k, v in lap3.items()},
+        "jac_quad": None if jq is None else {"level": jq["level"], "members": jq["members"],
+                                            "us_per_call": r3(jq["us_per_call"]), "gbs": r3(jq["gbs"]),
+                                            "frac_of_hbm": r3(jq["frac_of_hbm"])},
         "worst_solve_relres": r3(max(mixed["stats"]["worst_relres"], fp64["stats"]["worst_relres"])),
         "roofline": roof,
         "e2e": {"value": replicas.whole_job_rate(args.steps, e2e, ws), "unit": "steps/s",
@@ -530,6 +535,49 @@ def run_reference(args, ws, rank):
         "cpu_baseline": {"value": v, "unit": "steps/s", "cores": host_threads(), "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
+
+
+def run_jac_quad(level: int = 6, nv: int = 32, reps: int = 20):
+    """The element-loop Jacobian quadrature (split pass + k_jac_quad) on the
+    fields of an ensemble step: level 6, 32 members, timed with CUDA events on
+    its stream, L2 flushed before each call.  Algorithmic bytes: the split
+    pass reads both FP64 fields and writes their float pairs (32 V bytes per
+    member); the quadrature reads per row its ring (6 x 12 bytes) and the
+    row point's cos/sin (8), per member both fields as float pairs (16 V)
+    and writes the 8 FP64 right-hand sides (64 rows)."""
+    import torch
+    from mke_gb300 import fields, phelm
+    m = phelm.Mesh.sphere(level)
+    lat, lon = m.latlon()
+    ops = phelm.Operators(m, phelm.PHG_MIXED)
+    J = phelm.SphereJacobian(ops)
+    rng = np.random.default_rng(SEED)
+    U = np.stack([fields.sh_field(fields.random_coeffs(rng, 1, 12), lat, lon) for _ in range(nv)])
+    du = torch.tensor(U, device="cuda")
+    dw = torch.roll(du, 1, dims=1).contiguous()
+    out = torch.empty((nv, 8, m.inner_size), dtype=torch.float64, device="cuda")
+    st = torch.cuda.Stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    with torch.cuda.stream(st):
+        J.derivs(du, dw, out, quad=True, stream=st)
+        for a, b in ev:
+            flush.zero_()
+            a.record(st)
+            J.derivs(du, dw, out, quad=True, stream=st)
+            b.record(st)
+    st.synchronize()
+    us = sum(a.elapsed_time(b) for a, b in ev) / reps * 1e3
+    V, rs = m.size, m.inner_size
+    byts = nv * 2 * V * 16 + rs * (6 * 12 + 8) + nv * (2 * V * 8 + 8 * rs * 8)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    return {"level": level, "members": nv, "us_per_call": us, "bytes": byts, "gbs": byts / us / 1e3,
+            "frac_of_hbm": byts / us / 1e3 / peak}
 
 
 def run_laplace_l3(reps: int = 20):

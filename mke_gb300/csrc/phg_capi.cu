@@ -77,6 +77,8 @@ thread_local long long t_dev_bytes = 0;
 // bumped by every device (re)allocation: a captured step graph holds raw
 // buffer addresses and is re-captured when this moved since its capture
 std::atomic<long long> g_alloc_epoch{0};
+// bumped when the tuned launch shapes change: captured steps re-capture
+std::atomic<long long> g_shape_epoch{0};
 
 struct DBuf {
     void *p = nullptr;
@@ -505,7 +507,7 @@ struct phg_ops_s {
     ColsBufs bnd2, bnd3, d1b, d2b, d1cb, d2cb;
     JacOps J;
     // element-loop geometry of the FP32 Jacobian right-hand sides (mixed time steps)
-    DBuf jq_idx, jq_geo, jq_cs;
+    DBuf jq_ring, jq_rxy, jq_cs, jq_split;
     JacQuadDev jq;
     // which Picard iterations of a mixed-precision step use it: 2 (the default)
     // every iteration of a barotropic step but the last, whose Jacobian is the
@@ -862,11 +864,11 @@ extern "C" int phg_ops_create(phg_mesh h, int precision, phg_ops *out) {
     {
         JacQuadHost jh;
         build_jac_quad(m, jh);
-        if (jh.max_tri <= 6) {   // the kernel's 8-lane rows take at most 6 triangles per point
-            CK(upload(o->jq_idx, jh.idx)); CK(upload(o->jq_geo, jh.geo)); CK(upload(o->jq_cs, jh.cs0));
+        if (jh.max_tri <= 6) {   // the kernel's 8-lane rows take closed rings of at most 6 triangles
+            CK(upload(o->jq_ring, jh.ring)); CK(upload(o->jq_rxy, jh.rxy)); CK(upload(o->jq_cs, jh.cs0));
             o->jq.n = m.rs;
-            o->jq.idx = (const int2 *)o->jq_idx.p;
-            o->jq.geo = (const float4 *)o->jq_geo.p;
+            o->jq.ring = o->jq_ring.as<int>();
+            o->jq.rxy = (const float2 *)o->jq_rxy.p;
             o->jq.cs0 = (const float2 *)o->jq_cs.p;
             o->jq_mode = precision == PHG_MIXED ? env_int("PHG_JAC_QUAD", 2) : 0;
         }
@@ -1034,7 +1036,10 @@ int jacobian_derivs_dev(phg_ops_s *o, const double *u, const double *v, int ld, 
                         cudaStream_t s, double tol, bool quad = false) {
     CK(o->s_b.ensure(8 * (size_t)o->rs * 8 * nv));
     double *rhs = o->s_b.as<double>();
-    if (quad && o->jq.n) CK(jac_quad(o->jq, o->J, u, v, ld, o->imap(), o->bmap(), rhs, o->rs, nv, s));
+    if (quad && o->jq.n) {
+        CK(o->jq_split.ensure(16 * (size_t)o->V * nv));
+        CK(jac_quad(o->jq, o->J, u, v, ld, o->imap(), o->bmap(), rhs, o->rs, nv, o->V, (float2 *)o->jq_split.p, s));
+    }
     else CK(jac_rhs(o->J, u, v, ld, o->imap(), o->bmap(), rhs, o->rs, nv, s));
     CK(cudaMemsetAsync(sol, 0, 8 * (size_t)o->rs * 8 * nv, s));
     return solve(o, o->MJ.op, rhs, sol, 8 * nv, o->rs, tol, slot, s);
@@ -1537,7 +1542,7 @@ extern "C" int phg_ops_autotune(phg_ops o, int nmembers, char *report, int repor
     if ((r = tune_solve(o, "laplace", o->L.op, nmembers, s, rep))) return r;
     if ((r = tune_spmm(o, nmembers, s, rep))) return r;
     CK(cudaStreamSynchronize(s));
-    g_alloc_epoch++;   // captured steps pick up the new shapes
+    g_shape_epoch++;   // captured steps pick up the new shapes
     copy_out(rep.text, report, report_len);
     return PHG_OK;
     PHG_API_END
@@ -1562,7 +1567,7 @@ extern "C" int phg_tune_load(const char *path, int *entries) {
     PHG_API_BEGIN
     if (!path) return fail(PHG_ERR_ARG, "NULL path");
     const int k = tune_load(path);
-    g_alloc_epoch++;   // captured steps pick up the new shapes
+    g_shape_epoch++;   // captured steps pick up the new shapes
     if (k < 0) return fail(PHG_ERR_IO, "cannot read %s (missing or malformed)", path);
     if (entries) *entries = k;
     return PHG_OK;
@@ -1572,7 +1577,7 @@ extern "C" int phg_tune_load(const char *path, int *entries) {
 extern "C" void phg_tune_clear(void) {
     PHG_API_BEGIN
     tune_clear();
-    g_alloc_epoch++;
+    g_shape_epoch++;
     PHG_API_END_VOID
 }
 
@@ -1640,7 +1645,10 @@ extern "C" int phg_jacobian_derivs(phg_ops o, int quad, double *out, const doubl
         return fail(PHG_ERR_ARG, "phg_jacobian_derivs takes device pointers");
     if (quad && !o->jq.n) return fail(PHG_ERR_ARG, "this mesh has points with more than 6 triangles");
     cudaStream_t s = o->str(stream);
-    if (quad) CK(jac_quad(o->jq, o->J, u, v, o->V, o->imap(), o->bmap(), out, o->rs, nv, s));
+    if (quad) {
+        CK(o->jq_split.ensure(16 * (size_t)o->V * nv));
+        CK(jac_quad(o->jq, o->J, u, v, o->V, o->imap(), o->bmap(), out, o->rs, nv, o->V, (float2 *)o->jq_split.p, s));
+    }
     else CK(jac_rhs(o->J, u, v, o->V, o->imap(), o->bmap(), out, o->rs, nv, s));
     return PHG_OK;
     PHG_API_END
@@ -1736,17 +1744,33 @@ struct phg_barvortex_s {
         int nv = 0;
         const double *u = nullptr, *bnd_u = nullptr, *bnd_w = nullptr, *forcing = nullptr;
         cudaStream_t s = nullptr;
-        long long epoch = -1;
+        long long epoch = -1;           // tuned-shape epoch
+        unsigned long long sig = 0;     // addresses and sizes of the step's scratch buffers
         bool operator==(const GraphKey &k) const {
             return nv == k.nv && u == k.u && bnd_u == k.bnd_u && bnd_w == k.bnd_w && forcing == k.forcing &&
-                   s == k.s && epoch == k.epoch;
+                   s == k.s && epoch == k.epoch && sig == k.sig;
         }
-    } gkey;
-    cudaGraphExec_t gexec = nullptr;
-    long long g_launches = 0;   // kernels in one replay
+    };
+    // captured steps by key (member count, arrays, stream, tuned shapes and the
+    // scratch buffers' addresses),
+    // the least recently used dropped beyond GRAPHS: a caller whose member
+    // count changes between runs (a serving lane) replays the graph of each
+    // count it meets again instead of capturing anew
+    static constexpr int GRAPHS = 8;
+    struct Graph {
+        GraphKey key;
+        cudaGraphExec_t exec = nullptr;
+        long long launches = 0;   // kernels in one replay
+        long long used = 0;
+    };
+    std::vector<Graph> graphs;
+    long long graph_clock = 0;
     DBuf agg;                   // solve records folded over the steps of runs since the last check
     bool agg_pending = false;
-    ~phg_barvortex_s() { if (gexec) cudaGraphExecDestroy(gexec); }
+    ~phg_barvortex_s() {
+        for (auto &g : graphs)
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+    }
 };
 
 extern "C" int phg_barvortex_create(phg_ops o, const phg_bv_conf *c, const double *coriolis, phg_barvortex *out) {
@@ -1924,6 +1948,39 @@ static int bv_check_agg(phg_barvortex_s *b, cudaStream_t s) {
 // nsteps steps in place.  With a graph captured for this key every step is
 // one replay; otherwise the first step is enqueued kernel by kernel (it
 // sizes every buffer) and the next one is captured.
+// A signature of what a captured barotropic step bakes in beyond its
+// arguments: every scratch buffer it writes or reads (the handle's and the
+// stepper's) and the handle's solver settings and SM cap, which become
+// kernel parameters and grid sizes.  A captured step is valid only while the
+// signature is unchanged.  Per stepper, so that allocations by other handles
+// (other threads) do not invalidate its graphs.
+static unsigned long long bv_sig(const phg_barvortex_s *b) {
+    const phg_ops_s *o = b->o;
+    unsigned long long h = 1469598103934665603ull;
+    auto word = [&](unsigned long long v) { h = (h ^ v) * 1099511628211ull; };
+    auto mix = [&](const DBuf &d) {
+        word((unsigned long long)(uintptr_t)d.p);
+        word((unsigned long long)d.n);
+    };
+    word((unsigned long long)o->max_sms);
+    word((unsigned long long)o->restart);
+    word((unsigned long long)o->max_iter);
+    double tol = o->tol;
+    unsigned long long tb = 0;
+    memcpy(&tb, &tol, sizeof tb);
+    word(tb);
+    word((unsigned long long)o->wait_limit);
+    word((unsigned long long)o->jq_mode);
+    for (const DBuf *d : {&o->work, &o->stats, &o->s_a, &o->s_b, &o->s_c, &o->s_d, &o->s_e, &o->s_part, &o->s_out,
+                          &o->jq_split, &o->hist})
+        mix(*d);
+    for (const DBuf &d : o->st) mix(d);
+    for (const DBuf *d : {&b->w, &b->dw, &b->FC, &b->u_n, &b->w_n, &b->u_n1, &b->tmp1, &b->tmp2, &b->uin, &b->F,
+                          &b->rp, &b->x, &b->jsol, &b->nr0, &b->nr, &b->done, &b->ubnd, &b->wbnd, &b->frc, &b->agg})
+        mix(*d);
+    return h;
+}
+
 static int bv_run(phg_barvortex b, int nv, int nsteps, double *u, const double *bnd_u, const double *bnd_w,
                   const double *forcing, void *stream) {
     if (!b || !u || nv < 1 || nsteps < 0) return fail(PHG_ERR_ARG, "bad argument");
@@ -1950,14 +2007,26 @@ static int bv_run(phg_barvortex b, int nv, int nsteps, double *u, const double *
     b->agg_pending = true;
     phg_barvortex_s::GraphKey k;
     k.nv = nv; k.u = dio; k.bnd_u = dbu; k.bnd_w = dbw; k.forcing = df; k.s = s;
-    k.epoch = g_alloc_epoch.load();
+    k.epoch = g_shape_epoch.load();
+    k.sig = bv_sig(b);
     int left = nsteps;
-    if (!b->gexec || !(k == b->gkey)) {
-        if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; }
+    // drop graphs of other tuned shapes or moved buffers; find this key's
+    for (size_t q = 0; q < b->graphs.size();) {
+        if (b->graphs[q].key.epoch != k.epoch || b->graphs[q].key.sig != k.sig) {
+            cudaGraphExecDestroy(b->graphs[q].exec);
+            b->graphs.erase(b->graphs.begin() + q);
+        } else {
+            ++q;
+        }
+    }
+    phg_barvortex_s::Graph *gr = nullptr;
+    for (auto &g : b->graphs)
+        if (g.key == k) gr = &g;
+    if (!gr) {
         if ((r = bv_step_dev(b, nv, dio, dio, dbu, dbw, df, s))) return r;
         CK(stats_fold(slots, b->nslots, agg, s));
         --left;
-        k.epoch = g_alloc_epoch.load();
+        k.sig = bv_sig(b);   // the eager step may have grown a buffer
         if (left > 0) {
             const bool prof = o->prof;
             o->prof = false;
@@ -1975,23 +2044,40 @@ static int bv_run(phg_barvortex b, int nv, int nsteps, double *u, const double *
                 if (r) return r;
                 return fail(PHG_ERR_CUDA, "step capture: %s", cudaGetErrorString(ef != cudaSuccess ? ef : ec));
             }
-            cudaError_t ei = cudaGraphInstantiate(&b->gexec, g, 0);
+            cudaGraphExec_t ex = nullptr;
+            cudaError_t ei = cudaGraphInstantiate(&ex, g, 0);
             cudaGraphDestroy(g);
-            if (ei != cudaSuccess) {
-                b->gexec = nullptr;
-                return fail(PHG_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ei));
+            if (ei != cudaSuccess) return fail(PHG_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ei));
+            if (bv_sig(b) != k.sig) {   // the capture itself moved a buffer: run the rest uncaptured
+                cudaGraphExecDestroy(ex);
+                ex = nullptr;
+                for (; left > 0; --left) {
+                    if ((r = bv_step_dev(b, nv, dio, dio, dbu, dbw, df, s))) return r;
+                    CK(stats_fold(slots, b->nslots, agg, s));
+                }
             }
-            if (g_alloc_epoch.load() != k.epoch) {   // the capture itself moved a buffer
-                cudaGraphExecDestroy(b->gexec);
-                b->gexec = nullptr;
-                return fail(PHG_ERR_CUDA, "a buffer was reallocated while the step was captured");
+            if (ex && (int)b->graphs.size() >= phg_barvortex_s::GRAPHS) {   // drop the least recently used
+                size_t lru = 0;
+                for (size_t q = 1; q < b->graphs.size(); ++q)
+                    if (b->graphs[q].used < b->graphs[lru].used) lru = q;
+                cudaGraphExecDestroy(b->graphs[lru].exec);
+                b->graphs.erase(b->graphs.begin() + lru);
             }
-            b->gkey = k;
-            b->g_launches = nl;
+            if (ex) {
+                phg_barvortex_s::Graph ng;
+                ng.key = k;
+                ng.exec = ex;
+                ng.launches = nl;
+                b->graphs.push_back(ng);
+                gr = &b->graphs.back();
+            }
         }
     }
-    for (int i = 0; i < left; ++i) CK(cudaGraphLaunch(b->gexec, s));
-    g_kernel_launches += b->g_launches * left;
+    if (gr) {
+        gr->used = ++b->graph_clock;
+        for (int i = 0; i < left; ++i) CK(cudaGraphLaunch(gr->exec, s));
+        g_kernel_launches += gr->launches * left;
+    }
     b->last_stream = s;
     CK(st.finish());
     if (!st.host) return PHG_OK;   // device arguments: checked by phg_barvortex_last_stats

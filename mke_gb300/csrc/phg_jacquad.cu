@@ -19,8 +19,10 @@
 // Mapping: 8 lanes per row (lane = triangle slot; at most 6 triangles meet at a
 // point of an icosahedral mesh, lanes 6-7 carry zeros), 4 rows per warp.  The
 // quadrature is done once per row and kept in registers; the member loop then
-// gathers the two fields at the triangle's vertices (FP64 differences, then
-// FP32), forms the 8 per-triangle contributions and sums them over the row's
+// gathers the two fields at the triangle's vertices, splits each FP64 value
+// into two floats with integer instructions (split_f64: no FP64 pipe work in
+// the loop) and forms the field differences from them, forms the 8
+// per-triangle contributions in FP32 and sums them over the row's
 // lanes with a 3-stage butterfly of warp shuffles that leaves lane k holding
 // right-hand side k (7 shuffles per lane instead of 24 for 8 separate
 // reductions).  Lane k adds the row's boundary-column product of RHS k (the
@@ -69,6 +71,47 @@ __device__ __forceinline__ void rule_node(int q, float &l0, float &la, float &lb
     }
 }
 
+// x = hi + lo as two floats (|x - hi - lo| < 2^-46 |x|) by 32-bit integer
+// instructions on the two words of x.  GB300 runs FP64 arithmetic, FP64 <->
+// FP32 conversions and (by the counters) 64-bit integer work on its narrow
+// FP64 pipe: with a DSUB and a conversion per field difference that pipe was
+// 85 % busy and bounded this kernel (ncu, level 6 x 32 members).  hi takes the
+// top 24 significand bits, lo the next 24; zero gives zeros, magnitudes
+// outside [2^-96, 2^128) the hardware conversion.
+__device__ __forceinline__ void split_f64(double x, float &hi, float &lo) {
+    const unsigned w1 = (unsigned)__double2hiint(x), w0 = (unsigned)__double2loint(x);
+    if (((w1 << 1) | w0) == 0u) { hi = lo = 0.f; return; }
+    const unsigned sgn = w1 & 0x80000000u;
+    const int e = (int)((w1 >> 20) & 0x7ffu) - 1023;
+    if (e < -96 || e > 127) { hi = (float)x; lo = 0.f; return; }
+    // significand bits 51..29 (hi) and 28..0 (r)
+    hi = __uint_as_float(sgn | ((unsigned)(e + 127) << 23) | ((w1 & 0xFFFFFu) << 3) | (w0 >> 29));
+    const unsigned r = w0 & 0x1FFFFFFFu;
+    if (r == 0u) { lo = 0.f; return; }
+    const int msb = 31 - __clz(r);
+    const int ex = e - 52 + msb + 127;
+    if (ex < 1) { lo = 0.f; return; }
+    const unsigned mant = msb <= 23 ? (r << (23 - msb)) & 0x7fffffu : (r >> (msb - 23)) & 0x7fffffu;
+    lo = __uint_as_float(sgn | ((unsigned)ex << 23) | mant);
+}
+
+// the double of a float by 32-bit integer instructions (exact; subnormal
+// floats become zero, infinities and NaN stay so)
+__device__ __forceinline__ double widen(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    const unsigned sgn = u & 0x80000000u;
+    if (e == 0u) return __hiloint2double((int)sgn, 0);
+    const unsigned E = e == 255u ? 0x7ffu : e + 1023u - 127u;
+    const unsigned m = u & 0x7fffffu;
+    return __hiloint2double((int)(sgn | (E << 20) | (m >> 3)), (int)(m << 29));
+}
+
+// x_a - x_0 from the (hi, lo) splits: the hi difference is exact when the two
+// are within a factor 2 (Sterbenz), so the cancellation of nearby values
+// loses nothing; otherwise it is one rounding of a difference that did not cancel
+__device__ __forceinline__ float diff2(float ah, float al, float zh, float zl) { return (ah - zh) + (al - zl); }
+
 // keep the half of 2H values whose index bit is `hi`, add the partner's copy
 template <int H>
 __device__ __forceinline__ void fold(float (&s)[8], int hi, int off) {
@@ -80,11 +123,29 @@ __device__ __forceinline__ void fold(float (&s)[8], int hi, int off) {
     }
 }
 
-__global__ void __launch_bounds__(256) k_jac_quad(JacQuadDev G, JacOps J, const double *__restrict__ u,
+// both fields of nv members as (hi, lo) float pairs, member-major with
+// leading dimension V (one pass; the quadrature then gathers 8 bytes a value
+// and does no conversion work)
+__global__ void __launch_bounds__(256) k_split2(const double *__restrict__ u, const double *__restrict__ w, int ld,
+                                                int V, long long total, float2 *__restrict__ su,
+                                                float2 *__restrict__ sw) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long v = t / V, i = t - v * V;
+        float h, l;
+        split_f64(u[v * ld + i], h, l);
+        su[t] = make_float2(h, l);
+        split_f64(w[v * ld + i], h, l);
+        sw[t] = make_float2(h, l);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_jac_quad(JacQuadDev G, JacOps J, const float2 *__restrict__ su,
+                                                  const float2 *__restrict__ sw, int V, const double *__restrict__ u,
                                                   const double *__restrict__ w, int ld, const int *__restrict__ imap,
                                                   const int *__restrict__ bmap, double *__restrict__ out, int ldo,
                                                   int nv) {
-    const int slot = threadIdx.x & 7;
+    const int lane = threadIdx.x & 31, slot = lane & 7, base = lane & ~7;
     const int n = G.n;
     const int v0 = blockIdx.y * MCHUNK, v1 = min(nv, v0 + MCHUNK);
     // this lane's boundary-column operator and field (RHS k = slot)
@@ -96,46 +157,58 @@ __global__ void __launch_bounds__(256) k_jac_quad(JacQuadDev G, JacOps J, const 
     for (int i0 = blockIdx.x * ROWS_PER_BLOCK; i0 < n; i0 += gridDim.x * ROWS_PER_BLOCK) {
         const int i = i0 + (threadIdx.x >> 3);
         const bool row = i < n;
-        // quadrature of this lane's triangle (once per row)
-        float ca = 0.f, cb = 0.f, ea = 0.f, eb = 0.f, m = 0.f, mc = 0.f;
-        int pa = INT_MIN, pb = INT_MIN;
+        // ring vertex `slot` of the row (triangle slot = (row point, ring[slot], ring[slot + 1]))
+        int rk = INT_MIN;
+        float2 g = make_float2(0.f, 0.f);
         if (row && slot < 6) {
-            const int2 id = G.idx[(size_t)i * 8 + slot];
-            if (id.x != INT_MIN) {
-                const float4 g = G.geo[(size_t)i * 8 + slot];   // (xa, ya, xb, yb) - (x0, y0)
-                const float D = g.x * g.w - g.z * g.y;           // twice the signed area
-                const float iD = 1.0f / D;
-                // grad f = (ca (fa - f0) + cb (fb - f0), ea (fa - f0) + eb (fb - f0))
-                ca = g.w * iD; cb = -g.y * iD; ea = -g.z * iD; eb = g.x * iD;
-                const float area = 0.5f * fabsf(D);
-                m = area * (1.0f / 3.0f);                        // int_T phi_i (the rule is exact)
-                const float2 cs = G.cs0[i];                      // cos x0, sin x0
-                float acc = 0.f;
+            rk = G.ring[(size_t)i * 8 + slot];
+            if (rk != INT_MIN) g = G.rxy[(size_t)i * 8 + slot];
+        }
+        const unsigned valid = __ballot_sync(0xffffffffu, rk != INT_MIN);
+        const int deg = __popc((valid >> base) & 0xffu);
+        const int nxt = base + (deg > 0 ? (slot + 1) % deg : 0);   // the lane holding ring[slot + 1]
+        const float gbx = __shfl_sync(0xffffffffu, g.x, nxt), gby = __shfl_sync(0xffffffffu, g.y, nxt);
+        const bool tri = slot < deg;
+        // quadrature of this lane's triangle (once per row): vertices 0 (the
+        // row point, at the origin), a = ring[slot], b = ring[slot + 1]
+        float ca = 0.f, cb = 0.f, ea = 0.f, eb = 0.f, m = 0.f, mc = 0.f;
+        if (tri) {
+            const float D = g.x * gby - gbx * g.y;   // twice the signed area
+            const float iD = 1.0f / D;
+            // grad f = (ca (fa - f0) + cb (fb - f0), ea (fa - f0) + eb (fb - f0))
+            ca = gby * iD; cb = -g.y * iD; ea = -gbx * iD; eb = g.x * iD;
+            const float area = 0.5f * fabsf(D);
+            m = area * (1.0f / 3.0f);                // int_T phi_i (the rule is exact)
+            const float2 cs = G.cs0[i];              // cos x0, sin x0
+            float acc = 0.f;
 #pragma unroll
-                for (int q = 0; q < 7; ++q) {
-                    float l0, la, lb, wq;
-                    rule_node(q, l0, la, lb, wq);
-                    float sd, cd;
-                    sincosf(la * g.x + lb * g.z, &sd, &cd);     // x - x0 at the node (small)
-                    acc += wq * l0 * (cs.x * cd - cs.y * sd);   // phi_i cos(x) at the node
-                }
-                mc = area * acc;                                 // int_T phi_i cos(x)
-                pa = id.x; pb = id.y;
+            for (int q = 0; q < 7; ++q) {
+                float l0, la, lb, wq;
+                rule_node(q, l0, la, lb, wq);
+                float sd, cd;
+                sincosf(la * g.x + lb * gbx, &sd, &cd);     // x - x0 at the node (small)
+                acc += wq * l0 * (cs.x * cd - cs.y * sd);   // phi_i cos(x) at the node
             }
+            mc = area * acc;                         // int_T phi_i cos(x)
         }
         const int p = row ? imap[i] : 0;
         const int kb0 = (row && cptr) ? cptr[i] : 0, kb1 = (row && cptr) ? cptr[i + 1] : 0;
         for (int v = v0; v < v1; ++v) {
-            const double *fu = u + (size_t)v * ld, *fw = w + (size_t)v * ld;
+            const float2 *fu = su + (size_t)v * V, *fw = sw + (size_t)v * V;
+            // lane `slot` < deg: the fields at ring[slot]; lane 6: at the row point
+            float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
+            if (row && slot < 6 && rk >= 0) { a = fu[rk]; b = fw[rk]; }
+            if (row && slot == 6) { a = fu[p]; b = fw[p]; }
+            const int l6 = base + 6;
+            const float u0h = __shfl_sync(0xffffffffu, a.x, l6), u0l = __shfl_sync(0xffffffffu, a.y, l6);
+            const float w0h = __shfl_sync(0xffffffffu, b.x, l6), w0l = __shfl_sync(0xffffffffu, b.y, l6);
+            // differences from the row point: the hi parts cancel exactly for nearby values
+            const float du = (a.x - u0h) + (a.y - u0l), dw = (b.x - w0h) + (b.y - w0l);
+            const float dub = __shfl_sync(0xffffffffu, du, nxt), dwb = __shfl_sync(0xffffffffu, dw, nxt);
             float s[8];
-            if (pa != INT_MIN) {
-                const double u0 = fu[p], w0 = fw[p];
-                const double ua = pa >= 0 ? fu[pa] : 0.0, ub = pb >= 0 ? fu[pb] : 0.0;
-                const double wa = pa >= 0 ? fw[pa] : 0.0, wb = pb >= 0 ? fw[pb] : 0.0;
-                const float dua = (float)(ua - u0), dub = (float)(ub - u0);
-                const float dwa = (float)(wa - w0), dwb = (float)(wb - w0);
-                const float ux = ca * dua + cb * dub, uy = ea * dua + eb * dub;
-                const float wx = ca * dwa + cb * dwb, wy = ea * dwa + eb * dwb;
+            if (tri) {
+                const float ux = ca * du + cb * dub, uy = ea * du + eb * dub;
+                const float wx = ca * dw + cb * dwb, wy = ea * dw + eb * dwb;
                 s[0] = uy * mc; s[1] = wx * m; s[2] = ux * mc; s[3] = wy * m;
                 s[4] = uy * m; s[5] = wx * mc; s[6] = ux * m; s[7] = wy * mc;
             } else {
@@ -147,13 +220,19 @@ __global__ void __launch_bounds__(256) k_jac_quad(JacQuadDev G, JacOps J, const 
             fold<2>(s, (slot >> 1) & 1, 2);
             fold<1>(s, slot & 1, 1);
             if (row) {
-                double b = 0.0;
-                const double *fb = on_u ? fu : fw;
-                for (int k = kb0; k < kb1; ++k) {
-                    const int c = ccol[k];
-                    b += cval[k] * fb[bmap ? bmap[c] : c];
+                double r;
+                if (kb0 < kb1) {   // rows at the boundary point (FP64, a handful of rows)
+                    double bs = 0.0;
+                    const double *fb = (on_u ? u : w) + (size_t)v * ld;
+                    for (int k = kb0; k < kb1; ++k) {
+                        const int c = ccol[k];
+                        bs += cval[k] * fb[bmap ? bmap[c] : c];
+                    }
+                    r = bs + (double)s[0];
+                } else {
+                    r = widen(s[0]);
                 }
-                out[((size_t)v * 8 + slot) * ldo + i] = b + (double)s[0];
+                out[((size_t)v * 8 + slot) * ldo + i] = r;
             }
         }
     }
@@ -164,8 +243,8 @@ __global__ void __launch_bounds__(256) k_jac_quad(JacQuadDev G, JacOps J, const 
 void build_jac_quad(const Mesh &m, JacQuadHost &h) {
     const int rs = m.rs;
     h.max_tri = 0;
-    h.idx.assign((size_t)rs * 8 * 2, INT_MIN);
-    h.geo.assign((size_t)rs * 8 * 4, 0.f);
+    h.ring.assign((size_t)rs * 8, INT_MIN);
+    h.rxy.assign((size_t)rs * 8 * 2, 0.f);
     h.cs0.assign((size_t)rs * 2, 0.f);
     for (int i = 0; i < rs; ++i) {
         const int p = m.inner[i];
@@ -173,39 +252,70 @@ void build_jac_quad(const Mesh &m, JacQuadHost &h) {
         const double x0 = m.u(p, z), y0 = m.v(p, z);
         h.cs0[2 * i] = (float)std::cos(x0);
         h.cs0[2 * i + 1] = (float)std::sin(x0);
-        int k = 0;
-        h.max_tri = std::max(h.max_tri, m.adj_ptr[p + 1] - m.adj_ptr[p]);
-        for (int q = m.adj_ptr[p]; q < m.adj_ptr[p + 1] && k < 6; ++q, ++k) {
-            const int t = m.adj[q];
-            int other[2], no = 0;
+        const int nt = m.adj_ptr[p + 1] - m.adj_ptr[p];
+        h.max_tri = std::max(h.max_tri, nt);
+        if (nt > 6 || nt < 3) { h.max_tri = std::max(h.max_tri, 7); continue; }
+        // the triangles' other two vertices, then the closed ring around p
+        std::vector<int> ea(nt), eb(nt);
+        for (int q = 0; q < nt; ++q) {
+            const int t = m.adj[m.adj_ptr[p] + q];
+            int o[2], no = 0;
             for (int c = 0; c < 3; ++c)
-                if (m.tri[3 * t + c] != p && no < 2) other[no++] = m.tri[3 * t + c];
+                if (m.tri[3 * t + c] != p && no < 2) o[no++] = m.tri[3 * t + c];
+            ea[q] = o[0]; eb[q] = o[1];
+        }
+        std::vector<int> ring(1, ea[0]);
+        std::vector<char> used(nt, 0);
+        used[0] = 1;
+        int cur = eb[0];
+        bool closed = false;
+        for (int step = 1; step < nt; ++step) {
+            ring.push_back(cur);
+            int nextv = -1;
+            for (int q = 0; q < nt; ++q) {
+                if (used[q]) continue;
+                if (ea[q] == cur) nextv = eb[q];
+                else if (eb[q] == cur) nextv = ea[q];
+                if (nextv >= 0) { used[q] = 1; break; }
+            }
+            if (nextv < 0) break;
+            cur = nextv;
+            if (step == nt - 1) closed = cur == ring[0];
+        }
+        if (!closed || (int)ring.size() != nt) { h.max_tri = std::max(h.max_tri, 7); continue; }
+        for (int k = 0; k < nt; ++k) {
+            const int v = ring[k];
             const size_t e = (size_t)i * 8 + k;
-            for (int c = 0; c < 2; ++c)
-                h.idx[2 * e + c] = m.bnd[other[c]] ? -1 : other[c];
-            h.geo[4 * e + 0] = (float)(m.u(other[0], z) - x0);
-            h.geo[4 * e + 1] = (float)(m.v(other[0], z) - y0);
-            h.geo[4 * e + 2] = (float)(m.u(other[1], z) - x0);
-            h.geo[4 * e + 3] = (float)(m.v(other[1], z) - y0);
+            h.ring[e] = m.bnd[v] ? -1 : v;
+            h.rxy[2 * e] = (float)(m.u(v, z) - x0);
+            h.rxy[2 * e + 1] = (float)(m.v(v, z) - y0);
         }
     }
 }
 
 size_t jac_quad_bytes(int rs, int V, int nv) {
-    // per row: 6 triangles x (2 indices + 4 coordinates) + cos/sin of the row
-    // point; both fields read once per member; 8 FP64 right-hand sides written
-    return (size_t)rs * (6 * 24 + 8) + (size_t)nv * (2 * (size_t)V * 8 + 8 * (size_t)rs * 8);
+    // split pass: both fields read (FP64) and written (float pairs) once;
+    // quadrature: per row 6 ring vertices x (index + 2 coordinates) + cos/sin
+    // of the row point, both fields read once per member as float pairs, 8
+    // FP64 right-hand sides written
+    return (size_t)nv * 2 * (size_t)V * 16 + (size_t)rs * (6 * 12 + 8) +
+           (size_t)nv * (2 * (size_t)V * 8 + 8 * (size_t)rs * 8);
 }
 
 cudaError_t jac_quad(const JacQuadDev &G, const JacOps &J, const double *u, const double *v, int ld, const int *imap,
-                     const int *bmap, double *out, int ldo, int nv, cudaStream_t s) {
+                     const int *bmap, double *out, int ldo, int nv, int V, float2 *split, cudaStream_t s) {
     if (G.n <= 0 || nv <= 0) return cudaSuccess;
+    const long long total = (long long)nv * V;
+    float2 *su = split, *sw = split + total;
+    long long blocks = (total + 255) / 256;
+    if (blocks > 152LL * 16) blocks = 152LL * 16;
+    k_split2<<<(unsigned)blocks, 256, 0, s>>>(u, v, ld, V, total, su, sw);
     const int rowblocks = (G.n + ROWS_PER_BLOCK - 1) / ROWS_PER_BLOCK;
     const int chunks = (nv + MCHUNK - 1) / MCHUNK;
     if (chunks > 65535) return cudaErrorInvalidValue;
     dim3 grid(rowblocks, chunks);
-    k_jac_quad<<<grid, 256, 0, s>>>(G, J, u, v, ld, imap, bmap, out, ldo, nv);
-    g_kernel_launches++;
+    k_jac_quad<<<grid, 256, 0, s>>>(G, J, su, sw, V, u, v, ld, imap, bmap, out, ldo, nv);
+    g_kernel_launches += 2;
     return cudaGetLastError();
 }
 

@@ -175,6 +175,21 @@ int lane_run(Lane *L, int nv) {
     return r ? r : r2;
 }
 
+// `steps` time steps of the barotropic members [0, nv) in one call: the step
+// captured as a CUDA graph (one per member count, kept by the handle) and
+// replayed, then one synchronisation that checks every step's solves
+int lane_steps(Lane *L, int nv, int steps) {
+    Server *S = L->srv;
+    const int grant = sm_acquire(S, natural_sms(L, nv));
+    int r = phg_ops_set_sms(L->ops, grant);
+    if (r == PHG_OK)
+        r = phg_barvortex_run(L->bv, nv, steps, L->dU, L->os ? L->dB : nullptr, L->os ? L->dBw : nullptr, nullptr,
+                              L->stream);
+    int r2 = phg_barvortex_last_stats(L->bv, nullptr, nullptr, nullptr, nullptr, nullptr);   // waits, checks
+    sm_release(S, grant);
+    return r ? r : r2;
+}
+
 void free_slots(Lane *L) {
     cudaFree(L->dU); cudaFree(L->dOut); cudaFree(L->dB); cudaFree(L->dBw);
     cudaFreeHost(L->hIn); cudaFreeHost(L->hOut); cudaFreeHost(L->hB);
@@ -386,7 +401,17 @@ void bv_loop(Lane *L) {
                     st = PHG_ERR_CUDA;
             }
         }
-        if (!st) st = lane_run(L, n);   // one time step of every member
+        // A full lane (no request could join before a member leaves) runs as
+        // many steps as the nearest finish in one call, from the captured step
+        // graph; a lane with free slots steps once, so that requests arriving
+        // meanwhile join at the next step.
+        int ksteps = 1;
+        if (n >= L->cap) {
+            ksteps = act[0]->steps_left;
+            for (int k = 1; k < n; ++k) ksteps = std::min(ksteps, act[k]->steps_left);
+            ksteps = std::max(1, ksteps);
+        }
+        if (!st) st = ksteps > 1 ? lane_steps(L, n, ksteps) : lane_run(L, n);
         if (st) {
             std::lock_guard<std::mutex> lk(S->mu);
             for (Pending *p : act) push_done(S, p, st, n);
@@ -396,7 +421,7 @@ void bv_loop(Lane *L) {
         }
         fin.clear();
         for (int k = n - 1; k >= 0; --k)
-            if (--act[k]->steps_left == 0) {
+            if ((act[k]->steps_left -= std::max(1, ksteps)) <= 0) {
                 fin.push_back(k);
                 if (cudaMemcpyAsync(L->hOut + (size_t)k * V, L->dU + (size_t)k * V, 8 * (size_t)V,
                                     cudaMemcpyDeviceToHost, L->stream))

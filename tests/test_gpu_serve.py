@@ -153,3 +153,33 @@ def test_budget_evicts_idle_lane():
         assert st["bytes_in_use"] <= budget and st["lanes"] == 1
     finally:
         srv.close()
+
+
+def test_full_lane_runs_captured_steps():
+    """A barotropic lane whose slots are all taken advances its members by
+    several steps per call from the captured step graph (one graph per member
+    count); every request's result equals the same integration by direct
+    library calls.  Six 5-step requests on two slots: the lane is full
+    throughout, members leave and join between runs."""
+    level, steps = 3, 5
+    m = phelm.Mesh.sphere(level)
+    lat, lon = m.latlon()
+    psi = serve.barvortex_inputs(lat, lon, 6, 21)
+    srv = phelm.Server(precision=phelm.PHG_MIXED, hbm_budget_bytes=20e9, max_slots=2, solve_tol=1e-12,
+                       step_tol=1e-12)
+    try:
+        for k in range(6):
+            srv.submit(BV, level, psi[k], steps=steps + (k % 2), tag=k)
+        got = wait_for(srv, set(range(6)))
+    finally:
+        srv.close()
+    ops = phelm.Operators(m, phelm.PHG_MIXED, tol=1e-12)
+    conf = dict(tau=1e-3, sigma=1.6e-2, mu=8e-5, k1=1.0, k2=1.0, theta=0.5, picard_iters=3)
+    bv = phelm.BarVortex(ops, coriolis=np.sin(lat), **conf)
+    z = np.zeros(m.outer_size)
+    for k in range(6):
+        assert got[k]["status"] == 0, got[k]
+        x = psi[k].copy()
+        for _ in range(steps + (k % 2)):
+            x = bv.calc(x, z, z)
+        assert rel(got[k]["output"], x) <= TOL, k
