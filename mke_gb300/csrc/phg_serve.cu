@@ -48,9 +48,26 @@ struct Pending {
 
 struct Server;
 
+// One mesh level of a packed Laplace lane: its handle and member slots.
+struct Sub {
+    int level = 0;
+    phg_ops ops = nullptr;
+    int V = 0, os = 0, osb = 1, cap = 0;
+    long long bytes = 0;     // budget held for this level
+    double last_used = 0;    // server time of its last turn
+    double *dU = nullptr, *dOut = nullptr, *dB = nullptr;
+    double *hIn = nullptr, *hOut = nullptr, *hB = nullptr;
+};
+
 struct Lane {
     Server *srv = nullptr;
     int kind = 0, level = 0;
+    // packed Laplace lane: the solves of every level up to Server::pack_level
+    // go into one multi-level launch per turn (level = 0, one Sub per level met)
+    bool packed = false;
+    std::vector<std::unique_ptr<Sub>> subs;
+    std::vector<int> want;        // levels to open ahead of traffic (under Server::mu)
+    std::vector<int> opened;      // levels whose Sub is ready (under Server::mu)
     // device resources, owned by the lane thread
     phg_ops ops = nullptr;
     phg_barvortex bv = nullptr;
@@ -86,6 +103,7 @@ struct Server {
     std::condition_variable sm_cv;
     std::mutex mesh_mu;
     std::map<int, phg_mesh> meshes;
+    int pack_level = 0;   // Laplace requests of levels <= this share one lane and one launch per turn
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 };
 
@@ -217,11 +235,52 @@ long long slot_bytes(const Lane *L) {
     return (long long)L->V * 8 * (L->kind == PHG_REQ_LAPLACE_SOLVE ? 2 : 1) + (long long)L->osb * 8 * 2;
 }
 
+// Reserve base + cap x per bytes of the HBM budget for a lane (cap lowered to
+// what fits), evicting idle lanes and waiting for their memory when needed;
+// held receives the reservation.
+int reserve(Lane *L, long long base, long long per, int &cap, long long &held) {
+    Server *S = L->srv;
+    {
+        std::unique_lock<std::mutex> lk(S->mu);
+        for (;;) {
+            const long long freeb = S->budget - S->in_use;
+            const long long fit = per > 0 ? (freeb - base) / per : cap;
+            if (fit >= 1) {
+                cap = (int)std::min<long long>(cap, fit);
+                break;
+            }
+            if (base + per > S->budget) return PHG_ERR_BUDGET;   // never fits
+            // evict idle lanes, then wait for their memory
+            bool any = false;
+            for (auto &kv : S->lanes) {
+                Lane *o = kv.second;
+                if (o != L && o->ready && !o->stop && o->active == 0 && o->queue.empty()) {
+                    o->stop = true;
+                    o->cv.notify_all();
+                    any = true;
+                }
+            }
+            bool busy = false;
+            for (auto &kv : S->lanes) busy |= kv.second != L && !kv.second->closed;
+            if (!any && !busy) return PHG_ERR_BUDGET;
+            if (S->shutting) return PHG_ERR_BUDGET;
+            S->mem_cv.wait_for(lk, std::chrono::milliseconds(50));
+        }
+        held = base + (long long)cap * per;
+        S->in_use += held;
+    }
+    return PHG_OK;
+}
+
 // Build the handles, size the slots from two probe calls, reserve the budget
 // and allocate everything the lane will use.
 int lane_open(Lane *L) {
     Server *S = L->srv;
     const phg_serve_conf &c = S->conf;
+    if (L->packed) {   // the per-level handles open with their first requests
+        if (cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking) != cudaSuccess) return PHG_ERR_CUDA;
+        return PHG_OK;
+    }
     phg_mesh m = nullptr;
     int r = get_mesh(S, L->level, &m);
     if (r) return r;
@@ -250,35 +309,9 @@ int lane_open(Lane *L) {
     const long long per = std::max(0LL, b2 - b1) + slot_bytes(L);
     const long long base = b1 - (b2 - b1);
     int cap = c.max_slots > 0 ? c.max_slots : 64;
-    {
-        std::unique_lock<std::mutex> lk(S->mu);
-        for (;;) {
-            const long long freeb = S->budget - S->in_use;
-            const long long fit = per > 0 ? (freeb - base) / per : cap;
-            if (fit >= 1) {
-                cap = (int)std::min<long long>(cap, fit);
-                break;
-            }
-            if (base + per > S->budget) return PHG_ERR_BUDGET;   // never fits
-            // evict idle lanes, then wait for their memory
-            bool any = false;
-            for (auto &kv : S->lanes) {
-                Lane *o = kv.second;
-                if (o != L && o->ready && !o->stop && o->active == 0 && o->queue.empty()) {
-                    o->stop = true;
-                    o->cv.notify_all();
-                    any = true;
-                }
-            }
-            bool busy = false;
-            for (auto &kv : S->lanes) busy |= kv.second != L && !kv.second->closed;
-            if (!any && !busy) return PHG_ERR_BUDGET;
-            if (S->shutting) return PHG_ERR_BUDGET;
-            S->mem_cv.wait_for(lk, std::chrono::milliseconds(50));
-        }
-        L->bytes = base + (long long)cap * per;
-        S->in_use += L->bytes;
-    }
+    long long held = 0;
+    if ((r = reserve(L, base, per, cap, held))) return r;
+    L->bytes += held;
     L->cap = cap;
     if ((r = alloc_slots(L, cap))) return r;
     if ((r = lane_run(L, cap))) return r;   // allocate every workspace now
@@ -292,9 +325,130 @@ int lane_open(Lane *L) {
     return PHG_OK;
 }
 
+void sub_free(Sub *u) {
+    cudaFree(u->dU); cudaFree(u->dOut); cudaFree(u->dB);
+    cudaFreeHost(u->hIn); cudaFreeHost(u->hOut); cudaFreeHost(u->hB);
+    u->dU = u->dOut = u->dB = nullptr;
+    u->hIn = u->hOut = u->hB = nullptr;
+}
+
+int sub_alloc(Sub *u, int n) {
+    const size_t v = (size_t)u->V * n * 8, b = (size_t)u->osb * n * 8;
+    if (cudaMalloc(&u->dU, v) || cudaMalloc(&u->dOut, v) || cudaMalloc(&u->dB, b) ||
+        cudaHostAlloc(&u->hIn, v, cudaHostAllocDefault) || cudaHostAlloc(&u->hOut, v, cudaHostAllocDefault) ||
+        cudaHostAlloc(&u->hB, b, cudaHostAllocDefault)) {
+        cudaGetLastError();
+        sub_free(u);
+        return PHG_ERR_CUDA;
+    }
+    cudaMemset(u->dB, 0, b);
+    return PHG_OK;
+}
+
+// one batched solve of n members of a packed lane's level alone (the
+// probes that size its memory)
+int sub_probe(Lane *L, Sub *u, int n) {
+    int r = phg_laplace_solve_batch(u->ops, n, u->dOut, u->dU, u->os ? u->dB : nullptr, L->stream);
+    int r2 = phg_ops_check(u->ops, L->stream);
+    return r ? r : r2;
+}
+
+int sub_open_(Lane *L, int level, Sub **out, const std::vector<Sub *> &busy);
+
+// close a level of a packed lane and give its budget back
+void sub_close(Lane *L, size_t i) {
+    Server *S = L->srv;
+    Sub *u = L->subs[i].get();
+    if (L->stream) cudaStreamSynchronize(L->stream);
+    if (u->ops) phg_ops_destroy(u->ops);
+    sub_free(u);
+    cudaGetLastError();
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->in_use -= u->bytes;
+        L->bytes -= u->bytes;
+        S->mem_cv.notify_all();
+    }
+    L->subs.erase(L->subs.begin() + (long)i);
+}
+
+// open a level of a packed Laplace lane: handle, probes, budget, slots; a
+// level that fails to open leaves no Sub behind (its reservation stays with
+// the lane until it closes)
+int sub_open(Lane *L, int level, Sub **out, const std::vector<Sub *> &busy) {
+    const size_t n0 = L->subs.size();
+    const int r = sub_open_(L, level, out, busy);
+    if (r && L->subs.size() > n0) sub_close(L, L->subs.size() - 1);
+    return r;
+}
+
+int sub_open_(Lane *L, int level, Sub **out, const std::vector<Sub *> &busy) {
+    Server *S = L->srv;
+    const phg_serve_conf &c = S->conf;
+    auto u = std::make_unique<Sub>();
+    u->level = level;
+    phg_mesh m = nullptr;
+    int r = get_mesh(S, level, &m);
+    if (r) return r;
+    int T = 0, rs = 0;
+    if ((r = phg_mesh_info(m, &u->V, &T, &rs, &u->os))) return r;
+    u->osb = std::max(u->os, 1);
+    const long long b0 = thread_bytes();
+    if ((r = phg_ops_create(m, c.precision, &u->ops))) return r;
+    Sub *raw = u.get();
+    L->subs.push_back(std::move(u));   // closed with the lane from here on
+    if ((r = phg_ops_set_solver(raw->ops, 30, c.solve_tol, 20000))) return r;
+    if ((r = sub_alloc(raw, 2))) return r;
+    cudaMemset(raw->dU, 0, (size_t)raw->V * 2 * 8);
+    if ((r = sub_probe(L, raw, 1))) return r;
+    const long long b1 = thread_bytes() - b0;
+    if ((r = sub_probe(L, raw, 2))) return r;
+    const long long b2 = thread_bytes() - b0;
+    sub_free(raw);
+    const long long slot = (long long)raw->V * 16 + (long long)raw->osb * 8;
+    const long long per = std::max(0LL, b2 - b1) + slot;
+    const long long base = b1 - (b2 - b1);
+    int cap = c.max_slots > 0 ? c.max_slots : 64;
+    long long held = 0;
+    // when the budget is short, the lane's idle levels (least recently used
+    // first) make room before other lanes are waited for
+    while ((r = reserve(L, base, per, cap, held)) == PHG_ERR_BUDGET) {
+        size_t victim = L->subs.size();
+        for (size_t i = 0; i < L->subs.size(); ++i) {
+            Sub *x = L->subs[i].get();
+            if (x == raw || std::find(busy.begin(), busy.end(), x) != busy.end()) continue;
+            if (victim == L->subs.size() || x->last_used < L->subs[victim]->last_used) victim = i;
+        }
+        if (victim == L->subs.size()) return r;
+        sub_close(L, victim);
+    }
+    if (r) return r;
+    L->bytes += held;
+    raw->bytes = held;
+    raw->cap = cap;
+    if ((r = sub_alloc(raw, cap))) return r;
+    cudaMemset(raw->dU, 0, (size_t)raw->V * cap * 8);
+    if ((r = sub_probe(L, raw, cap))) return r;
+    const long long actual = thread_bytes() - b0 + (long long)cap * slot;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->in_use += actual - held;
+        L->bytes += actual - held;
+        raw->bytes = actual;
+    }
+    *out = raw;
+    return PHG_OK;
+}
+
 void lane_close(Lane *L) {
     Server *S = L->srv;
     if (L->stream) cudaStreamSynchronize(L->stream);
+    for (auto &u : L->subs) {
+        if (u->ops) phg_ops_destroy(u->ops);
+        u->ops = nullptr;
+        sub_free(u.get());
+    }
+    L->subs.clear();
     if (L->bv) phg_barvortex_destroy(L->bv);
     if (L->ops) phg_ops_destroy(L->ops);
     L->bv = nullptr;
@@ -357,6 +511,142 @@ void laplace_loop(Lane *L) {
         std::lock_guard<std::mutex> lk(S->mu);
         for (int k = 0; k < n; ++k) push_done(S, batch[k], st, n);
         batch.clear();
+        L->active = 0;
+        L->last_busy = S->now();
+    }
+}
+
+// A packed Laplace lane: every turn takes the queued requests of all its
+// levels (up to each level's slots) and solves them in ONE multi-level
+// persistent launch (phg_laplace_solve_levels): groups of blocks take
+// right-hand sides of any level, so small meshes share the GPU instead of
+// each holding a launch.
+void packed_loop(Lane *L) {
+    Server *S = L->srv;
+    const int maxs = S->conf.max_slots > 0 ? S->conf.max_slots : 64;
+    std::vector<Pending *> batch;
+    for (;;) {
+        batch.clear();
+        std::vector<int> open_now;
+        {
+            std::unique_lock<std::mutex> lk(S->mu);
+            L->cv.wait(lk, [&] { return L->stop || !L->queue.empty() || !L->want.empty(); });
+            open_now.swap(L->want);
+        }
+        for (int lv : open_now) {   // levels preloaded ahead of traffic
+            bool have = false;
+            for (auto &u : L->subs) have |= u->level == lv;
+            Sub *u = nullptr;
+            const int r = have ? PHG_OK : sub_open(L, lv, &u, {});
+            std::lock_guard<std::mutex> lk(S->mu);
+            L->opened.push_back(r ? -lv : lv);   // -lv: the level failed to open
+            S->ready_cv.notify_all();
+        }
+        {
+            std::unique_lock<std::mutex> lk(S->mu);
+            if (L->queue.empty()) {
+                if (L->stop) { L->closing = true; return; }
+                continue;
+            }
+            std::map<int, int> per;
+            std::deque<Pending *> keep;
+            while (!L->queue.empty()) {
+                Pending *p = L->queue.front();
+                L->queue.pop_front();
+                int cap = maxs;
+                for (auto &u : L->subs)
+                    if (u->level == p->r.level) cap = u->cap;
+                if (per[p->r.level] < cap) { per[p->r.level]++; batch.push_back(p); }
+                else keep.push_back(p);
+            }
+            L->queue.swap(keep);
+            L->active = (int)batch.size();
+        }
+        const double ta = S->now();
+        // the levels of this turn, opened on first use
+        std::vector<Sub *> used;
+        std::vector<std::vector<Pending *>> mem;
+        std::vector<Pending *> later;   // beyond the slots of a level opened this turn
+        int st = PHG_OK;
+        for (Pending *p : batch) {
+            p->t_admit = ta;
+            size_t k = 0;
+            while (k < used.size() && used[k]->level != p->r.level) ++k;
+            if (k == used.size()) {
+                Sub *u = nullptr;
+                for (auto &x : L->subs)
+                    if (x->level == p->r.level) u = x.get();
+                if (!u) {
+                    const int r = sub_open(L, p->r.level, &u, used);
+                    if (r) { std::lock_guard<std::mutex> lk(S->mu); push_done(S, p, r, 0); continue; }
+                }
+                used.push_back(u);
+                mem.emplace_back();
+            }
+            if ((int)mem[k].size() < used[k]->cap) mem[k].push_back(p);
+            else later.push_back(p);
+        }
+        if (!later.empty()) {
+            std::lock_guard<std::mutex> lk(S->mu);
+            for (auto it = later.rbegin(); it != later.rend(); ++it) L->queue.push_front(*it);
+            L->active -= (int)later.size();
+        }
+        const int nseg = (int)used.size();
+        std::vector<phg_ops> ops(nseg);
+        std::vector<int> nv(nseg);
+        std::vector<double *> ans(nseg), bnd(nseg);
+        std::vector<const double *> F(nseg);
+        long long rows = 0;
+        for (int k = 0; k < nseg && !st; ++k) {
+            Sub *u = used[k];
+            const int n = (int)mem[k].size();
+            for (int j = 0; j < n; ++j) {
+                Pending *p = mem[k][j];
+                memcpy(u->hIn + (size_t)j * u->V, p->r.input, 8 * (size_t)u->V);
+                if (u->os) {
+                    if (p->r.bnd) memcpy(u->hB + (size_t)j * u->os, p->r.bnd, 8 * (size_t)u->os);
+                    else memset(u->hB + (size_t)j * u->os, 0, 8 * (size_t)u->os);
+                }
+            }
+            if (cudaMemcpyAsync(u->dU, u->hIn, 8 * (size_t)u->V * n, cudaMemcpyHostToDevice, L->stream) ||
+                (u->os && cudaMemcpyAsync(u->dB, u->hB, 8 * (size_t)u->os * n, cudaMemcpyHostToDevice, L->stream)))
+                st = PHG_ERR_CUDA;
+            ops[k] = u->ops; nv[k] = n; ans[k] = u->dOut; F[k] = u->dU; bnd[k] = u->os ? u->dB : nullptr;
+            rows += (long long)(u->V - u->os) * n;
+        }
+        if (!st && nseg > 0) {
+            const int want = (int)std::max(1LL, std::min<long long>(S->sm_total, (rows + 511) / 512));
+            const int grant = sm_acquire(S, want);
+            const long long b0 = thread_bytes();
+            st = phg_ops_set_sms(ops[0], grant);
+            if (!st) st = phg_laplace_solve_levels(nseg, ops.data(), nv.data(), ans.data(), F.data(), bnd.data(),
+                                                   L->stream);
+            const int r2 = phg_ops_check(ops[0], L->stream);
+            sm_release(S, grant);
+            if (!st) st = r2;
+            const long long grown = thread_bytes() - b0;   // the multi-level workspace, first of its size
+            if (grown > 0) {   // held by the first level's handle
+                std::lock_guard<std::mutex> lk(S->mu);
+                S->in_use += grown;
+                L->bytes += grown;
+                used[0]->bytes += grown;
+            }
+            for (Sub *u : used) u->last_used = S->now();
+        }
+        for (int k = 0; k < nseg && !st; ++k)
+            if (cudaMemcpyAsync(used[k]->hOut, used[k]->dOut, 8 * (size_t)used[k]->V * nv[k], cudaMemcpyDeviceToHost,
+                                L->stream))
+                st = PHG_ERR_CUDA;
+        if (!st && cudaStreamSynchronize(L->stream)) st = PHG_ERR_CUDA;
+        int total = 0;
+        for (int k = 0; k < nseg; ++k) total += nv[k];
+        std::lock_guard<std::mutex> lk(S->mu);
+        for (int k = 0; k < nseg; ++k)
+            for (int j = 0; j < nv[k]; ++j) {
+                Pending *p = mem[k][j];
+                if (!st) memcpy(p->r.output, used[k]->hOut + (size_t)j * used[k]->V, 8 * (size_t)used[k]->V);
+                push_done(S, p, st, total);
+            }
         L->active = 0;
         L->last_busy = S->now();
     }
@@ -485,8 +775,12 @@ void lane_body(Lane *L) {
         S->ready_cv.notify_all();
     }
     if (!st) {
-        if (L->kind == PHG_REQ_LAPLACE_SOLVE) laplace_loop(L);
-        else bv_loop(L);
+        if (L->kind == PHG_REQ_LAPLACE_SOLVE) {
+            if (L->packed) packed_loop(L);
+            else laplace_loop(L);
+        } else {
+            bv_loop(L);
+        }
     }
 }
 
@@ -501,13 +795,15 @@ void lane_main(Lane *L) {
 
 // under S->mu: the lane that takes new requests for (kind, level)
 Lane *lane_for(Server *S, int kind, int level) {
-    auto key = std::make_pair(kind, level);
+    const bool packed = kind == PHG_REQ_LAPLACE_SOLVE && level <= S->pack_level;
+    auto key = std::make_pair(kind, packed ? 0 : level);
     auto it = S->lanes.find(key);
     if (it != S->lanes.end() && !it->second->closing && !it->second->closed) return it->second;
     auto L = std::make_unique<Lane>();
     L->srv = S;
     L->kind = kind;
-    L->level = level;
+    L->level = packed ? 0 : level;
+    L->packed = packed;
     Lane *raw = L.get();
     S->lanes[key] = raw;
     S->all.push_back(std::move(L));
@@ -533,6 +829,10 @@ extern "C" int phg_serve_create(const phg_serve_conf *conf, phg_serve *out) {
         return PHG_ERR_CUDA;
     s->sm_free = s->sm_total;
     s->t0 = Clock::now();
+    {   // Laplace requests of levels <= pack_level share one lane and one launch per turn
+        const char *e = getenv("PHG_SERVE_PACK");
+        s->pack_level = std::max(0, std::min(6, e ? atoi(e) : 5));
+    }
     *out = s.release();
     return PHG_OK;
     PHG_API_END
@@ -547,7 +847,21 @@ extern "C" int phg_serve_preload(phg_serve s, int kind, int level) {
     std::unique_lock<std::mutex> lk(s->mu);
     Lane *L = lane_for(s, kind, level);
     s->ready_cv.wait(lk, [&] { return L->ready || L->failed || L->closed; });
-    return L->failed ? L->fail_status : PHG_OK;
+    if (L->failed) return L->fail_status;
+    if (L->packed && !L->closed) {   // open this level's handle in the packed lane
+        L->want.push_back(level);
+        L->cv.notify_all();
+        auto done = [&] {
+            for (int x : L->opened)
+                if (x == level || x == -level) return true;
+            return L->failed || L->closed;
+        };
+        s->ready_cv.wait(lk, done);
+        for (int x : L->opened)
+            if (x == -level) return PHG_ERR_BUDGET;
+        return L->failed ? L->fail_status : PHG_OK;
+    }
+    return PHG_OK;
     PHG_API_END
 }
 

@@ -183,3 +183,36 @@ def test_full_lane_runs_captured_steps():
         for _ in range(steps + (k % 2)):
             x = bv.calc(x, z, z)
         assert rel(got[k]["output"], x) <= TOL, k
+
+
+@pytest.mark.parametrize("pack", ["5", "0"])
+def test_packed_laplace_levels(pack, monkeypatch):
+    """Laplace requests of levels 3..5 share one lane and one multi-level
+    launch per turn (PHG_SERVE_PACK=5, the default); with packing off each
+    level has its own lane.  Results equal the direct solves either way, and a
+    packed turn holds members of several levels."""
+    monkeypatch.setenv("PHG_SERVE_PACK", pack)
+    levels, per = (3, 4, 5), 4
+    Fs = {lv: serve.solve_inputs(*phelm.Mesh.sphere(lv).latlon(), per, 70 + lv) for lv in levels}
+    srv = phelm.Server(precision=phelm.PHG_MIXED, hbm_budget_bytes=40e9, max_slots=8, solve_tol=1e-12)
+    try:
+        for lv in levels:
+            srv.preload(SOLVE, lv)
+        lanes = srv.stats()["lanes"]
+        for j in range(per):
+            for lv in levels:
+                srv.submit(SOLVE, lv, Fs[lv][j], tag=100 * lv + j)
+        got = wait_for(srv, {100 * lv + j for lv in levels for j in range(per)})
+    finally:
+        srv.close()
+    assert lanes == (1 if pack == "5" else 3)
+    for lv in levels:
+        ops = phelm.Operators(phelm.Mesh.sphere(lv), phelm.PHG_MIXED, tol=1e-12)
+        want = phelm.SphereLaplace(ops).solve_batch(Fs[lv])
+        for j in range(per):
+            c = got[100 * lv + j]
+            assert c["status"] == 0, c
+            assert rel(c["output"], want[j]) <= TOL, (lv, j)
+    if pack == "5":
+        # a turn of more than `per` members holds more than one level
+        assert max(c["batch"] for c in got.values()) > per
