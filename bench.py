@@ -34,7 +34,9 @@ LEVEL = 6
 CONF = dict(tau=1e-3, sigma=1.6e-2, mu=8e-5, k1=1.0, k2=1.0, theta=0.5, picard_iters=3)
 SEED = 2024
 METRIC = "level-6 barvortex steps/s, mixed vs FP64 at 1e-10 rel err; serve p50/p99 ms"
-TOL = 1e-12  # every solve: relative residual <= 1e-12 (within the 1e-10 bound)
+TOL = 1e-11  # every solve: relative residual <= 1e-11: within the metric's 1e-10 per-solve bound and, unlike
+             # 1e-10 itself, within 1e-8 of the reference's 100-step level-6 state (test_gpu_trajectory)
+STRICT_TOL = 1e-12  # the same single-trajectory steps at a tighter tolerance, reported beside
 
 
 def dist_env():
@@ -140,6 +142,34 @@ def initial_state(mesh):
     lat, lon = mesh.latlon()
     psi, _ = fields.barvortex_initial(lat, lon, seed=SEED)
     return psi, np.sin(lat)
+
+
+def run_strict(mesh, psi0, cor, dev, stream, flush, steps: int, tol: float = STRICT_TOL):
+    """Single-trajectory steps/s of both precisions with every solve to `tol`
+    (graph-replayed steps, L2 flushed before each, CUDA events on the
+    stream): the headline workload at a tighter solve tolerance."""
+    import torch
+    from mke_gb300 import phelm
+    out = {}
+    zb = torch.zeros(max(mesh.outer_size, 1), dtype=torch.float64, device=dev)
+    for name, prec in (("mixed", phelm.PHG_MIXED), ("fp64", phelm.PHG_FP64)):
+        ops = phelm.Operators(mesh, prec, restart=30, tol=tol, max_iter=20000)
+        bv = phelm.BarVortex(ops, coriolis=cor, **CONF)
+        u = torch.tensor(psi0, dtype=torch.float64, device=dev)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        with torch.cuda.stream(stream):
+            bv.run(u, 3, zb, zb, stream=stream)
+            for e0, e1 in ev:
+                flush.zero_()
+                e0.record(stream)
+                bv.run(u, 1, zb, zb, stream=stream)
+                e1.record(stream)
+        stream.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+        st = bv.last_stats()
+        out[name] = {"steps_per_s": 1000.0 / ms, "worst_relres": st["worst_relres"]}
+        del bv, ops
+    return out
 
 
 def run_ours(args, ws, rank, local):
@@ -261,6 +291,8 @@ def run_ours(args, ws, rank, local):
             results[name]["e2e_graph_s"] = e2e_graph
         del bv, ops
 
+    strict = run_strict(mesh, psi0, cor, dev, stream, flush, args.steps) if args.tol != STRICT_TOL else None
+
     # batched ensembles (BASELINE config 3: 256 members on level 5, and 32 on level 6)
     batched = {}
     if not args.no_batch:
@@ -369,7 +401,7 @@ def run_ours(args, ws, rank, local):
     rel = float(np.linalg.norm(mixed["state"] - fp64["state"]) / np.linalg.norm(fp64["state"]))
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(args.level, steps=1)
+        cpu = cpu_baseline(args.level, steps=1, tol=args.tol)
         if lap3 is not None:   # config 1's error against the CPU reference algorithm's own solve
             ref = cpu.pop("laplace_l3_solution")
             lap3["rel_err_vs_cpu_reference_solve"] = float(np.linalg.norm(lap3.pop("solution") - ref)
@@ -386,7 +418,7 @@ def run_ours(args, ws, rank, local):
             "bytes_per_launch": r3(prof["bytes"] / max(prof["launches"], 1)),
             "ms_per_launch": r3(prof["ms"] / max(prof["launches"], 1)),
             "share_of_step": r3(prof["ms"] / (mixed["eager_ms"] * args.steps)),
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s"}
+            "peak_source": "of measured (MEASURED_PEAKS.json)" if peaks else "of fallback"}
     line = {
         "metric": METRIC,
         "value": ws * 1000.0 / ms,
@@ -401,8 +433,10 @@ def run_ours(args, ws, rank, local):
         "dtype": "f32+f64",
         "data": "synthetic (seeded Rossby-Haurwitz wave 4 + spherical-harmonic noise)",
         "config": {"workload": workload(args.level)},
-        "solve_tol": args.tol, "parallelism": f"replicas x{ws}", "l2": "flushed between steps (256 MB write, not timed)",
+        "solve_tol": args.tol, "parallelism": f"replicas x{ws}", "l2": "flushed between steps (256 MB write)",
         "fp64": {"value": r3(ws * 1000.0 / ms64), "mixed_over_fp64": r3(ms64 / ms)},
+        "at_tol_1e-12": None if strict is None else {
+            "mixed": r3(strict["mixed"]["steps_per_s"]), "fp64": r3(strict["fp64"]["steps_per_s"])},
         "state_rel_diff_mixed_vs_fp64": r3(rel),
         "batched": {k: {"mixed": r3(v["mixed"]["member_steps_per_s"]), "fp64": r3(v["fp64"]["member_steps_per_s"]),
                         "mixed_over_fp64": r3(v["mixed_over_fp64"]), "rel_err_vs_fp64": r3(v["rel_err_vs_fp64"]),
@@ -414,14 +448,14 @@ def run_ours(args, ws, rank, local):
                for p in ("mixed", "fp64")}},
         "spmv": None if spmv is None else {
             "level": spmv["level"], "fp32_x64_frac_of_hbm": r3(spmv["fp32_multivector"]["frac_of_peak"]),
-            "fp32_x64_gbs": r3(spmv["fp32_multivector"]["gbs"]), "fp64_frac_of_hbm": r3(spmv["fp64_single"]["frac_of_peak"])},
+            "fp64_frac_of_hbm": r3(spmv["fp64_single"]["frac_of_peak"])},
         "baroclin": None if baroclin is None else {
             "mixed": r3(baroclin["mixed"]["steps_per_s"]), "fp64": r3(baroclin["fp64"]["steps_per_s"]),
             "mixed_over_fp64": r3(baroclin["mixed_over_fp64"]),
             "rel_diff": r3(baroclin[f"state_rel_diff_mixed_vs_fp64_after_{baroclin['steps']}"])},
         "laplace_l3": None if lap3 is None else {k: (r3(v) if isinstance(v, float) else v) for k, v in lap3.items()},
         "jac_quad": None if jq is None else {"level": jq["level"], "members": jq["members"],
-                                            "us_per_call": r3(jq["us_per_call"]), "gbs": r3(jq["gbs"]),
+                                            "us_per_call": r3(jq["us_per_call"]),
                                             "frac_of_hbm": r3(jq["frac_of_hbm"])},
         "worst_solve_relres": r3(max(mixed["stats"]["worst_relres"], fp64["stats"]["worst_relres"])),
         "roofline": roof,
@@ -436,7 +470,7 @@ def run_ours(args, ws, rank, local):
                        "graph_ms": fp64["graph_ms"]},
               "step_path": {"mixed": mixed["path"], "eager_ms": mixed["eager_ms"], "graph_ms": mixed["graph_ms"],
                             "e2e_eager_s": mixed["e2e_eager_s"], "e2e_graph_s": mixed["e2e_graph_s"]},
-              "batched": batched, "serve": served, "spmv": spmv, "baroclin": baroclin,
+              "batched": batched, "serve": served, "spmv": spmv, "baroclin": baroclin, "strict": strict,
               "solver": {"mixed": mixed["stats"], "fp64": fp64["stats"]}, "autotuned": tuned or None,
               "roofline_all_solver_launches": {
                   "launches": mixed["prof_all"]["launches"],
@@ -473,7 +507,7 @@ THREAD_NOTE = ("OpenMP over the host cores in the port's parallel loops (assembl
                "per-row operator applies); its GMRES+ILU(0) solves are sequential code")
 
 
-def cpu_baseline(level, steps=1):
+def cpu_baseline(level, steps=1, tol=TOL):
     """The oracle (C restatement of the reference algorithm) on the host:
     timed steps of the bench workload, and (untimed) the level-3 Laplace
     solve of the accuracy leg, the CPU reference answer it is compared with."""
@@ -484,6 +518,7 @@ def cpu_baseline(level, steps=1):
     uv3 = o3.mesh_arrays()["uv"].reshape(-1, 4, 2)
     ustar, f = fields.laplace_problem(uv3[:, 0, 0], uv3[:, 0, 1], seed=SEED)
     ref3 = o3.laplace_solve(f, ustar[o3.mesh_arrays()["bnd"] == 1])
+    po.set_solver(rel_tol=tol)   # the timed steps: every solve to the GPU arm's tolerance
     o = po.Oracle(level)
     uv = o.mesh_arrays()["uv"].reshape(-1, 4, 2)
     lat, lon = uv[:, 0, 0], uv[:, 0, 1]
@@ -497,7 +532,7 @@ def cpu_baseline(level, steps=1):
     dt = time.perf_counter() - t0
     return {"value": steps / dt, "unit": "steps/s", "cores": host_threads(), "kind": "port",
             "sample": f"{steps} step(s) of the level-{level} workload after setup; OpenMP loops, sequential "
-                      "GMRES+ILU(0) solves to 1e-13",
+                      f"GMRES+ILU(0) solves to {tol:g}",
             "laplace_l3_solution": ref3}
 
 
@@ -510,6 +545,7 @@ def run_reference(args, ws, rank):
     import pyoracle as po
     from mke_gb300 import fields
     po.build()
+    po.set_solver(rel_tol=args.tol)   # every solve to the GPU arm's tolerance
     o = po.Oracle(args.level)
     uv = o.mesh_arrays()["uv"].reshape(-1, 4, 2)
     lat, lon = uv[:, 0, 0], uv[:, 0, 1]
@@ -524,7 +560,8 @@ def run_reference(args, ws, rank):
         s = o.bv_step(bv, s, z, z)
     dt = time.perf_counter() - t0
     v = steps / dt
-    sample = f"{steps} timed step(s) after {warm} warm-up, level {args.level}; " + THREAD_NOTE
+    sample = (f"{steps} timed step(s) after {warm} warm-up, level {args.level}, solves to {args.tol:g}; "
+              + THREAD_NOTE)
     print(json.dumps({
         "impl": "reference",
         "metric": METRIC,

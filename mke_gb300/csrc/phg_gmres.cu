@@ -68,6 +68,10 @@ constexpr int LSG_DEFAULT_ROWS = 10000;
 constexpr int MAXSEG = 6;
 struct MultiSeg {
     int v0, n, W, ld;
+    int nv;                  // right-hand sides of this segment
+    int blk0, G, groups;     // its blocks [blk0, blk0 + groups * G): groups of G
+    int gbase;               // launch-wide index of its first group
+
     const int *col;
     const double *aval;
     const double *sval64;
@@ -105,6 +109,8 @@ struct Params {
     // coefficients d_k = ca[k] d_{k-1} + cb[k] D^-1 r_k, d_0 = c0 D^-1 r_0
     int cheb_k;
     double cheb_c0, cheb_ca[CHEB_KMAX], cheb_cb[CHEB_KMAX];
+    // steps for a residual reduction eps: ceil((cheb_lg - log eps) / cheb_ls) + 1
+    double cheb_lg, cheb_ls;
     long long wait_limit;    // clock64 cycles a barrier wait may take before the launch gives up
     int cluster;             // > 0: clustered launch, V-cycle levels [ncl, nred) as a cluster tail
     unsigned long long *ccnt;  // groups: cluster-tail entry counters
@@ -765,16 +771,35 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const __grid_constant__
     __shared__ VT vscal[1];
 
     // everything the loops need, copied out of the parameter block
-    const int m = p.m, G = p.G, nv = p.nv, groups = p.groups, max_iter = p.max_iter;
+    const int m = p.m, max_iter = p.max_iter;
     int n = p.n;              // per right-hand side in a multi-operator launch
     size_t ld = (size_t)p.ld;
     const double tol = p.tol;
-    const int grp = blockIdx.x / G, bi = blockIdx.x % G;
-    if (grp >= groups) return;
+    // this block's group: groups of p.G blocks over the launch, or, in a
+    // multi-operator launch, groups sized for this block's segment (its mesh)
+    // that take that segment's right-hand sides only
+    int G = p.G, grp = blockIdx.x / G, bi = blockIdx.x % G;
+    int vbeg = grp, vend = p.nv, vstep = p.groups;
+    if (MULTI) {
+        int k = 0;
+        while (k + 1 < p.nseg && (int)blockIdx.x >= p.seg[k + 1].blk0) ++k;
+        const int lb = (int)blockIdx.x - p.seg[k].blk0;
+        G = p.seg[k].G;
+        const int lg = lb / G;
+        bi = lb % G;
+        if (lg >= p.seg[k].groups) return;
+        grp = p.seg[k].gbase + lg;
+        vbeg = p.seg[k].v0 + lg;
+        vend = p.seg[k].v0 + p.seg[k].nv;
+        vstep = p.seg[k].groups;
+    } else if (grp >= p.groups) {
+        return;
+    }
     if (threadIdx.x == 0) wait_limit_slot() = p.wait_limit;   // read by this thread only
     unsigned *bar = p.bar + 2 * grp;
     int *err = p.err;
-    double *part2 = p.part + (size_t)grp * 2 * G * (MAXM + 2);
+    // the group's partial sums: 2 (MAXM + 2) doubles per block from its first block
+    double *part2 = p.part + (size_t)(blockIdx.x - bi) * 2 * (MAXM + 2);
     int parity = 0;
     int r0, r1;
     own_rows(n, G, bi, r0, r1);
@@ -827,7 +852,7 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const __grid_constant__
     //   correction jlast es (V or Z reads) + 16 (x read/write) + 8
     double my_bytes = 0.0;
 
-    for (int v = grp; v < nv; v += groups) {
+    for (int v = vbeg; v < vend; v += vstep) {
         const double *__restrict__ b = Bp + (size_t)v * ld;
         double *x = Xp + (size_t)v * ld;
         VT *V = Vp + (size_t)v * (m + 1) * n;
@@ -1116,6 +1141,7 @@ __global__ void __launch_bounds__(BLOCK, 2) cheb_kernel(const Params p) {
     VT *cf = (VT *)(smem + 4);              // ca[k], cb[k] in the Krylov precision
     __shared__ double red[MAXM + 2][NWARP];
     __shared__ double scal[4];
+    __shared__ int kcyc;
     const int n = p.n, G = p.G, nv = p.nv, groups = p.groups, max_iter = p.max_iter, K = p.cheb_k;
     const size_t ld = (size_t)p.ld;
     const double tol = p.tol;
@@ -1194,9 +1220,20 @@ __global__ void __launch_bounds__(BLOCK, 2) cheb_kernel(const Params p) {
                 scal[1] = bt;
                 scal[2] = bt / bnorm;
                 scal[3] = bt > 0.0 ? 1.0 / bt : 0.0;
+                // this cycle's steps: K, or fewer when the reduction still
+                // needed (tol / rel, with a factor 2 margin) is smaller than
+                // the one K steps guarantee
+                int kc = K;
+                const double rl = bt / bnorm;
+                if (rl > tol && p.cheb_ls > 0.0) {
+                    const double need = (p.cheb_lg + log(2.0 * rl / tol)) / p.cheb_ls;
+                    if (need + 1.0 < (double)K) kc = max(2, (int)ceil(need) + 1);
+                }
+                kcyc = kc;
             }
             __syncthreads();
             const double beta = scal[1];
+            const int Kc = kcyc;
             my_bytes += nrows * (W * 12.0 + 24.0);
             rel = scal[2];
             if (rel <= tol) { status = 0; break; }
@@ -1216,7 +1253,7 @@ __global__ void __launch_bounds__(BLOCK, 2) cheb_kernel(const Params p) {
                 }
             }
             VT *ec = e0, *en = e1;
-            for (int k = 1; k < K; ++k) {
+            for (int k = 1; k < Kc; ++k) {
                 if (!group_sync(bar, G, err, nullptr)) return;   // e_k complete
                 const VT ca = cf[k], cb = cf[CHEB_KMAX + k];
                 for (int i = r0 + threadIdx.x; i < r1; i += BLOCK) {
@@ -2636,6 +2673,7 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
         p.inner_rtol = e ? atof(e) : INNER_RTOL;
     }
     p.cheb_k = 0;
+    p.cheb_lg = p.cheb_ls = 0.0;
     if (cheb) {
         // steps for an error reduction eps (residual: one more factor kappa)
         const double lo = op.cheb_lmin, hi = op.cheb_lmax;
@@ -2645,6 +2683,8 @@ cudaError_t gmres_solve(const DevSolveOp &op, const double *B, double *X, int nv
         K = K < 2 ? 2 : (K > CHEB_KMAX ? CHEB_KMAX : K);
         const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), s1 = theta / delta;
         p.cheb_k = K;
+        p.cheb_lg = log(2.0 * kappa);
+        p.cheb_ls = log(1.0 / sigma);
         p.cheb_c0 = 1.0 / theta;
         double rho_prev = 1.0 / s1;
         p.cheb_ca[0] = p.cheb_cb[0] = 0.0;
@@ -2781,13 +2821,37 @@ cudaError_t gmres_solve_multi(const DevSolveOp *const *ops, const int *nvk, cons
     if (per < 1) return cudaErrorInvalidConfiguration;
     const int sms = (max_sms > 0 && max_sms < sm_count()) ? max_sms : sm_count();
     const int cap = sms * per;
-    // groups of G blocks, G from the largest mesh (no block below 256 rows there)
-    int groups = nv < cap ? nv : cap;
-    if (groups > GROUPS_CAP) groups = GROUPS_CAP;
-    int G = cap / groups;
-    const int Gmax = (nmax + 255) / 256;
-    if (G > Gmax) G = Gmax;
-    if (G < 1) G = 1;
+    if (cap < nseg) return cudaErrorInvalidConfiguration;
+    // the resident blocks split between the segments in proportion to their
+    // work (right-hand sides x rows), at least one block each; within a
+    // segment as the single-operator launch does it: as many groups as
+    // right-hand sides fit, then groups of up to one block per 256 rows
+    int bk[MAXSEG], gk[MAXSEG], Gk[MAXSEG];
+    {
+        double tw = 0.0;
+        for (int k = 0; k < nseg; ++k) tw += (double)nvk[k] * ops[k]->A.n;
+        int used = 0;
+        for (int k = 0; k < nseg; ++k) {
+            bk[k] = std::max(1, (int)((double)cap * nvk[k] * ops[k]->A.n / tw));
+            used += bk[k];
+        }
+        while (used > cap) {   // rounding up the smallest shares: take back from the largest
+            int kmax = 0;
+            for (int k = 1; k < nseg; ++k) if (bk[k] > bk[kmax]) kmax = k;
+            --bk[kmax];
+            --used;
+        }
+        for (int k = 0; k < nseg; ++k) {
+            gk[k] = std::min(nvk[k], bk[k]);
+            Gk[k] = std::max(1, std::min(bk[k] / gk[k], (ops[k]->A.n + 255) / 256));
+        }
+    }
+    int groups = 0, blocks = 0;
+    for (int k = 0; k < nseg; ++k) { groups += gk[k]; blocks += gk[k] * Gk[k]; }
+    if (groups > GROUPS_CAP || blocks > cap) return cudaErrorInvalidConfiguration;
+    int G = 1;
+    for (int k = 0; k < nseg; ++k) G = std::max(G, Gk[k]);
+    (void)nmax;
     const MultiLayout L = multi_layout(ops, nvk, nseg, m, prec);
     char *w = (char *)work;
     Params p;
@@ -2803,6 +2867,7 @@ cudaError_t gmres_solve_multi(const DevSolveOp *const *ops, const int *nvk, cons
         p.inner_rtol = ev ? atof(ev) : INNER_RTOL;
     }
     p.cheb_k = 0;
+    p.cheb_lg = p.cheb_ls = 0.0;
     p.part = (double *)(w + L.part);
     p.bar = (unsigned *)(w + L.bar); p.err = (int *)(w + L.err); p.stats = stats_dev;
     p.groups = groups; p.G = G;
@@ -2812,12 +2877,16 @@ cudaError_t gmres_solve_multi(const DevSolveOp *const *ops, const int *nvk, cons
     p.mg_row_bytes = 0.0;
     p.timers = nullptr;
     p.nseg = nseg;
-    int v0 = 0;
+    int v0 = 0, blk0 = 0, gbase = 0;
     for (int k = 0; k < MAXSEG; ++k) p.seg[k] = MultiSeg{};
     for (int k = 0; k < nseg; ++k) {
         const DevSolveOp &op = *ops[k];
         MultiSeg &S = p.seg[k];
         S.v0 = v0; S.n = op.A.n; S.W = op.A.W; S.ld = ldk[k];
+        S.nv = nvk[k];
+        S.blk0 = blk0; S.G = Gk[k]; S.groups = gk[k]; S.gbase = gbase;
+        blk0 += gk[k] * Gk[k];
+        gbase += gk[k];
         S.col = op.A.col; S.aval = op.A.val; S.sval64 = op.A.val; S.sval32 = op.a32; S.dinv = op.dinv;
         S.mgd = op.mgd;
         S.B = B[k]; S.X = X[k];
@@ -2837,7 +2906,7 @@ cudaError_t gmres_solve_multi(const DevSolveOp *const *ops, const int *nvk, cons
     cudaLaunchAttribute coop[1];
     coop[0].id = cudaLaunchAttributeCooperative;
     coop[0].val.cooperative = 1;
-    cfg.gridDim = dim3(groups * G);
+    cfg.gridDim = dim3(blocks);
     cfg.blockDim = dim3(BLOCK);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
