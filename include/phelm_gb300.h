@@ -373,9 +373,9 @@ int phg_baroclin_calc_L_1(phg_baroclin b, double *u11, double *u21, const double
  * the lane opens and counted against the HBM budget.  Requests join a lane as
  * slots free up (barotropic members between two time steps, Laplace solves in
  * the next batched solve) and lanes run concurrently on their streams.  Idle
- * lanes are closed when a new lane needs their memory.  Laplace solves of
- * levels up to PHG_SERVE_PACK (environment, default 5) share one lane that
- * solves each turn's requests of all those levels in one
+ * lanes are closed when a new lane needs their memory.  With PHG_SERVE_PACK=L
+ * in the environment (default 0: off), Laplace solves of levels up to L share
+ * one lane that solves each turn's requests of all those levels in one
  * phg_laplace_solve_levels launch.  Barotropic lanes use
  * l + h = sin(latitude) (2 Omega = 1, no orography) and conf.bv. */
 #define PHG_REQ_LAPLACE_SOLVE 0 /* input: F[V]; output: solution[V]; bnd: os values or NULL */

@@ -76,6 +76,7 @@ struct Lane {
     double *dU = nullptr, *dOut = nullptr, *dB = nullptr, *dBw = nullptr;
     double *hIn = nullptr, *hOut = nullptr, *hB = nullptr;
     long long bytes = 0;   // reserved against the budget
+    double step_ms = 0.0;  // barotropic lanes: wall time of the last call, per step
     // shared state, under Server::mu
     std::deque<Pending *> queue;
     std::vector<Pending *> act;   // members in flight, act[k] owns slot k (lane thread only)
@@ -691,17 +692,22 @@ void bv_loop(Lane *L) {
                     st = PHG_ERR_CUDA;
             }
         }
-        // A full lane (no request could join before a member leaves) runs as
-        // many steps as the nearest finish in one call, from the captured step
-        // graph; a lane with free slots steps once, so that requests arriving
-        // meanwhile join at the next step.
+        // A full lane (no request could join before a member leaves) runs up
+        // to the nearest finish in one call, from the captured step graph; a
+        // lane with free slots steps once, so that requests arriving meanwhile
+        // join at the next step.  A call keeps its SM grant until it returns,
+        // so runs are capped at RUN_MS: a long run on a share granted while
+        // other lanes were busy would leave the SMs they free idle.
+        constexpr double RUN_MS = 20.0;
         int ksteps = 1;
-        if (n >= L->cap) {
+        if (n >= L->cap && L->step_ms > 0.0) {
             ksteps = act[0]->steps_left;
             for (int k = 1; k < n; ++k) ksteps = std::min(ksteps, act[k]->steps_left);
-            ksteps = std::max(1, ksteps);
+            ksteps = std::max(1, std::min(ksteps, (int)(RUN_MS / L->step_ms)));
         }
+        const auto t_run = Clock::now();
         if (!st) st = ksteps > 1 ? lane_steps(L, n, ksteps) : lane_run(L, n);
+        L->step_ms = std::chrono::duration<double, std::milli>(Clock::now() - t_run).count() / ksteps;
         if (st) {
             std::lock_guard<std::mutex> lk(S->mu);
             for (Pending *p : act) push_done(S, p, st, n);
@@ -829,9 +835,11 @@ extern "C" int phg_serve_create(const phg_serve_conf *conf, phg_serve *out) {
         return PHG_ERR_CUDA;
     s->sm_free = s->sm_total;
     s->t0 = Clock::now();
-    {   // Laplace requests of levels <= pack_level share one lane and one launch per turn
+    {   // Laplace requests of levels <= pack_level share one lane and one launch per
+        // turn; off by default (measured: a packed turn makes the small levels wait
+        // for the largest one, p50 77 -> 435 ms on the mixed 2,000-request trace)
         const char *e = getenv("PHG_SERVE_PACK");
-        s->pack_level = std::max(0, std::min(6, e ? atoi(e) : 5));
+        s->pack_level = std::max(0, std::min(6, e ? atoi(e) : 0));
     }
     *out = s.release();
     return PHG_OK;
