@@ -138,14 +138,23 @@ __device__ __forceinline__ long long &wait_limit_slot() {
     return lim;
 }
 
+// Barriers this block has passed in the launch, held by thread 0 (set to 0 at
+// kernel entry, with the wait limit).
+__device__ __forceinline__ unsigned long long &bar_epoch() {
+    __shared__ unsigned long long e;
+    return e;
+}
+
 // Barrier of the G blocks of one group.  The group's 64-bit word at bar
-// counts arrivals and is never reset within a launch (nor wraps): a block
-// arriving as the k-th (0-based) waits until the count reaches the next
-// multiple of G, so the last arrival's one atomic releases everyone (no
-// reset, no second flag) and a block that runs ahead into the next barrier
-// only raises the count further.  The wait gives up after the launch's wait
-// limit (wait_limit_slot, SPIN_LIMIT by default) and raises the launch's
-// error flag.
+// counts arrivals and is never reset within a launch (nor wraps).  Every
+// block of a group passes the same sequence of barriers, so at its k-th
+// barrier (k from 1) a block adds one and waits until the count reaches
+// k * G: the last arrival releases everyone (no reset, no second flag), and a
+// block that runs ahead into the next barrier only raises the count further.
+// The arrival is a release reduction that returns nothing: the block starts
+// polling at once instead of waiting a round trip to L2 for an atomic's old
+// value.  The wait gives up after the launch's wait limit (wait_limit_slot,
+// SPIN_LIMIT by default) and raises the launch's error flag.
 __device__ bool group_sync(unsigned *bar, int G, int *err, long long *tm) {
     __shared__ int ok;
     long long tb = (tm && threadIdx.x == 0) ? clock64() : 0;
@@ -157,11 +166,10 @@ __device__ bool group_sync(unsigned *bar, int G, int *err, long long *tm) {
     if (threadIdx.x == 0) {
         ok = 1;
         unsigned long long *cnt = reinterpret_cast<unsigned long long *>(bar);   // 8-byte aligned
+        const unsigned long long target = ++bar_epoch() * (unsigned long long)G;
         // release: the block's writes (ordered before this thread by the
         // __syncthreads above) are visible device-wide before the arrival
-        asm volatile("fence.acq_rel.gpu;" ::: "memory");
-        const unsigned long long old = atomicAdd(cnt, 1ull);
-        const unsigned long long target = old - old % (unsigned long long)G + (unsigned long long)G;
+        asm volatile("red.release.gpu.global.add.u64 [%0], 1;" ::"l"(cnt) : "memory");
         const long long t0 = clock64(), lim = wait_limit_slot();
         while (ld_acquire(cnt) < target) {
             if (ld_volatile(err)) { ok = 0; break; }
@@ -795,7 +803,10 @@ __global__ void __launch_bounds__(BLOCK, 2) gmres_kernel(const __grid_constant__
     } else if (grp >= p.groups) {
         return;
     }
-    if (threadIdx.x == 0) wait_limit_slot() = p.wait_limit;   // read by this thread only
+    if (threadIdx.x == 0) {   // read by this thread only
+        wait_limit_slot() = p.wait_limit;
+        bar_epoch() = 0;
+    }
     unsigned *bar = p.bar + 2 * grp;
     int *err = p.err;
     // the group's partial sums: 2 (MAXM + 2) doubles per block from its first block
@@ -1149,6 +1160,7 @@ __global__ void __launch_bounds__(BLOCK, 2) cheb_kernel(const Params p) {
     if (grp >= groups) return;
     if (threadIdx.x == 0) {   // constant indices: the parameter block stays in param space
         wait_limit_slot() = p.wait_limit;
+        bar_epoch() = 0;
 #pragma unroll
         for (int k = 0; k < CHEB_KMAX; ++k) {
             cf[k] = (VT)p.cheb_ca[k];
