@@ -1031,9 +1031,11 @@ int laplace_calc2_dev(phg_ops_s *o, double *ans, int lda, const double *F, int l
 
 // the 8 derivative solves of a Jacobian for nv members; sol: nv x 8 x rs.
 // quad: right-hand sides by the FP32 element-loop quadrature (the mixed
-// precision time steps) instead of the assembled FP64 operators
+// precision time steps) instead of the assembled FP64 operators.  warm: the
+// solves start from sol's contents (the previous Picard iteration's
+// derivatives of the same step) instead of zero
 int jacobian_derivs_dev(phg_ops_s *o, const double *u, const double *v, int ld, double *sol, int nv, int slot,
-                        cudaStream_t s, double tol, bool quad = false) {
+                        cudaStream_t s, double tol, bool quad = false, bool warm = false) {
     CK(o->s_b.ensure(8 * (size_t)o->rs * 8 * nv));
     double *rhs = o->s_b.as<double>();
     if (quad && o->jq.n) {
@@ -1041,7 +1043,7 @@ int jacobian_derivs_dev(phg_ops_s *o, const double *u, const double *v, int ld, 
         CK(jac_quad(o->jq, o->J, u, v, ld, o->imap(), o->bmap(), rhs, o->rs, nv, o->V, (float2 *)o->jq_split.p, s));
     }
     else CK(jac_rhs(o->J, u, v, ld, o->imap(), o->bmap(), rhs, o->rs, nv, s));
-    CK(cudaMemsetAsync(sol, 0, 8 * (size_t)o->rs * 8 * nv, s));
+    if (!warm) CK(cudaMemsetAsync(sol, 0, 8 * (size_t)o->rs * 8 * nv, s));
     return solve(o, o->MJ.op, rhs, sol, 8 * nv, o->rs, tol, slot, s);
 }
 
@@ -1871,7 +1873,7 @@ int bv_step_dev(phg_barvortex_s *b, int nv, double *u1, const double *u, const d
                   c.theta, 1.0 - c.theta, NV, s));
         // F = FC[inner] - J(tmp2, tmp1)
         const bool quad = o->jq_mode == 1 || (o->jq_mode == 2 && it + 1 < c.picard_iters);
-        if ((r = jacobian_derivs_dev(o, tmp2, tmp1, V, jsol, nv, slot++, s, o->tol, quad))) return r;
+        if ((r = jacobian_derivs_dev(o, tmp2, tmp1, V, jsol, nv, slot++, s, o->tol, quad, it > 0))) return r;
         CK(jac_combine(jsol, rs, rs, F, rs, FC, V, o->imap(), nv, s));
         // rp = M_L F + bnd_ bnd_w ; w_n = p2u(A^-1 rp, bnd_w)
         CK(apply_op(o->ML.op.A, b->Ab.c, F, rs, nullptr, bnd_w, os, nullptr, rp, rs, nv, s));
@@ -2521,7 +2523,7 @@ int bc_step_dev(phg_baroclin_s *b, double *u11, double *u21, const double *u1, c
         CK(bc_jin(b->ju.as<double>(), b->jv.as<double>(), U, U + V, w, w + V, un, un + V, wn, wn + V,
                   b->lh.as<double>(), th, V, s));
         if ((r = jacobian_derivs_dev(o, b->ju.as<double>(), b->jv.as<double>(), V, b->jsol.as<double>(), 5, slot++, s,
-                                     o->tol, o->jq_mode == 1)))
+                                     o->tol, o->jq_mode == 1, it > 0)))
             return r;
         CK(jac_combine(b->jsol.as<double>(), rs, rs, b->jac.as<double>(), rs, nullptr, 0, nullptr, 5, s));
         CK(bc_fg(F, G, b->jac.as<double>(), FC, GC, o->imap(), k.alpha2, rs, s));
