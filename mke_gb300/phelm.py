@@ -345,6 +345,10 @@ class Operators:
     def set_solver(self, restart=30, tol=1e-12, max_iter=20000):
         _check(lib().phg_ops_set_solver(self._h, restart, tol, max_iter))
 
+    def set_sms(self, max_sms: int = 0):
+        """Cap the SMs this handle's persistent solver launches use (0 = all)."""
+        _check(lib().phg_ops_set_sms(self._h, int(max_sms)))
+
     def set_wait_limit(self, cycles: int = 0):
         """Clock cycles a group-barrier wait of this handle's persistent solver
         kernels may spin before the launch gives up (0 = the default, ~1 s)."""

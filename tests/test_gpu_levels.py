@@ -64,3 +64,21 @@ def test_levels_refusals():
     with pytest.raises(phelm.PhgError) as e:
         phelm.laplace_solve_levels([a, b], [F, F])
     assert e.value.code == 1
+
+
+@pytest.mark.parametrize("sms", [3, 8, 40])
+def test_levels_few_sms(sms):
+    """The resident blocks split between the meshes in proportion to their
+    work, at least one block each: with the launch capped to a few SMs the
+    small meshes get single-block groups and several right-hand sides per
+    group; every solution still equals the mesh's own batched solve."""
+    nvs = (5, 3, 2)
+    probs = [problem(lv, nv, 60 + lv) for lv, nv in zip(LEVELS, nvs)]
+    ops = [phelm.Operators(m, phelm.PHG_MIXED, tol=1e-12) for m, _, _ in probs]
+    ops[0].set_sms(sms)
+    outs = phelm.laplace_solve_levels(ops, [F for _, F, _ in probs], [b for _, _, b in probs])
+    ops[0].set_sms(0)
+    for (m, F, bnd), o, got in zip(probs, ops, outs):
+        want = phelm.SphereLaplace(o).solve_batch(F, bnd)
+        for k in range(F.shape[0]):
+            assert rel(got[k], want[k]) <= 1e-9, (sms, m.size, k)
