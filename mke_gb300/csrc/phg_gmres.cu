@@ -1452,14 +1452,18 @@ __global__ void __launch_bounds__(256) k_ls_nrm(const double *rpart, const doubl
 }
 
 // per-member scales 1/||r|| (0 once converged), the stopping test and the stats
+// The cycle's steps (*kc): K, or fewer when every open member needs a smaller
+// reduction (tol / rel, factor 2 margin; steps for a reduction eps:
+// ceil((lg - log eps) / ls) + 1), rounded up to K's parity so that the
+// iterate ends in the buffer the K-step sequence ends in.
 __global__ void __launch_bounds__(256) k_ls_scale(const double *nrm, int nv, int nvp, double tol, double *beta,
                                                   double *sc, int *done, GmresStats *st, int cycle, int K,
-                                                  double bytes) {
+                                                  double bytes, double lg, double ls, int *kc) {
     if (*(volatile int *)done) return;
     __shared__ double rmax[NWARP];
-    __shared__ int open[NWARP];
+    __shared__ int open[NWARP], kneed[NWARP];
     double mx = 0.0;
-    int op = 0;
+    int op = 0, kn = 2;
     for (int v = threadIdx.x; v < nvp; v += blockDim.x) {
         if (v >= nv) { sc[v] = 0.0; beta[v] = 0.0; continue; }
         const double bt = sqrt(nrm[2 * v]), bn = sqrt(nrm[2 * v + 1]);
@@ -1470,23 +1474,31 @@ __global__ void __launch_bounds__(256) k_ls_scale(const double *nrm, int nv, int
         mx = max_nan(mx, rel);
         if (!(rel == rel)) mx = rel;   // NaN propagates into the stats
         op += conv ? 0 : 1;
+        if (!conv) {
+            const double need = ls > 0.0 ? (lg + log(2.0 * rel / tol)) / ls : (double)K;
+            kn = need + 1.0 < (double)K ? max(kn, (int)ceil(need) + 1) : K;   // NaN: K
+        }
     }
     for (int o = 16; o > 0; o >>= 1) {
         mx = max_nan(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         op += __shfl_xor_sync(0xffffffffu, op, o);
+        kn = max(kn, __shfl_xor_sync(0xffffffffu, kn, o));
     }
-    if ((threadIdx.x & 31) == 0) { rmax[threadIdx.x >> 5] = mx; open[threadIdx.x >> 5] = op; }
+    if ((threadIdx.x & 31) == 0) { rmax[threadIdx.x >> 5] = mx; open[threadIdx.x >> 5] = op; kneed[threadIdx.x >> 5] = kn; }
     __syncthreads();
     if (threadIdx.x == 0) {
         double m = 0.0;
-        int o = 0;
-        for (int w = 0; w < NWARP; ++w) { m = max_nan(m, rmax[w]); o += open[w]; }
+        int o = 0, k = 2;
+        for (int w = 0; w < NWARP; ++w) { m = max_nan(m, rmax[w]); o += open[w]; k = max(k, kneed[w]); }
+        k = min(K, k + ((K - k) & 1));
+        if (cycle == 0) st->steps_total = 0;
+        else st->steps_total += *kc;   // the previous cycle's steps
         st->relres = m;
         st->cycles = cycle;
-        st->iters = cycle * K;
-        st->steps_total = cycle * K;
+        st->iters = st->steps_total;
         st->status = o ? 1 : 0;
         st->bytes += bytes;
+        *kc = k;
         *done = o ? 0 : 1;
     }
 }
@@ -1524,12 +1536,21 @@ __global__ void __launch_bounds__(256) k_ls_init(const double *__restrict__ R, i
 // e_{k+1} = e_k + ca (e_k - e_{k-1}) + cb D^-1 (rv - s), written over e_{k-1}
 // (each element is read and then written by the same thread; other threads
 // gather only e_k) -- four vectors touched per step instead of five
+// the stop flag and the cycle's step count sit side by side (8-byte aligned):
+// one load decides whether step k of the cycle runs
+__device__ __forceinline__ bool ls_stop(const int *done, int k) {
+    int f, kc;
+    asm volatile("ld.volatile.global.v2.s32 {%0, %1}, [%2];" : "=r"(f), "=r"(kc) : "l"(done));
+    return f != 0 || k >= kc;
+}
+
 template <int W>
 __global__ void __launch_bounds__(256) k_ls_step(const int *__restrict__ col, const float *__restrict__ a32,
                                                  const float *__restrict__ dinv, int n, int q4,
                                                  const float4 *__restrict__ ec, const float4 *__restrict__ rv,
-                                                 float4 *ep, float ca, float cb, const int *done) {
-    if (*(volatile const int *)done) return;
+                                                 float4 *ep, float ca, float cb, const int *done, int k,
+                                                 const int *kc) {
+    if (ls_stop(done, k)) return;
     const unsigned total = (unsigned)n * (unsigned)q4;   // < 2^31 (checked by the caller)
     for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
         const int i = (int)(t / (unsigned)q4), q = (int)(t - (unsigned)i * (unsigned)q4);
@@ -1560,8 +1581,8 @@ __global__ void __launch_bounds__(256) k_ls_step(const int *__restrict__ col, co
 __global__ void __launch_bounds__(256) k_ls_step_pk(const uint4 *__restrict__ pk, const float *__restrict__ dinv,
                                                     int n, int q4, const float4 *__restrict__ ec,
                                                     const float4 *__restrict__ rv, float4 *ep, float ca, float cb,
-                                                    const int *done) {
-    if (*(volatile const int *)done) return;
+                                                    const int *done, int k, const int *kc) {
+    if (ls_stop(done, k)) return;   // converged, or past the cycle's steps
     const unsigned total = (unsigned)n * (unsigned)q4;   // < 2^31 (checked by the caller)
     for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
         const int i = (int)(t / (unsigned)q4), q = (int)(t - (unsigned)i * (unsigned)q4);
@@ -1659,17 +1680,18 @@ unsigned resid_grid(int W, long long tiles) { return capped(tiles, ls_grids().re
 
 template <int W>
 cudaError_t ls_steps(const DevSolveOp &op, int n, int q4, float *&ec, float *&ep, const float *rv,
-                     const double *ca, const double *cb, int K, const int *done, cudaStream_t s) {
+                     const double *ca, const double *cb, int K, const int *done, const int *kc, cudaStream_t s) {
     const long long work = (long long)n * q4;
     const bool pk = op.pk32 != nullptr;   // row records: one matrix stream (ensemble steps -0.6 %)
     const unsigned blocks = capped((work + 255) / 256, pk ? ls_grids().step_pk : ls_grids().step[W - 6]);
     for (int k = 1; k < K; ++k) {
         if (pk)
             k_ls_step_pk<<<blocks, 256, 0, s>>>(op.pk32, op.dinv32, n, q4, (const float4 *)ec, (const float4 *)rv,
-                                                (float4 *)ep, (float)ca[k], (float)cb[k], done);
+                                                (float4 *)ep, (float)ca[k], (float)cb[k], done, k, kc);
         else
             k_ls_step<W><<<blocks, 256, 0, s>>>(op.A.col, op.a32, op.dinv32, n, q4, (const float4 *)ec,
-                                                (const float4 *)rv, (float4 *)ep, (float)ca[k], (float)cb[k], done);
+                                                (const float4 *)rv, (float4 *)ep, (float)ca[k], (float)cb[k], done,
+                                                k, kc);
         float *t = ec; ec = ep; ep = t;   // e_{k+1} is in the old e_{k-1} buffer
     }
     return cudaGetLastError();
@@ -1691,12 +1713,13 @@ cudaError_t cheb_lockstep(const DevSolveOp &op, const double *B, double *X, int 
     double *rpart = (double *)(w + L.v + 3 * vec), *bpart = rpart + (size_t)nv * nbx;
     double *R = (double *)(w + L.r);
     double *nrm = (double *)(w + L.part), *beta = nrm + 2 * nvp, *sc = beta + nvp;
-    int *done = (int *)(sc + nvp);
+    int *done = (int *)(sc + nvp), *kcp = done + 1;   // stop flag; the cycle's steps
     // coefficients (as the per-member Chebyshev kernel)
     const double lo = op.cheb_lmin, hi = op.cheb_lmax;
     const double kappa = hi / lo, sq = sqrt(kappa), sigma = (sq - 1.0) / (sq + 1.0);
     int K = (int)ceil(log(2.0 * kappa / inner_rtol) / log(1.0 / sigma)) + 1;
     K = K < 2 ? 2 : (K > CHEB_KMAX ? CHEB_KMAX : K);
+    const double lg = log(2.0 * kappa), ls = log(1.0 / sigma);
     const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), s1 = theta / delta;
     double ca[CHEB_KMAX], cb[CHEB_KMAX], rho_prev = 1.0 / s1;
     ca[0] = cb[0] = 0.0;
@@ -1725,15 +1748,15 @@ cudaError_t cheb_lockstep(const DevSolveOp &op, const double *B, double *X, int 
         default: k_ls_resid<8><<<rblocks, 256, 0, s>>>(op.A.col, op.A.val, n, B, X, ld, R, nv, rpart, nbx, done); break;
         }
         k_ls_nrm<<<(nv + NWARP - 1) / NWARP, 256, 0, s>>>(rpart, bpart, nbx, nrm, nv, done);
-        k_ls_scale<<<1, 256, 0, s>>>(nrm, nv, nvp, tol, beta, sc, done, st, c, K, c ? cyc : 0.0);
+        k_ls_scale<<<1, 256, 0, s>>>(nrm, nv, nvp, tol, beta, sc, done, st, c, K, c ? cyc : 0.0, lg, ls, kcp);
         if (c == LS_MAXC) break;
         k_ls_init<<<capped(ntile, cap_init), 256, 0, s>>>(R, n, nv, nvp, sc, op.dinv32, (float)(1.0 / theta), rv, e0,
                                                           e1, done);
         float *ec = e1, *ep = e0;
         switch (W) {
-        case 6: e = ls_steps<6>(op, n, q4, ec, ep, rv, ca, cb, K, done, s); break;
-        case 7: e = ls_steps<7>(op, n, q4, ec, ep, rv, ca, cb, K, done, s); break;
-        default: e = ls_steps<8>(op, n, q4, ec, ep, rv, ca, cb, K, done, s); break;
+        case 6: e = ls_steps<6>(op, n, q4, ec, ep, rv, ca, cb, K, done, kcp, s); break;
+        case 7: e = ls_steps<7>(op, n, q4, ec, ep, rv, ca, cb, K, done, kcp, s); break;
+        default: e = ls_steps<8>(op, n, q4, ec, ep, rv, ca, cb, K, done, kcp, s); break;
         }
         if (e != cudaSuccess) return e;
         k_ls_update<<<capped(ntile, cap_upd), 256, 0, s>>>(X, ld, n, nv, nvp, beta, ec, done);
