@@ -2855,8 +2855,8 @@ cudaError_t gmres_solve_multi(const DevSolveOp *const *ops, const int *nvk, cons
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, BLOCK, smem)) != cudaSuccess) return e;
     if (per < 1) return cudaErrorInvalidConfiguration;
     const int sms = (max_sms > 0 && max_sms < sm_count()) ? max_sms : sm_count();
-    const int cap = sms * per;
-    if (cap < nseg) return cudaErrorInvalidConfiguration;
+    int cap = sms * per;
+    if (cap < nseg) cap = nseg;   // one block per mesh at least (an SM cap below that is exceeded)
     // the resident blocks split between the segments in proportion to their
     // work (right-hand sides x rows), at least one block each; within a
     // segment as the single-operator launch does it: as many groups as

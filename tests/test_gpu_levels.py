@@ -66,10 +66,11 @@ def test_levels_refusals():
     assert e.value.code == 1
 
 
-@pytest.mark.parametrize("sms", [3, 8, 40])
+@pytest.mark.parametrize("sms", [1, 3, 8, 40])
 def test_levels_few_sms(sms):
     """The resident blocks split between the meshes in proportion to their
-    work, at least one block each: with the launch capped to a few SMs the
+    work, at least one block each (one SM: three blocks for three meshes,
+    beyond the cap): with the launch capped to a few SMs the
     small meshes get single-block groups and several right-hand sides per
     group; every solution still equals the mesh's own batched solve."""
     nvs = (5, 3, 2)
