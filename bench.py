@@ -293,7 +293,7 @@ def run_ours(args, ws, rank, local):
 
     strict = run_strict(mesh, psi0, cor, dev, stream, flush, args.steps) if args.tol != STRICT_TOL else None
 
-    # batched ensembles (BASELINE config 3: 256 members on level 5, and 32 on level 6)
+    # batched ensembles: 256 members on level 5 (the ensemble workload), and 32 on level 6
     batched = {}
     if not args.no_batch:
         from mke_gb300 import fields
@@ -349,7 +349,7 @@ def run_ours(args, ws, rank, local):
     # operator apply at a streaming size (level 8, 64 FP32 vectors; one FP64 vector)
     spmv = None if args.no_spmv else run_spmv(8, 64)
 
-    # BASELINE config 1: the level-3 Laplace solve to 1e-12 against the exact solution
+    # the level-3 Laplace solve to 1e-12 against the exact solution
     lap3 = None if args.no_laplace3 else run_laplace_l3()
     # the element-loop Jacobian quadrature on an ensemble's fields
     jq = None if args.no_spmv else run_jac_quad()
@@ -402,7 +402,7 @@ def run_ours(args, ws, rank, local):
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args.level, steps=1, tol=args.tol)
-        if lap3 is not None:   # config 1's error against the CPU reference algorithm's own solve
+        if lap3 is not None:   # the level-3 solve's error against the CPU reference algorithm's own solve
             ref = cpu.pop("laplace_l3_solution")
             lap3["rel_err_vs_cpu_reference_solve"] = float(np.linalg.norm(lap3.pop("solution") - ref)
                                                            / np.linalg.norm(ref))
@@ -618,7 +618,7 @@ def run_jac_quad(level: int = 6, nv: int = 32, reps: int = 20):
 
 
 def run_laplace_l3(reps: int = 20):
-    """BASELINE config 1: the Laplace solve on the level-3 sphere (642 points).
+    """The Laplace solve on the level-3 sphere (642 points), GMRES(30) to 1e-12.
     u* = sum of c_lm Y_lm (l = 1..6, c ~ N(0, 1), seeded; l = 0 dropped, so the
     mean is removed), f = Laplacian of u* (exact: -l(l+1) per degree), the
     boundary (south pole) value u*(pole).  FP64 handle, FGMRES(30) to a 1e-12

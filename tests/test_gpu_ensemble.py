@@ -65,7 +65,7 @@ def ensemble(level, members, steps, check, oracle_steps):
 
 
 def test_level5_256_members():
-    """BASELINE's ensemble configuration: 256 members on level 5, 10 steps;
+    """The ensemble workload: 256 members on level 5, 10 steps;
     members 0, 97 and 255 against their FP64 single trajectories, member 0
     against the oracle."""
     ensemble(5, 256, 10, check=(0, 97, 255), oracle_steps=10)
