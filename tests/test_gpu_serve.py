@@ -216,3 +216,35 @@ def test_packed_laplace_levels(pack, monkeypatch):
     if pack == "5":
         # a turn of more than `per` members holds more than one level
         assert max(c["batch"] for c in got.values()) > per
+
+
+def test_packed_lane_closes_idle_level(monkeypatch):
+    """A packed Laplace lane under a budget that holds one level at a time:
+    the level opened first is closed (least recently used, idle) to make room
+    for the next, and both requests complete."""
+    monkeypatch.setenv("PHG_SERVE_PACK", "5")
+    F3, _ = inputs(3, 4)
+    F4, _ = inputs(4, 5)
+    probe = phelm.Server(precision=phelm.PHG_FP64, hbm_budget_bytes=40e9, max_slots=2, solve_tol=1e-12)
+    try:
+        probe.preload(SOLVE, 3)
+        b3 = probe.stats()["bytes_in_use"]
+        probe.preload(SOLVE, 4)
+        b4 = probe.stats()["bytes_in_use"] - b3
+    finally:
+        probe.close()
+    budget = 1.02 * max(b3, b4)
+    assert budget < b3 + b4
+    srv = phelm.Server(precision=phelm.PHG_FP64, hbm_budget_bytes=budget, max_slots=2, solve_tol=1e-12)
+    try:
+        srv.submit(SOLVE, 3, F3, tag=1)
+        a = wait_for(srv, {1})[1]
+        srv.submit(SOLVE, 4, F4, tag=2)
+        b = wait_for(srv, {2})[2]
+        assert a["status"] == 0 and b["status"] == 0, (a, b)
+        st = srv.stats()
+        assert st["bytes_in_use"] <= budget and st["lanes"] == 1
+    finally:
+        srv.close()
+    ops = phelm.Operators(phelm.Mesh.sphere(4), phelm.PHG_FP64, tol=1e-12)
+    assert rel(b["output"], phelm.SphereLaplace(ops).solve(F4)) <= TOL
