@@ -2433,12 +2433,32 @@ bool lsg_applicable(const DevSolveOp &op, int nv, Precision p, int restart) {
     return (long long)op.A.n * ((nv + 31) / 32 * 8) < (1LL << 31);
 }
 
-unsigned lsg_blocks(long long work) {
+unsigned lsg_blocks(long long work, unsigned resident = 0) {
     long long b = (work + 255) / 256;
-    const long long cap = 4LL * sm_count();
+    long long cap = 4LL * sm_count();
+    if (resident > 0 && resident < cap) cap = resident;   // no partial second wave
     if (b > cap) b = cap;
     if (b < 1) b = 1;
     return (unsigned)b;
+}
+
+// resident grids of the register-heavy lockstep multigrid kernels (80 registers:
+// 3 blocks of 256 threads per SM, fewer than the 4 per SM the other kernels
+// launch with), queried once at operator creation like ls_grids.  Capping
+// their grid at one resident wave instead of 4 blocks per SM avoids a second,
+// partial wave.
+struct LsgGrids {
+    unsigned down, smooth, spmm;
+};
+const LsgGrids &lsg_grids() {
+    static std::once_flag once;
+    static LsgGrids g;
+    std::call_once(once, [] {
+        g.down = resident_grid(k_mg_down, 0);
+        g.smooth = resident_grid(k_mg_smooth, 0);
+        g.spmm = resident_grid(k_lsg_spmm, 0);
+    });
+    return g;
 }
 
 cudaError_t lsg_solve(const DevSolveOp &op, const double *B, double *X, int nv, int ld, int restart, int max_iter,
@@ -2509,7 +2529,7 @@ cudaError_t lsg_solve(const DevSolveOp &op, const double *B, double *X, int nv, 
     k_ls_sq<<<rgrid, 256, 0, s>>>(B, n, ld, nv, P.bpart);
     launches += 2;
     const unsigned gsmall = (unsigned)std::min(P.q4, 4 * sm_count());
-    const unsigned gn = lsg_blocks((long long)n * P.q4);
+    const unsigned gn = lsg_blocks((long long)n * P.q4, lsg_grids().spmm);
     const dim3 red_grid((unsigned)Lo.RB, (unsigned)(nvp / 32));
     const unsigned tiles = lsg_blocks((long long)((n + 31) / 32) * (nvp / 32) * 256);
     P.maxc = lsg_maxc;
@@ -2534,7 +2554,7 @@ cudaError_t lsg_solve(const DevSolveOp &op, const double *B, double *X, int nv, 
             float *vout0 = j == 0 ? nullptr : vj;
             float *zj = P.Z + (size_t)j * n * nvp;
             for (int l = 0; l < lc; ++l) {
-                k_mg_down<<<lsg_blocks((long long)P.lev[l].n * P.q4), 256, 0, s>>>(
+                k_mg_down<<<lsg_blocks((long long)P.lev[l].n * P.q4, lsg_grids().down), 256, 0, s>>>(
                     P, P.lev[l], l == 0 ? src0 : P.lev[l].b, l == 0 ? vout0 : nullptr, j);
                 if (l + 1 < lc)
                     k_mg_restrict<<<lsg_blocks((long long)P.lev[l + 1].n * P.q4), 256, 0, s>>>(P, P.lev[l], P.lev[l + 1], j);
@@ -2546,8 +2566,8 @@ cudaError_t lsg_solve(const DevSolveOp &op, const double *B, double *X, int nv, 
                 const float *xc = (l + 1 == lc) ? P.lev[lc].x : P.lev[l + 1].xo;
                 k_mg_prolong<<<lsg_blocks((long long)P.lev[l].n * P.q4), 256, 0, s>>>(P, P.lev[l], xc, j);
                 float *out = l == 0 ? zj : P.lev[l].xo;
-                k_mg_smooth<<<lsg_blocks((long long)P.lev[l].n * P.q4), 256, 0, s>>>(P, P.lev[l], l == 0 ? vj : P.lev[l].b,
-                                                                                  out, j);
+                k_mg_smooth<<<lsg_blocks((long long)P.lev[l].n * P.q4, lsg_grids().smooth), 256, 0, s>>>(
+                    P, P.lev[l], l == 0 ? vj : P.lev[l].b, out, j);
                 launches += 2;
             }
             k_lsg_spmm<<<gn, 256, 0, s>>>(P, j);
@@ -2953,6 +2973,9 @@ cudaError_t gmres_solve_multi(const DevSolveOp *const *ops, const int *nvk, cons
     return cudaGetLastError();
 }
 
-void lockstep_prepare() { (void)ls_grids(); }
+void lockstep_prepare() {
+    (void)ls_grids();
+    (void)lsg_grids();
+}
 
 }  // namespace phg
