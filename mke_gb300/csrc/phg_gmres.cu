@@ -2014,13 +2014,17 @@ __global__ void __launch_bounds__(256) k_mg_restrict(LsgParams P, LsgLevel L, Ls
     }
 }
 
+// threads of a k_mg_small block: one per row of the 641-row level (a block runs
+// one 4-member chunk alone, so the small levels' sweeps are its latency)
+constexpr int MG_SMALL_TB = 1024;
+
 // Levels [lc, nlev) for one 4-member chunk per block, in shared memory (four
 // float4 vectors per level: x, t, b, r): b_lc = R r_{lc-1} (or the input when
 // lc = 0), down sweeps and restrictions, the dense coarsest solve, the
 // prolongations and up sweeps; x_lc is written to out (the coarse correction
 // of level lc - 1, or the V-cycle's output when lc = 0).  Replaces one launch
 // per small level and phase by a single launch.
-__global__ void __launch_bounds__(256) k_mg_small(LsgParams P, const float *src, float *vout, float *out, int j) {
+__global__ void __launch_bounds__(MG_SMALL_TB) k_mg_small(LsgParams P, const float *src, float *vout, float *out, int j) {
     if (lsg_skip(P, j)) return;
     extern __shared__ float4 sm4[];
     const int q4 = P.q4, lc = P.lc, last = P.nlev - 1;
@@ -2560,7 +2564,7 @@ cudaError_t lsg_solve(const DevSolveOp &op, const double *B, double *X, int nv, 
                     k_mg_restrict<<<lsg_blocks((long long)P.lev[l + 1].n * P.q4), 256, 0, s>>>(P, P.lev[l], P.lev[l + 1], j);
                 launches += l + 1 < lc ? 2 : 1;
             }
-            k_mg_small<<<gsmall, 256, small_smem, s>>>(P, src0, lc == 0 ? vout0 : nullptr, lc == 0 ? zj : P.lev[lc].x, j);
+            k_mg_small<<<gsmall, MG_SMALL_TB, small_smem, s>>>(P, src0, lc == 0 ? vout0 : nullptr, lc == 0 ? zj : P.lev[lc].x, j);
             ++launches;
             for (int l = lc - 1; l >= 0; --l) {
                 const float *xc = (l + 1 == lc) ? P.lev[lc].x : P.lev[l + 1].xo;
